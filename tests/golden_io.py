@@ -1,0 +1,33 @@
+"""Load the committed golden fixtures (reference outputs on seeded inputs)."""
+import glob
+import os
+
+import numpy as np
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def loss_case_names():
+    names = []
+    for p in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
+        n = os.path.basename(p)[:-4]
+        if not n.startswith("core_"):
+            names.append(n)
+    return names
+
+
+def load_case(name):
+    d = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    s = d["scalars"]
+    d.update(distance=float(s[0]), edge_mult=float(s[1]), wavelength=float(s[2]),
+             px=float(s[3]), cutoff=float(s[4]), rolloff=float(s[5]),
+             loss_weight=float(s[6]), batch=int(s[7]), step_probe=int(s[8]),
+             step_obj=int(s[9]), step_pos=int(s[10]), algorithm=str(d["algorithm"]),
+             double=bool(d["double"]))
+    return d
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
