@@ -1,0 +1,366 @@
+"""Benchmark: scan positions per second of one full loss + adjoint-gradient pass.
+
+Workload (default): the multislice configuration -- 512x512 px x 20 slices object at
+0.1 A/px, 128 px probe with 3 incoherent modes (powers 0.6/0.3/0.1) at 300 kV / 30 mrad,
+32x32 scan at 0.4 A with U(+-0.2 A) jitter, Poisson loss ("ml"), compute batch 256,
+complex64. One step = one call of the loss-and-direction path over all 1024 positions
+(forward multislice, far-field Poisson loss, adjoint multislice, object / probe / position
+gradients). Inputs are seeded synthetic data: the measured patterns are simulated with the
+library's own forward model from the true specimen plus Poisson noise, and the gradient is
+evaluated at a half-phase start, so no step is skipped or cached.
+
+`value`   positions/s with object, probe and patterns resident in HBM (device-timed).
+`e2e`     positions/s through the public call with host buffers: each step copies object,
+          probe and patterns host->device and gradients + loss device->host.
+`roofline` the dominant kernel (fused_multislice) timed live with CUDA events on its
+          stream; algorithmic bytes per launch as documented in the design doc.
+
+The working set of a step (object 42 MB, patterns 67 MB, per-batch wave stack 2 GB) is
+far larger than the 129 MB L2, so no explicit L2 flush is needed between steps.
+
+Under torchrun with N GPUs every rank runs the same workload on its own GPU (replicas:
+the path needs no collective), `value` is the sum over ranks of positions/s.
+
+`--impl reference` times the reference algorithm on the host cores: the NumPy restatement
+in oracle/ (the reference is pure Python and is not installed on the GPU host), on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (W, Ny, Z, Mp, n_scan, algorithm, batch)
+    "multislice": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=32, algorithm="ml", batch=256,
+                       desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 32x32 jittered scan, ml, batch 256"),
+    "single-slice": dict(W=64, N_obj=128, Z=1, Mp=1, n_scan=16, algorithm="lsq_sqrt", batch=256,
+                         desc="single-slice W64 Z1 Mp1, 128x128 object, 16x16 scan, lsq_sqrt, batch 256"),
+}
+
+
+def alg_bytes_per_position(W, Z, Mp, Mo=1):
+    """Algorithmic HBM bytes of one position (complex64 = 8 B, float32 patterns = 4 B):
+    W^2 * (32 Z Mo + 16 Z Mp Mo + 4): object windows read forward + adjoint, gradient
+    read-modify-write, wave stack write + read, measured pattern read."""
+    return W * W * (32 * Z * Mo + 16 * Z * Mp * Mo + 4)
+
+
+def fused_bytes_per_position(W, Z, Mp, Mo=1):
+    """Bytes the fused multislice kernel must move per position: band-limited object
+    windows read forward and adjoint (16 Z Mo), wave stack write + read (16 Z Mp Mo),
+    probe-mode-summed gradient windows written (8 Z Mo), measured pattern read (4),
+    per-position probe-gradient spectra written (8 Mp)."""
+    return W * W * (16 * Z * Mo + 16 * Z * Mp * Mo + 8 * Z * Mo + 4 + 8 * Mp)
+
+
+def fft_flops_per_position(W, Z, Mp, Mo=1):
+    """5 W^2 log2(W^2) flops per 2D FFT; FFTs per position of the reference algorithm:
+    4 Z Mo (object and gradient band limits) + 4 (Z-1) Mp Mo (propagation both ways)
+    + 2 Mp Mo (far field both ways) + 3 Mp (probe shift and its adjoint)."""
+    n_fft = 4 * Z * Mo + 4 * (Z - 1) * Mp * Mo + 2 * Mp * Mo + 3 * Mp
+    return n_fft * 5.0 * W * W * np.log2(W * W)
+
+
+def build_workload(cfg, seed=0):
+    """Seeded specimen, probe and scan for a configuration (host arrays)."""
+    from pypty_gb300 import synth
+    rng = np.random.default_rng(seed)
+    if cfg["W"] == 128:
+        px, kV, alpha, df, dz = 0.1, 300.0, 30.0, 50.0, 2.0
+        truth = synth.gaussian_phase_object(cfg["N_obj"], cfg["N_obj"], cfg["Z"], 150, 0.3, px, 0.2, 1.0, rng)
+        probe = synth.make_probe(cfg["W"], px, kV, alpha, df, cfg["Mp"], [0.6, 0.3, 0.1][:cfg["Mp"]], 1e5)
+        pos = synth.raster_positions(cfg["n_scan"], cfg["n_scan"], 0.4 / px, 0.2 / px, rng)
+        dose = 1e5
+    else:
+        px, kV, alpha, df, dz = 0.2, 200.0, 25.0, 100.0, 1.0
+        truth = synth.gaussian_phase_object(cfg["N_obj"], cfg["N_obj"], cfg["Z"], 60, 0.4, px, 0.5, 2.0, rng)
+        probe = synth.make_probe(cfg["W"], px, kV, alpha, df, cfg["Mp"], None, 1e4)
+        pos = synth.raster_positions(cfg["n_scan"], cfg["n_scan"], 0.5 / px)
+        dose = 1e4
+    ipos, corr = synth.split_positions(pos)
+    obj0 = np.exp(0.5j * np.angle(truth)).astype(np.complex64)
+    return dict(truth=truth, obj0=obj0, probe=probe, ipos=ipos, corr=corr, px=px, kV=kV, dz=dz, dose=dose,
+                wavelength=synth.wavelength_A(kV), rng=rng)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in open(self.file.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(cfg, wl, n_sample, algorithm, budget_s=25.0):
+    """The oracle (NumPy restatement of the reference path) on a bounded sample of positions,
+    on all host cores (scipy.fft workers)."""
+    import scipy.fft
+    from oracle import ptycho_oracle as orc
+    cores = os.cpu_count() or 1
+    seq = np.arange(n_sample)
+    meas = np.zeros((n_sample, cfg["W"], cfg["W"]), np.float32) + 1.0
+    with scipy.fft.set_workers(cores):
+        t0 = time.perf_counter()
+        orc.loss_and_direction(wl["obj0"], wl["probe"], wl["ipos"][:n_sample], wl["corr"][:n_sample], wl["dz"],
+                               1.0, meas, algorithm, wl["wavelength"], 1, 1, 1, wl["px"], wl["px"], 2 / 3, 0.0,
+                               seq, 1, n_sample)
+        dt = time.perf_counter() - t0
+    return {"value": n_sample / dt, "unit": "positions/s", "cores": cores, "kind": "port",
+            "sample": "%d positions of the %s workload (NumPy/SciPy oracle, complex64, %.1f s)" % (
+                n_sample, cfg["name"], dt), "seconds": dt}
+
+
+def run_reference(args, cfg):
+    """--impl reference: the reference algorithm on the host cores, same metric and config."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = build_workload(cfg)
+    n_sample = 8 if cfg["W"] == 128 else 64
+    for _ in range(args.warmup if args.warmup > 0 else 0):
+        pass   # the oracle has no warm-up state; warm-up steps would only lengthen the run
+    vals = []
+    last = None
+    for _ in range(max(args.steps, 1)):
+        last = cpu_baseline(cfg, wl, n_sample, cfg["algorithm"])
+        vals.append(last["value"])
+    value = float(np.mean(vals))
+    line = {"metric": "positions/s fwd+adjoint", "value": value, "unit": "positions/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n_sample / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": cfg["desc"], "sample_positions": n_sample},
+            "cpu_baseline": {"value": value, "unit": "positions/s", "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": value, "unit": "positions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="multislice", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    cfg = dict(CONFIGS[args.config], name=args.config)
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+
+    from pypty_gb300 import _lib
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+
+    wl = build_workload(cfg)
+    W, Z, Mp = cfg["W"], cfg["Z"], cfg["Mp"]
+    eng = Engine(dev)
+    geo = Geometry.make(wl["ipos"], wl["corr"])
+    n_pos = geo.positions.shape[0]
+    common = dict(algorithm=cfg["algorithm"], wavelength=wl["wavelength"], pixel_size_x=wl["px"],
+                  pixel_size_y=wl["px"], slice_distance=wl["dz"], compute_batch=cfg["batch"])
+    prob = make_problem(W, wl["obj0"].shape, Mp, geo, step_pos=True, **common)
+    # measured data: forward model at the true specimen + Poisson noise
+    truth_d = torch.from_numpy(wl["truth"]).to(dev)
+    probe_d = torch.from_numpy(wl["probe"]).to(dev)
+    sim = eng.simulate(prob, truth_d, probe_d, geo)
+    gen = torch.Generator(device=dev).manual_seed(1)
+    meas_d = torch.poisson(sim.clamp_min(0), generator=gen).contiguous()
+    del truth_d, sim
+    obj_d = torch.from_numpy(wl["obj0"]).to(dev)
+    out = (torch.empty(2, dtype=torch.float64, device=dev), torch.empty_like(obj_d), torch.empty_like(probe_d),
+           torch.empty((n_pos, 2), dtype=torch.float32, device=dev))
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---------------- device-resident timing
+    for _ in range(args.warmup):
+        eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)
+    torch.cuda.synchronize(dev)
+    barrier()
+    torch.cuda.synchronize(dev)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler(64 * max(args.steps, 1)) as prof:
+        start.record(stream)
+        for _ in range(args.steps):
+            eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier()
+    ms = start.elapsed_time(stop) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    loss_val = float(out[0][0].item())
+    if not np.isfinite(loss_val):
+        raise RuntimeError("non-finite loss in the benchmark")
+    value = world * n_pos / (ms / 1000.0)
+
+    # ---------------- end-to-end through the public call with host buffers
+    obj_h = torch.from_numpy(wl["obj0"]).pin_memory()
+    probe_h = torch.from_numpy(wl["probe"]).pin_memory()
+    meas_h = meas_d.cpu().pin_memory()
+    og_h = torch.empty_like(obj_h).pin_memory()
+    pg_h = torch.empty_like(probe_h).pin_memory()
+    posg_h = torch.empty((n_pos, 2), dtype=torch.float32).pin_memory()
+    ls_h = torch.empty(2, dtype=torch.float64).pin_memory()
+    obj_e, probe_e, meas_e = torch.empty_like(obj_d), torch.empty_like(probe_d), torch.empty_like(meas_d)
+
+    def e2e_step():
+        obj_e.copy_(obj_h, non_blocking=True)
+        probe_e.copy_(probe_h, non_blocking=True)
+        meas_e.copy_(meas_h, non_blocking=True)
+        eng.loss_and_direction(prob, obj_e, probe_e, geo, meas_e, out=out)
+        og_h.copy_(out[1], non_blocking=True)
+        pg_h.copy_(out[2], non_blocking=True)
+        posg_h.copy_(out[3], non_blocking=True)
+        ls_h.copy_(out[0], non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = obj_h.numel() * 8 + probe_h.numel() * 8 + meas_h.numel() * 4 + geo.positions.nbytes + \
+        geo.pos_correction.nbytes + geo.sequence.nbytes
+    d2h = og_h.numel() * 8 + pg_h.numel() * 8 + posg_h.numel() * 4 + 16
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---------------- roofline of the dominant kernel, timed live with CUDA events
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peaks = json.load(open(peaks_path))
+        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    else:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    fused_ms = prof.ms.get("fused_multislice", 0.0)
+    fused_n = max(prof.launches.get("fused_multislice", 0), 1)
+    fused_avg_s = fused_ms / fused_n / 1000.0
+    per_launch_pos = n_pos / (fused_n / args.steps)
+    fused_bytes = fused_bytes_per_position(W, Z, Mp) * per_launch_pos
+    achieved = fused_bytes / fused_avg_s / 1e9
+    path_bytes = alg_bytes_per_position(W, Z, Mp) * n_pos
+    total_prof_ms = sum(prof.ms.values())
+    kernel_share = {k: round(v / total_prof_ms, 4) for k, v in sorted(prof.ms.items(), key=lambda kv: -kv[1])
+                    if v > 0}
+    cs = clocks.summary()
+    line = {
+        "metric": "positions/s fwd+adjoint", "value": value, "unit": "positions/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": cfg["desc"], "positions_per_step": n_pos, "global_batch": n_pos * world,
+                   "parallelism": "replicas x%d" % world if world > 1 else "single GPU",
+                   "l2": "working set per step >> 129 MB L2 (inputs 110 MB + 2 GB wave stack per batch); no flush"},
+        "e2e": {"value": world * n_pos / (e2e_ms / 1000.0), "unit": "positions/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": "fused_multislice", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src + " (hbm_gbs)",
+                     "traffic": None, "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3},
+        "path_roofline": {"alg_bytes_per_position": alg_bytes_per_position(W, Z, Mp),
+                          "achieved_gbs": path_bytes / (ms / 1000.0) / 1e9,
+                          "frac": path_bytes / (ms / 1000.0) / 1e9 / hbm_peak,
+                          "fft_tflops": fft_flops_per_position(W, Z, Mp) * n_pos / (ms / 1000.0) / 1e12},
+        "kernel_share": kernel_share,
+        "gpu_launches": prof.total_launches,
+        "clocks": {"sm_mhz": cs.get("sm_mhz"), "sm_max_mhz": cs.get("sm_max_mhz"), "reasons": cs.get("reasons")},
+        "loss": loss_val,
+    }
+    if not args.no_cpu_baseline:
+        n_sample = 8 if W == 128 else 64
+        cb = cpu_baseline(cfg, wl, n_sample, cfg["algorithm"])
+        cb.pop("seconds", None)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

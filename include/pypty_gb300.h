@@ -1,0 +1,142 @@
+/*
+ * pypty_gb300 C ABI -- far-field multislice ptychography hot path on one GB300 (sm_103a).
+ *
+ * Plain C types only. Every device buffer (inputs, outputs, workspace) is allocated by the
+ * caller; no entry point allocates device memory. Entry points are asynchronous with
+ * respect to the host on the given CUDA stream (a cudaStream_t passed as void*; NULL is
+ * the legacy default stream) except for the small host-to-device copies of the scan
+ * geometry, which follow cudaMemcpyAsync semantics for the host memory they are given
+ * (fully asynchronous only from page-locked memory).
+ *
+ * Array layouts are the reference's (C order, complex64 = interleaved float pairs):
+ *   object        (obj_ny, obj_nx, n_slices, n_obj_modes)
+ *   probe         (window, window, n_probe_modes)
+ *   positions     (n_positions, 2) int32 [y, x] integer pixel positions
+ *   pos_correction(n_positions, 2) float32 [dy, dx] sub-pixel corrections
+ *   measured      (n_positions, window, window) float32 detector-plane intensities
+ *   sequence      (n_sequence) int32 indices into the position list
+ *
+ * Return value: PTY_OK (0) or a negative PTY_ERR_* code. Errors detected on the host
+ * (shapes, position range, workspace size) are returned before anything is launched.
+ */
+#ifndef PYPTY_GB300_H
+#define PYPTY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTY_OK 0
+#define PTY_ERR_INVALID (-1)     /* null pointer or non-positive size */
+#define PTY_ERR_UNSUPPORTED (-2) /* window not 64/128, Mp*Mo > 8, unknown algorithm */
+#define PTY_ERR_POSITION (-3)    /* a window leaves the object or a sequence entry is out of range */
+#define PTY_ERR_WORKSPACE (-4)   /* workspace smaller than pty_workspace_bytes() */
+#define PTY_ERR_CUDA (-5)        /* a CUDA launch or copy failed */
+
+/* loss functions: pypty/objective.py:527-558 (algorithm_type strings) */
+#define PTY_LSQ_SQRT 0   /* "lsq_sqrt"   amplitude L2 */
+#define PTY_ML 1         /* "ml"         Poisson negative log-likelihood */
+#define PTY_LSQ 2        /* "lsq"        intensity L2 */
+#define PTY_LSQ_SQRT_2 3 /* "lsq_sqrt_2" */
+
+typedef struct pty_problem {
+  int32_t window;         /* W, probe window size in px: 64 or 128 */
+  int32_t obj_ny, obj_nx; /* object extent in px */
+  int32_t n_slices;       /* Z */
+  int32_t n_obj_modes;    /* Mo */
+  int32_t n_probe_modes;  /* Mp */
+  int32_t n_positions;    /* rows of positions / pos_correction / measured */
+  int32_t n_sequence;     /* entries of the sequence (this_chopped_sequence) */
+  int32_t compute_batch;  /* positions per internal batch (compute_batch) */
+  int32_t algorithm;      /* PTY_LSQ_SQRT, PTY_ML, PTY_LSQ or PTY_LSQ_SQRT_2 */
+  int32_t step_obj;       /* nonzero: produce the object gradient */
+  int32_t step_probe;     /* nonzero: produce the probe gradient */
+  int32_t step_pos;       /* nonzero: produce the position gradient (needs probe_shift) */
+  int32_t probe_shift;    /* nonzero: sub-pixel shift of the probe by Fourier ramps */
+  float wavelength;       /* electron wavelength, Angstrom */
+  float pixel_size_x;     /* Angstrom */
+  float pixel_size_y;     /* Angstrom */
+  float slice_distance;   /* Angstrom, one distance for all slices */
+  float edge_mult;        /* first-slice thickness multiplier (propagator power) */
+  float damping_cutoff;   /* band-limit cutoff as a fraction of Nyquist (2/3 default) */
+  float smooth_rolloff;   /* cosine roll-off width of the band limit */
+  float loss_weight;      /* this_loss_weight */
+} pty_problem_t;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int pty_version(void);
+
+/* Human-readable text of a PTY_* status code (static storage). */
+const char* pty_status_string(int status);
+
+/* Device workspace (bytes) that pty_loss_and_direction / pty_simulate_patterns need. */
+int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes);
+
+/*
+ * Loss, sum of squared errors and Wirtinger gradients dL/dz* of the far-field multislice
+ * model over the positions of `sequence`, processed in batches of compute_batch.
+ * Replaces pypty.objective.loss_and_direction (pypty/objective.py:47-967) for
+ * recon_type "far_field", propmethod "multislice", no tilts, phase plates, aberration
+ * arrays, beam-current fluctuations, static background or regularisers.
+ *   obj, probe, measured        device, complex64 / float32, reference layouts
+ *   positions_host, pos_correction_host, sequence_host   host memory
+ *   loss_sse                    device, 2 doubles: loss * loss_weight, sse
+ *   object_grad                 device, complex64 (obj_ny, obj_nx, Z, Mo), overwritten
+ *   probe_grad                  device, complex64 (W, W, Mp), overwritten (band-limited)
+ *   pos_grad                    device, float32 (n_positions, 2), overwritten; rows not
+ *                               in the sequence are zero
+ */
+int pty_loss_and_direction(const pty_problem_t* problem, const void* obj, const void* probe,
+                           const int32_t* positions_host, const float* pos_correction_host,
+                           const int32_t* sequence_host, const float* measured,
+                           double* loss_sse, void* object_grad, void* probe_grad,
+                           float* pos_grad, void* workspace, size_t workspace_bytes,
+                           void* stream);
+
+/*
+ * Mean-over-modes far-field intensities of the positions of `sequence`
+ * (n_sequence, W, W) float32 in detector (fftshifted) order: the forward half of
+ * pypty.objective.loss_and_direction with data_simulation_flag set
+ * (pypty/objective.py:501-526). `measured` is not read.
+ */
+int pty_simulate_patterns(const pty_problem_t* problem, const void* obj, const void* probe,
+                          const int32_t* positions_host, const float* pos_correction_host,
+                          const int32_t* sequence_host, float* patterns, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/*
+ * Batched 2D FFT of `batch` contiguous W x W complex64 windows (W = 64 or 128).
+ * inverse = 0: unnormalised forward transform; inverse = 1: inverse scaled by 1/W^2.
+ * shift = 1 applies fftshift to the forward output / ifftshift to the inverse input.
+ * Replaces pypty.fft.fft2 / ifft2 / shift_fft2 / ifft2_ishift over axes (1, 2) of a
+ * (batch, W, W) array (pypty/fft.py:91-178). in and out may alias.
+ */
+int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
+             int32_t shift, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Workspace for pty_fft2 (twiddle tables). */
+int pty_fft2_workspace_bytes(int32_t window, size_t* bytes);
+
+/*
+ * Launch profiler (no counterpart in the reference, which only logs wall time,
+ * pypty/utils.py:1894). While enabled, every kernel launch of the library records a CUDA
+ * event on its stream just before the launch, and every call records one when its last
+ * launch is queued. pty_profile_end synchronises, disables profiling and returns, per
+ * kernel class, the summed device time between each launch's event and the next event
+ * (ms) and the launch count. Class names: pty_kernel_name(0 .. pty_kernel_count()-1).
+ * Single-threaded use only. Returns PTY_ERR_WORKSPACE if more than max_launches launches
+ * were made (the extra ones are not timed).
+ */
+int pty_profile_begin(int32_t max_launches);
+int pty_profile_end(double* ms_by_kernel, int32_t* launches_by_kernel, int32_t n_kinds);
+const char* pty_kernel_name(int32_t id);
+int pty_kernel_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYPTY_GB300_H */

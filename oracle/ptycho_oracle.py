@@ -198,6 +198,9 @@ def loss_and_direction(obj, probe, positions, pos_correction, distance, edge_mul
     Mp = probe.shape[2]
     Z, Mo = obj.shape[2], obj.shape[3]
     coherent = Mp == 1 and Mo == 1
+    # the reference receives these as default_float scalars (pypty/iterative.py:111-112,139)
+    pixel_size_x, pixel_size_y = float_dtype(pixel_size_x), float_dtype(pixel_size_y)
+    damping_cutoff, smooth_rolloff = float_dtype(damping_cutoff), float_dtype(smooth_rolloff)
     q2, qx, qy, mask_s, mask = spatial_frequencies(pixel_size_x, pixel_size_y, W,
                                                    damping_cutoff, smooth_rolloff, float_dtype)
     smy, smx = shift_ramp_tables(W, mask, complex_dtype)

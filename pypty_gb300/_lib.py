@@ -1,0 +1,136 @@
+"""ctypes binding of the C ABI declared in ``include/pypty_gb300.h``.
+
+The CUDA library is mandatory: if it is missing or fails to load, ``lib()`` raises. There
+is no CPU fallback anywhere in the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+PTY_OK = 0
+PTY_ERR_INVALID = -1
+PTY_ERR_UNSUPPORTED = -2
+PTY_ERR_POSITION = -3
+PTY_ERR_WORKSPACE = -4
+PTY_ERR_CUDA = -5
+
+ALGORITHMS = {"lsq_sqrt": 0, "ml": 1, "lsq": 2, "lsq_sqrt_2": 3}
+
+
+class Problem(ctypes.Structure):
+    """Mirror of ``pty_problem_t``."""
+    _fields_ = [
+        ("window", ctypes.c_int32), ("obj_ny", ctypes.c_int32), ("obj_nx", ctypes.c_int32),
+        ("n_slices", ctypes.c_int32), ("n_obj_modes", ctypes.c_int32),
+        ("n_probe_modes", ctypes.c_int32), ("n_positions", ctypes.c_int32),
+        ("n_sequence", ctypes.c_int32), ("compute_batch", ctypes.c_int32),
+        ("algorithm", ctypes.c_int32), ("step_obj", ctypes.c_int32),
+        ("step_probe", ctypes.c_int32), ("step_pos", ctypes.c_int32),
+        ("probe_shift", ctypes.c_int32), ("wavelength", ctypes.c_float),
+        ("pixel_size_x", ctypes.c_float), ("pixel_size_y", ctypes.c_float),
+        ("slice_distance", ctypes.c_float), ("edge_mult", ctypes.c_float),
+        ("damping_cutoff", ctypes.c_float), ("smooth_rolloff", ctypes.c_float),
+        ("loss_weight", ctypes.c_float),
+    ]
+
+
+class PtyError(RuntimeError):
+    """A PTY_ERR_* status returned by the library."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__("%s failed: %s (status %d)" % (what, _status_text(status), status))
+
+
+_LIB = None
+_VP = ctypes.c_void_p
+_SZ = ctypes.c_size_t
+_I32 = ctypes.c_int32
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_F32P = ctypes.POINTER(ctypes.c_float)
+_F64P = ctypes.POINTER(ctypes.c_double)
+_PP = ctypes.POINTER(Problem)
+
+SIGNATURES = {
+    "pty_version": ([], ctypes.c_int),
+    "pty_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "pty_workspace_bytes": ([_PP, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_loss_and_direction": ([_PP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP],
+                               ctypes.c_int),
+    "pty_simulate_patterns": ([_PP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_fft2": ([_VP, _VP, _I32, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_fft2_workspace_bytes": ([_I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_profile_begin": ([_I32], ctypes.c_int),
+    "pty_profile_end": ([_F64P, _I32P, _I32], ctypes.c_int),
+    "pty_kernel_name": ([_I32], ctypes.c_char_p),
+    "pty_kernel_count": ([], ctypes.c_int),
+}
+
+
+def _status_text(status: int) -> str:
+    if _LIB is None:
+        return "status %d" % status
+    return _LIB.pty_status_string(status).decode()
+
+
+def lib(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load ``libpypty_gb300.so`` (building it first only when asked)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.lib_path()
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise ImportError("pypty_gb300 CUDA library not built (%s); run "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    cdll = ctypes.CDLL(path)
+    for name, (argtypes, restype) in SIGNATURES.items():
+        fn = getattr(cdll, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    _LIB = cdll
+    return _LIB
+
+
+def check(status: int, what: str) -> None:
+    if status != PTY_OK:
+        raise PtyError(status, what)
+
+
+def workspace_bytes(problem: Problem) -> int:
+    n = _SZ(0)
+    check(lib().pty_workspace_bytes(ctypes.byref(problem), ctypes.byref(n)), "pty_workspace_bytes")
+    return int(n.value)
+
+
+class LaunchProfiler:
+    """Per-kernel device time and launch counts of the library's own kernels, measured with
+    CUDA events on the launching stream (``pty_profile_begin`` / ``pty_profile_end``)."""
+
+    def __init__(self, max_launches: int = 4096):
+        self.max_launches = max_launches
+        self.ms = {}
+        self.launches = {}
+
+    def __enter__(self):
+        check(lib().pty_profile_begin(self.max_launches), "pty_profile_begin")
+        return self
+
+    def __exit__(self, *exc):
+        n = lib().pty_kernel_count()
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int32 * n)()
+        check(lib().pty_profile_end(ms, cnt, n), "pty_profile_end")
+        for k in range(n):
+            name = lib().pty_kernel_name(k).decode()
+            self.ms[name] = float(ms[k])
+            self.launches[name] = int(cnt[k])
+        return False
+
+    @property
+    def total_launches(self) -> int:
+        return sum(self.launches.values())

@@ -1,0 +1,195 @@
+// C ABI of the GB300 ptychography path: host-side validation, workspace planning and
+// dispatch to the per-window-size launch paths. See include/pypty_gb300.h for the contract.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "plan.h"
+
+namespace {
+
+using namespace pty;
+
+int upload_geometry(const pty_problem_t* p, const Plan& q, void* ws, const int32_t* pos,
+                    const float* corr, const int32_t* seq, cudaStream_t st) {
+  if (cudaMemcpyAsync(at<int>(ws, q.o_pos), pos, (size_t)q.N * 2 * sizeof(int), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PTY_ERR_CUDA;
+  if (corr) {
+    if (cudaMemcpyAsync(at<float>(ws, q.o_corr), corr, (size_t)q.N * 2 * sizeof(float), cudaMemcpyHostToDevice,
+                        st) != cudaSuccess)
+      return PTY_ERR_CUDA;
+  } else if (cudaMemsetAsync(at<float>(ws, q.o_corr), 0, (size_t)q.N * 2 * sizeof(float), st) != cudaSuccess) {
+    return PTY_ERR_CUDA;
+  }
+  if (cudaMemcpyAsync(at<int>(ws, q.o_seq), seq, (size_t)q.nseq * sizeof(int), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PTY_ERR_CUDA;
+  return PTY_OK;
+}
+
+int run_common(const pty_problem_t* p, const void* obj, const void* probe, const int32_t* pos,
+               const float* corr, const int32_t* seq, const float* measured, double* loss_sse,
+               void* object_grad, void* probe_grad, float* pos_grad, float* patterns, void* ws,
+               size_t ws_bytes, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if (!obj || !probe || !pos || !seq || !ws) return PTY_ERR_INVALID;
+  if (!patterns && (!measured || !loss_sse)) return PTY_ERR_INVALID;
+  if ((rc = check_geometry(p, pos, seq))) return rc;
+  const Plan q = make_plan(p);
+  if (ws_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((rc = upload_geometry(p, q, ws, pos, corr, seq, st))) return rc;
+  if (q.W == 64)
+    return run_path<64>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
+                        loss_sse, static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad,
+                        patterns, ws, st);
+  return run_path<128>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
+                       loss_sse, static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad,
+                       patterns, ws, st);
+}
+
+// Launch profiler: one CUDA event per marked launch, read back in pty_profile_end.
+// Single-threaded use only (profiling / benchmarking).
+struct Profiler {
+  bool on = false;
+  int cap = 0, n = 0;
+  cudaEvent_t* ev = nullptr;
+  int* ids = nullptr;
+  bool overflow = false;
+};
+Profiler g_prof;
+
+const char* kKernelNames[KID_COUNT] = {
+    "build_twiddles", "tables", "probe_fft", "obj_to_slices", "object_windows", "fused_multislice",
+    "grad_windows", "tile_lists", "scatter_tiles", "probe_partial", "slices_to_obj", "probe_final",
+    "finalize_scalars", "fft2_batch"};
+
+}  // namespace
+
+namespace pty {
+void prof_mark(cudaStream_t st, int id) {
+  Profiler& P = g_prof;
+  if (!P.on) return;
+  if (P.n >= P.cap) {
+    P.overflow = true;
+    return;
+  }
+  cudaEventRecord(P.ev[P.n], st);
+  P.ids[P.n++] = id;
+}
+}  // namespace pty
+
+extern "C" {
+
+int pty_profile_begin(int32_t max_launches) {
+  Profiler& P = g_prof;
+  if (max_launches <= 0) return PTY_ERR_INVALID;
+  if (2 * max_launches > P.cap) {
+    for (int i = 0; i < P.cap; ++i) cudaEventDestroy(P.ev[i]);
+    delete[] P.ev;
+    delete[] P.ids;
+    P.cap = 0;
+    P.ev = new cudaEvent_t[2 * max_launches];
+    P.ids = new int[2 * max_launches];
+    for (int i = 0; i < 2 * max_launches; ++i) {
+      if (cudaEventCreate(&P.ev[i]) != cudaSuccess) return PTY_ERR_CUDA;
+      P.cap = i + 1;
+    }
+  }
+  P.n = 0;
+  P.overflow = false;
+  P.on = true;
+  return PTY_OK;
+}
+
+int pty_profile_end(double* ms_by_kernel, int32_t* launches_by_kernel, int32_t n_kinds) {
+  Profiler& P = g_prof;
+  if (!P.on) return PTY_ERR_INVALID;
+  P.on = false;
+  for (int k = 0; k < n_kinds; ++k) {
+    if (ms_by_kernel) ms_by_kernel[k] = 0.0;
+    if (launches_by_kernel) launches_by_kernel[k] = 0;
+  }
+  if (P.n == 0) return PTY_OK;
+  if (cudaEventSynchronize(P.ev[P.n - 1]) != cudaSuccess) return PTY_ERR_CUDA;
+  for (int i = 0; i + 1 < P.n; ++i) {
+    const int id = P.ids[i];
+    if (id < 0 || id >= n_kinds) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, P.ev[i], P.ev[i + 1]) != cudaSuccess) return PTY_ERR_CUDA;
+    if (ms_by_kernel) ms_by_kernel[id] += ms;
+    if (launches_by_kernel) launches_by_kernel[id] += 1;
+  }
+  return P.overflow ? PTY_ERR_WORKSPACE : PTY_OK;
+}
+
+const char* pty_kernel_name(int32_t id) { return (id >= 0 && id < KID_COUNT) ? kKernelNames[id] : "unknown"; }
+
+int pty_kernel_count(void) { return KID_COUNT; }
+
+
+int pty_version(void) { return 100; }
+
+const char* pty_status_string(int status) {
+  switch (status) {
+    case PTY_OK: return "ok";
+    case PTY_ERR_INVALID: return "invalid argument";
+    case PTY_ERR_UNSUPPORTED: return "unsupported problem (window must be 64 or 128, Mp*Mo <= 8)";
+    case PTY_ERR_POSITION: return "scan position or sequence entry out of range";
+    case PTY_ERR_WORKSPACE: return "workspace too small";
+    case PTY_ERR_CUDA: return "CUDA launch or copy failed";
+    default: return "unknown status";
+  }
+}
+
+int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes) {
+  int rc = validate(problem);
+  if (rc) return rc;
+  if (!bytes) return PTY_ERR_INVALID;
+  *bytes = make_plan(problem).total;
+  return PTY_OK;
+}
+
+int pty_loss_and_direction(const pty_problem_t* problem, const void* obj, const void* probe,
+                           const int32_t* positions_host, const float* pos_correction_host,
+                           const int32_t* sequence_host, const float* measured, double* loss_sse,
+                           void* object_grad, void* probe_grad, float* pos_grad, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  return run_common(problem, obj, probe, positions_host, pos_correction_host, sequence_host, measured, loss_sse,
+                    object_grad, probe_grad, pos_grad, nullptr, workspace, workspace_bytes, stream);
+}
+
+int pty_simulate_patterns(const pty_problem_t* problem, const void* obj, const void* probe,
+                          const int32_t* positions_host, const float* pos_correction_host,
+                          const int32_t* sequence_host, float* patterns, void* workspace,
+                          size_t workspace_bytes, void* stream) {
+  if (!patterns) return PTY_ERR_INVALID;
+  return run_common(problem, obj, probe, positions_host, pos_correction_host, sequence_host, nullptr, nullptr,
+                    nullptr, nullptr, nullptr, patterns, workspace, workspace_bytes, stream);
+}
+
+int pty_fft2_workspace_bytes(int32_t window, size_t* bytes) {
+  if (window != 64 && window != 128) return PTY_ERR_UNSUPPORTED;
+  if (!bytes) return PTY_ERR_INVALID;
+  *bytes = align_up(tw_count(window) * sizeof(float2));
+  return PTY_OK;
+}
+
+int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, int32_t shift,
+             void* workspace, size_t workspace_bytes, void* stream) {
+  if (window != 64 && window != 128) return PTY_ERR_UNSUPPORTED;
+  if (!in || !out || !workspace || batch <= 0) return PTY_ERR_INVALID;
+  size_t need = 0;
+  pty_fft2_workspace_bytes(window, &need);
+  if (workspace_bytes < need) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  float2* tw = static_cast<float2*>(workspace);
+  const float2* src = static_cast<const float2*>(in);
+  float2* dst = static_cast<float2*>(out);
+  if (window == 64) return run_fft2<64>(src, dst, batch, inverse, shift, tw, st);
+  return run_fft2<128>(src, dst, batch, inverse, shift, tw, st);
+}
+
+}  // extern "C"

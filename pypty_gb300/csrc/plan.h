@@ -1,0 +1,131 @@
+// Workspace plan shared by the C ABI and the per-window-size launch paths.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "../../include/pypty_gb300.h"
+#include "window_fft.cuh"
+
+namespace pty {
+
+constexpr int kTileSize = 32;   // object tile edge of the deterministic scatter
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Byte offsets of every buffer inside the caller's workspace.
+struct Plan {
+  int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
+  size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_sx, o_sy, o_probe_f;
+  size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
+  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, total;
+};
+
+inline int tw_count(int W) { return W == 64 ? Geo<64>::TW1 + Geo<64>::TW2 : Geo<128>::TW1 + Geo<128>::TW2; }
+
+inline int validate(const pty_problem_t* p) {
+  if (!p) return PTY_ERR_INVALID;
+  if (p->window != 64 && p->window != 128) return PTY_ERR_UNSUPPORTED;
+  if (p->obj_ny <= 0 || p->obj_nx <= 0 || p->n_slices <= 0 || p->n_obj_modes <= 0 ||
+      p->n_probe_modes <= 0 || p->n_positions <= 0 || p->n_sequence <= 0 || p->compute_batch <= 0)
+    return PTY_ERR_INVALID;
+  if (p->n_obj_modes * p->n_probe_modes > 8) return PTY_ERR_UNSUPPORTED;
+  if (p->algorithm < PTY_LSQ_SQRT || p->algorithm > PTY_LSQ_SQRT_2) return PTY_ERR_UNSUPPORTED;
+  if (p->step_pos && !p->probe_shift) return PTY_ERR_INVALID;
+  if ((int64_t)p->obj_ny * p->obj_nx >= (int64_t)1 << 31) return PTY_ERR_UNSUPPORTED;
+  return PTY_OK;
+}
+
+inline Plan make_plan(const pty_problem_t* p) {
+  Plan q{};
+  q.W = p->window;
+  q.Ny = p->obj_ny;
+  q.Nx = p->obj_nx;
+  q.Z = p->n_slices;
+  q.Mo = p->n_obj_modes;
+  q.Mp = p->n_probe_modes;
+  q.N = p->n_positions;
+  q.nseq = p->n_sequence;
+  q.Bb = std::min(p->compute_batch, p->n_sequence);
+  q.nbatch = (q.nseq + q.Bb - 1) / q.Bb;
+  q.zm = q.Z * q.Mo;
+  q.ntx = (q.Nx + kTileSize - 1) / kTileSize;
+  q.nty = (q.Ny + kTileSize - 1) / kTileSize;
+  q.ntiles = q.ntx * q.nty;
+  q.chunk = 8;
+  q.nchunk = (q.Bb + q.chunk - 1) / q.chunk;
+  const size_t WW = (size_t)q.W * q.W, c8 = sizeof(float2), f4 = sizeof(float);
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes); return r; };
+  q.o_tw = take(tw_count(q.W) * c8);
+  q.o_mask = take(WW * f4);
+  q.o_mask_sc = take(WW * f4);
+  q.o_prop = take(WW * c8);
+  q.o_prop_edge = take(WW * c8);
+  q.o_sx = take(q.W * f4);
+  q.o_sy = take(q.W * f4);
+  q.o_probe_f = take(q.Mp * WW * c8);
+  q.o_pos = take((size_t)q.N * 2 * sizeof(int));
+  q.o_corr = take((size_t)q.N * 2 * f4);
+  q.o_seq = take((size_t)q.nseq * sizeof(int));
+  q.o_obj = take((size_t)q.zm * q.Ny * q.Nx * c8);
+  q.o_grad = take((size_t)q.zm * q.Ny * q.Nx * c8);
+  q.o_obl = take((size_t)q.Bb * q.zm * WW * c8);
+  q.o_stack = take((size_t)q.Bb * q.Z * q.Mp * q.Mo * WW * c8);
+  q.o_gsum = take((size_t)q.Bb * q.zm * WW * c8);
+  q.o_fprobe = take((size_t)q.Bb * q.Mp * WW * c8);
+  q.o_partial = take((size_t)q.nchunk * q.Mp * WW * c8);
+  q.o_lists = take((size_t)q.ntiles * q.Bb * sizeof(int));
+  q.o_counts = take((size_t)q.ntiles * sizeof(int));
+  q.o_loss_part = take((size_t)q.nseq * 2 * sizeof(double));
+  q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
+  q.o_sim = take((size_t)q.Bb * WW * f4);
+  q.total = o;
+  return q;
+}
+
+inline int check_geometry(const pty_problem_t* p, const int32_t* pos, const int32_t* seq) {
+  for (int i = 0; i < p->n_sequence; ++i) {
+    const int s = seq[i];
+    if (s < 0 || s >= p->n_positions) return PTY_ERR_POSITION;
+    const int y = pos[2 * s], x = pos[2 * s + 1];
+    if (y < 0 || x < 0 || y + p->window > p->obj_ny || x + p->window > p->obj_nx) return PTY_ERR_POSITION;
+  }
+  return PTY_OK;
+}
+
+template <typename T>
+T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? PTY_OK : PTY_ERR_CUDA; }
+
+template <typename K>
+int set_smem(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess
+             ? PTY_OK
+             : PTY_ERR_CUDA;
+}
+
+
+// Kernel classes reported by the launch profiler (pty_profile_begin / pty_profile_end).
+enum KernelId : int {
+  KID_TWIDDLES = 0, KID_TABLES, KID_PROBE_FFT, KID_OBJ_TO_SLICES, KID_OBJECT_WINDOWS, KID_FUSED,
+  KID_GRAD_WINDOWS, KID_TILE_LISTS, KID_SCATTER, KID_PROBE_PARTIAL, KID_SLICES_TO_OBJ, KID_PROBE_FINAL,
+  KID_FINALIZE, KID_FFT2, KID_COUNT
+};
+
+// Records an event on `st` before a launch of kernel class `id` while profiling is on
+// (id < 0 closes the last interval). No-op otherwise.
+void prof_mark(cudaStream_t st, int id);
+
+template <int W>
+int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const float2* probe,
+             const float* measured, double* loss_sse, float2* object_grad, float2* probe_grad,
+             float* pos_grad, float* patterns, void* ws, cudaStream_t st);
+
+template <int W>
+int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st);
+
+}  // namespace pty

@@ -1,0 +1,698 @@
+// Kernels of the far-field multislice loss-and-gradient path (pypty objective /
+// multislice_core restated for sm_103a). All kernels are templated on the window size W
+// and use WinFFT<W> for their transforms. Windows that live only inside one call are
+// stored in the "native" order of WinFFT (element i of thread t at offset i*T + t) so that
+// every load/store of a window is a fully coalesced 256-byte warp access.
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "window_fft.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pty {
+
+enum Algorithm : int { ALG_LSQ_SQRT = 0, ALG_ML = 1, ALG_LSQ = 2, ALG_LSQ_SQRT_2 = 3 };
+
+// Kernels that are not templates are declared static: each launch-path translation unit
+// (one per window size) carries its own copy.
+
+// ------------------------------------------------------------------ tables
+// mask        exclude_mask_ishift of create_spatial_frequencies (pypty/utils.py:176-194)
+// mask_sc     mask / W^2 (the ifft2 normalisation folded into the band limit; exact)
+// prop        Fresnel propagator * mask / W^2 (pypty/objective.py:343), natural (ky,kx)
+// prop_edge   prop^edge_mult / W^2 for the first slice step (multislice_core.py:73-74)
+// sx, sy      float32(-6.2831855 * fftfreq(W)) : sub-pixel shift exponents
+//             (pypty/objective.py:308-313), multiplied by mask where used
+struct TableArgs {
+  float* mask;
+  float* mask_sc;
+  float2* prop;
+  float2* prop_edge;
+  float* sx;
+  float* sy;
+  float px, py, cutoff, rolloff, distance, wavelength, edge_mult;
+  int use_edge;
+};
+
+// scipy.fft.fftfreq(n, d) as the reference evaluates it with a float32 pixel size d:
+// val = float32(1 / float32(n * d)); f_k = float64(k) * val; then cast to float32
+// (pypty/utils.py:174-176). Replicated bit for bit so that the band-limit mask, whose edge
+// is a <= comparison, selects exactly the same pixels.
+__device__ __forceinline__ float fftfreq_f32(int k, int n, float d) {
+  const int kk = (k < (n + 1) / 2) ? k : k - n;
+  const float nd = __fmul_rn((float)n, d);
+  const float val = __fdiv_rn(1.0f, nd);
+  return (float)((double)kk * (double)val);
+}
+
+template <int W>
+__global__ void tables_kernel(TableArgs a) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < W) {
+    // fftfreq(W) with d = 1 is exact in float64: k / W
+    const int kk = (idx < W / 2) ? idx : idx - W;
+    a.sx[idx] = (float)(-6.2831855 * ((double)kk / (double)W));
+    a.sy[idx] = a.sx[idx];
+  }
+  if (idx >= W * W) return;
+  const int ky = idx / W, kx = idx % W;
+  const float qx = fftfreq_f32(kx, W, a.px);
+  const float qy = fftfreq_f32(ky, W, a.py);
+  const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
+  const float max_x = fftfreq_f32((W - 1) / 2, W, a.px);
+  const float mc = __fmul_rn(max_x, a.cutoff);
+  const float r_max = __fmul_rn(mc, mc);
+  float mk = (q2 <= r_max) ? 1.0f : 0.0f;
+  if (a.rolloff != 0.0f) {
+    const float m0 = __fmul_rn(max_x, __fsub_rn(a.cutoff, a.rolloff));
+    const float r0 = __fmul_rn(m0, m0);
+    if (q2 > r0)
+      mk *= 0.5f * (1.0f + cosf(__fdiv_rn(__fmul_rn(3.141592654f, __fsub_rn(q2, r0)), __fsub_rn(r_max, r0))));
+  }
+  const float inv = 1.0f / (float)(W * W);
+  a.mask[idx] = mk;
+  a.mask_sc[idx] = mk * inv;
+  // exp(-i*pi*d*(lambda*q2)) * mask, evaluated as the reference does in complex64:
+  // the phase is (-pi_trunc * d) * (lambda * q2) rounded to float32 first
+  const float phase = __fmul_rn(__fmul_rn(-3.141592654f, a.distance), __fmul_rn(a.wavelength, q2));
+  float s, c;
+  sincosf(phase, &s, &c);
+  const float2 p = make_float2(c * mk, s * mk);
+  a.prop[idx] = make_float2(p.x * inv, p.y * inv);
+  if (a.use_edge) {
+    // principal-branch power, as numpy's complex ** float (|p|^e * exp(i e arg p))
+    float r = sqrtf(p.x * p.x + p.y * p.y);
+    float2 pe = make_float2(0.f, 0.f);
+    if (r > 0.f) {
+      float ang = atan2f(p.y, p.x) * a.edge_mult;
+      float re = powf(r, a.edge_mult);
+      float se, ce;
+      sincosf(ang, &se, &ce);
+      pe = make_float2(re * ce, re * se);
+    }
+    a.prop_edge[idx] = make_float2(pe.x * inv, pe.y * inv);
+  }
+}
+
+// ------------------------------------------------------------------ layout transposes
+// (Ny, Nx, Z*Mo) reference layout  <->  (Z*Mo, Ny, Nx) slice-major working layout
+static __global__ void obj_to_slices_kernel(const float2* __restrict__ src, float2* __restrict__ dst,
+                                     int nyx, int zm) {
+  const int yx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (yx >= nyx) return;
+  for (int k = 0; k < zm; ++k) dst[(size_t)k * nyx + yx] = src[(size_t)yx * zm + k];
+}
+
+static __global__ void slices_to_obj_kernel(const float2* __restrict__ src, float2* __restrict__ dst,
+                                     int nyx, int zm) {
+  const int yx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (yx >= nyx) return;
+  for (int k = 0; k < zm; ++k) dst[(size_t)yx * zm + k] = src[(size_t)k * nyx + yx];
+}
+
+// ------------------------------------------------------------------ shared-memory plan
+template <int W>
+struct Smem {
+  using G = Geo<W>;
+  static constexpr size_t bytes = sizeof(float2) * (G::XBUF + G::TW1 + G::TW2) + sizeof(double) * 64;
+};
+
+template <int W>
+__device__ __forceinline__ void carve(unsigned char* smem, float2*& xbuf, float2*& tw1,
+                                      float2*& tw2, double*& red) {
+  using G = Geo<W>;
+  xbuf = reinterpret_cast<float2*>(smem);
+  tw1 = xbuf + G::XBUF;
+  tw2 = tw1 + G::TW1;
+  red = reinterpret_cast<double*>(tw2 + G::TW2);
+}
+
+// sum of (a, b) over the block; result valid in thread 0
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = a;
+    red[32 + warp] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int w = 0; w < nw; ++w) {
+      sa += red[w];
+      sb += red[32 + w];
+    }
+    a = sa;
+    b = sb;
+  }
+}
+
+// ------------------------------------------------------------------ probe spectrum
+// probe (W, W, Mp) reference layout -> FFT per mode, native frequency layout [Mp]
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) probe_fft_kernel(const float2* __restrict__ probe, int Mp,
+                                                              const float2* __restrict__ g_tw,
+                                                              float2* __restrict__ probe_f) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  __syncthreads();
+  const int t = threadIdx.x, p = blockIdx.x;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * Mp + p];
+  WinFFT<W>::forward(v, xbuf, tw1, tw2);
+  float2* out = probe_f + (size_t)p * W * W;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) out[i * G::T + t] = v[i];
+}
+
+// ------------------------------------------------------------------ object windows
+// Gather the W x W window of every (position, slice, object mode) from the slice-major
+// object and band-limit it: O_b = IFFT(FFT(window) * mask)  (pypty/objective.py:436-441).
+struct WindowArgs {
+  const float2* obj;      // (Z*Mo, Ny, Nx)
+  const int* pos;         // (N, 2) int [y, x]
+  const int* seq;         // batch's sequence entries
+  const float* mask_sc;
+  const float2* tw;
+  float2* out;            // native real layout [Bb*Z*Mo]
+  int Ny, Nx, zm;
+};
+
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) object_windows_kernel(WindowArgs a) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, a.tw);
+  const int t = threadIdx.x;
+  const int win = blockIdx.x;             // (b * zm + k)
+  const int b = win / a.zm, k = win % a.zm;
+  const int gi = a.seq[b];
+  const int y0 = a.pos[2 * gi], x0 = a.pos[2 * gi + 1];
+  const float2* src = a.obj + (size_t)k * a.Ny * a.Nx + (size_t)(y0 + G::ry(t)) * a.Nx + x0;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = src[G::rx(t, i)];
+  __syncthreads();
+  WinFFT<W>::forward(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], a.mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
+  WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+  float2* dst = a.out + (size_t)win * W * W;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[i * G::T + t] = v[i];
+}
+
+// ------------------------------------------------------------------ fused multislice
+struct FusedArgs {
+  int Z, Mp, Mo, algorithm, step_obj, step_probe, step_pos, probe_shift, simulate, use_edge;
+  float loss_weight;
+  const float2* probe;      // (W, W, Mp) reference layout (used without probe shift)
+  const float2* probe_f;    // native frequency layout [Mp]
+  const float2* obl;        // band-limited object windows, native real [Bb*Z*Mo]
+  const float2* prop;       // natural (ky, kx), scaled by 1/W^2
+  const float2* prop_edge;
+  const float* mask;        // natural, unscaled
+  const float* sx;
+  const float* sy;
+  const float* corr;        // (N, 2) [dy, dx]
+  const int* seq;           // batch's sequence entries
+  const float* measured;    // (N, W, W) detector (fftshifted) order
+  const float2* tw;
+  float2* stack;            // conj input waves, native real [Bb*Z*Mp*Mo]
+  float2* gsum;             // probe-mode-summed object gradient, native real [Bb*Z*Mo]
+  float2* fprobe;           // FFT of the per-position probe gradient, native freq [Bb*Mp]
+  double* loss_part;        // [Bb][2]
+  double* pos_part;         // [Bb][Mp][2]
+  float* sim_out;           // [Bb][W][W] simulated mean intensity (detector order)
+};
+
+template <int W>
+__device__ __forceinline__ float2 shift_ramp(const FusedArgs& a, int ky, int kx, float mk,
+                                             float dy, float dx) {
+  // exp(smx*dx + smy*dy) * mask with smx = i * sx[kx] * mask (pypty/objective.py:473)
+  const float th = __fadd_rn(__fmul_rn(__fmul_rn(a.sx[kx], mk), dx),
+                             __fmul_rn(__fmul_rn(a.sy[ky], mk), dy));
+  float s, c;
+  sincosf(th, &s, &c);
+  return make_float2(c * mk, s * mk);
+}
+
+// One thread block per (position, probe mode, object mode); the Mp*Mo blocks of a position
+// form a thread-block cluster and exchange intensities / gradients through distributed
+// shared memory. Forward multislice (multislice_core.py:61-82), far field + loss
+// (objective.py:501-597), adjoint multislice (multislice_core.py:158-199), probe-shift
+// adjoint and position gradient (objective.py:641-658).
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) fused_multislice_kernel(FusedArgs a) {
+  using G = Geo<W>;
+  using F = WinFFT<W>;
+  constexpr int T = G::T;
+  constexpr size_t WW = (size_t)W * W;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int t = threadIdx.x;
+  const int nmodes = a.Mp * a.Mo;
+  const int crank = (int)cluster.block_rank();
+  const int p = crank % a.Mp, m = crank / a.Mp;
+  const int b = blockIdx.x / nmodes;
+  const int gi = a.seq[b];
+  const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
+  load_twiddles<W>(tw1, tw2, a.tw);
+  __syncthreads();
+
+  float2 v[32];
+  // ---- incoming (shifted) probe, objective.py:469-476
+  if (a.probe_shift) {
+    const float2* pf = a.probe_f + (size_t)p * WW;
+    const float inv = 1.0f / (float)WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int ky = G::fky(t, i), kx = G::fkx(t, i);
+      const float mk = a.mask[ky * W + kx];
+      v[i] = cscale(cmul(pf[i * T + t], shift_ramp<W>(a, ky, kx, mk, dy, dx)), inv);
+    }
+    F::inverse(v, xbuf, tw1, tw2);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
+  }
+
+  // ---- forward multislice
+  for (int z = 0; z < a.Z; ++z) {
+    if (a.step_obj && !a.simulate) {
+      float2* st = a.stack + ((((size_t)b * a.Z + z) * a.Mp + p) * a.Mo + m) * WW;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) st[i * T + t] = cconj(v[i]);
+    }
+    const float2* ob = a.obl + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], ob[i * T + t]);
+    if (z < a.Z - 1) {
+      F::forward(v, xbuf, tw1, tw2);
+      const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+      F::inverse(v, xbuf, tw1, tw2);
+    }
+  }
+
+  // ---- far field: Psi = FFT(exit) * mask; I = mean over modes |Psi|^2
+  F::forward(v, xbuf, tw1, tw2);
+  float* ibuf = reinterpret_cast<float*>(xbuf);
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    v[i] = cscale(v[i], a.mask[G::fky(t, i) * W + G::fkx(t, i)]);
+    ibuf[i * T + t] = cabs2(v[i]);
+  }
+  cluster.sync();
+  double lsum = 0.0, ssum = 0.0;
+  const float inv_modes = 1.0f / (float)nmodes;
+  const float* meas = a.measured + (size_t)gi * WW;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    float s = 0.0f;
+    for (int r = 0; r < nmodes; ++r) s += cluster.map_shared_rank(ibuf, r)[i * T + t];
+    const float I = (nmodes == 1) ? s : s * inv_modes;
+    const int ky = G::fky(t, i), kx = G::fkx(t, i);
+    const int dy_i = (ky + W / 2) & (W - 1), dx_i = (kx + W / 2) & (W - 1);
+    if (a.simulate) {
+      if (crank == 0) a.sim_out[(size_t)b * WW + dy_i * W + dx_i] = I;
+      continue;
+    }
+    const float Mv = meas[dy_i * W + dx_i];
+    float d, lp, sp;
+    if (a.algorithm == ALG_LSQ_SQRT) {           // objective.py:529-538
+      const float sI = sqrtf(I), sM = sqrtf(Mv);
+      const float df = sI - sM;
+      sp = (Mv - I) * (Mv - I);
+      lp = df * df;
+      d = df / (sI == 0.0f ? 1.0f : sI);
+    } else if (a.algorithm == ALG_ML) {          // objective.py:540-547
+      const float df = I - Mv;
+      sp = df * df;
+      lp = I - Mv * logf(I + (I == 0.0f ? 1.0f : 0.0f));
+      d = df / (I == 0.0f ? 1.0f : I);
+    } else if (a.algorithm == ALG_LSQ) {         // objective.py:548-552
+      const float df = I - Mv;
+      sp = df * df;
+      lp = sp;
+      d = 2.0f * df;
+    } else {                                     // lsq_sqrt_2, objective.py:553-559
+      const float df = Mv - I;
+      sp = df * df;
+      if (Mv > 0.5f) {
+        lp = 0.5f * (sp / Mv);
+        d = I / Mv - 1.0f;
+      } else {
+        lp = I;
+        d = 1.0f;
+      }
+    }
+    if (nmodes > 1) d = d / (float)nmodes;       // objective.py:586-587
+    lsum += (double)lp;
+    ssum += (double)sp;
+    // dL/dPsi = dLdI * Psi * (w * W^2); the W^2 cancels the 1/W^2 of ifft2 (exact)
+    v[i] = cscale(cscale(v[i], d), a.loss_weight);
+  }
+  cluster.sync();   // every block is done reading this block's intensities
+  if (a.simulate) return;
+  block_sum2(lsum, ssum, red);
+  if (t == 0 && crank == 0) {
+    a.loss_part[2 * b] = lsum;
+    a.loss_part[2 * b + 1] = ssum;
+  }
+  F::inverse(v, xbuf, tw1, tw2);   // g = dL/d(exit wave), objective.py:597
+
+  // ---- adjoint multislice, multislice_core.py:158-183
+  for (int z = a.Z - 1; z >= 0; --z) {
+    if (a.step_obj) {
+      const float2* st = a.stack + ((((size_t)b * a.Z + z) * a.Mp + p) * a.Mo + m) * WW;
+      float2* gs = a.gsum + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
+      if (a.Mp == 1) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) gs[i * T + t] = cmul(st[i * T + t], v[i]);
+      } else {
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) xbuf[i * T + t] = cmul(st[i * T + t], v[i]);
+        cluster.sync();
+        // this block sums elements i = p, p + Mp, ... over the probe modes of object mode m
+        for (int i = p; i < 32; i += a.Mp) {
+          float2 s = make_float2(0.f, 0.f);
+          for (int pp = 0; pp < a.Mp; ++pp) s = cadd(s, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[i * T + t]);
+          gs[i * T + t] = s;
+        }
+        cluster.sync();
+      }
+    }
+    const float2* ob = a.obl + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], ob[i * T + t]);
+    if (z > 0) {
+      F::forward(v, xbuf, tw1, tw2);
+      const float2* pr = (z == 1 && a.use_edge) ? a.prop_edge : a.prop;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+      F::inverse(v, xbuf, tw1, tw2);
+    }
+  }
+
+  // ---- probe gradient (sum over object modes), shift adjoint, position gradient
+  if (!(a.step_probe || a.step_pos)) return;
+  if (a.Mo > 1) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 32; ++i) xbuf[i * T + t] = v[i];
+    cluster.sync();
+    if (m == 0) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int mm = 0; mm < a.Mo; ++mm) s = cadd(s, cluster.map_shared_rank(xbuf, p + mm * a.Mp)[i * T + t]);
+        v[i] = s;
+      }
+    }
+    cluster.sync();
+    if (m != 0) return;
+  }
+  F::forward(v, xbuf, tw1, tw2);
+  const float2* pf = a.probe_f + (size_t)p * WW;
+  double gy = 0.0, gx = 0.0;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int ky = G::fky(t, i), kx = G::fkx(t, i);
+    if (a.probe_shift) {
+      const float mk = a.mask[ky * W + kx];
+      v[i] = cmulc(v[i], shift_ramp<W>(a, ky, kx, mk, dy, dx));
+      if (a.step_pos) {
+        // Re(smyx * conj(Pf) * F) with smyx = i*s*mask  ->  -(s*mask) * Im(conj(Pf) * F)
+        const float im = cmulc(v[i], pf[i * T + t]).y;
+        gy += (double)(-(a.sy[ky] * mk) * im);
+        gx += (double)(-(a.sx[kx] * mk) * im);
+      }
+    }
+  }
+  if (a.step_probe) {
+    float2* fp = a.fprobe + ((size_t)b * a.Mp + p) * WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) fp[i * T + t] = v[i];
+  }
+  if (a.step_pos) {
+    block_sum2(gy, gx, red);
+    if (t == 0) {
+      a.pos_part[(b * a.Mp + p) * 2] = gy;
+      a.pos_part[(b * a.Mp + p) * 2 + 1] = gx;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ gradient windows
+// Band-limit the probe-mode-summed gradient window: IFFT(FFT(G) * mask)
+// (multislice_core.py:189-191); native real layout in, natural (y, x) layout out, in place.
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) grad_windows_kernel(float2* buf, const float* __restrict__ mask_sc,
+                                                                 const float2* __restrict__ g_tw) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  const int t = threadIdx.x;
+  float2* win = buf + (size_t)blockIdx.x * W * W;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = win[i * G::T + t];
+  __syncthreads();
+  WinFFT<W>::forward(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
+  WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+  // all reads of this window finished before the first barrier of forward()
+#pragma unroll
+  for (int i = 0; i < 32; ++i) win[G::ry(t) * W + G::rx(t, i)] = v[i];
+}
+
+// ------------------------------------------------------------------ deterministic scatter
+// Object-gradient accumulation without atomics: the object plane is cut into TS x TS tiles;
+// for every tile the positions whose window overlaps it are listed in batch order, and the
+// block owning the tile adds their contributions pixel by pixel in that order
+// (the fixed order of np.add.at in multislice_core.py:226-227).
+constexpr int TS = 32;
+
+static __global__ void tile_lists_kernel(const int* __restrict__ pos, const int* __restrict__ seq, int Bb,
+                                  int W, int ntx, int* __restrict__ lists, int* __restrict__ counts) {
+  __shared__ int warp_tot[32];
+  __shared__ int base_s;
+  const int tile = blockIdx.x;
+  const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) base_s = 0;
+  __syncthreads();
+  int* my = lists + (size_t)tile * Bb;
+  for (int b0 = 0; b0 < Bb; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    bool hit = false;
+    if (b < Bb) {
+      const int gi = seq[b];
+      const int y = pos[2 * gi], x = pos[2 * gi + 1];
+      hit = (y < ty0 + TS) && (y + W > ty0) && (x < tx0 + TS) && (x + W > tx0);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      if (w < warp) before += warp_tot[w];
+      total += warp_tot[w];
+    }
+    const int base = base_s;
+    if (hit) my[base + before + __popc(bal & ((1u << lane) - 1u))] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) base_s = base + total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) counts[tile] = base_s;
+}
+
+// blockDim = (32, 8); grid = (ntiles, Z*Mo)
+static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const int* __restrict__ pos,
+                                     const int* __restrict__ seq, const int* __restrict__ lists,
+                                     const int* __restrict__ counts, float2* __restrict__ grad,
+                                     int Bb, int W, int Ny, int Nx, int ntx, int zm, int accumulate) {
+  __shared__ int s_b[256], s_y[256], s_x[256];
+  const int tile = blockIdx.x, k = blockIdx.y;
+  const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
+  const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+  const int x = tx0 + lx;
+  float2 acc[4];
+  float2* plane = grad + (size_t)k * Ny * Nx;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int y = ty0 + ly + 8 * r;
+    acc[r] = (accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
+  }
+  const int n = counts[tile];
+  const int* lst = lists + (size_t)tile * Bb;
+  const size_t WW = (size_t)W * W;
+  for (int j0 = 0; j0 < n; j0 += 256) {
+    __syncthreads();
+    if (j0 + tid < n) {
+      const int b = lst[j0 + tid];
+      const int gi = seq[b];
+      s_b[tid] = b;
+      s_y[tid] = pos[2 * gi];
+      s_x[tid] = pos[2 * gi + 1];
+    }
+    __syncthreads();
+    const int jn = min(256, n - j0);
+    for (int j = 0; j < jn; ++j) {
+      const int b = s_b[j];
+      const int ox = x - s_x[j];
+      if ((unsigned)ox >= (unsigned)W) continue;
+      const float2* src = gw + ((size_t)b * zm + k) * WW + ox;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int oy = ty0 + ly + 8 * r - s_y[j];
+        if ((unsigned)oy < (unsigned)W) acc[r] = cadd(acc[r], src[(size_t)oy * W]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int y = ty0 + ly + 8 * r;
+    if (y < Ny && x < Nx) plane[(size_t)y * Nx + x] = acc[r];
+  }
+}
+
+// ------------------------------------------------------------------ probe gradient
+// partial[c][p][e] (+)= sum over positions b of chunk c of fprobe[b][p][e], in order
+static __global__ void probe_partial_kernel(const float2* __restrict__ fprobe, float2* __restrict__ partial,
+                                     int Bb, int Mp, int WW, int chunk, int accumulate) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y, c = blockIdx.z;
+  if (e >= WW) return;
+  float2 s = make_float2(0.f, 0.f);
+  const int b1 = min(Bb, (c + 1) * chunk);
+  for (int b = c * chunk; b < b1; ++b) s = cadd(s, fprobe[((size_t)b * Mp + p) * WW + e]);
+  float2* dst = partial + ((size_t)c * Mp + p) * WW + e;
+  *dst = accumulate ? cadd(*dst, s) : s;
+}
+
+// probe_grad = IFFT(mask * sum_c partial[c]) (objective.py:703 and :927-933), written in the
+// reference layout (W, W, Mp)
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) probe_final_kernel(const float2* __restrict__ partial, int nchunk,
+                                                                int Mp, const float* __restrict__ mask_sc,
+                                                                const float2* __restrict__ g_tw,
+                                                                float2* __restrict__ probe_grad) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  __syncthreads();
+  const int t = threadIdx.x, p = blockIdx.x;
+  const size_t WW = (size_t)W * W;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    float2 s = make_float2(0.f, 0.f);
+    for (int c = 0; c < nchunk; ++c) s = cadd(s, partial[((size_t)c * Mp + p) * WW + i * G::T + t]);
+    v[i] = cscale(s, mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
+  }
+  WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) probe_grad[(size_t)(G::ry(t) * W + G::rx(t, i)) * Mp + p] = v[i];
+}
+
+// ------------------------------------------------------------------ scalars
+// loss = w * sum(loss_part), sse = sum(sse_part) in FP64 (fixed order); the position
+// gradient pos_grad[seq[b]] = -2/W^2 * sum_p pos_part[b][p]  (objective.py:651-656)
+static __global__ void finalize_scalars_kernel(const double* __restrict__ loss_part,
+                                        const double* __restrict__ pos_part, const int* __restrict__ seq,
+                                        int nseq, int Mp, int W, double loss_weight, int step_pos,
+                                        double* __restrict__ loss_sse, float* __restrict__ pos_grad) {
+  __shared__ double red[64];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nseq; i += blockDim.x) {
+    a += loss_part[2 * i];
+    b += loss_part[2 * i + 1];
+  }
+  block_sum2(a, b, red);
+  if (threadIdx.x == 0) {
+    loss_sse[0] = a * loss_weight;
+    loss_sse[1] = b;
+  }
+  if (!step_pos) return;
+  const double sh = -2.0 / ((double)W * (double)W);
+  for (int i = threadIdx.x; i < nseq; i += blockDim.x) {
+    double gy = 0.0, gx = 0.0;
+    for (int p = 0; p < Mp; ++p) {
+      gy += pos_part[((size_t)i * Mp + p) * 2];
+      gx += pos_part[((size_t)i * Mp + p) * 2 + 1];
+    }
+    pos_grad[2 * seq[i]] = (float)(sh * gy);
+    pos_grad[2 * seq[i] + 1] = (float)(sh * gx);
+  }
+}
+
+// ------------------------------------------------------------------ plain batched FFT
+// fft2 / ifft2 / shift_fft2 / ifft2_ishift of contiguous W x W windows (pypty/fft.py:91-178)
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) fft2_batch_kernel(const float2* __restrict__ in, float2* __restrict__ out,
+                                                               int inverse, int shift,
+                                                               const float2* __restrict__ g_tw) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  __syncthreads();
+  const int t = threadIdx.x;
+  const size_t WW = (size_t)W * W;
+  const float2* src = in + (size_t)blockIdx.x * WW;
+  float2* dst = out + (size_t)blockIdx.x * WW;
+  float2 v[32];
+  const int h = shift ? W / 2 : 0;
+  if (!inverse) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = src[G::ry(t) * W + G::rx(t, i)];
+    WinFFT<W>::forward(v, xbuf, tw1, tw2);
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      dst[((G::fky(t, i) + h) & (W - 1)) * W + ((G::fkx(t, i) + h) & (W - 1))] = v[i];
+  } else {
+    const float inv = 1.0f / (float)WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      v[i] = cscale(src[((G::fky(t, i) + h) & (W - 1)) * W + ((G::fkx(t, i) + h) & (W - 1))], inv);
+    WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) dst[G::ry(t) * W + G::rx(t, i)] = v[i];
+  }
+}
+
+}  // namespace pty

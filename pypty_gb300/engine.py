@@ -1,0 +1,198 @@
+"""Device-resident driver of the C ABI: workspace, pinned staging and torch tensors.
+
+PyTorch supplies device memory, streams and pinned host memory; every arithmetic step of
+the path runs in the library's own CUDA kernels (``pypty_gb300/csrc``).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+@dataclass
+class Geometry:
+    """Scan geometry in host memory: the reference's integer positions, sub-pixel
+    corrections and processing sequence (``pypty/utils.py:1742-1746``)."""
+    positions: np.ndarray       # (N, 2) int32 [y, x]
+    pos_correction: np.ndarray  # (N, 2) float32 [dy, dx]
+    sequence: np.ndarray        # (n,) int32
+
+    @staticmethod
+    def make(positions, pos_correction, sequence=None) -> "Geometry":
+        pos = np.ascontiguousarray(np.asarray(positions), dtype=np.int32)
+        corr = np.ascontiguousarray(np.asarray(pos_correction), dtype=np.float32)
+        if sequence is None:
+            sequence = np.arange(pos.shape[0])
+        seq = np.ascontiguousarray(np.asarray(sequence), dtype=np.int32)
+        return Geometry(pos, corr, seq)
+
+    def probe_shift(self, step_pos: bool) -> bool:
+        """``probe_shift_flag`` of ``pypty/objective.py:347``."""
+        return bool(np.sum(self.pos_correction.astype(np.float64) ** 2) != 0.0) or bool(step_pos)
+
+
+def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, wavelength,
+                 pixel_size_x, pixel_size_y, slice_distance, edge_mult=1.0,
+                 damping_cutoff=2 / 3, smooth_rolloff=0.0, loss_weight=1.0, compute_batch=None,
+                 step_obj=True, step_probe=True, step_pos=False, probe_shift=None) -> _lib.Problem:
+    ny, nx, nz, mo = obj_shape
+    if isinstance(algorithm, str):
+        if algorithm not in _lib.ALGORITHMS:
+            raise NotImplementedError("loss %r is not implemented on the GPU path" % algorithm)
+        algorithm = _lib.ALGORITHMS[algorithm]
+    if damping_cutoff is None:
+        damping_cutoff = 2.0
+    if damping_cutoff < 0:
+        damping_cutoff = 2 / 3
+    n = geometry.positions.shape[0]
+    ns = geometry.sequence.shape[0]
+    if probe_shift is None:
+        probe_shift = geometry.probe_shift(step_pos)
+    p = _lib.Problem()
+    p.window, p.obj_ny, p.obj_nx, p.n_slices, p.n_obj_modes = W, ny, nx, nz, mo
+    p.n_probe_modes, p.n_positions, p.n_sequence = n_probe_modes, n, ns
+    p.compute_batch = int(compute_batch if compute_batch else ns)
+    p.algorithm = int(algorithm)
+    p.step_obj, p.step_probe, p.step_pos = int(bool(step_obj)), int(bool(step_probe)), int(bool(step_pos))
+    p.probe_shift = int(bool(probe_shift))
+    p.wavelength, p.pixel_size_x, p.pixel_size_y = wavelength, pixel_size_x, pixel_size_y
+    p.slice_distance, p.edge_mult = slice_distance, edge_mult
+    p.damping_cutoff, p.smooth_rolloff, p.loss_weight = damping_cutoff, smooth_rolloff, loss_weight
+    return p
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class Engine:
+    """Workspace and staging buffers for repeated calls on one CUDA device."""
+
+    def __init__(self, device=None):
+        _lib.lib()
+        self.device = torch.device(device if device is not None else "cuda")
+        self._ws = None
+        self._stage = None
+        self._stage_event = None
+
+    # ---------------------------------------------------------------- buffers
+    def workspace(self, nbytes: int) -> torch.Tensor:
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = None
+            self._ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def _staging(self, geo: Geometry):
+        """Page-locked copies of the geometry (the C ABI uploads them asynchronously)."""
+        need = geo.positions.nbytes + geo.pos_correction.nbytes + geo.sequence.nbytes + 64
+        if self._stage_event is not None:
+            self._stage_event.synchronize()     # the previous upload has left the buffer
+        if self._stage is None or self._stage.numel() < need:
+            self._stage = torch.empty(need, dtype=torch.uint8, pin_memory=True)
+        buf = self._stage.numpy()
+        o = 0
+        ptrs = []
+        for arr in (geo.positions, geo.pos_correction, geo.sequence):
+            n = arr.nbytes
+            buf[o:o + n] = arr.view(np.uint8).reshape(-1)
+            ptrs.append(self._stage.data_ptr() + o)
+            o += (n + 15) // 16 * 16
+        return ptrs
+
+    def _mark_staging(self, stream):
+        if self._stage_event is None:
+            self._stage_event = torch.cuda.Event()
+        self._stage_event.record(stream)
+
+    # ---------------------------------------------------------------- calls
+    def loss_and_direction(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor,
+                           geo: Geometry, measured: torch.Tensor, out=None, stream=None):
+        """Run the fused path. obj (Ny,Nx,Z,Mo) complex64, probe (W,W,Mp) complex64 and
+        measured (N,W,W) float32 on the device. Returns (loss_sse float64[2], object_grad,
+        probe_grad, pos_grad) device tensors (loss_sse = [loss * loss_weight, sse])."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        self._check_inputs(problem, obj, probe, measured)
+        if out is None:
+            out = (torch.empty(2, dtype=torch.float64, device=self.device),
+                   torch.empty_like(obj), torch.empty_like(probe),
+                   torch.empty((problem.n_positions, 2), dtype=torch.float32, device=self.device))
+        loss_sse, og, pg, posg = out
+        ws = self.workspace(_lib.workspace_bytes(problem))
+        pp, pc, ps = self._staging(geo)
+        st = _lib.lib().pty_loss_and_direction(
+            ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
+            _ptr(loss_sse), _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)
+        self._mark_staging(stream)
+        _lib.check(st, "pty_loss_and_direction")
+        return loss_sse, og, pg, posg
+
+    def simulate(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
+                 out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """Mean-over-modes far-field patterns (n_sequence, W, W) float32, detector order."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        self._check_inputs(problem, obj, probe, None)
+        W = problem.window
+        if out is None:
+            out = torch.empty((problem.n_sequence, W, W), dtype=torch.float32, device=self.device)
+        ws = self.workspace(_lib.workspace_bytes(problem))
+        pp, pc, ps = self._staging(geo)
+        st = _lib.lib().pty_simulate_patterns(ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps,
+                                              _ptr(out), _ptr(ws), ws.numel(), stream.cuda_stream)
+        self._mark_staging(stream)
+        _lib.check(st, "pty_simulate_patterns")
+        return out
+
+    def fft2(self, x: torch.Tensor, inverse: bool = False, shift: bool = False, out=None, stream=None):
+        """Batched 2D FFT over the last two axes of a (..., W, W) complex64 device tensor."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        if x.dtype != torch.complex64 or not x.is_cuda:
+            raise TypeError("fft2 needs a complex64 CUDA tensor")
+        W = x.shape[-1]
+        if x.shape[-2] != W:
+            raise ValueError("fft2 needs square windows")
+        x = x.contiguous()
+        out = torch.empty_like(x) if out is None else out
+        n = ctypes.c_size_t(0)
+        _lib.check(_lib.lib().pty_fft2_workspace_bytes(W, ctypes.byref(n)), "pty_fft2_workspace_bytes")
+        ws = self.workspace(int(n.value))
+        batch = x.numel() // (W * W)
+        st = _lib.lib().pty_fft2(_ptr(x), _ptr(out), batch, W, int(inverse), int(shift), _ptr(ws),
+                                 ws.numel(), stream.cuda_stream)
+        _lib.check(st, "pty_fft2")
+        return out
+
+    @staticmethod
+    def _check_inputs(problem, obj, probe, measured):
+        W = problem.window
+        want_obj = (problem.obj_ny, problem.obj_nx, problem.n_slices, problem.n_obj_modes)
+        if tuple(obj.shape) != want_obj or obj.dtype != torch.complex64 or not obj.is_contiguous():
+            raise ValueError("object must be a contiguous complex64 tensor of shape %s" % (want_obj,))
+        if tuple(probe.shape) != (W, W, problem.n_probe_modes) or probe.dtype != torch.complex64 \
+                or not probe.is_contiguous():
+            raise ValueError("probe must be a contiguous complex64 tensor of shape %s" %
+                             ((W, W, problem.n_probe_modes),))
+        if measured is not None and (tuple(measured.shape) != (problem.n_positions, W, W) or
+                                     measured.dtype != torch.float32 or not measured.is_contiguous()):
+            raise ValueError("measured must be a contiguous float32 tensor of shape %s" %
+                             ((problem.n_positions, W, W),))
+        for t in (obj, probe) + ((measured,) if measured is not None else ()):
+            if not t.is_cuda:
+                raise ValueError("inputs must be CUDA tensors")
+
+
+_ENGINES = {}
+
+
+def default_engine(device=None) -> Engine:
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    eng = _ENGINES.get(dev)
+    if eng is None:
+        eng = _ENGINES[dev] = Engine(dev)
+    return eng

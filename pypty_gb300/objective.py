@@ -1,0 +1,146 @@
+"""Drop-in ``loss_and_direction`` with the reference's signature, on the GPU path.
+
+``loss_and_direction`` takes exactly the arguments of ``pypty.objective.loss_and_direction``
+(``pypty/objective.py:47``), in the same order, and returns the same 10-tuple
+(``pypty/objective.py:967``). Installing it in place of the reference function
+(``pypty_gb300.shim.install``) lets ``pypty.iterative.run`` drive the GB300 kernels.
+
+Supported flag set: far-field propagation, ``propmethod="multislice"``, one slice distance,
+no tilts (``tilt_mode`` 0, zero tilt arrays), no phase plates, aberration arrays, probe
+markers, beam-current fluctuations, static background, data padding / binning / shifting /
+upsampling, compressed detectors or regularisers, algorithms ``lsq_sqrt``, ``ml``, ``lsq``,
+``lsq_sqrt_2``. Any other combination raises ``NotImplementedError`` naming the flag: the
+product path never falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import Geometry, default_engine, make_problem
+
+N_CONSTRAINTS = 14   # entries of constraint_contributions (pypty/objective.py:768-921)
+
+
+def _unsupported(cond, what):
+    if cond:
+        raise NotImplementedError("pypty_gb300 GPU path does not implement %s" % what)
+
+
+def _is_zero(x):
+    if x is None:
+        return True
+    try:
+        return float(np.sum(np.abs(np.asarray(x)))) == 0.0
+    except (TypeError, ValueError):
+        return False
+
+
+def _to_numpy(a):
+    if isinstance(a, torch.Tensor):
+        return a.detach().cpu().numpy()
+    if hasattr(a, "get"):          # a CuPy array
+        return a.get()
+    return np.asarray(a)
+
+
+def _device_tensor(a, dtype, device):
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(_to_numpy(a))).to(device=device, dtype=dtype)
+
+
+def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
+                       this_tilts_correction, this_distances, edge_slice_thickness_multiplier,
+                       measured_array, algorithm_type, this_wavelength, this_step_probe, this_step_obj,
+                       this_step_pos_correction, this_step_tilts, masks, pixel_size_x_A, pixel_size_y_A,
+                       recon_type, Cs, defocus_array, alpha_near_field, damping_cutoff_multislice,
+                       smooth_rolloff, propmethod, this_chopped_sequence, load_one_by_one, data_multiplier,
+                       data_pad, phase_plate_in_h5, this_loss_weight, data_bin, data_shift_vector,
+                       upsample_pattern, static_background, this_step_static_background, tilt_mode,
+                       aberration_marker, probe_marker, aberrations_array, compute_batch, phase_only_obj,
+                       beam_current, this_beam_current_step, this_step_aberrations_array, default_float,
+                       default_complex, xp, is_first_epoch, scan_size, scan_step_A,
+                       fast_axis_reg_weight_positions, slow_axis_reg_weight_positions,
+                       slow_axis_reg_weight_tilts, current_deformation_reg_weight_positions,
+                       current_deformation_reg_weight_tilts, fast_axis_reg_weight_tilts, aperture_mask,
+                       probe_reg_weight, current_window_weight, current_window, phase_norm_weight,
+                       abs_norm_weight, atv_weight, atv_q, atv_p, mixed_variance_weight, mixed_variance_sigma,
+                       wedge_mu, beta_wedge, probe_mod_reg_weight, probe_mod_tol, smart_memory, print_flag,
+                       data_simulation_flag, data_simulation_exitwave, use_padded_intensity):
+    """GPU restatement of ``pypty/objective.py:47-967`` (see the module docstring for the
+    supported flag set). Returns (loss, sse, object_grad, probe_grad, pos_grad, tilts_grad,
+    static_background_grad, aberrations_array_grad, beam_current_grad,
+    constraint_contributions) with the reference's shapes. Arrays come back as NumPy arrays
+    when the object was given as a NumPy array, else as CUDA tensors.
+    """
+    _unsupported(recon_type != "far_field", "recon_type=%r" % (recon_type,))
+    _unsupported(propmethod != "multislice", "propmethod=%r" % (propmethod,))
+    _unsupported(algorithm_type not in _lib.ALGORITHMS, "algorithm_type=%r" % (algorithm_type,))
+    _unsupported(bool(this_step_tilts) or tilt_mode not in (0, None), "beam tilts (tilt_mode/this_step_tilts)")
+    _unsupported(not _is_zero(this_tilt_array) or not _is_zero(this_tilts_correction), "nonzero beam tilts")
+    _unsupported(np.asarray(_to_numpy(this_distances)).reshape(-1).shape[0] != 1, "per-slice distances")
+    _unsupported(phase_plate_in_h5 is not None, "phase plates")
+    _unsupported(aberration_marker is not None or bool(this_step_aberrations_array), "aberration arrays")
+    _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
+    _unsupported(beam_current is not None or bool(this_beam_current_step), "beam-current fluctuations")
+    _unsupported(static_background is not None and not _is_zero(static_background), "static background")
+    _unsupported(bool(this_step_static_background), "static-background refinement")
+    _unsupported(int(data_pad) != 0 or int(data_bin) != 1 or int(upsample_pattern) != 1,
+                 "data padding / binning / upsampling")
+    _unsupported(not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0,
+                 "data shift vectors or multipliers")
+    _unsupported(bool(data_simulation_flag), "data simulation output files")
+    for name, w in [("fast_axis_reg_weight_positions", fast_axis_reg_weight_positions),
+                    ("slow_axis_reg_weight_positions", slow_axis_reg_weight_positions),
+                    ("current_deformation_reg_weight_positions", current_deformation_reg_weight_positions)]:
+        _unsupported(bool(this_step_pos_correction) and w != 0, name)
+    for name, w in [("phase_norm_weight", phase_norm_weight), ("abs_norm_weight", abs_norm_weight),
+                    ("atv_weight", atv_weight), ("wedge_mu", wedge_mu)]:
+        _unsupported(w != 0, name)
+    for name, w in [("probe_reg_weight", probe_reg_weight), ("current_window_weight", current_window_weight),
+                    ("probe_mod_reg_weight", probe_mod_reg_weight)]:
+        _unsupported(bool(this_step_probe) and w != 0, name)
+    obj_is_numpy = not isinstance(this_obj, torch.Tensor)
+    obj_shape = tuple(this_obj.shape)
+    _unsupported(len(obj_shape) != 4, "objects that are not 4D (y, x, slice, mode)")
+    _unsupported(len(tuple(full_probe.shape)) != 3, "probes that are not 3D (y, x, mode)")
+    _unsupported(mixed_variance_weight != 0 and obj_shape[3] > 1, "mixed_variance_weight")
+    W = int(full_probe.shape[0])
+    Mp = int(full_probe.shape[2])
+    in_dtype = this_obj.dtype
+
+    geo = Geometry.make(_to_numpy(this_pos_array), _to_numpy(this_pos_correction),
+                        _to_numpy(this_chopped_sequence))
+    eng = default_engine()
+    dev = eng.device
+    obj_d = _device_tensor(this_obj, torch.complex64, dev)
+    probe_d = _device_tensor(full_probe, torch.complex64, dev)
+    meas_d = _device_tensor(measured_array, torch.float32, dev)
+    problem = make_problem(
+        W, obj_shape, Mp, geo, algorithm=algorithm_type, wavelength=float(this_wavelength),
+        pixel_size_x=float(pixel_size_x_A), pixel_size_y=float(pixel_size_y_A),
+        slice_distance=float(np.asarray(_to_numpy(this_distances)).reshape(-1)[0]),
+        edge_mult=float(edge_slice_thickness_multiplier),
+        damping_cutoff=None if damping_cutoff_multislice is None else float(damping_cutoff_multislice),
+        smooth_rolloff=float(smooth_rolloff), loss_weight=float(this_loss_weight),
+        compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
+        step_pos=bool(this_step_pos_correction))
+    loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
+    ls = loss_sse.cpu().numpy()
+    loss, sse = float(ls[0]), float(ls[1])
+    if loss != loss:
+        raise ValueError('A very specific bad thing. Loss is Nan.')   # objective.py:925-926
+    if not this_step_probe:
+        pg = torch.zeros((1,) + tuple(pg.shape), dtype=pg.dtype, device=pg.device)  # objective.py:747-751
+    tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))
+    aberr_grad = 0 if aberrations_array is None else np.zeros_like(_to_numpy(aberrations_array))
+    constraints = np.zeros(N_CONSTRAINTS)
+    if obj_is_numpy:
+        og_out = og.cpu().numpy().astype(in_dtype, copy=False)
+        pg_out = pg.cpu().numpy().astype(np.asarray(full_probe).dtype, copy=False)
+        posg_out = posg.cpu().numpy().astype(np.asarray(_to_numpy(this_pos_correction)).dtype, copy=False)
+    else:
+        og_out, pg_out, posg_out = og, pg, posg
+    return loss, sse, og_out, pg_out, posg_out, tilts_grad, 0, aberr_grad, 0, constraints

@@ -1,0 +1,155 @@
+"""GPU path against the reference (golden vectors) and the NumPy oracle.
+
+Tolerances (complex64 path): loss relative error <= 1e-5, gradient relative L2 <= 1e-4
+(object, probe and position gradients), FFTs relative L2 <= 2e-6 against float64 NumPy.
+"""
+import numpy as np
+import pytest
+
+from golden_io import load_case, loss_case_names, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+LOSS_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import torch
+    from pypty_gb300.engine import Engine
+    return Engine(torch.device("cuda", 0))
+
+
+@pytest.mark.parametrize("W", [64, 128])
+@pytest.mark.parametrize("inverse,shift", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_window_fft_matches_numpy(engine, W, inverse, shift):
+    import torch
+    rng = np.random.default_rng(W + 2 * inverse + shift)
+    x = (rng.normal(size=(5, W, W)) + 1j * rng.normal(size=(5, W, W))).astype(np.complex64)
+    out = engine.fft2(torch.from_numpy(x).cuda(), inverse=bool(inverse), shift=bool(shift)).cpu().numpy()
+    xd = x.astype(np.complex128)
+    if not inverse:
+        ref = np.fft.fft2(xd, axes=(1, 2))
+        ref = np.fft.fftshift(ref, axes=(1, 2)) if shift else ref
+    else:
+        ref = np.fft.ifft2(np.fft.ifftshift(xd, axes=(1, 2)) if shift else xd, axes=(1, 2))
+    assert rel_l2(out, ref) <= 2e-6
+
+
+def test_fft_mirror_over_reference_axes():
+    from pypty_gb300 import fft as gfft
+    rng = np.random.default_rng(3)
+    x = (rng.normal(size=(3, 64, 64, 2, 1)) + 1j * rng.normal(size=(3, 64, 64, 2, 1))).astype(np.complex64)
+    assert rel_l2(gfft.fft2(x, axes=(1, 2)), np.fft.fft2(x.astype(np.complex128), axes=(1, 2))) <= 2e-6
+    y = np.fft.fftshift(np.fft.fft2(x.astype(np.complex128), axes=(1, 2)), axes=(1, 2))
+    assert rel_l2(gfft.shift_fft2(x, axes=(1, 2)), y) <= 2e-6
+    assert rel_l2(gfft.ifft2_ishift(y.astype(np.complex64), axes=(1, 2)), x) <= 2e-6
+
+
+@pytest.mark.parametrize("name", loss_case_names())
+def test_loss_and_direction_matches_reference(engine, name):
+    from gpu_helpers import run_gpu
+    c = load_case(name)
+    loss, sse, og, pg, posg = run_gpu(c, engine=engine)
+    assert abs(loss - float(c["ref_loss"])) <= LOSS_TOL * abs(float(c["ref_loss"]))
+    assert abs(sse - float(c["ref_sse"])) <= LOSS_TOL * abs(float(c["ref_sse"]))
+    assert rel_l2(og, c["ref_object_grad"]) <= GRAD_TOL
+    if c["step_probe"]:
+        assert rel_l2(pg, np.asarray(c["ref_probe_grad"]).reshape(pg.shape)) <= GRAD_TOL
+    if c["step_pos"]:
+        assert rel_l2(posg, c["ref_pos_grad"]) <= GRAD_TOL
+
+
+def test_batch_size_does_not_change_result(engine):
+    from gpu_helpers import run_gpu
+    c = load_case("multislice_ml_c64")
+    a = run_gpu(c, compute_batch=36, engine=engine)
+    b = run_gpu(c, compute_batch=5, engine=engine)
+    assert abs(a[0] - b[0]) <= 1e-9 * abs(a[0])
+    assert rel_l2(b[2], a[2]) <= 1e-6 and rel_l2(b[3], a[3]) <= 1e-6 and rel_l2(b[4], a[4]) <= 1e-6
+
+
+def test_results_are_bitwise_deterministic(engine):
+    from gpu_helpers import run_gpu
+    c = load_case("w128_modes_c64")
+    a = run_gpu(c, engine=engine)
+    b = run_gpu(c, engine=engine)
+    assert a[0] == b[0] and a[1] == b[1]
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
+
+
+def test_drop_in_objective_matches_reference():
+    """The reference-signature mirror, called positionally like pypty/iterative.py:524."""
+    from pypty_gb300 import objective
+    c = load_case("modes_lsq_c64")
+    f = np.float32
+    tilts = np.zeros((1, 6), f)
+    args = [c["obj"], c["probe"], c["positions"], c["pos_correction"], tilts, np.zeros_like(tilts),
+            np.array([c["distance"]], f), c["edge_mult"], c["measured"], c["algorithm"], f(c["wavelength"]),
+            c["step_probe"], c["step_obj"], c["step_pos"], 0, None, f(c["px"]), f(c["px"]), "far_field", 0,
+            np.array([0.0]), 0, f(c["cutoff"]), f(c["rolloff"]), "multislice", c["sequence"], False, 1, 0,
+            None, c["loss_weight"], 1, [0, 0], 1, None, 0, 0, None, None, None, c["batch"], False, None, 0, 0,
+            f, np.complex64, np, True, None, 1, 0, 0, 0, 0, 0, 0, None, 0, 0, None, 0, 0, 0, 1, 2, 0, 0.5,
+            0, 0, 0, 0.05, False, 0, False, False, True]
+    res = objective.loss_and_direction(*args)
+    assert len(res) == 10
+    assert abs(res[0] - float(c["ref_loss"])) <= LOSS_TOL * abs(float(c["ref_loss"]))
+    assert rel_l2(res[2], c["ref_object_grad"]) <= GRAD_TOL
+    assert rel_l2(res[3], c["ref_probe_grad"]) <= GRAD_TOL
+    assert rel_l2(res[4], c["ref_pos_grad"]) <= GRAD_TOL
+    assert res[2].dtype == np.complex64 and res[2].shape == c["obj"].shape
+
+
+def _oracle_case(W, Z, Mp, Mo, n_scan, algorithm, seed, batch, double=False):
+    from oracle import ptycho_oracle as orc
+    from pypty_gb300 import synth
+    rng = np.random.default_rng(seed)
+    px, kV = 0.1, 300.0
+    n = W + int(n_scan * 7) + 8
+    truth = synth.gaussian_phase_object(n, n, Z, 60, 0.3, px, 0.2, 1.0, rng, n_modes=Mo)
+    probe = synth.make_probe(W, px, kV, 30.0, 50.0, Mp, 0.5 ** np.arange(Mp), 1e5)
+    ipos, corr = synth.split_positions(synth.raster_positions(n_scan, n_scan, 7.0, 2.0, rng))
+    lam = synth.wavelength_A(kV)
+    seq = np.arange(ipos.shape[0])
+    sim = orc.loss_and_direction(truth, probe, ipos, corr, 2.0, 1.0, None, algorithm, lam, 1, 1, 1, px, px,
+                                 2 / 3, 0.0, seq, 1, batch, simulate=True)
+    meas = synth.poisson_patterns(sim, 1.0, rng)
+    obj0 = np.exp(0.6j * np.angle(truth)).astype(np.complex64)
+    c = dict(obj=obj0, probe=probe, positions=ipos, pos_correction=corr, sequence=seq, measured=meas,
+             algorithm=algorithm, wavelength=lam, px=px, cutoff=2 / 3, rolloff=0.0, distance=2.0,
+             edge_mult=1.0, loss_weight=1, batch=batch, step_obj=1, step_probe=1, step_pos=1)
+    f, cx = (np.float64, np.complex128) if double else (np.float32, np.complex64)
+    ref = orc.loss_and_direction(obj0.astype(cx), probe.astype(cx), ipos, corr.astype(f), 2.0, 1.0,
+                                 meas.astype(f), algorithm, lam, 1, 1, 1, px, px, 2 / 3, 0.0, seq, 1, batch,
+                                 float_dtype=f, complex_dtype=cx)
+    return c, ref
+
+
+@pytest.mark.parametrize("W,Z,Mp,Mo,alg", [(128, 6, 3, 1, "ml"), (64, 5, 2, 2, "lsq_sqrt"),
+                                           (128, 2, 8, 1, "lsq")])
+def test_against_fp64_oracle(engine, W, Z, Mp, Mo, alg):
+    """Larger shapes than the goldens (multislice, many modes) against the FP64 oracle."""
+    from gpu_helpers import run_gpu
+    c, ref = _oracle_case(W, Z, Mp, Mo, 3, alg, seed=W + Z + Mp, batch=4, double=True)
+    loss, sse, og, pg, posg = run_gpu(c, engine=engine)
+    assert abs(loss - ref[0]) <= LOSS_TOL * abs(ref[0])
+    assert rel_l2(og, ref[2]) <= GRAD_TOL
+    assert rel_l2(pg, ref[3]) <= GRAD_TOL
+    assert rel_l2(posg, ref[4]) <= GRAD_TOL
+
+
+def test_simulated_patterns_match_oracle(engine):
+    import torch
+    from oracle import ptycho_oracle as orc
+    from pypty_gb300.engine import Geometry, make_problem
+    c, _ = _oracle_case(64, 3, 2, 1, 3, "ml", seed=5, batch=4)
+    sim_ref = orc.loss_and_direction(c["obj"], c["probe"], c["positions"], c["pos_correction"], 2.0, 1.0,
+                                     None, "ml", c["wavelength"], 1, 1, 0, c["px"], c["px"], 2 / 3, 0.0,
+                                     c["sequence"], 1, 4, float_dtype=np.float64,
+                                     complex_dtype=np.complex128, simulate=True)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    prob = make_problem(64, c["obj"].shape, 2, geo, algorithm="ml", wavelength=c["wavelength"],
+                        pixel_size_x=c["px"], pixel_size_y=c["px"], slice_distance=2.0, compute_batch=4)
+    out = engine.simulate(prob, torch.from_numpy(c["obj"]).cuda(), torch.from_numpy(c["probe"]).cuda(), geo)
+    assert rel_l2(out.cpu().numpy(), sim_ref) <= 2e-6

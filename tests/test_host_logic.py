@@ -1,0 +1,83 @@
+"""Host-side logic of the drop-in: flag screening, geometry, problem construction."""
+import numpy as np
+import pytest
+
+from pypty_gb300 import _lib, synth
+from pypty_gb300.engine import Geometry, make_problem
+from pypty_gb300 import objective
+
+
+def base_kwargs(**over):
+    W = 64
+    kw = dict(this_obj=np.ones((96, 96, 1, 1), np.complex64), full_probe=np.ones((W, W, 1), np.complex64),
+              this_pos_array=np.zeros((2, 2), np.int32), this_pos_correction=np.zeros((2, 2), np.float32),
+              this_tilt_array=np.zeros((1, 6), np.float32), this_tilts_correction=np.zeros((1, 6), np.float32),
+              this_distances=np.array([1.0], np.float32), edge_slice_thickness_multiplier=1.0,
+              measured_array=np.zeros((2, W, W), np.float32), algorithm_type="lsq_sqrt",
+              this_wavelength=np.float32(0.025), this_step_probe=1, this_step_obj=1,
+              this_step_pos_correction=0, this_step_tilts=0, masks=None, pixel_size_x_A=0.2,
+              pixel_size_y_A=0.2, recon_type="far_field", Cs=0, defocus_array=np.array([0.0]),
+              alpha_near_field=0, damping_cutoff_multislice=2 / 3, smooth_rolloff=0,
+              propmethod="multislice", this_chopped_sequence=np.arange(2), load_one_by_one=False,
+              data_multiplier=1, data_pad=0, phase_plate_in_h5=None, this_loss_weight=1, data_bin=1,
+              data_shift_vector=[0, 0], upsample_pattern=1, static_background=None,
+              this_step_static_background=0, tilt_mode=0, aberration_marker=None, probe_marker=None,
+              aberrations_array=None, compute_batch=2, phase_only_obj=False, beam_current=None,
+              this_beam_current_step=0, this_step_aberrations_array=0, default_float=np.float32,
+              default_complex=np.complex64, xp=np, is_first_epoch=True, scan_size=None, scan_step_A=1,
+              fast_axis_reg_weight_positions=0, slow_axis_reg_weight_positions=0,
+              slow_axis_reg_weight_tilts=0, current_deformation_reg_weight_positions=0,
+              current_deformation_reg_weight_tilts=0, fast_axis_reg_weight_tilts=0, aperture_mask=None,
+              probe_reg_weight=0, current_window_weight=0, current_window=None, phase_norm_weight=0,
+              abs_norm_weight=0, atv_weight=0, atv_q=1, atv_p=2, mixed_variance_weight=0,
+              mixed_variance_sigma=0.5, wedge_mu=0, beta_wedge=0, probe_mod_reg_weight=0,
+              probe_mod_tol=0.05, smart_memory=False, print_flag=0, data_simulation_flag=False,
+              data_simulation_exitwave=False, use_padded_intensity=True)
+    kw.update(over)
+    return kw
+
+
+@pytest.mark.parametrize("over", [
+    dict(recon_type="near_field"), dict(propmethod="yoshida"), dict(algorithm_type="lsq_compressed"),
+    dict(this_step_tilts=1), dict(tilt_mode=3), dict(this_tilt_array=np.ones((1, 6), np.float32)),
+    dict(this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
+    dict(probe_marker=np.zeros(2, int)), dict(beam_current=np.ones(2)), dict(data_pad=4),
+    dict(upsample_pattern=2), dict(atv_weight=0.1), dict(static_background=np.ones((64, 64))),
+    dict(data_simulation_flag="sim.npy"),
+])
+def test_unsupported_flags_raise_before_any_gpu_work(over):
+    with pytest.raises(NotImplementedError):
+        objective.loss_and_direction(**base_kwargs(**over))
+
+
+def test_reference_signature_is_mirrored():
+    import inspect
+    params = list(inspect.signature(objective.loss_and_direction).parameters)
+    assert params[:4] == ["this_obj", "full_probe", "this_pos_array", "this_pos_correction"]
+    assert len(params) == 77 and params[-1] == "use_padded_intensity"
+
+
+def test_probe_shift_flag_follows_reference_rule():
+    g = Geometry.make(np.zeros((3, 2)), np.zeros((3, 2)))
+    assert not g.probe_shift(step_pos=False)
+    assert g.probe_shift(step_pos=True)
+    g = Geometry.make(np.zeros((3, 2)), np.array([[0, 0], [0.1, 0], [0, 0]]))
+    assert g.probe_shift(step_pos=False)
+
+
+def test_make_problem_fields():
+    ipos, corr = synth.split_positions(synth.raster_positions(4, 4, 3.3))
+    g = Geometry.make(ipos, corr)
+    p = make_problem(128, (256, 256, 20, 1), 3, g, algorithm="ml", wavelength=0.0197,
+                     pixel_size_x=0.1, pixel_size_y=0.1, slice_distance=2.0, compute_batch=8)
+    assert (p.window, p.n_slices, p.n_probe_modes, p.n_positions, p.compute_batch) == (128, 20, 3, 16, 8)
+    assert p.algorithm == _lib.ALGORITHMS["ml"] and p.probe_shift == 1
+    assert abs(p.damping_cutoff - 2 / 3) < 1e-7
+
+
+def test_split_positions_matches_reference_rounding():
+    pos = np.array([[0.4, 1.6], [2.5, 3.49], [-1.2, 0.0]])
+    ipos, corr = synth.split_positions(pos)
+    shifted = pos - pos.min(axis=0)
+    assert np.array_equal(ipos, np.round(shifted).astype(np.int32))
+    assert np.allclose(corr, shifted - np.round(shifted), atol=1e-7)
