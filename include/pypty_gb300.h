@@ -121,6 +121,23 @@ int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t i
 int pty_fft2_workspace_bytes(int32_t window, size_t* bytes);
 
 /*
+ * pty_fft2 without a workspace argument; it allocates nothing. No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory -- an application
+ * whose own memory pool owns every device allocation, code running while a CUDA graph is
+ * captured (cudaMalloc is not allowed then), or a loop that must not pay for an allocation.
+ * The twiddle tables live in a fixed 3 KiB array of device memory inside the library,
+ * created on every GPU that loads the library and kept until the process exits.
+ * Limits: window 64 or 128 only (anything else returns PTY_ERR_UNSUPPORTED); batch > 0.
+ * The first call on a device looks up the array's device address (with that device
+ * current); make that first call before any stream capture. All calls share the array and
+ * each call rewrites the table it uses, so calls that overlap on the GPU (different
+ * streams) race: serialise them, or use pty_fft2 with a workspace per stream.
+ * Same arguments and results as pty_fft2.
+ */
+int pty_fft2_noalloc(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
+                     int32_t shift, void* stream);
+
+/*
  * Launch profiler (no counterpart in the reference, which only logs wall time,
  * pypty/utils.py:1894). While enabled, every kernel launch of the library records a CUDA
  * event on its stream just before the launch, and every call records one when its last
