@@ -45,6 +45,9 @@ CONFIGS = {
     # name: (W, Ny, Z, Mp, n_scan, algorithm, batch)
     "multislice": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=32, algorithm="ml", batch=256,
                        desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 32x32 jittered scan, ml, batch 256"),
+    # same kernels and shapes per position as "multislice", 8x8 positions: for ncu captures
+    "multislice-small": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=8, algorithm="ml", batch=64,
+                             desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 8x8 jittered scan, ml, batch 64"),
     "single-slice": dict(W=64, N_obj=128, Z=1, Mp=1, n_scan=16, algorithm="lsq_sqrt", batch=256,
                          desc="single-slice W64 Z1 Mp1, 128x128 object, 16x16 scan, lsq_sqrt, batch 256"),
 }

@@ -253,13 +253,59 @@ __device__ __forceinline__ float2 shift_ramp(const FusedArgs& a, int ky, int kx,
   return make_float2(c * mk, s * mk);
 }
 
+// dL/dI of one detector pixel for the loss `alg` (pypty/objective.py:527-559), with the
+// per-pixel loss and squared error added to the FP64 accumulators. Float32 arithmetic per
+// pixel, as the reference's arrays; only the sums are FP64.
+__device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& lsum, double& ssum) {
+  float d, lp, sp;
+  if (alg == ALG_LSQ_SQRT) {
+    const float sI = sqrtf(I), sM = sqrtf(Mv);
+    const float df = sI - sM;
+    sp = (Mv - I) * (Mv - I);
+    lp = df * df;
+    d = df / (sI == 0.0f ? 1.0f : sI);
+  } else if (alg == ALG_ML) {
+    const float df = I - Mv;
+    sp = df * df;
+    lp = I - Mv * logf(I + (I == 0.0f ? 1.0f : 0.0f));
+    d = df / (I == 0.0f ? 1.0f : I);
+  } else if (alg == ALG_LSQ) {
+    const float df = I - Mv;
+    sp = df * df;
+    lp = sp;
+    d = 2.0f * df;
+  } else {
+    const float df = Mv - I;
+    sp = df * df;
+    if (Mv > 0.5f) {
+      lp = 0.5f * (sp / Mv);
+      d = I / Mv - 1.0f;
+    } else {
+      lp = I;
+      d = 1.0f;
+    }
+  }
+  lsum += (double)lp;
+  ssum += (double)sp;
+  return d;
+}
+
 // One thread block per (position, probe mode, object mode); the Mp*Mo blocks of a position
 // form a thread-block cluster and exchange intensities / gradients through distributed
 // shared memory. Forward multislice (multislice_core.py:61-82), far field + loss
 // (objective.py:501-597), adjoint multislice (multislice_core.py:158-199), probe-shift
 // adjoint and position gradient (objective.py:641-658).
+//
+// The whole computation is one loop of steps, each "real-space op -> FFT -> frequency op ->
+// inverse FFT", so the forward and inverse transforms are each inlined once (a small
+// instruction footprint) and the window never leaves the registers:
+//   step 0          incoming probe (shift ramp in frequency, inverse FFT)
+//   steps 1..Z      slice z = s-1: store conj(psi_z), psi *= O_z, FFT, *= P (or the far
+//                   field, loss and dL/dPsi after the last slice), IFFT
+//   steps Z+1..2Z   slice z = 2Z-s: object-gradient contribution, g *= conj(O_z), FFT,
+//                   *= conj(P), IFFT (z = 0: probe-gradient spectrum and position gradient)
 template <int W>
-__global__ void __launch_bounds__(Geo<W>::T) fused_multislice_kernel(FusedArgs a) {
+__global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kernel(FusedArgs a) {
   using G = Geo<W>;
   using F = WinFFT<W>;
   constexpr int T = G::T;
@@ -268,6 +314,8 @@ __global__ void __launch_bounds__(Geo<W>::T) fused_multislice_kernel(FusedArgs a
   float2 *xbuf, *tw1, *tw2;
   double* red;
   carve<W>(smem, xbuf, tw1, tw2, red);
+  float* fs0 = reinterpret_cast<float*>(xbuf);   // WW floats: this block's |Psi|^2
+  float* fs1 = fs0 + WW;                          // WW floats: mode-summed I, then dL/dI
   cg::cluster_group cluster = cg::this_cluster();
   const int t = threadIdx.x;
   const int nmodes = a.Mp * a.Mo;
@@ -276,193 +324,178 @@ __global__ void __launch_bounds__(Geo<W>::T) fused_multislice_kernel(FusedArgs a
   const int b = blockIdx.x / nmodes;
   const int gi = a.seq[b];
   const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
+  const int Z = a.Z;
   load_twiddles<W>(tw1, tw2, a.tw);
   __syncthreads();
 
   float2 v[32];
-  // ---- incoming (shifted) probe, objective.py:469-476
-  if (a.probe_shift) {
-    const float2* pf = a.probe_f + (size_t)p * WW;
-    const float inv = 1.0f / (float)WW;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int ky = G::fky(t, i), kx = G::fkx(t, i);
-      const float mk = a.mask[ky * W + kx];
-      v[i] = cscale(cmul(pf[i * T + t], shift_ramp<W>(a, ky, kx, mk, dy, dx)), inv);
-    }
-    F::inverse(v, xbuf, tw1, tw2);
-  } else {
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
-  }
+  const int nsteps = a.simulate ? Z + 1 : 2 * Z + 1;
+  for (int s = 0; s < nsteps; ++s) {
+    const bool fwd = (s >= 1 && s <= Z);
+    const int z = fwd ? s - 1 : 2 * Z - s;
 
-  // ---- forward multislice
-  for (int z = 0; z < a.Z; ++z) {
-    if (a.step_obj && !a.simulate) {
-      float2* st = a.stack + ((((size_t)b * a.Z + z) * a.Mp + p) * a.Mo + m) * WW;
+    // ------------------------------------------------ real-space op
+    if (s == 0) {
+      if (!a.probe_shift) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) st[i * T + t] = cconj(v[i]);
+        for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
+      }
+    } else if (fwd) {
+      if (a.step_obj && !a.simulate) {
+        float2* st = a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) st[i * T + t] = cconj(v[i]);
+      }
+      const float2* ob = a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], ob[i * T + t]);
+    } else {
+      if (a.step_obj) {
+        // contribution conj(psi_z) * g, summed over the probe modes of object mode m
+        const float2* st = a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW;
+        float2* gs = a.gsum + (((size_t)b * Z + z) * a.Mo + m) * WW;
+        if (a.Mp == 1) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) gs[i * T + t] = cmul(st[i * T + t], v[i]);
+        } else {
+          __syncthreads();
+#pragma unroll
+          for (int i = 0; i < 32; ++i) xbuf[i * T + t] = cmul(st[i * T + t], v[i]);
+          cluster.sync();
+#pragma unroll 1
+          for (int i = p; i < 32; i += a.Mp) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (int pp = 0; pp < a.Mp; ++pp)
+              acc = cadd(acc, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[i * T + t]);
+            gs[i * T + t] = acc;
+          }
+          cluster.sync();
+        }
+      }
+      const float2* ob = a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], ob[i * T + t]);
+      if (z == 0) {
+        if (!(a.step_probe || a.step_pos)) break;
+        if (a.Mo > 1) {
+          // probe gradient: sum over object modes (multislice_core.py:193-197)
+          __syncthreads();
+#pragma unroll
+          for (int i = 0; i < 32; ++i) xbuf[i * T + t] = v[i];
+          cluster.sync();
+          if (m == 0) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              float2 acc = make_float2(0.f, 0.f);
+              for (int mm = 0; mm < a.Mo; ++mm)
+                acc = cadd(acc, cluster.map_shared_rank(xbuf, p + mm * a.Mp)[i * T + t]);
+              v[i] = acc;
+            }
+          }
+          cluster.sync();
+          if (m != 0) break;
+        }
+      }
     }
-    const float2* ob = a.obl + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
+
+    // ------------------------------------------------ forward FFT
+    if (s > 0) F::forward(v, xbuf, tw1, tw2);
+
+    // ------------------------------------------------ frequency op
+    if (s == 0) {
+      if (!a.probe_shift) continue;   // the unshifted probe is already in real space
+      const float2* pf = a.probe_f + (size_t)p * WW;
+      const float inv = 1.0f / (float)WW;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], ob[i * T + t]);
-    if (z < a.Z - 1) {
-      F::forward(v, xbuf, tw1, tw2);
+      for (int i = 0; i < 32; ++i) {
+        const int ky = G::fky(t, i), kx = G::fkx(t, i);
+        v[i] = cscale(cmul(pf[i * T + t], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
+      }
+    } else if (fwd && z < Z - 1) {
       const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
-      F::inverse(v, xbuf, tw1, tw2);
-    }
-  }
-
-  // ---- far field: Psi = FFT(exit) * mask; I = mean over modes |Psi|^2
-  F::forward(v, xbuf, tw1, tw2);
-  float* ibuf = reinterpret_cast<float*>(xbuf);
-  __syncthreads();
+    } else if (fwd) {
+      // far field: Psi = FFT(exit) * mask, I = mean over modes |Psi|^2 (objective.py:501-512)
+      __syncthreads();
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    v[i] = cscale(v[i], a.mask[G::fky(t, i) * W + G::fkx(t, i)]);
-    ibuf[i * T + t] = cabs2(v[i]);
-  }
-  cluster.sync();
-  double lsum = 0.0, ssum = 0.0;
-  const float inv_modes = 1.0f / (float)nmodes;
-  const float* meas = a.measured + (size_t)gi * WW;
-#pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    float s = 0.0f;
-    for (int r = 0; r < nmodes; ++r) s += cluster.map_shared_rank(ibuf, r)[i * T + t];
-    const float I = (nmodes == 1) ? s : s * inv_modes;
-    const int ky = G::fky(t, i), kx = G::fkx(t, i);
-    const int dy_i = (ky + W / 2) & (W - 1), dx_i = (kx + W / 2) & (W - 1);
-    if (a.simulate) {
-      if (crank == 0) a.sim_out[(size_t)b * WW + dy_i * W + dx_i] = I;
-      continue;
-    }
-    const float Mv = meas[dy_i * W + dx_i];
-    float d, lp, sp;
-    if (a.algorithm == ALG_LSQ_SQRT) {           // objective.py:529-538
-      const float sI = sqrtf(I), sM = sqrtf(Mv);
-      const float df = sI - sM;
-      sp = (Mv - I) * (Mv - I);
-      lp = df * df;
-      d = df / (sI == 0.0f ? 1.0f : sI);
-    } else if (a.algorithm == ALG_ML) {          // objective.py:540-547
-      const float df = I - Mv;
-      sp = df * df;
-      lp = I - Mv * logf(I + (I == 0.0f ? 1.0f : 0.0f));
-      d = df / (I == 0.0f ? 1.0f : I);
-    } else if (a.algorithm == ALG_LSQ) {         // objective.py:548-552
-      const float df = I - Mv;
-      sp = df * df;
-      lp = sp;
-      d = 2.0f * df;
-    } else {                                     // lsq_sqrt_2, objective.py:553-559
-      const float df = Mv - I;
-      sp = df * df;
-      if (Mv > 0.5f) {
-        lp = 0.5f * (sp / Mv);
-        d = I / Mv - 1.0f;
-      } else {
-        lp = I;
-        d = 1.0f;
+      for (int i = 0; i < 32; ++i) {
+        v[i] = cscale(v[i], a.mask[G::fky(t, i) * W + G::fkx(t, i)]);
+        fs0[i * T + t] = cabs2(v[i]);
       }
-    }
-    if (nmodes > 1) d = d / (float)nmodes;       // objective.py:586-587
-    lsum += (double)lp;
-    ssum += (double)sp;
-    // dL/dPsi = dLdI * Psi * (w * W^2); the W^2 cancels the 1/W^2 of ifft2 (exact)
-    v[i] = cscale(cscale(v[i], d), a.loss_weight);
-  }
-  cluster.sync();   // every block is done reading this block's intensities
-  if (a.simulate) return;
-  block_sum2(lsum, ssum, red);
-  if (t == 0 && crank == 0) {
-    a.loss_part[2 * b] = lsum;
-    a.loss_part[2 * b + 1] = ssum;
-  }
-  F::inverse(v, xbuf, tw1, tw2);   // g = dL/d(exit wave), objective.py:597
-
-  // ---- adjoint multislice, multislice_core.py:158-183
-  for (int z = a.Z - 1; z >= 0; --z) {
-    if (a.step_obj) {
-      const float2* st = a.stack + ((((size_t)b * a.Z + z) * a.Mp + p) * a.Mo + m) * WW;
-      float2* gs = a.gsum + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
-      if (a.Mp == 1) {
-#pragma unroll
-        for (int i = 0; i < 32; ++i) gs[i * T + t] = cmul(st[i * T + t], v[i]);
-      } else {
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < 32; ++i) xbuf[i * T + t] = cmul(st[i * T + t], v[i]);
-        cluster.sync();
-        // this block sums elements i = p, p + Mp, ... over the probe modes of object mode m
-        for (int i = p; i < 32; i += a.Mp) {
-          float2 s = make_float2(0.f, 0.f);
-          for (int pp = 0; pp < a.Mp; ++pp) s = cadd(s, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[i * T + t]);
-          gs[i * T + t] = s;
+      cluster.sync();
+#pragma unroll 1
+      for (int i = 0; i < 32; ++i) {
+        float acc = 0.0f;
+        for (int r = 0; r < nmodes; ++r) acc += cluster.map_shared_rank(fs0, r)[i * T + t];
+        fs1[i * T + t] = acc;
+      }
+      cluster.sync();   // every block is done reading this block's intensities
+      const float inv_modes = 1.0f / (float)nmodes;
+      const float* meas = a.measured + (size_t)gi * WW;
+      double lsum = 0.0, ssum = 0.0;
+#pragma unroll 1
+      for (int i = 0; i < 32; ++i) {
+        const float acc = fs1[i * T + t];
+        const float I = (nmodes == 1) ? acc : acc * inv_modes;
+        const int ky = G::fky(t, i), kx = G::fkx(t, i);
+        const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
+        if (a.simulate) {
+          if (crank == 0) a.sim_out[(size_t)b * WW + didx] = I;
+          continue;
         }
-        cluster.sync();
+        float d = loss_pixel(a.algorithm, I, meas[didx], lsum, ssum);
+        if (nmodes > 1) d = d / (float)nmodes;           // objective.py:586-587
+        fs1[i * T + t] = d;
       }
-    }
-    const float2* ob = a.obl + (((size_t)b * a.Z + z) * a.Mo + m) * WW;
+      if (a.simulate) return;
+      block_sum2(lsum, ssum, red);
+      if (t == 0 && crank == 0) {
+        a.loss_part[2 * b] = lsum;
+        a.loss_part[2 * b + 1] = ssum;
+      }
+      // dL/dPsi = dLdI * Psi * (w * W^2); the W^2 cancels the 1/W^2 of ifft2 (objective.py:595-597)
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], ob[i * T + t]);
-    if (z > 0) {
-      F::forward(v, xbuf, tw1, tw2);
+      for (int i = 0; i < 32; ++i) v[i] = cscale(cscale(v[i], fs1[i * T + t]), a.loss_weight);
+    } else if (z > 0) {
       const float2* pr = (z == 1 && a.use_edge) ? a.prop_edge : a.prop;
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
-      F::inverse(v, xbuf, tw1, tw2);
-    }
-  }
-
-  // ---- probe gradient (sum over object modes), shift adjoint, position gradient
-  if (!(a.step_probe || a.step_pos)) return;
-  if (a.Mo > 1) {
-    __syncthreads();
+    } else {
+      // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
+      const float2* pf = a.probe_f + (size_t)p * WW;
+      double gy = 0.0, gx = 0.0;
+      if (a.probe_shift) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) xbuf[i * T + t] = v[i];
-    cluster.sync();
-    if (m == 0) {
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        float2 s = make_float2(0.f, 0.f);
-        for (int mm = 0; mm < a.Mo; ++mm) s = cadd(s, cluster.map_shared_rank(xbuf, p + mm * a.Mp)[i * T + t]);
-        v[i] = s;
+        for (int i = 0; i < 32; ++i) {
+          const int ky = G::fky(t, i), kx = G::fkx(t, i);
+          const float mk = a.mask[ky * W + kx];
+          v[i] = cmulc(v[i], shift_ramp<W>(a, ky, kx, mk, dy, dx));
+          if (a.step_pos) {
+            // Re(smyx * conj(Pf) * F) with smyx = i*s*mask  ->  -(s*mask) * Im(conj(Pf) * F)
+            const float im = cmulc(v[i], pf[i * T + t]).y;
+            gy += (double)(-(a.sy[ky] * mk) * im);
+            gx += (double)(-(a.sx[kx] * mk) * im);
+          }
+        }
       }
-    }
-    cluster.sync();
-    if (m != 0) return;
-  }
-  F::forward(v, xbuf, tw1, tw2);
-  const float2* pf = a.probe_f + (size_t)p * WW;
-  double gy = 0.0, gx = 0.0;
+      if (a.step_probe) {
+        float2* fp = a.fprobe + ((size_t)b * a.Mp + p) * WW;
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const int ky = G::fky(t, i), kx = G::fkx(t, i);
-    if (a.probe_shift) {
-      const float mk = a.mask[ky * W + kx];
-      v[i] = cmulc(v[i], shift_ramp<W>(a, ky, kx, mk, dy, dx));
+        for (int i = 0; i < 32; ++i) fp[i * T + t] = v[i];
+      }
       if (a.step_pos) {
-        // Re(smyx * conj(Pf) * F) with smyx = i*s*mask  ->  -(s*mask) * Im(conj(Pf) * F)
-        const float im = cmulc(v[i], pf[i * T + t]).y;
-        gy += (double)(-(a.sy[ky] * mk) * im);
-        gx += (double)(-(a.sx[kx] * mk) * im);
+        block_sum2(gy, gx, red);
+        if (t == 0) {
+          a.pos_part[(b * a.Mp + p) * 2] = gy;
+          a.pos_part[(b * a.Mp + p) * 2 + 1] = gx;
+        }
       }
+      break;
     }
-  }
-  if (a.step_probe) {
-    float2* fp = a.fprobe + ((size_t)b * a.Mp + p) * WW;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) fp[i * T + t] = v[i];
-  }
-  if (a.step_pos) {
-    block_sum2(gy, gx, red);
-    if (t == 0) {
-      a.pos_part[(b * a.Mp + p) * 2] = gy;
-      a.pos_part[(b * a.Mp + p) * 2 + 1] = gx;
-    }
+
+    // ------------------------------------------------ inverse FFT
+    F::inverse(v, xbuf, tw1, tw2);
   }
 }
 

@@ -156,6 +156,7 @@ struct Geo {
   static constexpr int TW1 = A * 32;       // round-1 twiddle table size
   static constexpr int TW2 = W;            // round-2 twiddle table size
   static constexpr int XBUF = W * W;       // exchange buffer (float2)
+  static constexpr int MINB = W == 64 ? 4 : 1;   // resident blocks per SM the kernels aim for
 
   // real layout: element i of thread t is pixel (y, x)
   static __device__ __forceinline__ int ry(int t) { return t / A; }
