@@ -19,7 +19,8 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   const bool simulate = patterns != nullptr;
   int rc;
   if ((rc = set_smem(probe_fft_kernel<W>, smem)) || (rc = set_smem(object_windows_kernel<W>, smem)) ||
-      (rc = set_smem(fused_multislice_kernel<W>, smem)) || (rc = set_smem(grad_windows_kernel<W>, smem)) ||
+      (rc = set_smem(fused_multislice_kernel<W>, FusedSmem<W>::bytes)) ||
+      (rc = set_smem(grad_windows_kernel<W>, smem)) ||
       (rc = set_smem(probe_final_kernel<W>, smem)))
     return rc;
 
@@ -50,6 +51,7 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   const int nyx = q.Ny * q.Nx;
   prof_mark(st, KID_OBJ_TO_SLICES);
   obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(obj, at<float2>(ws, q.o_obj), nyx, q.zm);
+  if (cudaMemsetAsync(at<int>(ws, q.o_err), 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
   if ((rc = cuda_status())) return rc;
 
   const bool do_obj = p->step_obj && !simulate;
@@ -106,11 +108,12 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
     fa.loss_part = at<double>(ws, q.o_loss_part) + 2 * (size_t)s0;
     fa.pos_part = at<double>(ws, q.o_pos_part) + 2 * (size_t)s0 * q.Mp;
     fa.sim_out = simulate ? patterns + (size_t)s0 * WW : nullptr;
+    fa.err = at<int>(ws, q.o_err);
 
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(Bn * nmodes));
     cfg.blockDim = dim3(T);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = FusedSmem<W>::bytes;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -165,8 +168,8 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   if (pos_grad) cudaMemsetAsync(pos_grad, 0, (size_t)q.N * 2 * sizeof(float), st);
   prof_mark(st, KID_FINALIZE);
   finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part), d_seq,
-                                              q.nseq, q.Mp, W, (double)p->loss_weight, do_pos ? 1 : 0, loss_sse,
-                                              pos_grad);
+                                              q.nseq, q.Mp, W, (double)p->loss_weight, do_pos ? 1 : 0,
+                                              at<int>(ws, q.o_err), loss_sse, pos_grad);
   prof_mark(st, -1);
   return cuda_status();
 }

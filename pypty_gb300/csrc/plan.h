@@ -20,7 +20,7 @@ struct Plan {
   int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
   size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_sx, o_sy, o_probe_f;
   size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
-  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, total;
+  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, total;
 };
 
 inline int tw_count(int W) { return W == 64 ? Geo<64>::TW1 + Geo<64>::TW2 : Geo<128>::TW1 + Geo<128>::TW2; }
@@ -82,6 +82,7 @@ inline Plan make_plan(const pty_problem_t* p) {
   q.o_loss_part = take((size_t)q.nseq * 2 * sizeof(double));
   q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
   q.o_sim = take((size_t)q.Bb * WW * f4);
+  q.o_err = take(sizeof(int));
   q.total = o;
   return q;
 }

@@ -173,9 +173,7 @@ __global__ void __launch_bounds__(Geo<W>::T) probe_fft_kernel(const float2* __re
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * Mp + p];
   WinFFT<W>::forward(v, xbuf, tw1, tw2);
-  float2* out = probe_f + (size_t)p * W * W;
-#pragma unroll
-  for (int i = 0; i < 32; ++i) out[i * G::T + t] = v[i];
+  st_native<W>(probe_f + (size_t)p * W * W, v);
 }
 
 // ------------------------------------------------------------------ object windows
@@ -213,9 +211,7 @@ __global__ void __launch_bounds__(Geo<W>::T) object_windows_kernel(WindowArgs a)
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], a.mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
   WinFFT<W>::inverse(v, xbuf, tw1, tw2);
-  float2* dst = a.out + (size_t)win * W * W;
-#pragma unroll
-  for (int i = 0; i < 32; ++i) dst[i * G::T + t] = v[i];
+  st_native<W>(a.out + (size_t)win * W * W, v);
 }
 
 // ------------------------------------------------------------------ fused multislice
@@ -240,6 +236,7 @@ struct FusedArgs {
   double* loss_part;        // [Bb][2]
   double* pos_part;         // [Bb][Mp][2]
   float* sim_out;           // [Bb][W][W] simulated mean intensity (detector order)
+  int* err;                 // set to 1 if a bounded wait on an async copy ran out
 };
 
 template <int W>
@@ -290,6 +287,17 @@ __device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& 
   return d;
 }
 
+// Shared memory of the fused kernel: the FFT exchange buffer (which also receives each
+// step's main operand by TMA bulk copy), twiddles, reduction scratch, a side buffer for the
+// first NST elements per thread of the adjoint step's object window, and two mbarriers.
+template <int W>
+struct FusedSmem {
+  static constexpr int NST = (W == 128) ? 24 : 16;
+  static constexpr size_t side_off = Smem<W>::bytes;
+  static constexpr size_t bar_off = side_off + sizeof(float2) * NST * Geo<W>::T;
+  static constexpr size_t bytes = bar_off + 2 * sizeof(uint64_t);
+};
+
 // One thread block per (position, probe mode, object mode); the Mp*Mo blocks of a position
 // form a thread-block cluster and exchange intensities / gradients through distributed
 // shared memory. Forward multislice (multislice_core.py:61-82), far field + loss
@@ -297,23 +305,30 @@ __device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& 
 // adjoint and position gradient (objective.py:641-658).
 //
 // The whole computation is one loop of steps, each "real-space op -> FFT -> frequency op ->
-// inverse FFT", so the forward and inverse transforms are each inlined once (a small
-// instruction footprint) and the window never leaves the registers:
+// inverse FFT", so the forward and inverse transforms are each inlined once and the window
+// never leaves the registers:
 //   step 0          incoming probe (shift ramp in frequency, inverse FFT)
 //   steps 1..Z      slice z = s-1: store conj(psi_z), psi *= O_z, FFT, *= P (or the far
 //                   field, loss and dL/dPsi after the last slice), IFFT
 //   steps Z+1..2Z   slice z = 2Z-s: object-gradient contribution, g *= conj(O_z), FFT,
 //                   *= conj(P), IFFT (z = 0: probe-gradient spectrum and position gradient)
+// Operands are prefetched by TMA bulk copies: the next step's window (O_z, or conj(psi_z) in
+// the adjoint) lands in the exchange buffer while the inverse transform finishes its last
+// register-only round; the adjoint's O_z arrives in the side buffer one step ahead.
 template <int W>
 __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kernel(FusedArgs a) {
   using G = Geo<W>;
   using F = WinFFT<W>;
+  using S = FusedSmem<W>;
   constexpr int T = G::T;
+  constexpr int NST = S::NST;
   constexpr size_t WW = (size_t)W * W;
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
   double* red;
   carve<W>(smem, xbuf, tw1, tw2, red);
+  float2* side = reinterpret_cast<float2*>(smem + S::side_off);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);   // [0]: xbuf, [1]: side
   float* fs0 = reinterpret_cast<float*>(xbuf);   // WW floats: this block's |Psi|^2
   float* fs1 = fs0 + WW;                          // WW floats: mode-summed I, then dL/dI
   cg::cluster_group cluster = cg::this_cluster();
@@ -325,11 +340,40 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   const int gi = a.seq[b];
   const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
   const int Z = a.Z;
+  const bool adj_stack = a.step_obj && !a.simulate;   // the adjoint reads conj(psi_z)
+  if (t == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_async_shared();
+  }
   load_twiddles<W>(tw1, tw2, a.tw);
   __syncthreads();
+  uint32_t ph_x = 0, ph_side = 0;
+
+  auto obl_ptr = [&](int z) { return a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW; };
+  auto stack_ptr = [&](int z) { return a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW; };
+  // the window step s reads from the exchange buffer (s >= 1)
+  auto xsrc = [&](int s) -> const float2* {
+    if (s <= Z) return obl_ptr(s - 1);
+    const int z = 2 * Z - s;
+    return adj_stack ? stack_ptr(z) : obl_ptr(z);
+  };
+  auto issue_x = [&](int s) {
+    if (t == 0) {
+      fence_async_shared();
+      bulk_load(xbuf, xsrc(s), (uint32_t)(WW * sizeof(float2)), &bars[0]);
+    }
+  };
+  auto issue_side = [&](int z) {
+    if (t == 0) {
+      fence_async_shared();
+      bulk_load(side, obl_ptr(z), (uint32_t)(NST * T * sizeof(float2)), &bars[1]);
+    }
+  };
 
   float2 v[32];
   const int nsteps = a.simulate ? Z + 1 : 2 * Z + 1;
+  if (!a.probe_shift) issue_x(1);   // step 0 has no inverse transform to hide the copy behind
   for (int s = 0; s < nsteps; ++s) {
     const bool fwd = (s >= 1 && s <= Z);
     const int z = fwd ? s - 1 : 2 * Z - s;
@@ -341,40 +385,84 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
       }
     } else if (fwd) {
-      if (a.step_obj && !a.simulate) {
-        float2* st = a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW;
+      if (adj_stack) {
+        float2 c[32];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) st[i * T + t] = cconj(v[i]);
+        for (int i = 0; i < 32; ++i) c[i] = cconj(v[i]);
+        st_native<W>(stack_ptr(z), c);
+        fence_async_global();   // these stores are read back by TMA in the adjoint
       }
-      const float2* ob = a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW;
+      if (z == Z - 1 && adj_stack) issue_side(Z - 1);
+      mbar_wait(&bars[0], ph_x, a.err);
+      {
+        const float4* ob = reinterpret_cast<const float4*>(xbuf);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], ob[i * T + t]);
+        for (int j = 0; j < 16; ++j) {
+          const float4 q = ob[j * T + t];
+          v[2 * j] = cmul(v[2 * j], make_float2(q.x, q.y));
+          v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
+        }
+      }
     } else {
-      if (a.step_obj) {
+      mbar_wait(&bars[0], ph_x, a.err);
+      if (adj_stack) {
+        // elements NST.. of O_z come straight from global memory; issue them first
+        float4 otail[(32 - NST) / 2];
+        {
+          const float4* og = reinterpret_cast<const float4*>(obl_ptr(z));
+#pragma unroll
+          for (int j = NST / 2; j < 16; ++j) otail[j - NST / 2] = og[j * T + t];
+        }
         // contribution conj(psi_z) * g, summed over the probe modes of object mode m
-        const float2* st = a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW;
         float2* gs = a.gsum + (((size_t)b * Z + z) * a.Mo + m) * WW;
+        float4* x4 = reinterpret_cast<float4*>(xbuf);
         if (a.Mp == 1) {
+          float4* g4 = reinterpret_cast<float4*>(gs);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) gs[i * T + t] = cmul(st[i * T + t], v[i]);
+          for (int j = 0; j < 16; ++j) {
+            const float4 q = x4[j * T + t];
+            const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
+            const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
+            g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
+          }
         } else {
-          __syncthreads();
 #pragma unroll
-          for (int i = 0; i < 32; ++i) xbuf[i * T + t] = cmul(st[i * T + t], v[i]);
+          for (int j = 0; j < 16; ++j) {
+            const float4 q = x4[j * T + t];
+            const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
+            const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
+            x4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
+          }
           cluster.sync();
 #pragma unroll 1
           for (int i = p; i < 32; i += a.Mp) {
             float2 acc = make_float2(0.f, 0.f);
-            for (int pp = 0; pp < a.Mp; ++pp)
-              acc = cadd(acc, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[i * T + t]);
-            gs[i * T + t] = acc;
+            const int e = nidx<W>(i, t);
+            for (int pp = 0; pp < a.Mp; ++pp) acc = cadd(acc, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[e]);
+            gs[e] = acc;
           }
           cluster.sync();
         }
-      }
-      const float2* ob = a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW;
+        // g *= conj(O_z): elements < NST from the side buffer, the rest from the registers
+        mbar_wait(&bars[1], ph_side, a.err);
+        const float4* sd = reinterpret_cast<const float4*>(side);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], ob[i * T + t]);
+        for (int j = 0; j < 16; ++j) {
+          const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
+          v[2 * j] = cmulc(v[2 * j], make_float2(q.x, q.y));
+          v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
+        }
+        __syncthreads();   // the side buffer has been read by every thread
+        if (z > 0) issue_side(z - 1);
+      } else {
+        const float4* ob = reinterpret_cast<const float4*>(xbuf);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const float4 q = ob[j * T + t];
+          v[2 * j] = cmulc(v[2 * j], make_float2(q.x, q.y));
+          v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
+        }
+      }
       if (z == 0) {
         if (!(a.step_probe || a.step_pos)) break;
         if (a.Mo > 1) {
@@ -409,7 +497,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         const int ky = G::fky(t, i), kx = G::fkx(t, i);
-        v[i] = cscale(cmul(pf[i * T + t], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
+        v[i] = cscale(cmul(pf[nidx<W>(i, t)], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
       }
     } else if (fwd && z < Z - 1) {
       const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
@@ -473,17 +561,13 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           v[i] = cmulc(v[i], shift_ramp<W>(a, ky, kx, mk, dy, dx));
           if (a.step_pos) {
             // Re(smyx * conj(Pf) * F) with smyx = i*s*mask  ->  -(s*mask) * Im(conj(Pf) * F)
-            const float im = cmulc(v[i], pf[i * T + t]).y;
+            const float im = cmulc(v[i], pf[nidx<W>(i, t)]).y;
             gy += (double)(-(a.sy[ky] * mk) * im);
             gx += (double)(-(a.sx[kx] * mk) * im);
           }
         }
       }
-      if (a.step_probe) {
-        float2* fp = a.fprobe + ((size_t)b * a.Mp + p) * WW;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) fp[i * T + t] = v[i];
-      }
+      if (a.step_probe) st_native<W>(a.fprobe + ((size_t)b * a.Mp + p) * WW, v);
       if (a.step_pos) {
         block_sum2(gy, gx, red);
         if (t == 0) {
@@ -494,8 +578,14 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       break;
     }
 
-    // ------------------------------------------------ inverse FFT
-    F::inverse(v, xbuf, tw1, tw2);
+    // ------------------------------------------------ inverse FFT (next operand copied in
+    // behind its register-only last round)
+    F::inverse_head(v, xbuf, tw1, tw2);
+    if (s + 1 < nsteps) {
+      __syncthreads();   // every thread has finished reading the exchange buffer
+      issue_x(s + 1);
+    }
+    F::inverse_tail(v, tw1);
   }
 }
 
@@ -514,8 +604,7 @@ __global__ void __launch_bounds__(Geo<W>::T) grad_windows_kernel(float2* buf, co
   const int t = threadIdx.x;
   float2* win = buf + (size_t)blockIdx.x * W * W;
   float2 v[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = win[i * G::T + t];
+  ld_native<W>(win, v);
   __syncthreads();
   WinFFT<W>::forward(v, xbuf, tw1, tw2);
 #pragma unroll
@@ -652,7 +741,7 @@ __global__ void __launch_bounds__(Geo<W>::T) probe_final_kernel(const float2* __
 #pragma unroll
   for (int i = 0; i < 32; ++i) {
     float2 s = make_float2(0.f, 0.f);
-    for (int c = 0; c < nchunk; ++c) s = cadd(s, partial[((size_t)c * Mp + p) * WW + i * G::T + t]);
+    for (int c = 0; c < nchunk; ++c) s = cadd(s, partial[((size_t)c * Mp + p) * WW + nidx<W>(i, t)]);
     v[i] = cscale(s, mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
   }
   WinFFT<W>::inverse(v, xbuf, tw1, tw2);
@@ -666,7 +755,8 @@ __global__ void __launch_bounds__(Geo<W>::T) probe_final_kernel(const float2* __
 static __global__ void finalize_scalars_kernel(const double* __restrict__ loss_part,
                                         const double* __restrict__ pos_part, const int* __restrict__ seq,
                                         int nseq, int Mp, int W, double loss_weight, int step_pos,
-                                        double* __restrict__ loss_sse, float* __restrict__ pos_grad) {
+                                        const int* __restrict__ err, double* __restrict__ loss_sse,
+                                        float* __restrict__ pos_grad) {
   __shared__ double red[64];
   double a = 0.0, b = 0.0;
   for (int i = threadIdx.x; i < nseq; i += blockDim.x) {
@@ -675,7 +765,9 @@ static __global__ void finalize_scalars_kernel(const double* __restrict__ loss_p
   }
   block_sum2(a, b, red);
   if (threadIdx.x == 0) {
-    loss_sse[0] = a * loss_weight;
+    // a device-side wait that ran out leaves the result unusable: report it as a NaN loss
+    const bool failed = err != nullptr && *err != 0;
+    loss_sse[0] = failed ? __longlong_as_double(0x7ff8000000000000ll) : a * loss_weight;
     loss_sse[1] = b;
   }
   if (!step_pos) return;

@@ -238,8 +238,24 @@ struct WinFFT {
   // frequency layout -> real layout, unnormalised, exp(+2 pi i ...) kernel (no 1/W^2)
   static __device__ __forceinline__ void inverse(float2 (&v)[32], float2* xbuf,
                                                  const float2* tw1, const float2* tw2) {
+    inverse_head(v, xbuf, tw1, tw2);
+    inverse_tail(v, tw1);
+  }
+
+  // The register-only end of the inverse transform (round 1): callers that reuse xbuf may
+  // run inverse_head (everything up to the last xbuf read), synchronise, refill xbuf
+  // asynchronously, and then run inverse_tail while the copy is in flight.
+  static __device__ __forceinline__ void inverse_tail(float2 (&v)[32], const float2* tw1) {
+    const int n2 = threadIdx.x % A;
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmulc(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
+    DFT<32, +1>::template run<32, 1, 0>(v);
+  }
+
+  // inverse() without its register-only tail: after it returns (and a barrier), xbuf is free.
+  static __device__ __forceinline__ void inverse_head(float2 (&v)[32], float2* xbuf,
+                                                      const float2* tw1, const float2* tw2) {
     const int t = threadIdx.x;
-    // ---- round 3 inverse
     {
       const int g = t % S3, j1 = t / S3;
       static_for<0, Q>([&](auto QQ) { DFT<Bq, +1>::template run<32, 1, decltype(QQ)::value * Bq>(v); });
@@ -250,7 +266,6 @@ struct WinFFT {
         for (int m2 = 0; m2 < Bq; ++m2) xbuf[x2(m2 * C + j1, g + S3 * q)] = v[q * Bq + m2];
     }
     __syncthreads();
-    // ---- round 2 inverse
     {
       const int k1 = t % 32, m2 = t / 32;
 #pragma unroll
@@ -274,17 +289,109 @@ struct WinFFT {
         for (int n2 = 0; n2 < A; ++n2) xbuf[x1((Bq * m1 + m2) * A + n2, k1)] = v[m1 * A + n2];
     }
     __syncthreads();
-    // ---- round 1 inverse
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) v[k1] = xbuf[x1(t, k1)];
-    {
-      const int n2 = t % A;
-#pragma unroll
-      for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmulc(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
-    }
-    DFT<32, +1>::template run<32, 1, 0>(v);
   }
 };
+
+// ------------------------------------------------------------------ native window layout
+// Windows that live only inside the library are stored in the order the FFT threads own
+// them: element i of thread t at float2 offset 2*((i/2)*T + t) + i%2. A thread's element
+// pair (2j, 2j+1) is one 16-byte word and a warp touches 512 contiguous bytes per access.
+// Elements i < 2j of every thread form one contiguous prefix (2j*T float2).
+template <int W>
+__device__ __forceinline__ int nidx(int i, int t) {
+  return 2 * ((i >> 1) * Geo<W>::T + t) + (i & 1);
+}
+
+template <int W>
+__device__ __forceinline__ void ld_native(const float2* base, float2 (&v)[32]) {
+  const float4* p = reinterpret_cast<const float4*>(base);
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const float4 q = p[j * Geo<W>::T + t];
+    v[2 * j] = make_float2(q.x, q.y);
+    v[2 * j + 1] = make_float2(q.z, q.w);
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void st_native(float2* base, const float2 (&v)[32]) {
+  float4* p = reinterpret_cast<float4*>(base);
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) p[j * Geo<W>::T + t] = make_float4(v[2 * j].x, v[2 * j].y, v[2 * j + 1].x, v[2 * j + 1].y);
+}
+
+// ------------------------------------------------------------------ bulk async copies
+// One-dimensional TMA bulk copies global -> shared completed on an mbarrier, with bounded
+// waits: a wait that runs out sets *err and returns instead of spinning forever.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// orders this thread's earlier generic-proxy shared-memory accesses before later
+// async-proxy (TMA) accesses
+__device__ __forceinline__ void fence_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// the same for global memory written with ordinary stores and read back by TMA
+__device__ __forceinline__ void fence_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+constexpr int kMbarWaitLimit = 1 << 20;   // try_wait rounds before a wait is declared failed
+
+__device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t& parity, int* err) {
+  for (int it = 0; !mbar_try_wait(bar, parity); ++it) {
+    if (it >= kMbarWaitLimit) {
+      if (err) *err = 1;
+      break;
+    }
+  }
+  parity ^= 1u;
+}
+
+// Issue (one thread) a copy of `bytes` from global `src` into shared `dst` in chunks of at
+// most 64 KiB, all completing on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  mbar_expect_tx(bar, bytes);
+  constexpr uint32_t kChunk = 64u * 1024u;
+  for (uint32_t o = 0; o < bytes; o += kChunk) {
+    const uint32_t n = bytes - o < kChunk ? bytes - o : kChunk;
+    bulk_copy_g2s(static_cast<char*>(dst) + o, static_cast<const char*>(src) + o, n, bar);
+  }
+}
 
 // Host/device builder of the twiddle tables in global memory (see load_twiddles).
 template <int W>
