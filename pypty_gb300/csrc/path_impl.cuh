@@ -28,6 +28,7 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   prof_mark(st, KID_TWIDDLES);
   build_twiddles_kernel<W><<<1, 256, 0, st>>>(tw);
   TableArgs ta{};
+  ta.pyx = at<float2>(ws, q.o_pyx);
   ta.mask = at<float>(ws, q.o_mask);
   ta.mask_sc = at<float>(ws, q.o_mask_sc);
   ta.prop = at<float2>(ws, q.o_prop);
@@ -95,6 +96,8 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
     fa.obl = wa.out;
     fa.prop = ta.prop;
     fa.prop_edge = ta.prop_edge;
+    fa.pyx = ta.pyx;
+    fa.use_sep = p->smooth_rolloff == 0.0f ? 1 : 0;
     fa.mask = ta.mask;
     fa.sx = ta.sx;
     fa.sy = ta.sy;

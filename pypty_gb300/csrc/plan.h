@@ -18,7 +18,7 @@ inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 // Byte offsets of every buffer inside the caller's workspace.
 struct Plan {
   int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
-  size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_sx, o_sy, o_probe_f;
+  size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_pyx, o_sx, o_sy, o_probe_f;
   size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
   size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, total;
 };
@@ -64,6 +64,7 @@ inline Plan make_plan(const pty_problem_t* p) {
   q.o_mask_sc = take(WW * f4);
   q.o_prop = take(WW * c8);
   q.o_prop_edge = take(WW * c8);
+  q.o_pyx = take(2 * (size_t)q.W * c8);
   q.o_sx = take(q.W * f4);
   q.o_sy = take(q.W * f4);
   q.o_probe_f = take(q.Mp * WW * c8);

@@ -27,6 +27,7 @@ enum Algorithm : int { ALG_LSQ_SQRT = 0, ALG_ML = 1, ALG_LSQ = 2, ALG_LSQ_SQRT_2
 // sx, sy      float32(-6.2831855 * fftfreq(W)) : sub-pixel shift exponents
 //             (pypty/objective.py:308-313), multiplied by mask where used
 struct TableArgs {
+  float2* pyx;          // separable propagator factors: exp(i a lambda qy^2) [W], exp(i a lambda qx^2)/W^2 [W]
   float* mask;
   float* mask_sc;
   float2* prop;
@@ -56,6 +57,16 @@ __global__ void tables_kernel(TableArgs a) {
     const int kk = (idx < W / 2) ? idx : idx - W;
     a.sx[idx] = (float)(-6.2831855 * ((double)kk / (double)W));
     a.sy[idx] = a.sx[idx];
+    // exp(-i pi d lambda (qx^2 + qy^2)) = exp(-i pi d lambda qy^2) * exp(-i pi d lambda qx^2); the
+    // factored phases differ from the reference's single float32 phase by one rounding
+    const float a_pd = __fmul_rn(-3.141592654f, a.distance);
+    const float qyk = fftfreq_f32(idx, W, a.py), qxk = fftfreq_f32(idx, W, a.px);
+    float sy_, cy_, sx_, cx_;
+    sincosf(__fmul_rn(a_pd, __fmul_rn(a.wavelength, __fmul_rn(qyk, qyk))), &sy_, &cy_);
+    sincosf(__fmul_rn(a_pd, __fmul_rn(a.wavelength, __fmul_rn(qxk, qxk))), &sx_, &cx_);
+    const float inv_ww = 1.0f / (float)(W * W);
+    a.pyx[idx] = make_float2(cy_, sy_);
+    a.pyx[W + idx] = make_float2(cx_ * inv_ww, sx_ * inv_ww);
   }
   if (idx >= W * W) return;
   const int ky = idx / W, kx = idx % W;
@@ -223,6 +234,8 @@ struct FusedArgs {
   const float2* obl;        // band-limited object windows, native real [Bb*Z*Mo]
   const float2* prop;       // natural (ky, kx), scaled by 1/W^2
   const float2* prop_edge;
+  const float2* pyx;        // separable propagator factors (used when the mask is binary)
+  int use_sep;
   const float* mask;        // natural, unscaled
   const float* sx;
   const float* sy;
@@ -292,9 +305,11 @@ __device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& 
 // first NST elements per thread of the adjoint step's object window, and two mbarriers.
 template <int W>
 struct FusedSmem {
-  static constexpr int NST = (W == 128) ? 24 : 16;
+  static constexpr int NST = (W == 128) ? 22 : 16;
   static constexpr size_t side_off = Smem<W>::bytes;
-  static constexpr size_t bar_off = side_off + sizeof(float2) * NST * Geo<W>::T;
+  static constexpr size_t pyx_off = side_off + sizeof(float2) * NST * Geo<W>::T;
+  static constexpr size_t bits_off = pyx_off + sizeof(float2) * 2 * W;
+  static constexpr size_t bar_off = bits_off + sizeof(uint32_t) * Geo<W>::T;
   static constexpr size_t bytes = bar_off + 2 * sizeof(uint64_t);
 };
 
@@ -328,6 +343,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   double* red;
   carve<W>(smem, xbuf, tw1, tw2, red);
   float2* side = reinterpret_cast<float2*>(smem + S::side_off);
+  float2* spy = reinterpret_cast<float2*>(smem + S::pyx_off);   // [W] y factor, then [W] x factor
+  const float2* spx = spy + W;
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem + S::bits_off);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);   // [0]: xbuf, [1]: side
   float* fs0 = reinterpret_cast<float*>(xbuf);   // WW floats: this block's |Psi|^2
   float* fs1 = fs0 + WW;                          // WW floats: mode-summed I, then dL/dI
@@ -347,6 +365,14 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     fence_async_shared();
   }
   load_twiddles<W>(tw1, tw2, a.tw);
+  for (int i = t; i < 2 * W; i += T) spy[i] = a.pyx[i];
+  // bit i: element i (frequency layout) of this thread lies inside the band limit
+  {
+    uint32_t mbits = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) mbits |= (a.mask[G::fky(t, i) * W + G::fkx(t, i)] != 0.0f ? 1u : 0u) << i;
+    sbits[t] = mbits;   // kept in shared memory: registers are needed for the window
+  }
   __syncthreads();
   uint32_t ph_x = 0, ph_side = 0;
 
@@ -434,12 +460,28 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
             x4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
           }
           cluster.sync();
+          // this block sums elements p, p + Mp, ... (two at a time, loads independent)
 #pragma unroll 1
-          for (int i = p; i < 32; i += a.Mp) {
-            float2 acc = make_float2(0.f, 0.f);
-            const int e = nidx<W>(i, t);
-            for (int pp = 0; pp < a.Mp; ++pp) acc = cadd(acc, cluster.map_shared_rank(xbuf, pp + m * a.Mp)[e]);
-            gs[e] = acc;
+          for (int i0 = p; i0 < 32; i0 += 2 * a.Mp) {
+            float2 acc[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) acc[k] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int pp = 0; pp < 8; ++pp) {   // probe modes in ascending order
+              if (pp < a.Mp) {
+                const float2* rb = cluster.map_shared_rank(xbuf, pp + m * a.Mp);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                  const int i = i0 + k * a.Mp;
+                  if (i < 32) acc[k] = cadd(acc[k], rb[nidx<W>(i, t)]);
+                }
+              }
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              const int i = i0 + k * a.Mp;
+              if (i < 32) gs[nidx<W>(i, t)] = acc[k];
+            }
           }
           cluster.sync();
         }
@@ -500,9 +542,18 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         v[i] = cscale(cmul(pf[nidx<W>(i, t)], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
       }
     } else if (fwd && z < Z - 1) {
-      const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
+      if (a.use_sep && !(z == 0 && a.use_edge)) {
+        const uint32_t mbits = sbits[t];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+        for (int i = 0; i < 32; ++i) {
+          const float2 P = cmul(spy[G::fky(t, i)], spx[G::fkx(t, i)]);
+          v[i] = ((mbits >> i) & 1u) ? cmul(v[i], P) : make_float2(0.f, 0.f);
+        }
+      } else {
+        const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+      }
     } else if (fwd) {
       // far field: Psi = FFT(exit) * mask, I = mean over modes |Psi|^2 (objective.py:501-512)
       __syncthreads();
@@ -513,10 +564,20 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       }
       cluster.sync();
 #pragma unroll 1
-      for (int i = 0; i < 32; ++i) {
-        float acc = 0.0f;
-        for (int r = 0; r < nmodes; ++r) acc += cluster.map_shared_rank(fs0, r)[i * T + t];
-        fs1[i * T + t] = acc;
+      for (int i0 = 0; i0 < 32; i0 += 8) {
+        float acc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc[k] = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {      // ranks in ascending order: a fixed summation order
+          if (r < nmodes) {
+            const float* rb = cluster.map_shared_rank(fs0, r);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc[k] += rb[(i0 + k) * T + t];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) fs1[(i0 + k) * T + t] = acc[k];
       }
       cluster.sync();   // every block is done reading this block's intensities
       const float inv_modes = 1.0f / (float)nmodes;
@@ -546,9 +607,18 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = cscale(cscale(v[i], fs1[i * T + t]), a.loss_weight);
     } else if (z > 0) {
-      const float2* pr = (z == 1 && a.use_edge) ? a.prop_edge : a.prop;
+      if (a.use_sep && !(z == 1 && a.use_edge)) {
+        const uint32_t mbits = sbits[t];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+        for (int i = 0; i < 32; ++i) {
+          const float2 P = cmul(spy[G::fky(t, i)], spx[G::fkx(t, i)]);
+          v[i] = ((mbits >> i) & 1u) ? cmulc(v[i], P) : make_float2(0.f, 0.f);
+        }
+      } else {
+        const float2* pr = (z == 1 && a.use_edge) ? a.prop_edge : a.prop;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
+      }
     } else {
       // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
       const float2* pf = a.probe_f + (size_t)p * WW;
