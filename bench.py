@@ -150,23 +150,32 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(cfg, wl, n_sample, algorithm, budget_s=25.0):
+def cpu_baseline(cfg, wl, algorithm, budget_s=15.0):
     """The oracle (NumPy restatement of the reference path) on a bounded sample of positions,
-    on all host cores (scipy.fft workers)."""
+    on all host cores (scipy.fft workers): a short calibration call sizes the sample so that
+    the timed call takes about `budget_s` seconds."""
     import scipy.fft
     from oracle import ptycho_oracle as orc
     cores = os.cpu_count() or 1
-    seq = np.arange(n_sample)
-    meas = np.zeros((n_sample, cfg["W"], cfg["W"]), np.float32) + 1.0
-    with scipy.fft.set_workers(cores):
+    n_max = wl["ipos"].shape[0]
+
+    def run(n):
+        seq = np.arange(n)
+        meas = np.zeros((n, cfg["W"], cfg["W"]), np.float32) + 1.0
         t0 = time.perf_counter()
-        orc.loss_and_direction(wl["obj0"], wl["probe"], wl["ipos"][:n_sample], wl["corr"][:n_sample], wl["dz"],
-                               1.0, meas, algorithm, wl["wavelength"], 1, 1, 1, wl["px"], wl["px"], 2 / 3, 0.0,
-                               seq, 1, n_sample)
-        dt = time.perf_counter() - t0
-    return {"value": n_sample / dt, "unit": "positions/s", "cores": cores, "kind": "port",
+        orc.loss_and_direction(wl["obj0"], wl["probe"], wl["ipos"][:n], wl["corr"][:n], wl["dz"], 1.0, meas,
+                               algorithm, wl["wavelength"], 1, 1, 1, wl["px"], wl["px"], 2 / 3, 0.0, seq, 1,
+                               cfg["batch"])
+        return time.perf_counter() - t0
+
+    with scipy.fft.set_workers(cores):
+        n0 = min(4, n_max)
+        t_cal = run(n0)
+        n = int(max(n0, min(n_max, budget_s * n0 / max(t_cal, 1e-6))))
+        dt = run(n)
+    return {"value": n / dt, "unit": "positions/s", "cores": cores, "kind": "port",
             "sample": "%d positions of the %s workload (NumPy/SciPy oracle, complex64, %.1f s)" % (
-                n_sample, cfg["name"], dt), "seconds": dt}
+                n, cfg["name"], dt), "seconds": dt, "positions": n}
 
 
 def run_reference(args, cfg):
@@ -175,15 +184,15 @@ def run_reference(args, cfg):
     if rank != 0:
         return
     wl = build_workload(cfg)
-    n_sample = 8 if cfg["W"] == 128 else 64
-    for _ in range(args.warmup if args.warmup > 0 else 0):
-        pass   # the oracle has no warm-up state; warm-up steps would only lengthen the run
+    # each step times a bounded sample; the whole run stays within a few minutes
+    budget = max(2.0, min(15.0, 150.0 / max(args.steps, 1)))
     vals = []
     last = None
     for _ in range(max(args.steps, 1)):
-        last = cpu_baseline(cfg, wl, n_sample, cfg["algorithm"])
+        last = cpu_baseline(cfg, wl, cfg["algorithm"], budget_s=budget)
         vals.append(last["value"])
     value = float(np.mean(vals))
+    n_sample = last["positions"]
     line = {"metric": "positions/s fwd+adjoint", "value": value, "unit": "positions/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n_sample / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
@@ -356,9 +365,9 @@ def main():
         "loss": loss_val,
     }
     if not args.no_cpu_baseline:
-        n_sample = 8 if W == 128 else 64
-        cb = cpu_baseline(cfg, wl, n_sample, cfg["algorithm"])
+        cb = cpu_baseline(cfg, wl, cfg["algorithm"])
         cb.pop("seconds", None)
+        cb.pop("positions", None)
         line["cpu_baseline"] = cb
     print(json.dumps(line))
     if world > 1:
