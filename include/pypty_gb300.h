@@ -108,6 +108,25 @@ int pty_simulate_patterns(const pty_problem_t* problem, const void* obj, const v
                           size_t workspace_bytes, void* stream);
 
 /*
+ * The same computation as pty_loss_and_direction split into its two halves, for autograd
+ * and for callers that want the loss before deciding on a gradient. pty_forward runs the
+ * forward multislice and the loss for every position of the sequence (compute_batch is
+ * ignored: one batch) and keeps the wave stack and dL/d(exit wave) in the workspace;
+ * pty_backward, called later on the same stream with the same problem and the same
+ * untouched workspace, runs the adjoint and writes the gradients (and loss_sse again).
+ * No counterpart in the reference, which always computes both (pypty/objective.py:47).
+ * The workspace size is pty_split_workspace_bytes (it holds every position at once).
+ */
+int pty_split_workspace_bytes(const pty_problem_t* problem, size_t* bytes);
+int pty_forward(const pty_problem_t* problem, const void* obj, const void* probe,
+                const int32_t* positions_host, const float* pos_correction_host,
+                const int32_t* sequence_host, const float* measured, double* loss_sse,
+                void* workspace, size_t workspace_bytes, void* stream);
+int pty_backward(const pty_problem_t* problem, double* loss_sse, void* object_grad,
+                 void* probe_grad, float* pos_grad, void* workspace, size_t workspace_bytes,
+                 void* stream);
+
+/*
  * Batched 2D FFT of `batch` contiguous W x W complex64 windows (W = 64 or 128).
  * inverse = 0: unnormalised forward transform; inverse = 1: inverse scaled by 1/W^2.
  * shift = 1 applies fftshift to the forward output / ifftshift to the inverse input.

@@ -63,6 +63,9 @@ SIGNATURES = {
     "pty_simulate_patterns": ([_PP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fft2": ([_VP, _VP, _I32, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fft2_workspace_bytes": ([_I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_split_workspace_bytes": ([_PP, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_forward": ([_PP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_backward": ([_PP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_profile_begin": ([_I32], ctypes.c_int),
     "pty_profile_end": ([_F64P, _I32P, _I32], ctypes.c_int),
     "pty_kernel_name": ([_I32], ctypes.c_char_p),
@@ -99,6 +102,12 @@ def lib(build_if_missing: bool = False) -> ctypes.CDLL:
 def check(status: int, what: str) -> None:
     if status != PTY_OK:
         raise PtyError(status, what)
+
+
+def split_workspace_bytes(problem: Problem) -> int:
+    n = _SZ(0)
+    check(lib().pty_split_workspace_bytes(ctypes.byref(problem), ctypes.byref(n)), "pty_split_workspace_bytes")
+    return int(n.value)
 
 
 def workspace_bytes(problem: Problem) -> int:

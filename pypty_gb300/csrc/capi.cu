@@ -170,6 +170,50 @@ int pty_simulate_patterns(const pty_problem_t* problem, const void* obj, const v
                     nullptr, nullptr, nullptr, patterns, workspace, workspace_bytes, stream);
 }
 
+int pty_split_workspace_bytes(const pty_problem_t* problem, size_t* bytes) {
+  int rc = validate(problem);
+  if (rc) return rc;
+  if (!bytes) return PTY_ERR_INVALID;
+  *bytes = make_plan(problem, true).total;
+  return PTY_OK;
+}
+
+int pty_forward(const pty_problem_t* problem, const void* obj, const void* probe, const int32_t* positions_host,
+                const float* pos_correction_host, const int32_t* sequence_host, const float* measured,
+                double* loss_sse, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc = validate(problem);
+  if (rc) return rc;
+  if (!obj || !probe || !positions_host || !sequence_host || !measured || !loss_sse || !workspace)
+    return PTY_ERR_INVALID;
+  if ((rc = check_geometry(problem, positions_host, sequence_host))) return rc;
+  const Plan q = make_plan(problem, true);
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((rc = upload_geometry(problem, q, workspace, positions_host, pos_correction_host, sequence_host, st)))
+    return rc;
+  const float2* o = static_cast<const float2*>(obj);
+  const float2* pr = static_cast<const float2*>(probe);
+  if (q.W == 64) return run_forward<64>(problem, q, o, pr, measured, loss_sse, workspace, st);
+  return run_forward<128>(problem, q, o, pr, measured, loss_sse, workspace, st);
+}
+
+int pty_backward(const pty_problem_t* problem, double* loss_sse, void* object_grad, void* probe_grad,
+                 float* pos_grad, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc = validate(problem);
+  if (rc) return rc;
+  if (!loss_sse || !workspace) return PTY_ERR_INVALID;
+  if ((problem->step_obj && !object_grad) || (problem->step_probe && !probe_grad) ||
+      (problem->step_pos && !pos_grad))
+    return PTY_ERR_INVALID;
+  const Plan q = make_plan(problem, true);
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  float2* og = static_cast<float2*>(object_grad);
+  float2* pg = static_cast<float2*>(probe_grad);
+  if (q.W == 64) return run_backward<64>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
+  return run_backward<128>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
+}
+
 int pty_fft2_workspace_bytes(int32_t window, size_t* bytes) {
   if (window != 64 && window != 128) return PTY_ERR_UNSUPPORTED;
   if (!bytes) return PTY_ERR_INVALID;

@@ -4,5 +4,9 @@
 namespace pty {
 template int run_path<64>(const pty_problem_t*, const Plan&, const float2*, const float2*, const float*,
                           double*, float2*, float2*, float*, float*, void*, cudaStream_t);
+template int run_forward<64>(const pty_problem_t*, const Plan&, const float2*, const float2*, const float*,
+                             double*, void*, cudaStream_t);
+template int run_backward<64>(const pty_problem_t*, const Plan&, double*, float2*, float2*, float*, void*,
+                              cudaStream_t);
 template int run_fft2<64>(const float2*, float2*, int, int, int, float2*, cudaStream_t);
 }  // namespace pty

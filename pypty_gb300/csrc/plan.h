@@ -20,7 +20,8 @@ struct Plan {
   int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
   size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_pyx, o_sx, o_sy, o_probe_f;
   size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
-  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, total;
+  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, o_gbuf, total;
+  bool split;   // one batch with every position: pty_forward / pty_backward
 };
 
 inline int tw_count(int W) { return W == 64 ? Geo<64>::TW1 + Geo<64>::TW2 : Geo<128>::TW1 + Geo<128>::TW2; }
@@ -38,8 +39,11 @@ inline int validate(const pty_problem_t* p) {
   return PTY_OK;
 }
 
-inline Plan make_plan(const pty_problem_t* p) {
+// split = true plans one batch holding every position of the sequence, kept in the
+// workspace between pty_forward and pty_backward.
+inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   Plan q{};
+  q.split = split;
   q.W = p->window;
   q.Ny = p->obj_ny;
   q.Nx = p->obj_nx;
@@ -48,7 +52,7 @@ inline Plan make_plan(const pty_problem_t* p) {
   q.Mp = p->n_probe_modes;
   q.N = p->n_positions;
   q.nseq = p->n_sequence;
-  q.Bb = std::min(p->compute_batch, p->n_sequence);
+  q.Bb = split ? p->n_sequence : std::min(p->compute_batch, p->n_sequence);
   q.nbatch = (q.nseq + q.Bb - 1) / q.Bb;
   q.zm = q.Z * q.Mo;
   q.ntx = (q.Nx + kTileSize - 1) / kTileSize;
@@ -84,6 +88,7 @@ inline Plan make_plan(const pty_problem_t* p) {
   q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
   q.o_sim = take((size_t)q.Bb * WW * f4);
   q.o_err = take(sizeof(int));
+  q.o_gbuf = take(split ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
   q.total = o;
   return q;
 }
@@ -126,6 +131,14 @@ template <int W>
 int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const float2* probe,
              const float* measured, double* loss_sse, float2* object_grad, float2* probe_grad,
              float* pos_grad, float* patterns, void* ws, cudaStream_t st);
+
+template <int W>
+int run_forward(const pty_problem_t* p, const Plan& q, const float2* obj, const float2* probe,
+                const float* measured, double* loss_sse, void* ws, cudaStream_t st);
+
+template <int W>
+int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2* object_grad,
+                 float2* probe_grad, float* pos_grad, void* ws, cudaStream_t st);
 
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st);

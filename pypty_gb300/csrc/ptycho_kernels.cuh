@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(Geo<W>::T) object_windows_kernel(WindowArgs a)
 // ------------------------------------------------------------------ fused multislice
 struct FusedArgs {
   int Z, Mp, Mo, algorithm, step_obj, step_probe, step_pos, probe_shift, simulate, use_edge;
+  int phase;                // 0: whole pass; 1: forward half; 2: adjoint half
   float loss_weight;
   const float2* probe;      // (W, W, Mp) reference layout (used without probe shift)
   const float2* probe_f;    // native frequency layout [Mp]
@@ -246,6 +247,7 @@ struct FusedArgs {
   float2* stack;            // conj input waves, native real [Bb*Z*Mp*Mo]
   float2* gsum;             // probe-mode-summed object gradient, native real [Bb*Z*Mo]
   float2* fprobe;           // FFT of the per-position probe gradient, native freq [Bb*Mp]
+  float2* gbuf;             // dL/d(exit wave) between the two halves, native real [Bb*Mp*Mo]
   double* loss_part;        // [Bb][2]
   double* pos_part;         // [Bb][Mp][2]
   float* sim_out;           // [Bb][W][W] simulated mean intensity (detector order)
@@ -398,9 +400,18 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   };
 
   float2 v[32];
-  const int nsteps = a.simulate ? Z + 1 : 2 * Z + 1;
-  if (!a.probe_shift) issue_x(1);   // step 0 has no inverse transform to hide the copy behind
-  for (int s = 0; s < nsteps; ++s) {
+  float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
+  const int s_begin = (a.phase == 2) ? Z + 1 : 0;
+  const int s_end = (a.simulate || a.phase == 1) ? Z + 1 : 2 * Z + 1;
+  if (a.phase == 2) {
+    // adjoint half: resume from dL/d(exit wave) kept by the forward half
+    ld_native<W>(gb, v);
+    issue_x(Z + 1);
+    if (adj_stack) issue_side(Z - 1);
+  } else if (!a.probe_shift) {
+    issue_x(1);   // step 0 has no inverse transform to hide the copy behind
+  }
+  for (int s = s_begin; s < s_end; ++s) {
     const bool fwd = (s >= 1 && s <= Z);
     const int z = fwd ? s - 1 : 2 * Z - s;
 
@@ -418,7 +429,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         st_native<W>(stack_ptr(z), c);
         fence_async_global();   // these stores are read back by TMA in the adjoint
       }
-      if (z == Z - 1 && adj_stack) issue_side(Z - 1);
+      if (z == Z - 1 && adj_stack && a.phase == 0) issue_side(Z - 1);
       mbar_wait(&bars[0], ph_x, a.err);
       {
         const float4* ob = reinterpret_cast<const float4*>(xbuf);
@@ -651,12 +662,13 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // ------------------------------------------------ inverse FFT (next operand copied in
     // behind its register-only last round)
     F::inverse_head(v, xbuf, tw1, tw2);
-    if (s + 1 < nsteps) {
+    if (s + 1 < s_end) {
       __syncthreads();   // every thread has finished reading the exchange buffer
       issue_x(s + 1);
     }
     F::inverse_tail(v, tw1);
   }
+  if (a.phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
 }
 
 // ------------------------------------------------------------------ gradient windows

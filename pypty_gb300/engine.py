@@ -131,6 +131,36 @@ class Engine:
         _lib.check(st, "pty_loss_and_direction")
         return loss_sse, og, pg, posg
 
+    def forward(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
+                measured: torch.Tensor, stream=None):
+        """Forward half (pty_forward): returns (loss_sse, workspace). The workspace holds the
+        wave stack and dL/d(exit wave) of every position until `backward` consumes it."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        self._check_inputs(problem, obj, probe, measured)
+        ws = torch.empty(max(_lib.split_workspace_bytes(problem), 256), dtype=torch.uint8, device=self.device)
+        loss_sse = torch.empty(2, dtype=torch.float64, device=self.device)
+        pp, pc, ps = self._staging(geo)
+        st = _lib.lib().pty_forward(ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
+                                    _ptr(loss_sse), _ptr(ws), ws.numel(), stream.cuda_stream)
+        self._mark_staging(stream)
+        _lib.check(st, "pty_forward")
+        return loss_sse, ws
+
+    def backward(self, problem: _lib.Problem, ws: torch.Tensor, stream=None):
+        """Adjoint half (pty_backward) on the workspace of `forward`: returns (loss_sse,
+        object_grad, probe_grad, pos_grad) with the shapes of loss_and_direction."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        W = problem.window
+        loss_sse = torch.empty(2, dtype=torch.float64, device=self.device)
+        og = torch.empty((problem.obj_ny, problem.obj_nx, problem.n_slices, problem.n_obj_modes),
+                         dtype=torch.complex64, device=self.device)
+        pg = torch.empty((W, W, problem.n_probe_modes), dtype=torch.complex64, device=self.device)
+        posg = torch.empty((problem.n_positions, 2), dtype=torch.float32, device=self.device)
+        st = _lib.lib().pty_backward(ctypes.byref(problem), _ptr(loss_sse), _ptr(og), _ptr(pg), _ptr(posg),
+                                     _ptr(ws), ws.numel(), stream.cuda_stream)
+        _lib.check(st, "pty_backward")
+        return loss_sse, og, pg, posg
+
     def simulate(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
                  out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         """Mean-over-modes far-field patterns (n_sequence, W, W) float32, detector order."""
