@@ -127,6 +127,41 @@ int pty_backward(const pty_problem_t* problem, double* loss_sse, void* object_gr
                  void* stream);
 
 /*
+ * The multislice_core functions on caller-given windows, reference layouts (modes innermost):
+ *   probe_b   (batch, W, W, Mp)          incoming probe of every position
+ *   obj_b     (batch, W, W, Z, Mo)       object windows (already band-limited by the caller)
+ *   propagator (W, W) complex64          Fresnel propagator with the mask applied
+ *   waves     (batch, W, W, Z, Mp, Mo)   conjugated input wave of every slice
+ *   exit_wave / d_exit (batch, W, W, Mp, Mo)
+ *   mask_clean (W, W) float32            band limit of the gradient windows
+ *   object_grad (obj_ny, obj_nx, Z, Mo)  accumulated (+=), as the reference does
+ *   probe_grad (batch, W, W, Mp)         sum over object modes of the probe-plane gradient
+ * pty_multislice replaces pypty.multislice_core.multislice (pypty/multislice_core.py:9-82,
+ * one slice distance, no tilts); pty_multislice_grads replaces multislice_grads
+ * (pypty/multislice_core.py:85-200, no tilts; positions_host (batch, 2) are the windows'
+ * top-left pixels, i.e. masked_pixels_y/x[:, 0, 0]); pty_scatteradd replaces scatteradd
+ * (pypty/multislice_core.py:206-230) for window-shaped index arrays: chop (batch, W, W,
+ * n_planes) is added into full (obj_ny, obj_nx, n_planes) in position order without atomics.
+ */
+int pty_multislice_workspace_bytes(int32_t batch, int32_t window, int32_t n_slices, int32_t n_probe_modes,
+                                   int32_t n_obj_modes, int32_t obj_ny, int32_t obj_nx, size_t* bytes);
+int pty_multislice(const void* probe_b, const void* obj_b, const void* propagator, float edge_mult,
+                   int32_t batch, int32_t window, int32_t n_slices, int32_t n_probe_modes,
+                   int32_t n_obj_modes, void* waves, void* exit_wave, void* workspace,
+                   size_t workspace_bytes, void* stream);
+int pty_multislice_grads(const void* d_exit, const void* waves, const void* obj_b, const void* propagator,
+                         float edge_mult, const float* mask_clean, const int32_t* positions_host,
+                         int32_t batch, int32_t window, int32_t n_slices, int32_t n_probe_modes,
+                         int32_t n_obj_modes, int32_t obj_ny, int32_t obj_nx, int32_t step_obj,
+                         void* object_grad, void* probe_grad, void* workspace, size_t workspace_bytes,
+                         void* stream);
+int pty_scatteradd_workspace_bytes(int32_t batch, int32_t window, int32_t n_planes, int32_t obj_ny,
+                                   int32_t obj_nx, size_t* bytes);
+int pty_scatteradd(void* full, int32_t obj_ny, int32_t obj_nx, int32_t n_planes,
+                   const int32_t* positions_host, int32_t batch, int32_t window, const void* chop,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Batched 2D FFT of `batch` contiguous W x W complex64 windows (W = 64 or 128).
  * inverse = 0: unnormalised forward transform; inverse = 1: inverse scaled by 1/W^2.
  * shift = 1 applies fftshift to the forward output / ifftshift to the inverse input.

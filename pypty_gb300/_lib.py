@@ -66,6 +66,12 @@ SIGNATURES = {
     "pty_split_workspace_bytes": ([_PP, ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_forward": ([_PP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_backward": ([_PP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_multislice_workspace_bytes": ([_I32] * 7 + [ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_multislice": ([_VP, _VP, _VP, ctypes.c_float] + [_I32] * 5 + [_VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_multislice_grads": ([_VP, _VP, _VP, _VP, ctypes.c_float, _VP, _VP] + [_I32] * 8 +
+                             [_VP, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_scatteradd_workspace_bytes": ([_I32] * 5 + [ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_scatteradd": ([_VP, _I32, _I32, _I32, _VP, _I32, _I32, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_profile_begin": ([_I32], ctypes.c_int),
     "pty_profile_end": ([_F64P, _I32P, _I32], ctypes.c_int),
     "pty_kernel_name": ([_I32], ctypes.c_char_p),

@@ -10,6 +10,11 @@ namespace {
 
 using namespace pty;
 
+__global__ void iota_kernel(int* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
+}
+
 int upload_geometry(const pty_problem_t* p, const Plan& q, void* ws, const int32_t* pos,
                     const float* corr, const int32_t* seq, cudaStream_t st) {
   if (cudaMemcpyAsync(at<int>(ws, q.o_pos), pos, (size_t)q.N * 2 * sizeof(int), cudaMemcpyHostToDevice, st) !=
@@ -64,7 +69,7 @@ Profiler g_prof;
 const char* kKernelNames[KID_COUNT] = {
     "build_twiddles", "tables", "probe_fft", "obj_to_slices", "object_windows", "fused_multislice",
     "grad_windows", "tile_lists", "scatter_tiles", "probe_partial", "slices_to_obj", "probe_final",
-    "finalize_scalars", "fft2_batch"};
+    "finalize_scalars", "fft2_batch", "layout"};
 
 }  // namespace
 
@@ -212,6 +217,99 @@ int pty_backward(const pty_problem_t* problem, double* loss_sse, void* object_gr
   float2* pg = static_cast<float2*>(probe_grad);
   if (q.W == 64) return run_backward<64>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
   return run_backward<128>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
+}
+
+// ------------------------------------------------------------------ multislice_core seams
+static int ms_validate(int32_t B, int32_t W, int32_t Z, int32_t Mp, int32_t Mo, int32_t Ny, int32_t Nx) {
+  if (W != 64 && W != 128) return PTY_ERR_UNSUPPORTED;
+  if (B <= 0 || Z <= 0 || Mp <= 0 || Mo <= 0 || Ny < 0 || Nx < 0) return PTY_ERR_INVALID;
+  if (Mp * Mo > 8) return PTY_ERR_UNSUPPORTED;
+  return PTY_OK;
+}
+
+static int ms_upload_positions(const MsPlan& q, const int32_t* pos, void* ws, cudaStream_t st) {
+  for (int b = 0; b < q.B; ++b) {
+    const int y = pos[2 * b], x = pos[2 * b + 1];
+    if (y < 0 || x < 0 || y + q.W > q.Ny || x + q.W > q.Nx) return PTY_ERR_POSITION;
+  }
+  if (cudaMemcpyAsync(at<int>(ws, q.o_pos), pos, (size_t)q.B * 2 * sizeof(int), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PTY_ERR_CUDA;
+  iota_kernel<<<(q.B + 255) / 256, 256, 0, st>>>(at<int>(ws, q.o_seq), q.B);
+  return cuda_status();
+}
+
+int pty_multislice_workspace_bytes(int32_t batch, int32_t window, int32_t n_slices, int32_t n_probe_modes,
+                                   int32_t n_obj_modes, int32_t obj_ny, int32_t obj_nx, size_t* bytes) {
+  int rc = ms_validate(batch, window, n_slices, n_probe_modes, n_obj_modes, obj_ny, obj_nx);
+  if (rc) return rc;
+  if (!bytes) return PTY_ERR_INVALID;
+  *bytes = make_ms_plan(window, batch, n_slices, n_probe_modes, n_obj_modes, obj_ny, obj_nx).total;
+  return PTY_OK;
+}
+
+int pty_multislice(const void* probe_b, const void* obj_b, const void* propagator, float edge_mult, int32_t batch,
+                   int32_t window, int32_t n_slices, int32_t n_probe_modes, int32_t n_obj_modes, void* waves,
+                   void* exit_wave, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc = ms_validate(batch, window, n_slices, n_probe_modes, n_obj_modes, 0, 0);
+  if (rc) return rc;
+  if (!probe_b || !obj_b || !propagator || !waves || !exit_wave || !workspace) return PTY_ERR_INVALID;
+  const MsPlan q = make_ms_plan(window, batch, n_slices, n_probe_modes, n_obj_modes, 0, 0);
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  iota_kernel<<<(q.B + 255) / 256, 256, 0, st>>>(at<int>(workspace, q.o_seq), q.B);
+  auto f = [](const void* x) { return static_cast<const float2*>(x); };
+  auto g = [](void* x) { return static_cast<float2*>(x); };
+  if (window == 64)
+    return run_ms_forward<64>(q, f(probe_b), f(obj_b), f(propagator), edge_mult, g(waves), g(exit_wave), workspace, st);
+  return run_ms_forward<128>(q, f(probe_b), f(obj_b), f(propagator), edge_mult, g(waves), g(exit_wave), workspace,
+                             st);
+}
+
+int pty_multislice_grads(const void* d_exit, const void* waves, const void* obj_b, const void* propagator,
+                         float edge_mult, const float* mask_clean, const int32_t* positions_host, int32_t batch,
+                         int32_t window, int32_t n_slices, int32_t n_probe_modes, int32_t n_obj_modes,
+                         int32_t obj_ny, int32_t obj_nx, int32_t step_obj, void* object_grad, void* probe_grad,
+                         void* workspace, size_t workspace_bytes, void* stream) {
+  int rc = ms_validate(batch, window, n_slices, n_probe_modes, n_obj_modes, obj_ny, obj_nx);
+  if (rc) return rc;
+  if (!d_exit || !obj_b || !propagator || !workspace) return PTY_ERR_INVALID;
+  if (step_obj && (!waves || !mask_clean || !positions_host || !object_grad)) return PTY_ERR_INVALID;
+  const MsPlan q = make_ms_plan(window, batch, n_slices, n_probe_modes, n_obj_modes, obj_ny, obj_nx);
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (step_obj) {
+    if ((rc = ms_upload_positions(q, positions_host, workspace, st))) return rc;
+  } else {
+    iota_kernel<<<(q.B + 255) / 256, 256, 0, st>>>(at<int>(workspace, q.o_seq), q.B);
+  }
+  auto f = [](const void* x) { return static_cast<const float2*>(x); };
+  auto g = [](void* x) { return static_cast<float2*>(x); };
+  if (window == 64)
+    return run_ms_grads<64>(q, f(d_exit), f(waves), f(obj_b), f(propagator), edge_mult, mask_clean, step_obj ? 1 : 0,
+                            g(object_grad), g(probe_grad), workspace, st);
+  return run_ms_grads<128>(q, f(d_exit), f(waves), f(obj_b), f(propagator), edge_mult, mask_clean, step_obj ? 1 : 0,
+                           g(object_grad), g(probe_grad), workspace, st);
+}
+
+int pty_scatteradd_workspace_bytes(int32_t batch, int32_t window, int32_t n_planes, int32_t obj_ny,
+                                   int32_t obj_nx, size_t* bytes) {
+  return pty_multislice_workspace_bytes(batch, window, n_planes, 1, 1, obj_ny, obj_nx, bytes);
+}
+
+int pty_scatteradd(void* full, int32_t obj_ny, int32_t obj_nx, int32_t n_planes, const int32_t* positions_host,
+                   int32_t batch, int32_t window, const void* chop, void* workspace, size_t workspace_bytes,
+                   void* stream) {
+  int rc = ms_validate(batch, window, n_planes, 1, 1, obj_ny, obj_nx);
+  if (rc) return rc;
+  if (!full || !positions_host || !chop || !workspace) return PTY_ERR_INVALID;
+  const MsPlan q = make_ms_plan(window, batch, n_planes, 1, 1, obj_ny, obj_nx);
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((rc = ms_upload_positions(q, positions_host, workspace, st))) return rc;
+  if (window == 64)
+    return run_scatteradd<64>(q, static_cast<float2*>(full), static_cast<const float2*>(chop), workspace, st);
+  return run_scatteradd<128>(q, static_cast<float2*>(full), static_cast<const float2*>(chop), workspace, st);
 }
 
 int pty_fft2_workspace_bytes(int32_t window, size_t* bytes) {

@@ -246,6 +246,165 @@ int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2
   return P.finalize(loss_sse, object_grad, probe_grad, pos_grad, true);
 }
 
+// ------------------------------------------------------------------ multislice_core seams
+// Shared launch of the fused kernel on caller-given windows (phase 3 or 4).
+template <int W>
+int ms_fused(const MsPlan& q, int phase, int step_obj, int step_probe, int use_edge, void* ws, cudaStream_t st) {
+  const size_t WW = (size_t)W * W;
+  FusedArgs fa{};
+  fa.Z = q.Z;
+  fa.Mp = q.Mp;
+  fa.Mo = q.Mo;
+  fa.algorithm = 0;
+  fa.step_obj = step_obj;
+  fa.step_probe = step_probe;
+  fa.step_pos = 0;
+  fa.probe_shift = 0;
+  fa.simulate = 0;
+  fa.use_edge = use_edge;
+  fa.phase = phase;
+  fa.loss_weight = 1.0f;
+  fa.probe_b = phase == 3 ? at<float2>(ws, q.o_probe_b) : nullptr;
+  fa.exit_out = at<float2>(ws, q.o_gbuf);
+  fa.obl = at<float2>(ws, q.o_obl);
+  fa.prop = at<float2>(ws, q.o_prop);
+  fa.prop_edge = at<float2>(ws, q.o_prop_edge);
+  fa.pyx = at<float2>(ws, q.o_pyx);
+  fa.use_sep = 0;
+  fa.mask = at<float>(ws, q.o_mask);
+  fa.sx = at<float>(ws, q.o_corr);     // not read without a probe shift
+  fa.sy = at<float>(ws, q.o_corr);
+  fa.corr = at<float>(ws, q.o_corr);
+  fa.seq = at<int>(ws, q.o_seq);
+  fa.tw = at<float2>(ws, q.o_tw);
+  fa.stack = at<float2>(ws, q.o_stack);
+  fa.gsum = at<float2>(ws, q.o_gsum);
+  fa.fprobe = at<float2>(ws, q.o_fprobe);
+  fa.gbuf = at<float2>(ws, q.o_gbuf);
+  fa.loss_part = at<double>(ws, q.o_parts);
+  fa.pos_part = at<double>(ws, q.o_parts) + 2 * (size_t)q.B;
+  fa.err = at<int>(ws, q.o_err);
+  const int nmodes = q.Mp * q.Mo;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)(q.B * nmodes));
+  cfg.blockDim = dim3(Geo<W>::T);
+  cfg.dynamicSmemBytes = FusedSmem<W>::bytes;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)nmodes;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  prof_mark(st, KID_FUSED);
+  if (cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W>, fa) != cudaSuccess) return PTY_ERR_CUDA;
+  return cuda_status();
+}
+
+template <int W>
+int ms_tables(const MsPlan& q, const float2* propagator, float edge_mult, const float* mask_clean, void* ws,
+              cudaStream_t st) {
+  const size_t WW = (size_t)W * W;
+  int rc = Path<W>::attributes();
+  if (rc) return rc;
+  prof_mark(st, KID_TWIDDLES);
+  build_twiddles_kernel<W><<<1, 256, 0, st>>>(at<float2>(ws, q.o_tw));
+  prof_mark(st, KID_TABLES);
+  external_tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(
+      propagator, mask_clean, edge_mult, (edge_mult > 1.0f && q.Z > 1) ? 1 : 0, at<float2>(ws, q.o_prop),
+      at<float2>(ws, q.o_prop_edge), at<float>(ws, q.o_mask), at<float>(ws, q.o_mask_sc), at<float2>(ws, q.o_pyx));
+  if (cudaMemsetAsync(at<float>(ws, q.o_corr), 0, (size_t)q.B * 2 * sizeof(float), st) != cudaSuccess ||
+      cudaMemsetAsync(at<int>(ws, q.o_err), 0, sizeof(int), st) != cudaSuccess)
+    return PTY_ERR_CUDA;
+  return cuda_status();
+}
+
+template <int W>
+int run_ms_forward(const MsPlan& q, const float2* probe_b, const float2* obj_b, const float2* propagator,
+                   float edge_mult, float2* waves, float2* exit_wave, void* ws, cudaStream_t st) {
+  constexpr int T = Geo<W>::T;
+  int rc = ms_tables<W>(q, propagator, edge_mult, nullptr, ws, st);
+  if (rc) return rc;
+  prof_mark(st, KID_LAYOUT);
+  ref_to_native_kernel<W><<<q.B * q.Mp, T, 0, st>>>(probe_b, at<float2>(ws, q.o_probe_b), q.Mp);
+  ref_to_native_kernel<W><<<q.B * q.zm, T, 0, st>>>(obj_b, at<float2>(ws, q.o_obl), q.zm);
+  if ((rc = ms_fused<W>(q, 3, 1, 0, (edge_mult > 1.0f && q.Z > 1) ? 1 : 0, ws, st))) return rc;
+  prof_mark(st, KID_LAYOUT);
+  native_to_ref_kernel<W><<<q.B * q.Z * q.Mp * q.Mo, T, 0, st>>>(at<float2>(ws, q.o_stack), waves,
+                                                                q.Z * q.Mp * q.Mo);
+  native_to_ref_kernel<W><<<q.B * q.Mp * q.Mo, T, 0, st>>>(at<float2>(ws, q.o_gbuf), exit_wave, q.Mp * q.Mo);
+  prof_mark(st, -1);
+  return cuda_status();
+}
+
+template <int W>
+int run_ms_grads(const MsPlan& q, const float2* d_exit, const float2* waves, const float2* obj_b,
+                 const float2* propagator, float edge_mult, const float* mask_clean, int step_obj,
+                 float2* object_grad, float2* probe_grad, void* ws, cudaStream_t st) {
+  constexpr int T = Geo<W>::T;
+  const size_t WW = (size_t)W * W;
+  int rc = ms_tables<W>(q, propagator, edge_mult, mask_clean, ws, st);
+  if (rc) return rc;
+  prof_mark(st, KID_LAYOUT);
+  ref_to_native_kernel<W><<<q.B * q.Mp * q.Mo, T, 0, st>>>(d_exit, at<float2>(ws, q.o_gbuf), q.Mp * q.Mo);
+  ref_to_native_kernel<W><<<q.B * q.zm, T, 0, st>>>(obj_b, at<float2>(ws, q.o_obl), q.zm);
+  if (step_obj)
+    ref_to_native_kernel<W><<<q.B * q.Z * q.Mp * q.Mo, T, 0, st>>>(waves, at<float2>(ws, q.o_stack),
+                                                                  q.Z * q.Mp * q.Mo);
+  if ((rc = ms_fused<W>(q, 4, step_obj, probe_grad != nullptr, (edge_mult > 1.0f && q.Z > 1) ? 1 : 0, ws, st)))
+    return rc;
+  if (step_obj) {
+    float2* gs = at<float2>(ws, q.o_gsum);
+    float2* grad = at<float2>(ws, q.o_grad);
+    const int nyx = q.Ny * q.Nx;
+    prof_mark(st, KID_GRAD_WINDOWS);
+    grad_windows_kernel<W><<<(unsigned)(q.B * q.zm), T, Smem<W>::bytes, st>>>(gs, at<float>(ws, q.o_mask_sc),
+                                                                            at<float2>(ws, q.o_tw));
+    prof_mark(st, KID_OBJ_TO_SLICES);
+    obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(object_grad, grad, nyx, q.zm);
+    prof_mark(st, KID_TILE_LISTS);
+    tile_lists_kernel<<<q.ntiles, 256, 0, st>>>(at<int>(ws, q.o_pos), at<int>(ws, q.o_seq), q.B, W, q.ntx,
+                                                 at<int>(ws, q.o_lists), at<int>(ws, q.o_counts));
+    prof_mark(st, KID_SCATTER);
+    scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, st>>>(
+        gs, at<int>(ws, q.o_pos), at<int>(ws, q.o_seq), at<int>(ws, q.o_lists), at<int>(ws, q.o_counts), grad, q.B,
+        W, q.Ny, q.Nx, q.ntx, q.zm, 1);
+    prof_mark(st, KID_SLICES_TO_OBJ);
+    slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(grad, object_grad, nyx, q.zm);
+  }
+  if (probe_grad) {
+    prof_mark(st, KID_LAYOUT);
+    native_to_ref_kernel<W><<<q.B * q.Mp, T, 0, st>>>(at<float2>(ws, q.o_fprobe), probe_grad, q.Mp);
+  }
+  (void)WW;
+  prof_mark(st, -1);
+  return cuda_status();
+}
+
+template <int W>
+int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, cudaStream_t st) {
+  const int WW = W * W;
+  const int nyx = q.Ny * q.Nx;
+  float2* planes = at<float2>(ws, q.o_gsum);
+  float2* grad = at<float2>(ws, q.o_grad);
+  prof_mark(st, KID_LAYOUT);
+  ref_to_planes_kernel<<<(unsigned)(((size_t)q.B * WW + 255) / 256), 256, 0, st>>>(chop, planes, q.B, WW, q.zm);
+  prof_mark(st, KID_OBJ_TO_SLICES);
+  obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(full, grad, nyx, q.zm);
+  prof_mark(st, KID_TILE_LISTS);
+  tile_lists_kernel<<<q.ntiles, 256, 0, st>>>(at<int>(ws, q.o_pos), at<int>(ws, q.o_seq), q.B, W, q.ntx,
+                                               at<int>(ws, q.o_lists), at<int>(ws, q.o_counts));
+  prof_mark(st, KID_SCATTER);
+  scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, st>>>(
+      planes, at<int>(ws, q.o_pos), at<int>(ws, q.o_seq), at<int>(ws, q.o_lists), at<int>(ws, q.o_counts), grad, q.B,
+      W, q.Ny, q.Nx, q.ntx, q.zm, 1);
+  prof_mark(st, KID_SLICES_TO_OBJ);
+  slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(grad, full, nyx, q.zm);
+  prof_mark(st, -1);
+  return cuda_status();
+}
+
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st) {
   if (set_smem(fft2_batch_kernel<W>, Smem<W>::bytes)) return PTY_ERR_CUDA;

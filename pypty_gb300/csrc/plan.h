@@ -116,11 +116,59 @@ int set_smem(K kernel, size_t bytes) {
 }
 
 
+// Workspace of the multislice_core-style entry points (pty_multislice,
+// pty_multislice_grads, pty_scatteradd): caller-given windows in the reference layout.
+struct MsPlan {
+  int W, B, Z, Mp, Mo, Ny, Nx, zm, ntx, nty, ntiles;
+  size_t o_tw, o_prop, o_prop_edge, o_mask, o_mask_sc, o_pyx, o_probe_b, o_obl, o_stack, o_gbuf, o_gsum;
+  size_t o_fprobe, o_grad, o_lists, o_counts, o_pos, o_seq, o_corr, o_err, o_parts, total;
+};
+
+inline MsPlan make_ms_plan(int W, int B, int Z, int Mp, int Mo, int Ny, int Nx) {
+  MsPlan q{};
+  q.W = W;
+  q.B = B;
+  q.Z = Z;
+  q.Mp = Mp;
+  q.Mo = Mo;
+  q.Ny = Ny;
+  q.Nx = Nx;
+  q.zm = Z * Mo;
+  q.ntx = (Nx + kTileSize - 1) / kTileSize;
+  q.nty = (Ny + kTileSize - 1) / kTileSize;
+  q.ntiles = q.ntx * q.nty;
+  const size_t WW = (size_t)W * W, c8 = sizeof(float2);
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes); return r; };
+  q.o_tw = take(tw_count(W) * c8);
+  q.o_prop = take(WW * c8);
+  q.o_prop_edge = take(WW * c8);
+  q.o_mask = take(WW * sizeof(float));
+  q.o_mask_sc = take(WW * sizeof(float));
+  q.o_pyx = take(2 * (size_t)W * c8);
+  q.o_probe_b = take((size_t)B * Mp * WW * c8);
+  q.o_obl = take((size_t)B * q.zm * WW * c8);
+  q.o_stack = take((size_t)B * Z * Mp * Mo * WW * c8);
+  q.o_gbuf = take((size_t)B * Mp * Mo * WW * c8);
+  q.o_gsum = take((size_t)B * q.zm * WW * c8);
+  q.o_fprobe = take((size_t)B * Mp * WW * c8);
+  q.o_grad = take((size_t)q.zm * Ny * Nx * c8);
+  q.o_lists = take((size_t)q.ntiles * B * sizeof(int));
+  q.o_counts = take((size_t)q.ntiles * sizeof(int));
+  q.o_pos = take((size_t)B * 2 * sizeof(int));
+  q.o_seq = take((size_t)B * sizeof(int));
+  q.o_corr = take((size_t)B * 2 * sizeof(float));
+  q.o_err = take(sizeof(int));
+  q.o_parts = take((size_t)B * (2 + 2 * Mp) * sizeof(double));
+  q.total = o;
+  return q;
+}
+
 // Kernel classes reported by the launch profiler (pty_profile_begin / pty_profile_end).
 enum KernelId : int {
   KID_TWIDDLES = 0, KID_TABLES, KID_PROBE_FFT, KID_OBJ_TO_SLICES, KID_OBJECT_WINDOWS, KID_FUSED,
   KID_GRAD_WINDOWS, KID_TILE_LISTS, KID_SCATTER, KID_PROBE_PARTIAL, KID_SLICES_TO_OBJ, KID_PROBE_FINAL,
-  KID_FINALIZE, KID_FFT2, KID_COUNT
+  KID_FINALIZE, KID_FFT2, KID_LAYOUT, KID_COUNT
 };
 
 // Records an event on `st` before a launch of kernel class `id` while profiling is on
@@ -139,6 +187,19 @@ int run_forward(const pty_problem_t* p, const Plan& q, const float2* obj, const 
 template <int W>
 int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2* object_grad,
                  float2* probe_grad, float* pos_grad, void* ws, cudaStream_t st);
+
+// multislice_core-style entry points (reference layouts, caller-given windows)
+template <int W>
+int run_ms_forward(const MsPlan& q, const float2* probe_b, const float2* obj_b, const float2* propagator,
+                   float edge_mult, float2* waves, float2* exit_wave, void* ws, cudaStream_t st);
+
+template <int W>
+int run_ms_grads(const MsPlan& q, const float2* d_exit, const float2* waves, const float2* obj_b,
+                 const float2* propagator, float edge_mult, const float* mask_clean, int step_obj,
+                 float2* object_grad, float2* probe_grad, void* ws, cudaStream_t st);
+
+template <int W>
+int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, cudaStream_t st);
 
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st);

@@ -228,7 +228,11 @@ __global__ void __launch_bounds__(Geo<W>::T) object_windows_kernel(WindowArgs a)
 // ------------------------------------------------------------------ fused multislice
 struct FusedArgs {
   int Z, Mp, Mo, algorithm, step_obj, step_probe, step_pos, probe_shift, simulate, use_edge;
-  int phase;                // 0: whole pass; 1: forward half; 2: adjoint half
+  int phase;                // 0: whole pass; 1: forward half; 2: adjoint half;
+                            // 3: forward multislice only (exit wave out); 4: adjoint from a given
+                            //    exit-wave gradient with a real-space probe gradient out
+  const float2* probe_b;    // per-position incoming probes, native real [Bb*Mp] (phase 3)
+  float2* exit_out;         // exit waves, native real [Bb*Mp*Mo] (phase 3)
   float loss_weight;
   const float2* probe;      // (W, W, Mp) reference layout (used without probe shift)
   const float2* probe_f;    // native frequency layout [Mp]
@@ -401,9 +405,10 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 
   float2 v[32];
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
-  const int s_begin = (a.phase == 2) ? Z + 1 : 0;
-  const int s_end = (a.simulate || a.phase == 1) ? Z + 1 : 2 * Z + 1;
-  if (a.phase == 2) {
+  const bool adjoint_only = (a.phase == 2 || a.phase == 4);
+  const int s_begin = adjoint_only ? Z + 1 : 0;
+  const int s_end = (a.simulate || a.phase == 1 || a.phase == 3) ? Z + 1 : 2 * Z + 1;
+  if (adjoint_only) {
     // adjoint half: resume from dL/d(exit wave) kept by the forward half
     ld_native<W>(gb, v);
     issue_x(Z + 1);
@@ -417,7 +422,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 
     // ------------------------------------------------ real-space op
     if (s == 0) {
-      if (!a.probe_shift) {
+      if (a.probe_b) {
+        ld_native<W>(a.probe_b + ((size_t)b * a.Mp + p) * WW, v);
+      } else if (!a.probe_shift) {
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
       }
@@ -439,6 +446,10 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           v[2 * j] = cmul(v[2 * j], make_float2(q.x, q.y));
           v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
         }
+      }
+      if (a.phase == 3 && z == Z - 1) {
+        st_native<W>(a.exit_out + (((size_t)b * a.Mp + p) * a.Mo + m) * WW, v);   // the exit wave
+        break;
       }
     } else {
       mbar_wait(&bars[0], ph_x, a.err);
@@ -535,6 +546,10 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           }
           cluster.sync();
           if (m != 0) break;
+        }
+        if (a.phase == 4) {   // interm_probe_grad of multislice_core.py:193-197, real space
+          if (a.step_probe) st_native<W>(a.fprobe + ((size_t)b * a.Mp + p) * WW, v);
+          break;
         }
       }
     }
@@ -669,6 +684,71 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     F::inverse_tail(v, tw1);
   }
   if (a.phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
+}
+
+// ------------------------------------------------------------------ reference-layout windows
+// (B, W, W, K) arrays with the mode axes innermost (the reference's layout) <-> the native
+// window layout [B*K] used by the kernels; one block per window.
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) ref_to_native_kernel(const float2* __restrict__ src,
+                                                                  float2* __restrict__ dst, int K) {
+  using G = Geo<W>;
+  const int t = threadIdx.x, win = blockIdx.x, b = win / K, k = win % K;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = src[(((size_t)b * W + G::ry(t)) * W + G::rx(t, i)) * K + k];
+  st_native<W>(dst + (size_t)win * W * W, v);
+}
+
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) native_to_ref_kernel(const float2* __restrict__ src,
+                                                                  float2* __restrict__ dst, int K) {
+  using G = Geo<W>;
+  const int t = threadIdx.x, win = blockIdx.x, b = win / K, k = win % K;
+  float2 v[32];
+  ld_native<W>(src + (size_t)win * W * W, v);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[(((size_t)b * W + G::ry(t)) * W + G::rx(t, i)) * K + k] = v[i];
+}
+
+// (B, W*W, K) -> (B, K, W*W): per-position windows to per-plane natural windows
+static __global__ void ref_to_planes_kernel(const float2* __restrict__ src, float2* __restrict__ dst, int B,
+                                            int WW, int K) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)B * WW) return;
+  const size_t b = idx / WW, e = idx % WW;
+  for (int k = 0; k < K; ++k) dst[(b * K + k) * WW + e] = src[idx * K + k];
+}
+
+// A caller-given propagator P (W x W, mask applied, the reference's
+// master_propagator_phase_space) and band-limit mask as the kernels' tables: P / W^2,
+// P^edge / W^2 (principal branch) and mask / W^2.
+template <int W>
+__global__ void external_tables_kernel(const float2* __restrict__ P, const float* __restrict__ mask_clean,
+                                       float edge, int use_edge, float2* __restrict__ prop,
+                                       float2* __restrict__ prop_edge, float* __restrict__ mask,
+                                       float* __restrict__ mask_sc, float2* __restrict__ pyx) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < 2 * W) pyx[idx] = make_float2(0.f, 0.f);   // separable factors unused here
+  if (idx >= W * W) return;
+  const float inv = 1.0f / (float)(W * W);
+  const float2 p = P[idx];
+  prop[idx] = make_float2(p.x * inv, p.y * inv);
+  if (use_edge) {
+    const float r = sqrtf(p.x * p.x + p.y * p.y);
+    float2 pe = make_float2(0.f, 0.f);
+    if (r > 0.f) {
+      const float ang = atan2f(p.y, p.x) * edge;
+      const float re = powf(r, edge);
+      float se, ce;
+      sincosf(ang, &se, &ce);
+      pe = make_float2(re * ce, re * se);
+    }
+    prop_edge[idx] = make_float2(pe.x * inv, pe.y * inv);
+  }
+  const float mk = mask_clean ? mask_clean[idx] : 1.0f;
+  mask[idx] = mk;
+  mask_sc[idx] = mk * inv;
 }
 
 // ------------------------------------------------------------------ gradient windows

@@ -11,16 +11,27 @@ from . import objective as _objective
 _SAVED = {}
 
 
-def install(pypty_module) -> None:
-    """Point ``pypty.objective.loss_and_direction`` at the GPU implementation."""
+def install(pypty_module, multislice_core: bool = False) -> None:
+    """Point ``pypty.objective.loss_and_direction`` at the GPU implementation; with
+    ``multislice_core=True`` also ``pypty.multislice_core.multislice`` /
+    ``multislice_grads`` / ``scatteradd`` (used by reference code that calls them
+    directly; ``loss_and_direction`` on the GPU path does not go through them)."""
     obj_mod = pypty_module.objective
     if "loss_and_direction" not in _SAVED:
         _SAVED["loss_and_direction"] = (obj_mod, obj_mod.loss_and_direction)
     obj_mod.loss_and_direction = _objective.loss_and_direction
+    if multislice_core:
+        from . import multislice_core as _mc
+        ms_mod = pypty_module.multislice_core
+        for name in ("multislice", "multislice_grads", "scatteradd"):
+            key = "multislice_core." + name
+            if key not in _SAVED:
+                _SAVED[key] = (ms_mod, getattr(ms_mod, name))
+            setattr(ms_mod, name, getattr(_mc, name))
 
 
 def uninstall() -> None:
     """Restore the attributes replaced by ``install``."""
-    for name, (mod, fn) in list(_SAVED.items()):
-        setattr(mod, name, fn)
-        del _SAVED[name]
+    for key, (mod, fn) in list(_SAVED.items()):
+        setattr(mod, key.split(".")[-1], fn)
+        del _SAVED[key]

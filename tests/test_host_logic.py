@@ -81,3 +81,15 @@ def test_split_positions_matches_reference_rounding():
     shifted = pos - pos.min(axis=0)
     assert np.array_equal(ipos, np.round(shifted).astype(np.int32))
     assert np.allclose(corr, shifted - np.round(shifted), atol=1e-7)
+
+
+def test_window_index_arrays_are_recognised_and_others_rejected():
+    from pypty_gb300.multislice_core import _window_positions
+    W = 64
+    runx, runy = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
+    pos = np.array([[3, 5], [10, 0]])
+    my = pos[:, 0][:, None, None] + runy[None]
+    mx = pos[:, 1][:, None, None] + runx[None]
+    assert np.array_equal(_window_positions(my, mx, W), pos)
+    with pytest.raises(NotImplementedError):
+        _window_positions(my[:, ::-1], mx, W)
