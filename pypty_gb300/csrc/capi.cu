@@ -50,6 +50,10 @@ int run_common(const pty_problem_t* p, const void* obj, const void* probe, const
     return run_path<64>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
                         loss_sse, static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad,
                         patterns, ws, st);
+  if (q.W == 256)
+    return run_path<256>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
+                         loss_sse, static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad,
+                         patterns, ws, st);
   return run_path<128>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
                        loss_sse, static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad,
                        patterns, ws, st);
@@ -141,7 +145,8 @@ const char* pty_status_string(int status) {
   switch (status) {
     case PTY_OK: return "ok";
     case PTY_ERR_INVALID: return "invalid argument";
-    case PTY_ERR_UNSUPPORTED: return "unsupported problem (window must be 64 or 128, Mp*Mo <= 8)";
+    case PTY_ERR_UNSUPPORTED:
+      return "unsupported problem (window 64, 128 or 256; Mp*Mo <= 8 for 64/128, <= 64 for 256)";
     case PTY_ERR_POSITION: return "scan position or sequence entry out of range";
     case PTY_ERR_WORKSPACE: return "workspace too small";
     case PTY_ERR_CUDA: return "CUDA launch or copy failed";
@@ -199,6 +204,7 @@ int pty_forward(const pty_problem_t* problem, const void* obj, const void* probe
   const float2* o = static_cast<const float2*>(obj);
   const float2* pr = static_cast<const float2*>(probe);
   if (q.W == 64) return run_forward<64>(problem, q, o, pr, measured, loss_sse, workspace, st);
+  if (q.W == 256) return run_forward<256>(problem, q, o, pr, measured, loss_sse, workspace, st);
   return run_forward<128>(problem, q, o, pr, measured, loss_sse, workspace, st);
 }
 
@@ -216,6 +222,7 @@ int pty_backward(const pty_problem_t* problem, double* loss_sse, void* object_gr
   float2* og = static_cast<float2*>(object_grad);
   float2* pg = static_cast<float2*>(probe_grad);
   if (q.W == 64) return run_backward<64>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
+  if (q.W == 256) return run_backward<256>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
   return run_backward<128>(problem, q, loss_sse, og, pg, pos_grad, workspace, st);
 }
 
@@ -313,7 +320,7 @@ int pty_scatteradd(void* full, int32_t obj_ny, int32_t obj_nx, int32_t n_planes,
 }
 
 int pty_fft2_workspace_bytes(int32_t window, size_t* bytes) {
-  if (window != 64 && window != 128) return PTY_ERR_UNSUPPORTED;
+  if (window != 64 && window != 128 && window != 256) return PTY_ERR_UNSUPPORTED;
   if (!bytes) return PTY_ERR_INVALID;
   *bytes = align_up(tw_count(window) * sizeof(float2));
   return PTY_OK;
@@ -321,7 +328,7 @@ int pty_fft2_workspace_bytes(int32_t window, size_t* bytes) {
 
 int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, int32_t shift,
              void* workspace, size_t workspace_bytes, void* stream) {
-  if (window != 64 && window != 128) return PTY_ERR_UNSUPPORTED;
+  if (window != 64 && window != 128 && window != 256) return PTY_ERR_UNSUPPORTED;
   if (!in || !out || !workspace || batch <= 0) return PTY_ERR_INVALID;
   size_t need = 0;
   pty_fft2_workspace_bytes(window, &need);
@@ -331,6 +338,7 @@ int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t i
   const float2* src = static_cast<const float2*>(in);
   float2* dst = static_cast<float2*>(out);
   if (window == 64) return run_fft2<64>(src, dst, batch, inverse, shift, tw, st);
+  if (window == 256) return run_fft2<256>(src, dst, batch, inverse, shift, tw, st);
   return run_fft2<128>(src, dst, batch, inverse, shift, tw, st);
 }
 

@@ -20,19 +20,22 @@ struct Plan {
   int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
   size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_pyx, o_sx, o_sy, o_probe_f;
   size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
-  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, o_gbuf, total;
+  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, o_gbuf, o_psi, o_dldi, o_pgr, total;
   bool split;   // one batch with every position: pty_forward / pty_backward
 };
 
+// twiddle tables in global memory: W = 256 windows use the 128 tables of their sub-transforms
 inline int tw_count(int W) { return W == 64 ? Geo<64>::TW1 + Geo<64>::TW2 : Geo<128>::TW1 + Geo<128>::TW2; }
 
 inline int validate(const pty_problem_t* p) {
   if (!p) return PTY_ERR_INVALID;
-  if (p->window != 64 && p->window != 128) return PTY_ERR_UNSUPPORTED;
+  if (p->window != 64 && p->window != 128 && p->window != 256) return PTY_ERR_UNSUPPORTED;
   if (p->obj_ny <= 0 || p->obj_nx <= 0 || p->n_slices <= 0 || p->n_obj_modes <= 0 ||
       p->n_probe_modes <= 0 || p->n_positions <= 0 || p->n_sequence <= 0 || p->compute_batch <= 0)
     return PTY_ERR_INVALID;
-  if (p->n_obj_modes * p->n_probe_modes > 8) return PTY_ERR_UNSUPPORTED;
+  // W <= 128: the modes of a position form one cluster (<= 8 blocks); W = 256: the modes run
+  // one after another inside the position's 4-block cluster
+  if (p->n_obj_modes * p->n_probe_modes > (p->window == 256 ? 64 : 8)) return PTY_ERR_UNSUPPORTED;
   if (p->algorithm < PTY_LSQ_SQRT || p->algorithm > PTY_LSQ_SQRT_2) return PTY_ERR_UNSUPPORTED;
   if (p->step_pos && !p->probe_shift) return PTY_ERR_INVALID;
   if ((int64_t)p->obj_ny * p->obj_nx >= (int64_t)1 << 31) return PTY_ERR_UNSUPPORTED;
@@ -88,7 +91,11 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
   q.o_sim = take((size_t)q.Bb * WW * f4);
   q.o_err = take(sizeof(int));
-  q.o_gbuf = take(split ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
+  const bool w256 = q.W == 256;
+  q.o_gbuf = take(split && !w256 ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
+  q.o_psi = take(w256 ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
+  q.o_dldi = take(w256 && split ? (size_t)q.Bb * WW * f4 : 0);
+  q.o_pgr = take(w256 && q.Mo > 1 ? (size_t)q.Bb * q.Mp * WW * c8 : 0);
   q.total = o;
   return q;
 }
@@ -175,6 +182,8 @@ enum KernelId : int {
 // (id < 0 closes the last interval). No-op otherwise.
 void prof_mark(cudaStream_t st, int id);
 
+// Launch paths, instantiated in path_w64.cu / path_w128.cu and specialised for W = 256 in
+// path_w256.cu.
 template <int W>
 int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const float2* probe,
              const float* measured, double* loss_sse, float2* object_grad, float2* probe_grad,
@@ -187,6 +196,15 @@ int run_forward(const pty_problem_t* p, const Plan& q, const float2* obj, const 
 template <int W>
 int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2* object_grad,
                  float2* probe_grad, float* pos_grad, void* ws, cudaStream_t st);
+
+template <>
+int run_path<256>(const pty_problem_t*, const Plan&, const float2*, const float2*, const float*, double*, float2*,
+                  float2*, float*, float*, void*, cudaStream_t);
+template <>
+int run_forward<256>(const pty_problem_t*, const Plan&, const float2*, const float2*, const float*, double*, void*,
+                     cudaStream_t);
+template <>
+int run_backward<256>(const pty_problem_t*, const Plan&, double*, float2*, float2*, float*, void*, cudaStream_t);
 
 // multislice_core-style entry points (reference layouts, caller-given windows)
 template <int W>
@@ -203,5 +221,7 @@ int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, 
 
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st);
+template <>
+int run_fft2<256>(const float2*, float2*, int, int, int, float2*, cudaStream_t);
 
 }  // namespace pty

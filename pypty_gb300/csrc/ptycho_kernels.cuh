@@ -252,6 +252,9 @@ struct FusedArgs {
   float2* gsum;             // probe-mode-summed object gradient, native real [Bb*Z*Mo]
   float2* fprobe;           // FFT of the per-position probe gradient, native freq [Bb*Mp]
   float2* gbuf;             // dL/d(exit wave) between the two halves, native real [Bb*Mp*Mo]
+  float2* psi;              // 256 windows: far-field wave per mode [Bb*Mp*Mo]
+  float* dldi;              // 256 windows: dL/dI between the two halves [Bb]
+  float2* pgr;              // 256 windows: object-mode sum of the probe gradient [Bb*Mp]
   double* loss_part;        // [Bb][2]
   double* pos_part;         // [Bb][Mp][2]
   float* sim_out;           // [Bb][W][W] simulated mean intensity (detector order)
