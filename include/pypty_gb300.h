@@ -64,6 +64,9 @@ typedef struct pty_problem {
   float damping_cutoff;   /* band-limit cutoff as a fraction of Nyquist (2/3 default) */
   float smooth_rolloff;   /* cosine roll-off width of the band limit */
   float loss_weight;      /* this_loss_weight */
+  int32_t checkpoint_every; /* 256-px windows: keep every k-th slice's wave and recompute the
+                               others in the adjoint (k <= 1: keep all). No counterpart in the
+                               reference, which keeps every slice (multislice_core.py:66). */
 } pty_problem_t;
 
 /* Library version (major * 10000 + minor * 100 + patch). */

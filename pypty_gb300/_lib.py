@@ -33,7 +33,7 @@ class Problem(ctypes.Structure):
         ("pixel_size_x", ctypes.c_float), ("pixel_size_y", ctypes.c_float),
         ("slice_distance", ctypes.c_float), ("edge_mult", ctypes.c_float),
         ("damping_cutoff", ctypes.c_float), ("smooth_rolloff", ctypes.c_float),
-        ("loss_weight", ctypes.c_float),
+        ("loss_weight", ctypes.c_float), ("checkpoint_every", ctypes.c_int32),
     ]
 
 

@@ -220,18 +220,24 @@ __global__ void __launch_bounds__(512, 1) fft2_batch256_kernel(const float2* __r
 }
 
 // ------------------------------------------------------------------ fused multislice, 256
-// One cluster of 4 blocks per position; modes k = m * Mp + p one after another.
-// Extra buffers (FusedArgs): psi [Bb][Mp*Mo] far-field waves, dldi [Bb] dL/dI (split
-// passes), pgr [Bb][Mp] real-space probe gradient summed over object modes (Mo > 1).
+// One cluster of 4 blocks per position; modes one after another (forward: k = m*Mp + p
+// ascending; adjoint: probe mode outer, object mode inner). Extra buffers (FusedArgs): psi
+// [Bb][Mp*Mo] far-field waves, dldi [Bb] dL/dI (split passes), pgr [Bb][Mp] object-mode sum
+// of the probe gradient (Mo > 1), seg [Bb][ckpt] recomputed waves and gpark [Bb] the parked
+// adjoint wave (ckpt > 1).
 //
-// The work is one flat loop of steps "real-space op -> FFT -> frequency op -> inverse FFT"
-// (each transform inlined once):
-//   forward, per mode k:   START (probe spectrum -> IFFT), SLICE z = 0..Z-1 (store conj psi,
-//                          * O_z, FFT, * P, IFFT; the last slice ends with the far field)
-//   LOSS                   dL/dI of the mode-mean intensity (no transform)
-//   adjoint, per mode k:   ASTART (dL/dI * Psi_k -> IFFT), ASLICE z = Z-1..0 (gradient
-//                          contribution, * conj O_z, FFT, * conj P, IFFT; after z = 0 the
-//                          probe-gradient spectrum and the position gradient)
+// Per-slice recomputation: with ckpt = K > 1 the forward keeps conj(psi_z) only for
+// z % K == 0; the adjoint, on reaching a segment [z0, zl], parks its wave, re-runs the
+// forward from the checkpoint z0 (same arithmetic, so the same waves bit for bit) into seg,
+// and reloads its wave. The stack then holds ceil(Z/K) instead of Z waves per mode.
+//
+// Steps form a small state machine, each "real-space op -> FFT -> frequency op -> inverse
+// FFT" with the two transforms inlined once:
+//   F_START  probe spectrum -> IFFT           F_SLICE  * O_z, FFT, * P (or far field), IFFT
+//   LOSS     dL/dI (no transform)             A_START  dL/dI * Psi_k -> IFFT
+//   A_RECOMP segment recomputation            A_SLICE  gradient, * conj O_z, FFT, * conj P, IFFT
+enum Stage256 : int { F_START = 0, F_SLICE, S_LOSS, A_START, A_RECOMP, A_SLICE, S_DONE };
+
 __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
   using G = Geo256;
   constexpr int T = G::T;
@@ -248,6 +254,9 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
   const int c = (int)cl.block_rank(), t = threadIdx.x;
   const int b = blockIdx.x / 4;
   const int Z = a.Z, Mp = a.Mp, Mo = a.Mo, nmodes = Mp * Mo;
+  const bool store_stack = a.step_obj && !a.simulate;
+  const int K = (a.ckpt > 1 && store_stack) ? a.ckpt : 1;   // no stack, nothing to recompute
+  const int nck = (Z + K - 1) / K;
   load_twiddles<128>(s.tw1, s.tw2, a.tw);
   load_tw256(s.tw256);
   for (int i = t; i < 512; i += T) spy[i] = a.pyx[i];
@@ -258,39 +267,26 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
     sbits[t] = mb;
   }
   for (int i = 0; i < 32; ++i) facc[i * T + t] = 0.0f;
-  __syncthreads();
-  const bool store_stack = a.step_obj && !a.simulate;
   const bool want_probe = a.step_probe || a.step_pos;
   auto part = [&](const float2* base, size_t win) { return base + win * WW + c * PART; };
   auto wpart = [&](float2* base, size_t win) { return base + win * WW + c * PART; };
+  auto stack_win = [&](int z, int p, int m) { return (((size_t)b * nck + z / K) * Mp + p) * Mo + m; };
 
-  const int per_mode = Z + 1;
-  const int n_fwd = nmodes * per_mode;           // steps [0, n_fwd): forward
-  const int s_loss = n_fwd;                       // the loss step
-  const int n_total = a.simulate ? n_fwd + 1 : n_fwd + 1 + nmodes * per_mode;
-  int s_begin = 0, s_end = n_total;
-  if (a.phase == 1) s_end = n_fwd + 1;
+  int stage = F_START, k = 0, z = 0, z0 = 0, zl = 0;
   if (a.phase == 2) {
-    s_begin = n_fwd + 1;
+    stage = A_START;
     for (int i = 0; i < 32; ++i) facc[i * T + t] = a.dldi[(size_t)b * WW + c * PART + i * T + t];
-    __syncthreads();
   }
+  __syncthreads();
 
   float2 v[32];
-  for (int s_ = s_begin; s_ < s_end; ++s_) {
-    // ------------------------------------------------ decode the step
-    const bool is_loss = (s_ == s_loss);
-    const bool fwd = s_ < s_loss;
-    const int r = fwd ? s_ : s_ - s_loss - 1;
-    const int kk = is_loss ? 0 : r / per_mode, j = is_loss ? 0 : r % per_mode;
-    // forward: modes in order k = m*Mp + p; adjoint: probe mode outer, object mode inner
-    const int p = fwd ? kk % Mp : kk / Mo;
-    const int m = fwd ? kk / Mp : kk % Mo;
-    const int k = m * Mp + p;
-    const bool start = !is_loss && j == 0;
-    const int z = fwd ? j - 1 : Z - j;        // slice of a SLICE / ASLICE step
+  while (stage != S_DONE) {
+    const bool fwd_stage = stage == F_START || stage == F_SLICE;
+    const int p = fwd_stage ? k % Mp : k / Mo;
+    const int m = fwd_stage ? k / Mp : k % Mo;
+    const int kidx = m * Mp + p;
 
-    if (is_loss) {
+    if (stage == S_LOSS) {
       // ------------------------------------------------ loss and dL/dI of this quadrant
       const int gi = a.seq[b];
       const float inv_modes = 1.0f / (float)nmodes;
@@ -332,40 +328,59 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
         for (int i = 0; i < 32; ++i) a.dldi[(size_t)b * WW + c * PART + i * T + t] = facc[i * T + t];
         return;
       }
+      stage = A_START;
+      k = 0;
       continue;
     }
 
     // ------------------------------------------------ real-space op
-    bool do_fwd = false, do_inv = false;
-    if (start) {
+    bool do_fwd = false, do_inv = false, epilogue = false, skip = false;
+    if (stage == F_START || stage == A_START) {
       do_inv = true;
-    } else if (fwd) {
-      if (store_stack) st_native128_conj(wpart(a.stack, (((size_t)b * Z + z) * Mp + p) * Mo + m), v);
+    } else if (stage == F_SLICE) {
+      if (store_stack && z % K == 0) st_native128_conj(wpart(a.stack, stack_win(z, p, m)), v);
       mul_native128(v, part(a.obl, ((size_t)b * Z + z) * Mo + m), false);
       do_fwd = true;
       do_inv = z < Z - 1;
-    } else {
+    } else if (stage == A_RECOMP) {
+      if (z == z0) {
+        st_native<128>(wpart(a.gpark, b), v);                 // park the adjoint wave
+        ld_native<128>(part(a.stack, stack_win(z0, p, m)), v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = cconj(v[i]);     // the checkpoint holds conj(psi)
+      }
+      st_native128_conj(wpart(a.seg, (size_t)b * K + (z - z0)), v);
+      if (z < zl) {
+        mul_native128(v, part(a.obl, ((size_t)b * Z + z) * Mo + m), false);
+        do_fwd = true;
+        do_inv = true;
+      } else {
+        ld_native<128>(part(a.gpark, b), v);                  // the adjoint wave back
+      }
+    } else {   // A_SLICE
       if (store_stack) {
         // conj(psi_z) * g, summed over probe modes in order p = 0, 1, ... (multislice_core.py:186-188)
-        madd_native128(wpart(a.gsum, ((size_t)b * Z + z) * Mo + m),
-                       part(a.stack, (((size_t)b * Z + z) * Mp + p) * Mo + m), v, p > 0);
+        const float2* src = K == 1 ? part(a.stack, stack_win(z, p, m)) : part(a.seg, (size_t)b * K + (z - z0));
+        madd_native128(wpart(a.gsum, ((size_t)b * Z + z) * Mo + m), src, v, p > 0);
       }
       mul_native128(v, part(a.obl, ((size_t)b * Z + z) * Mo + m), true);
       if (z > 0) {
         do_fwd = true;
         do_inv = true;
-      } else {
-        if (!want_probe) continue;
+      } else if (want_probe) {
         if (Mo > 1) {
           // sum over object modes (multislice_core.py:193-197), in order m = 0, 1, ...
           float2* pr = wpart(a.pgr, (size_t)b * Mp + p);
           if (m > 0) add_native128(v, pr);
           if (m < Mo - 1) {
             st_native<128>(pr, v);
-            continue;
+            skip = true;
           }
         }
-        do_fwd = true;   // probe-gradient spectrum
+        if (!skip) {
+          do_fwd = true;   // probe-gradient spectrum
+          epilogue = true;
+        }
       }
     }
 
@@ -373,7 +388,7 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
     if (do_fwd) WinFFT256::forward(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
 
     // ------------------------------------------------ frequency op
-    if (start && fwd) {
+    if (stage == F_START) {
       // incoming probe: FFT(P) * shift ramp * mask / W^2 (objective.py:469-476); without a
       // shift the probe is taken back unchanged (FFT(P) / W^2)
       const float2* pf = part(a.probe_f, p);
@@ -393,39 +408,40 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
         }
         v[i] = cmul(pf[nidx<128>(i, t)], w);
       }
-    } else if (start) {
-      // adjoint start: dL/dPsi = dL/dI * Psi * w (objective.py:595-597)
-      ld_native<128>(part(a.psi, (size_t)b * nmodes + k), v);
+    } else if (stage == A_START) {
+      // dL/dPsi = dL/dI * Psi * w (objective.py:595-597)
+      ld_native<128>(part(a.psi, (size_t)b * nmodes + kidx), v);
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = cscale(cscale(v[i], facc[i * T + t]), a.loss_weight);
-    } else if (fwd && z == Z - 1) {
+    } else if (stage == F_SLICE && z == Z - 1) {
       // far field of this mode: Psi = FFT(exit) * mask; accumulate |Psi|^2
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         v[i] = cscale(v[i], a.mask[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
         facc[i * T + t] += cabs2(v[i]);
       }
-      if (!a.simulate) st_native<128>(wpart(a.psi, (size_t)b * nmodes + k), v);
+      if (!a.simulate) st_native<128>(wpart(a.psi, (size_t)b * nmodes + kidx), v);
     } else if (do_inv) {
       // propagator (conjugated in the adjoint); the thick first slice uses the table
-      const int zstep = fwd ? z : z - 1;
+      const bool adjoint = stage == A_SLICE;
+      const int zstep = adjoint ? z - 1 : z;
       const bool edge = a.use_edge && zstep == 0;
       if (a.use_sep && !edge) {
         const uint32_t mb = sbits[t];
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           const float2 P = cmul(spy[G::fky(c, t, i)], spx[G::fkx(c, t, i)]);
-          v[i] = ((mb >> i) & 1u) ? (fwd ? cmul(v[i], P) : cmulc(v[i], P)) : make_float2(0.f, 0.f);
+          v[i] = ((mb >> i) & 1u) ? (adjoint ? cmulc(v[i], P) : cmul(v[i], P)) : make_float2(0.f, 0.f);
         }
       } else {
         const float2* pr = edge ? a.prop_edge : a.prop;
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           const float2 P = pr[G::fky(c, t, i) * 256 + G::fkx(c, t, i)];
-          v[i] = fwd ? cmul(v[i], P) : cmulc(v[i], P);
+          v[i] = adjoint ? cmulc(v[i], P) : cmul(v[i], P);
         }
       }
-    } else if (!fwd) {
+    } else if (epilogue) {
       // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
       double gy = 0.0, gx = 0.0;
       if (a.probe_shift) {
@@ -471,6 +487,45 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
 
     // ------------------------------------------------ inverse FFT
     if (do_inv) WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
+
+    // ------------------------------------------------ next step
+    if (stage == F_START) {
+      stage = F_SLICE;
+      z = 0;
+    } else if (stage == F_SLICE) {
+      if (z < Z - 1) {
+        ++z;
+      } else if (++k < nmodes) {
+        stage = F_START;
+      } else {
+        stage = S_LOSS;
+      }
+    } else if (stage == A_START || (stage == A_SLICE && z > 0 && K > 1 && z == z0)) {
+      // enter the segment below (from A_START: the top segment)
+      zl = stage == A_START ? Z - 1 : z0 - 1;
+      z0 = (zl / K) * K;
+      if (K > 1) {
+        stage = A_RECOMP;
+        z = z0;
+      } else {
+        stage = A_SLICE;
+        z = zl;
+      }
+    } else if (stage == A_RECOMP) {
+      if (z < zl) {
+        ++z;
+      } else {
+        stage = A_SLICE;
+      }
+    } else {   // A_SLICE
+      if (z > 0) {
+        --z;
+      } else if (++k < nmodes) {
+        stage = A_START;
+      } else {
+        stage = S_DONE;
+      }
+    }
   }
 }
 

@@ -136,6 +136,9 @@ struct Path256 {
     fa.psi = at<float2>(ws, q.o_psi);
     fa.dldi = at<float>(ws, q.o_dldi);
     fa.pgr = at<float2>(ws, q.o_pgr);
+    fa.ckpt = q.ckpt;
+    fa.seg = at<float2>(ws, q.o_seg);
+    fa.gpark = at<float2>(ws, q.o_gpark);
     fa.loss_part = at<double>(ws, q.o_loss_part) + 2 * (size_t)s0;
     fa.pos_part = at<double>(ws, q.o_pos_part) + 2 * (size_t)s0 * q.Mp;
     fa.sim_out = simulate ? patterns + (size_t)s0 * WW : nullptr;

@@ -20,7 +20,9 @@ struct Plan {
   int W, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, nbatch, zm, ntx, nty, ntiles, nchunk, chunk;
   size_t o_tw, o_mask, o_mask_sc, o_prop, o_prop_edge, o_pyx, o_sx, o_sy, o_probe_f;
   size_t o_pos, o_corr, o_seq, o_obj, o_grad, o_obl, o_stack, o_gsum, o_fprobe, o_partial;
-  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, o_gbuf, o_psi, o_dldi, o_pgr, total;
+  size_t o_lists, o_counts, o_loss_part, o_pos_part, o_sim, o_err, o_gbuf, o_psi, o_dldi, o_pgr, o_seg, o_gpark;
+  size_t total;
+  int ckpt;   // kept slices every ckpt (256 windows)
   bool split;   // one batch with every position: pty_forward / pty_backward
 };
 
@@ -39,6 +41,7 @@ inline int validate(const pty_problem_t* p) {
   if (p->algorithm < PTY_LSQ_SQRT || p->algorithm > PTY_LSQ_SQRT_2) return PTY_ERR_UNSUPPORTED;
   if (p->step_pos && !p->probe_shift) return PTY_ERR_INVALID;
   if ((int64_t)p->obj_ny * p->obj_nx >= (int64_t)1 << 31) return PTY_ERR_UNSUPPORTED;
+  if (p->checkpoint_every > 1 && p->window != 256) return PTY_ERR_UNSUPPORTED;
   return PTY_OK;
 }
 
@@ -81,7 +84,9 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_obj = take((size_t)q.zm * q.Ny * q.Nx * c8);
   q.o_grad = take((size_t)q.zm * q.Ny * q.Nx * c8);
   q.o_obl = take((size_t)q.Bb * q.zm * WW * c8);
-  q.o_stack = take((size_t)q.Bb * q.Z * q.Mp * q.Mo * WW * c8);
+  q.ckpt = (p->window == 256 && p->checkpoint_every > 1) ? std::min(p->checkpoint_every, q.Z) : 1;
+  const int n_kept = (q.Z + q.ckpt - 1) / q.ckpt;
+  q.o_stack = take((size_t)q.Bb * n_kept * q.Mp * q.Mo * WW * c8);
   q.o_gsum = take((size_t)q.Bb * q.zm * WW * c8);
   q.o_fprobe = take((size_t)q.Bb * q.Mp * WW * c8);
   q.o_partial = take((size_t)q.nchunk * q.Mp * WW * c8);
@@ -96,6 +101,8 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_psi = take(w256 ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
   q.o_dldi = take(w256 && split ? (size_t)q.Bb * WW * f4 : 0);
   q.o_pgr = take(w256 && q.Mo > 1 ? (size_t)q.Bb * q.Mp * WW * c8 : 0);
+  q.o_seg = take(q.ckpt > 1 ? (size_t)q.Bb * q.ckpt * WW * c8 : 0);
+  q.o_gpark = take(q.ckpt > 1 ? (size_t)q.Bb * WW * c8 : 0);
   q.total = o;
   return q;
 }

@@ -255,6 +255,9 @@ struct FusedArgs {
   float2* psi;              // 256 windows: far-field wave per mode [Bb*Mp*Mo]
   float* dldi;              // 256 windows: dL/dI between the two halves [Bb]
   float2* pgr;              // 256 windows: object-mode sum of the probe gradient [Bb*Mp]
+  int ckpt;                 // 256 windows: keep every ckpt-th slice's wave, recompute the rest
+  float2* seg;              // 256 windows: recomputed waves of one segment [Bb*ckpt]
+  float2* gpark;            // 256 windows: adjoint wave parked during a recomputation [Bb]
   double* loss_part;        // [Bb][2]
   double* pos_part;         // [Bb][Mp][2]
   float* sim_out;           // [Bb][W][W] simulated mean intensity (detector order)

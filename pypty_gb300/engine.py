@@ -39,7 +39,8 @@ class Geometry:
 def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, wavelength,
                  pixel_size_x, pixel_size_y, slice_distance, edge_mult=1.0,
                  damping_cutoff=2 / 3, smooth_rolloff=0.0, loss_weight=1.0, compute_batch=None,
-                 step_obj=True, step_probe=True, step_pos=False, probe_shift=None) -> _lib.Problem:
+                 step_obj=True, step_probe=True, step_pos=False, probe_shift=None,
+                 checkpoint_every=1) -> _lib.Problem:
     ny, nx, nz, mo = obj_shape
     if isinstance(algorithm, str):
         if algorithm not in _lib.ALGORITHMS:
@@ -63,6 +64,7 @@ def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, 
     p.wavelength, p.pixel_size_x, p.pixel_size_y = wavelength, pixel_size_x, pixel_size_y
     p.slice_distance, p.edge_mult = slice_distance, edge_mult
     p.damping_cutoff, p.smooth_rolloff, p.loss_weight = damping_cutoff, smooth_rolloff, loss_weight
+    p.checkpoint_every = int(checkpoint_every)
     return p
 
 

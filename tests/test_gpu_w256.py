@@ -80,3 +80,76 @@ def test_w256_forward_adjoint_split_matches_one_shot():
     assert rel_l2(og.cpu().numpy(), one[2]) <= 1e-6
     assert rel_l2(pg.cpu().numpy(), one[3]) <= 1e-6
     assert rel_l2(posg.cpu().numpy(), one[4]) <= 1e-6
+
+
+def _run_with(c, **kw):
+    import torch
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    dev = torch.device("cuda", 0)
+    eng = Engine(dev)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    W = c["probe"].shape[0]
+    prob = make_problem(W, c["obj"].shape, c["probe"].shape[2], geo, algorithm=c["algorithm"],
+                        wavelength=c["wavelength"], pixel_size_x=c["px"], pixel_size_y=c["px"],
+                        slice_distance=c["distance"], edge_mult=c["edge_mult"], smooth_rolloff=c["rolloff"],
+                        compute_batch=c["batch"], step_pos=True, **kw)
+    out = eng.loss_and_direction(prob, torch.from_numpy(np.ascontiguousarray(c["obj"])).to(dev),
+                                 torch.from_numpy(np.ascontiguousarray(c["probe"])).to(dev), geo,
+                                 torch.from_numpy(np.ascontiguousarray(c["measured"])).to(dev))
+    torch.cuda.synchronize()
+    return [x.cpu().numpy() for x in out]
+
+
+@pytest.mark.parametrize("ckpt", [2, 3, 5])
+def test_recomputation_checkpointing_gives_identical_gradients(ckpt):
+    """Keeping every k-th slice and recomputing the rest reproduces the gradients bit for bit."""
+    c, _ = _case(5, 2, 1, "lsq_sqrt", seed=21, edge=1.5)
+    full = _run_with(c, checkpoint_every=1)
+    part = _run_with(c, checkpoint_every=ckpt)
+    for x, y in zip(full, part):
+        assert np.array_equal(x, y)
+
+
+def test_checkpointed_gradient_matches_finite_differences():
+    """Large-adjoint style check: phases of 64 random object pixels and the probe-mode
+    amplitudes, central differences of the loss against the checkpointed gradient."""
+    import torch
+    from pypty_gb300.autograd import multislice_loss
+    c, _ = _case(6, 3, 1, "lsq_sqrt", seed=33)
+    dev = torch.device("cuda", 0)
+    obj = torch.from_numpy(c["obj"]).to(dev)
+    probe = torch.from_numpy(c["probe"]).to(dev)
+    corr = torch.from_numpy(c["pos_correction"])
+    meas = torch.from_numpy(c["measured"]).to(dev)
+    kw = dict(algorithm="lsq_sqrt", wavelength=c["wavelength"], pixel_size_x=c["px"], pixel_size_y=c["px"],
+              slice_distance=c["distance"])
+    # gradient with checkpointing (every 3rd slice kept)
+    res = _run_with(c, checkpoint_every=3)
+    loss0, g_obj, g_probe = float(res[0][0]), res[1], res[2]
+    z0 = c["obj"].astype(np.complex128)
+    # dL/dphi per pixel: 2 Re(conj(dL/dz*) * i z); perturb the phases of the 64 pixels with the
+    # largest |dL/dphi| (sign along it), so the loss change stands well above float32 noise
+    dldphi = 2 * np.real(np.conj(g_obj.astype(np.complex128)) * 1j * z0)
+    top = np.argsort(np.abs(dldphi).ravel())[-64:]
+    dphi = np.zeros(z0.size, np.float64)
+    dphi[top] = np.sign(dldphi.ravel()[top])
+    dphi = dphi.reshape(z0.shape)
+    slope = float(np.sum(dldphi * dphi))
+
+    def L(o, p):
+        with torch.no_grad():
+            return multislice_loss(torch.from_numpy(o.astype(np.complex64)).to(dev),
+                                   torch.from_numpy(p.astype(np.complex64)).to(dev), corr, c["positions"], meas,
+                                   **kw).item()
+    h = 5e-3
+    fd = (L(z0 * np.exp(1j * h * dphi), c["probe"]) - L(z0 * np.exp(-1j * h * dphi), c["probe"])) / (2 * h)
+    assert abs(fd - slope) <= 2e-2 * abs(slope) + 1e-6 * abs(loss0), (fd, slope)
+    # probe-mode amplitude coefficients: P_j -> (1 + t) P_j
+    p0 = c["probe"].astype(np.complex128)
+    for j in range(p0.shape[2]):
+        dp = np.zeros_like(p0)
+        dp[:, :, j] = p0[:, :, j]
+        slope = float(np.sum(2 * np.real(np.conj(g_probe.astype(np.complex128)) * dp)))
+        hp = 1e-3
+        fd = (L(c["obj"], p0 + hp * dp) - L(c["obj"], p0 - hp * dp)) / (2 * hp)
+        assert abs(fd - slope) <= 2e-2 * abs(slope) + 1e-6 * abs(loss0), (j, fd, slope)
