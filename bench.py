@@ -48,6 +48,12 @@ CONFIGS = {
     # same kernels and shapes per position as "multislice", 8x8 positions: for ncu captures
     "multislice-small": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=8, algorithm="ml", batch=64,
                              desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 8x8 jittered scan, ml, batch 64"),
+    # 256-px windows, 5 modes, 40 slices over a 1024^2 object, 64x64 scan (FP32 FFT path)
+    "precision-sweep": dict(W=256, N_obj=1024, Z=40, Mp=5, n_scan=64, algorithm="lsq_sqrt", batch=512,
+                            desc="precision sweep W256 Z40 Mp5 Mo1, 1024x1024 object, 64x64 scan, lsq_sqrt, batch 512"),
+    # 256-px windows, 8 modes, 60 slices over a 2048^2 object, 128x128 scan, batch 512
+    "large-adjoint": dict(W=256, N_obj=2048, Z=60, Mp=8, n_scan=128, algorithm="lsq_sqrt", batch=512,
+                          desc="large adjoint W256 Z60 Mp8 Mo1, 2048x2048 object, 128x128 scan, lsq_sqrt, batch 512"),
     "single-slice": dict(W=64, N_obj=128, Z=1, Mp=1, n_scan=16, algorithm="lsq_sqrt", batch=256,
                          desc="single-slice W64 Z1 Mp1, 128x128 object, 16x16 scan, lsq_sqrt, batch 256"),
 }
@@ -80,7 +86,15 @@ def build_workload(cfg, seed=0):
     """Seeded specimen, probe and scan for a configuration (host arrays)."""
     from pypty_gb300 import synth
     rng = np.random.default_rng(seed)
-    if cfg["W"] == 128:
+    if cfg["W"] == 256:
+        px, kV, alpha, df = 0.1, 300.0, 30.0, 80.0
+        dz = 1.0 if cfg["Z"] == 40 else 2.0
+        atoms = 400 * (cfg["N_obj"] // 1024) ** 2
+        truth = synth.gaussian_phase_object(cfg["N_obj"], cfg["N_obj"], cfg["Z"], atoms, 0.3, px, 0.2, 1.0, rng)
+        probe = synth.make_probe(cfg["W"], px, kV, alpha, df, cfg["Mp"], 0.6 ** np.arange(cfg["Mp"]), 1e5)
+        pos = synth.raster_positions(cfg["n_scan"], cfg["n_scan"], 0.4 / px, 0.2 / px, rng)
+        dose = 1e5
+    elif cfg["W"] == 128:
         px, kV, alpha, df, dz = 0.1, 300.0, 30.0, 50.0, 2.0
         truth = synth.gaussian_phase_object(cfg["N_obj"], cfg["N_obj"], cfg["Z"], 150, 0.3, px, 0.2, 1.0, rng)
         probe = synth.make_probe(cfg["W"], px, kV, alpha, df, cfg["Mp"], [0.6, 0.3, 0.1][:cfg["Mp"]], 1e5)
@@ -212,6 +226,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="multislice", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--checkpoint", type=int, default=1,
+                    help="256-px windows: keep every k-th slice's wave, recompute the rest")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config], name=args.config)
     if args.impl == "reference":
@@ -238,7 +254,7 @@ def main():
     n_pos = geo.positions.shape[0]
     common = dict(algorithm=cfg["algorithm"], wavelength=wl["wavelength"], pixel_size_x=wl["px"],
                   pixel_size_y=wl["px"], slice_distance=wl["dz"], compute_batch=cfg["batch"])
-    prob = make_problem(W, wl["obj0"].shape, Mp, geo, step_pos=True, **common)
+    prob = make_problem(W, wl["obj0"].shape, Mp, geo, step_pos=True, checkpoint_every=args.checkpoint, **common)
     # measured data: forward model at the true specimen + Poisson noise
     truth_d = torch.from_numpy(wl["truth"]).to(dev)
     probe_d = torch.from_numpy(wl["probe"]).to(dev)
@@ -262,7 +278,8 @@ def main():
     barrier()
     torch.cuda.synchronize(dev)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler(64 * max(args.steps, 1)) as prof:
+    n_batches = -(-n_pos // cfg["batch"])
+    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler((16 + 8 * n_batches) * max(args.steps, 1)) as prof:
         start.record(stream)
         for _ in range(args.steps):
             eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)
@@ -348,6 +365,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": cfg["desc"], "positions_per_step": n_pos, "global_batch": n_pos * world,
+                   "checkpoint_every": args.checkpoint,
+                   "workspace_gb": round(_lib.workspace_bytes(prob) / 1e9, 2),
                    "parallelism": "replicas x%d" % world if world > 1 else "single GPU",
                    "l2": "working set per step >> 129 MB L2 (inputs 110 MB + 2 GB wave stack per batch); no flush"},
         "e2e": {"value": world * n_pos / (e2e_ms / 1000.0), "unit": "positions/s", "ms_per_step": e2e_ms,

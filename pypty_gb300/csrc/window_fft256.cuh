@@ -49,33 +49,33 @@ struct WinFFT256 {
   using G = Geo<128>;
   static constexpr int T = G::T;
 
-  // combine the four blocks' windows (held in their xbuf, native order) for block `me`:
-  // out_i = sum_r sign(me, r) * block_r[i], r = 0, 1, 2, 3 in that order. The same code runs
-  // in every block (only the signs differ); four elements per batch of shared-memory loads
-  // keep the register footprint bounded.
-  static __device__ __forceinline__ void cross(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl, int me) {
+  // Radix-2 x 2 butterfly across the four blocks, block `me` keeping output quadrant `me`:
+  //   out_me = sum_r (-1)^(me_y r_y + me_x r_x) in_r.
+  // It is separable: a stage with the x partner (me ^ 1) then a stage with the y partner
+  // (me ^ 2). In each stage every block stores its values into the partner's exchange
+  // buffer (remote shared-memory stores, which do not wait), the cluster synchronises, and
+  // the block combines its own values with the partner's from its local buffer:
+  //   bit of me clear: out = own + partner,  bit set: out = partner - own.
+  static __device__ __forceinline__ void cross_stage(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl,
+                                                     int me, int bit) {
     const int t = threadIdx.x;
-    __syncthreads();
+    cl.sync();   // the partner has finished with its exchange buffer
+    float2* dst = cl.map_shared_rank(xbuf, me ^ bit);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) xbuf[nidx<128>(i, t)] = v[i];
-    cl.sync();
-    const float2* r0 = cl.map_shared_rank(xbuf, 0);
-    const float2* r1 = cl.map_shared_rank(xbuf, 1);
-    const float2* r2 = cl.map_shared_rank(xbuf, 2);
-    const float2* r3 = cl.map_shared_rank(xbuf, 3);
-    const float s1 = quad_sign(me, 1), s2 = quad_sign(me, 2), s3 = quad_sign(me, 3);
+    for (int i = 0; i < 32; ++i) dst[nidx<128>(i, t)] = v[i];
+    cl.sync();   // the partner's values have arrived
+    const bool upper = (me & bit) != 0;
 #pragma unroll
-    for (int i0 = 0; i0 < 32; i0 += 4) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int e = nidx<128>(i0 + k, t);
-        const float2 a = r0[e], b = r1[e], c = r2[e], d = r3[e];
-        v[i0 + k] = make_float2(fmaf(s3, d.x, fmaf(s2, c.x, fmaf(s1, b.x, a.x))),
-                                fmaf(s3, d.y, fmaf(s2, c.y, fmaf(s1, b.y, a.y))));
-      }
-      asm volatile("" ::: "memory");   // keep the next batch's loads after this one
+    for (int i = 0; i < 32; ++i) {
+      const float2 o = xbuf[nidx<128>(i, t)];
+      v[i] = upper ? csub(o, v[i]) : cadd(v[i], o);
     }
-    cl.sync();   // every block is done reading the others' xbuf
+  }
+
+  static __device__ __forceinline__ void cross(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl, int me) {
+    cross_stage(v, xbuf, cl, me, 1);
+    cross_stage(v, xbuf, cl, me, 2);
+    cl.sync();   // every block is done with the exchange buffers
   }
 
   static __device__ __forceinline__ void forward(float2 (&v)[32], float2* xbuf, const float2* tw1, const float2* tw2,
