@@ -85,7 +85,8 @@ int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes);
  * recon_type "far_field", propmethod "multislice", no tilts, phase plates, aberration
  * arrays, beam-current fluctuations, static background or regularisers.
  *   obj, probe, measured        device, complex64 / float32, reference layouts
- *   positions_host, pos_correction_host, sequence_host   host memory
+ *   positions_host, sequence_host   host memory (checked on the host)
+ *   pos_correction_host         host or device memory (NULL: all zero)
  *   loss_sse                    device, 2 doubles: loss * loss_weight, sse
  *   object_grad                 device, complex64 (obj_ny, obj_nx, Z, Mo), overwritten
  *   probe_grad                  device, complex64 (W, W, Mp), overwritten (band-limited)
@@ -193,6 +194,80 @@ int pty_fft2_workspace_bytes(int32_t window, size_t* bytes);
  */
 int pty_fft2_noalloc(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
                      int32_t shift, void* stream);
+
+/*
+ * ---------------------------------------------------------------------------------------
+ * Optimizer step around loss_and_direction: the band limit `fourier_clean` and the
+ * L-BFGS / Wolfe line-search algebra of `bfgs_update`. The host keeps the loop (trial
+ * steps, Wolfe decisions, history list); every array operation and every scalar of the
+ * recursion runs on the device.
+ */
+
+/*
+ * out = fourier_clean(x + step * dx) over axes 0 and 1 of an (ny, nx, k) complex64 array
+ * (k = every trailing axis flattened; replaces pypty/utils.py:102-150 for 2D, 3D and 4D
+ * arrays): fftshift(fft2) times the band-limit mask, then ifft2(ifftshift).
+ * The mask is utils.fourier_clean's: radius 0.5 * cutoff in cycles per pixel, cosine roll-off
+ * of width `rolloff` (0: none), computed with the reference's float32 / float64 promotions;
+ * or, when mask_shifted is not NULL, the caller's (ny, nx) float32 mask in fftshifted order
+ * (the `mask=` argument). dx may be NULL (then step is ignored); x may be NULL (in place on
+ * out); x and out may alias. ny and nx: powers of two in [64, 8192], else
+ * PTY_ERR_UNSUPPORTED.
+ */
+int pty_fourier_clean_workspace_bytes(int32_t ny, int32_t nx, size_t* bytes);
+int pty_fourier_clean(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx,
+                      int64_t k, float cutoff, float rolloff, const float* mask_shifted,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * The optimizer's vector space: up to three float32 segments (the object, the probe and the
+ * position corrections of pypty/iterative.py:583-606; a complex64 element counts as two
+ * floats). Every inner product is sum_seg weight[seg] * <a_seg, b_seg>; the reference's
+ * weights are 2 for the complex segments and 1 for the positions (iterative.py:597-606).
+ * obj_seg names the object segment for the first step's normalisation (-1: none).
+ * Vectors are passed as arrays of n_seg device pointers.
+ */
+typedef struct pty_vspace {
+  int32_t n_seg;
+  int32_t obj_seg;
+  int64_t n[3];
+  double weight[3];
+} pty_vspace_t;
+
+/* Device bytes of the optimizer state (FP64 scalars, partial sums); caller-allocated. */
+int pty_lbfgs_state_bytes(size_t* bytes);
+/* Clear the state: weights from vs, gammas 1 (pypty/iterative.py:1055-1103). */
+int pty_lbfgs_reset(const pty_vspace_t* vs, void* state, void* stream);
+/* Empty history: dir = -g scaled per segment so that every segment's step matches the
+ * object's (iterative.py:562-571); d_value = <dir, g>. */
+int pty_lbfgs_first_direction(const pty_vspace_t* vs, float* const* grad, float* const* dir, void* state,
+                              void* stream);
+/* Steepest-descent fallback of a non-negative d_value (iterative.py:691-724): dir = -gamma g. */
+int pty_lbfgs_steepest(const pty_vspace_t* vs, float* const* grad, float* const* dir, void* state,
+                       void* stream);
+/* L-BFGS two-loop recursion (iterative.py:583-681): dir = -H g from m history pairs
+ * (s_hist, y_hist: m x n_seg pointers, oldest first; slots: their rho/alpha slots < 64).
+ * The caller band-limits the object segment of dir afterwards and calls pty_lbfgs_dot. */
+int pty_lbfgs_two_loop(const pty_vspace_t* vs, float* const* grad, float* const* dir, int32_t m,
+                       float* const* s_hist, float* const* y_hist, const int32_t* slots, void* state,
+                       void* stream);
+/* Weighted inner product <x, y> into d_value (target 0, iterative.py:684-690) or
+ * new_d_value (target 1, iterative.py:811-817). */
+int pty_lbfgs_dot(const pty_vspace_t* vs, float* const* x, float* const* y, int32_t target, void* state,
+                  void* stream);
+/* out = a + step * b per segment (trial points, iterative.py:759-771). */
+int pty_lbfgs_axpy(const pty_vspace_t* vs, float* const* out, float* const* a, float* const* b, double step,
+                   void* stream);
+/* Accepted step (iterative.py:849-916): s_out = step * dir, y_out = new_grad - grad,
+ * gamma_seg = weight <y, s> / <y, y>, rho[slot] = 1 / sum_seg weight <y, s>. */
+int pty_lbfgs_accept(const pty_vspace_t* vs, double step, float* const* dir, float* const* grad,
+                     float* const* new_grad, float* const* s_out, float* const* y_out, int32_t slot,
+                     void* state, void* stream);
+/* Synchronising read of 8 doubles: d_value, new_d_value, gamma[3], last reduced dots[3]. */
+int pty_lbfgs_read(const void* state, double* out, void* stream);
+/* Gram-Schmidt over the modes of a (n_pixels, n_modes) complex64 probe, in place
+ * (pypty/objective.py:1119-1141, keep_probe_states_orthogonal). */
+int pty_orthogonalize_modes(void* probe, int64_t n_pixels, int32_t n_modes, void* stream);
 
 /*
  * Launch profiler (no counterpart in the reference, which only logs wall time,

@@ -37,6 +37,12 @@ class Problem(ctypes.Structure):
     ]
 
 
+class VSpace(ctypes.Structure):
+    """Mirror of ``pty_vspace_t``: the optimizer's (object, probe, positions) segments."""
+    _fields_ = [("n_seg", ctypes.c_int32), ("obj_seg", ctypes.c_int32),
+                ("n", ctypes.c_int64 * 3), ("weight", ctypes.c_double * 3)]
+
+
 class PtyError(RuntimeError):
     """A PTY_ERR_* status returned by the library."""
 
@@ -53,6 +59,11 @@ _I32P = ctypes.POINTER(ctypes.c_int32)
 _F32P = ctypes.POINTER(ctypes.c_float)
 _F64P = ctypes.POINTER(ctypes.c_double)
 _PP = ctypes.POINTER(Problem)
+_VS = ctypes.POINTER(VSpace)
+_PPV = ctypes.POINTER(ctypes.c_void_p)
+_F64 = ctypes.c_double
+_F32 = ctypes.c_float
+_I64 = ctypes.c_int64
 
 SIGNATURES = {
     "pty_version": ([], ctypes.c_int),
@@ -76,6 +87,18 @@ SIGNATURES = {
     "pty_profile_end": ([_F64P, _I32P, _I32], ctypes.c_int),
     "pty_kernel_name": ([_I32], ctypes.c_char_p),
     "pty_kernel_count": ([], ctypes.c_int),
+    "pty_fourier_clean_workspace_bytes": ([_I32, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_fourier_clean": ([_VP, _VP, _F64, _VP, _I32, _I32, _I64, _F32, _F32, _VP, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_lbfgs_state_bytes": ([ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_lbfgs_reset": ([_VS, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_first_direction": ([_VS, _PPV, _PPV, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_steepest": ([_VS, _PPV, _PPV, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_two_loop": ([_VS, _PPV, _PPV, _I32, _PPV, _PPV, _I32P, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_dot": ([_VS, _PPV, _PPV, _I32, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_axpy": ([_VS, _PPV, _PPV, _PPV, _F64, _VP], ctypes.c_int),
+    "pty_lbfgs_accept": ([_VS, _F64, _PPV, _PPV, _PPV, _PPV, _PPV, _I32, _VP, _VP], ctypes.c_int),
+    "pty_lbfgs_read": ([_VP, _F64P, _VP], ctypes.c_int),
+    "pty_orthogonalize_modes": ([_VP, _I64, _I32, _VP], ctypes.c_int),
 }
 
 

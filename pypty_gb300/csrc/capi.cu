@@ -21,7 +21,8 @@ int upload_geometry(const pty_problem_t* p, const Plan& q, void* ws, const int32
       cudaSuccess)
     return PTY_ERR_CUDA;
   if (corr) {
-    if (cudaMemcpyAsync(at<float>(ws, q.o_corr), corr, (size_t)q.N * 2 * sizeof(float), cudaMemcpyHostToDevice,
+    // host or device memory: the optimizer passes device-resident trial corrections
+    if (cudaMemcpyAsync(at<float>(ws, q.o_corr), corr, (size_t)q.N * 2 * sizeof(float), cudaMemcpyDefault,
                         st) != cudaSuccess)
       return PTY_ERR_CUDA;
   } else if (cudaMemsetAsync(at<float>(ws, q.o_corr), 0, (size_t)q.N * 2 * sizeof(float), st) != cudaSuccess) {
@@ -73,7 +74,8 @@ Profiler g_prof;
 const char* kKernelNames[KID_COUNT] = {
     "build_twiddles", "tables", "probe_fft", "obj_to_slices", "object_windows", "fused_multislice",
     "grad_windows", "tile_lists", "scatter_tiles", "probe_partial", "slices_to_obj", "probe_final",
-    "finalize_scalars", "fft2_batch", "layout"};
+    "finalize_scalars", "fft2_batch", "layout", "clean_tables", "clean_pass_x", "clean_pass_y",
+    "clean_pass_x_inverse", "opt_vector", "opt_scalar", "opt_accept", "orthogonalize_modes"};
 
 }  // namespace
 

@@ -182,7 +182,8 @@ inline MsPlan make_ms_plan(int W, int B, int Z, int Mp, int Mo, int Ny, int Nx) 
 enum KernelId : int {
   KID_TWIDDLES = 0, KID_TABLES, KID_PROBE_FFT, KID_OBJ_TO_SLICES, KID_OBJECT_WINDOWS, KID_FUSED,
   KID_GRAD_WINDOWS, KID_TILE_LISTS, KID_SCATTER, KID_PROBE_PARTIAL, KID_SLICES_TO_OBJ, KID_PROBE_FINAL,
-  KID_FINALIZE, KID_FFT2, KID_LAYOUT, KID_COUNT
+  KID_FINALIZE, KID_FFT2, KID_LAYOUT, KID_CLEAN_TABLES, KID_CLEAN_X, KID_CLEAN_Y, KID_CLEAN_XI,
+  KID_VEC, KID_SCALAR, KID_ACCEPT, KID_ORTHO, KID_COUNT
 };
 
 // Records an event on `st` before a launch of kernel class `id` while profiling is on

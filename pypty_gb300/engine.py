@@ -79,6 +79,7 @@ class Engine:
         _lib.lib()
         self.device = torch.device(device if device is not None else "cuda")
         self._ws = None
+        self._aux = {}
         self._stage = None
         self._stage_event = None
 
@@ -88,6 +89,14 @@ class Engine:
             self._ws = None
             self._ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
         return self._ws
+
+    def aux(self, key: str, nbytes: int) -> torch.Tensor:
+        """A device buffer of at least nbytes kept per key (small tables, optimizer state),
+        separate from the loss-and-gradient workspace."""
+        buf = self._aux.get(key)
+        if buf is None or buf.numel() < nbytes:
+            buf = self._aux[key] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
+        return buf
 
     def _staging(self, geo: Geometry):
         """Page-locked copies of the geometry (the C ABI uploads them asynchronously)."""
@@ -113,10 +122,13 @@ class Engine:
 
     # ---------------------------------------------------------------- calls
     def loss_and_direction(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor,
-                           geo: Geometry, measured: torch.Tensor, out=None, stream=None):
+                           geo: Geometry, measured: torch.Tensor, out=None, stream=None,
+                           pos_correction: torch.Tensor | None = None):
         """Run the fused path. obj (Ny,Nx,Z,Mo) complex64, probe (W,W,Mp) complex64 and
         measured (N,W,W) float32 on the device. Returns (loss_sse float64[2], object_grad,
-        probe_grad, pos_grad) device tensors (loss_sse = [loss * loss_weight, sse])."""
+        probe_grad, pos_grad) device tensors (loss_sse = [loss * loss_weight, sse]).
+        pos_correction: optional (N, 2) float32 CUDA tensor used instead of the geometry's
+        host corrections (the optimizer's device-resident trial positions)."""
         stream = stream or torch.cuda.current_stream(self.device)
         self._check_inputs(problem, obj, probe, measured)
         if out is None:
@@ -126,6 +138,12 @@ class Engine:
         loss_sse, og, pg, posg = out
         ws = self.workspace(_lib.workspace_bytes(problem))
         pp, pc, ps = self._staging(geo)
+        if pos_correction is not None:
+            if (not pos_correction.is_cuda or pos_correction.dtype != torch.float32
+                    or tuple(pos_correction.shape) != (problem.n_positions, 2)
+                    or not pos_correction.is_contiguous()):
+                raise ValueError("pos_correction must be a contiguous (N, 2) float32 CUDA tensor")
+            pc = pos_correction.data_ptr()
         st = _lib.lib().pty_loss_and_direction(
             ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
             _ptr(loss_sse), _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)

@@ -51,7 +51,7 @@ def _device_tensor(a, dtype, device):
     return torch.from_numpy(np.ascontiguousarray(_to_numpy(a))).to(device=device, dtype=dtype)
 
 
-def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
+def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
                        this_tilts_correction, this_distances, edge_slice_thickness_multiplier,
                        measured_array, algorithm_type, this_wavelength, this_step_probe, this_step_obj,
                        this_step_pos_correction, this_step_tilts, masks, pixel_size_x_A, pixel_size_y_A,
@@ -69,12 +69,9 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
                        abs_norm_weight, atv_weight, atv_q, atv_p, mixed_variance_weight, mixed_variance_sigma,
                        wedge_mu, beta_wedge, probe_mod_reg_weight, probe_mod_tol, smart_memory, print_flag,
                        data_simulation_flag, data_simulation_exitwave, use_padded_intensity):
-    """GPU restatement of ``pypty/objective.py:47-967`` (see the module docstring for the
-    supported flag set). Returns (loss, sse, object_grad, probe_grad, pos_grad, tilts_grad,
-    static_background_grad, aberrations_array_grad, beam_current_grad,
-    constraint_contributions) with the reference's shapes. Arrays come back as NumPy arrays
-    when the object was given as a NumPy array, else as CUDA tensors.
-    """
+    """Check the arguments of ``loss_and_direction`` against the supported flag set and
+    build the C-ABI problem and scan geometry: returns (problem, geometry).
+    ``NotImplementedError`` names the first unsupported flag."""
     _unsupported(recon_type != "far_field", "recon_type=%r" % (recon_type,))
     _unsupported(propmethod != "multislice", "propmethod=%r" % (propmethod,))
     _unsupported(algorithm_type not in _lib.ALGORITHMS, "algorithm_type=%r" % (algorithm_type,))
@@ -102,22 +99,14 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     for name, w in [("probe_reg_weight", probe_reg_weight), ("current_window_weight", current_window_weight),
                     ("probe_mod_reg_weight", probe_mod_reg_weight)]:
         _unsupported(bool(this_step_probe) and w != 0, name)
-    obj_is_numpy = not isinstance(this_obj, torch.Tensor)
     obj_shape = tuple(this_obj.shape)
     _unsupported(len(obj_shape) != 4, "objects that are not 4D (y, x, slice, mode)")
     _unsupported(len(tuple(full_probe.shape)) != 3, "probes that are not 3D (y, x, mode)")
     _unsupported(mixed_variance_weight != 0 and obj_shape[3] > 1, "mixed_variance_weight")
     W = int(full_probe.shape[0])
     Mp = int(full_probe.shape[2])
-    in_dtype = this_obj.dtype
-
     geo = Geometry.make(_to_numpy(this_pos_array), _to_numpy(this_pos_correction),
                         _to_numpy(this_chopped_sequence))
-    eng = default_engine()
-    dev = eng.device
-    obj_d = _device_tensor(this_obj, torch.complex64, dev)
-    probe_d = _device_tensor(full_probe, torch.complex64, dev)
-    meas_d = _device_tensor(measured_array, torch.float32, dev)
     problem = make_problem(
         W, obj_shape, Mp, geo, algorithm=algorithm_type, wavelength=float(this_wavelength),
         pixel_size_x=float(pixel_size_x_A), pixel_size_y=float(pixel_size_y_A),
@@ -127,6 +116,42 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         smooth_rolloff=float(smooth_rolloff), loss_weight=float(this_loss_weight),
         compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
         step_pos=bool(this_step_pos_correction))
+    return problem, geo
+
+
+def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
+                       this_tilts_correction, this_distances, edge_slice_thickness_multiplier,
+                       measured_array, algorithm_type, this_wavelength, this_step_probe, this_step_obj,
+                       this_step_pos_correction, this_step_tilts, masks, pixel_size_x_A, pixel_size_y_A,
+                       recon_type, Cs, defocus_array, alpha_near_field, damping_cutoff_multislice,
+                       smooth_rolloff, propmethod, this_chopped_sequence, load_one_by_one, data_multiplier,
+                       data_pad, phase_plate_in_h5, this_loss_weight, data_bin, data_shift_vector,
+                       upsample_pattern, static_background, this_step_static_background, tilt_mode,
+                       aberration_marker, probe_marker, aberrations_array, compute_batch, phase_only_obj,
+                       beam_current, this_beam_current_step, this_step_aberrations_array, default_float,
+                       default_complex, xp, is_first_epoch, scan_size, scan_step_A,
+                       fast_axis_reg_weight_positions, slow_axis_reg_weight_positions,
+                       slow_axis_reg_weight_tilts, current_deformation_reg_weight_positions,
+                       current_deformation_reg_weight_tilts, fast_axis_reg_weight_tilts, aperture_mask,
+                       probe_reg_weight, current_window_weight, current_window, phase_norm_weight,
+                       abs_norm_weight, atv_weight, atv_q, atv_p, mixed_variance_weight, mixed_variance_sigma,
+                       wedge_mu, beta_wedge, probe_mod_reg_weight, probe_mod_tol, smart_memory, print_flag,
+                       data_simulation_flag, data_simulation_exitwave, use_padded_intensity):
+    """GPU restatement of ``pypty/objective.py:47-967`` (see the module docstring for the
+    supported flag set). Returns (loss, sse, object_grad, probe_grad, pos_grad, tilts_grad,
+    static_background_grad, aberrations_array_grad, beam_current_grad,
+    constraint_contributions) with the reference's shapes. Arrays come back as NumPy arrays
+    when the object was given as a NumPy array, else as CUDA tensors.
+    """
+    args = dict(locals())
+    problem, geo = prepare(**args)
+    obj_is_numpy = not isinstance(this_obj, torch.Tensor)
+    in_dtype = this_obj.dtype
+    eng = default_engine()
+    dev = eng.device
+    obj_d = _device_tensor(this_obj, torch.complex64, dev)
+    probe_d = _device_tensor(full_probe, torch.complex64, dev)
+    meas_d = _device_tensor(measured_array, torch.float32, dev)
     loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
     ls = loss_sse.cpu().numpy()
     loss, sse = float(ls[0]), float(ls[1])

@@ -11,7 +11,7 @@ def loss_case_names():
     names = []
     for p in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
         n = os.path.basename(p)[:-4]
-        if not n.startswith("core_"):
+        if not n.startswith(("core_", "fourier_clean", "lbfgs_")):
             names.append(n)
     return names
 

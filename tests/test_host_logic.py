@@ -93,3 +93,31 @@ def test_window_index_arrays_are_recognised_and_others_rejected():
     assert np.array_equal(_window_positions(my, mx, W), pos)
     with pytest.raises(NotImplementedError):
         _window_positions(my[:, ::-1], mx, W)
+
+
+def test_bfgs_update_signature_is_mirrored():
+    import inspect
+    from pypty_gb300 import iterative
+    params = list(inspect.signature(iterative.bfgs_update).parameters)
+    assert len(params) == 95
+    assert params[:4] == ["algorithm_type", "this_slice_distances", "edge_slice_thickness_multiplier",
+                          "this_step_probe"]
+    assert params[-1] == "counter_failed_epochs"
+    assert params[params.index("hist_length") + 1] == "actual_step"
+    bound = iterative.bind(object())
+    assert list(inspect.signature(bound).parameters) == params
+
+
+@pytest.mark.parametrize("flag", ["phase_only_obj", "tune_only_probe_phase", "this_step_tilts", "do_charge_flip",
+                                  "current_gaussian_filter", "this_beam_current_step"])
+def test_bfgs_update_unsupported_options_raise_before_any_gpu_work(flag):
+    import inspect
+    import types
+    from pypty_gb300 import iterative
+    ns = types.ModuleType("ns")
+    ns.probe = np.zeros((64, 64, 1), np.complex64)
+    kw = {p: 0 for p in inspect.signature(iterative.bfgs_update).parameters}
+    kw.update(this_step_obj=1, this_step_probe=1, this_step_pos_correction=0, warnings="")
+    kw[flag] = 1
+    with pytest.raises(NotImplementedError):
+        iterative.bind(ns)(**kw)
