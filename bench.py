@@ -192,6 +192,61 @@ def cpu_baseline(cfg, wl, algorithm, budget_s=15.0):
                 n, cfg["name"], dt), "seconds": dt, "positions": n}
 
 
+def optimizer_step(eng, prob, geo, meas_d, obj_d, probe_d, wl, lad_ms, hbm_peak, peak_src, epochs=4):
+    """The optimizer around loss_and_direction on the same workload: the full-object band
+    limit of a trial point (pty_fourier_clean_apply, timed with CUDA events, HBM roofline over
+    its algorithmic bytes: read x and dx, write the result) and whole L-BFGS epochs
+    (LBFGS.step, wall time around device work and the per-trial host reads)."""
+    import torch
+    from pypty_gb300 import _lib
+    from pypty_gb300.optim import LBFGS, LineSearchConfig, fourier_clean_
+    dev = obj_d.device
+    stream = torch.cuda.current_stream(dev)
+    cut = np.float32(2 / 3) - np.float32(0.005)
+    dx = torch.randn_like(obj_d)
+    tmp = torch.empty_like(obj_d)
+    for _ in range(3):
+        fourier_clean_(obj_d, cut, 0.0, out=tmp, dx=dx, step=0.3, engine=eng)
+    torch.cuda.synchronize(dev)
+    n = 10
+    with _lib.LaunchProfiler(64 * n) as prof:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fourier_clean_(obj_d, cut, 0.0, out=tmp, dx=dx, step=0.3, engine=eng)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    clean_ms = e0.elapsed_time(e1) / n
+    clean_bytes = 3 * obj_d.numel() * 8
+    clean_gbs = clean_bytes / (clean_ms / 1e3) / 1e9
+    passes = {k: round(prof.ms.get(k, 0.0) / n, 4) for k in ("clean_pass_x", "clean_pass_y", "clean_pass_x_inverse")}
+    del dx, tmp
+    corr_d = torch.from_numpy(np.ascontiguousarray(geo.pos_correction)).to(dev)
+    opt = LBFGS(prob, geo, meas_d, obj_d.clone(), probe_d.clone(), corr_d,
+                LineSearchConfig(update_obj=True, update_probe=True, update_pos=True, wolfe_c1=0.1, max_count=20),
+                engine=eng)
+    np.random.seed(0)
+    rows = []
+    for e in range(epochs):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        # the first step from an empty history is -grad at unit scale: start it small, as the
+        # reference's own example schedule does ('update_step_bfgs': tiny if epoch == 0 else 1)
+        r = opt.step(1e-6 if e == 0 else 1)
+        torch.cuda.synchronize(dev)
+        wall = (time.perf_counter() - t0) * 1e3
+        n_lad = r.count + 1 + (1 if not rows else 0)
+        rows.append(dict(ms=round(wall, 3), lad_calls=n_lad, accepted=r.accepted,
+                         overhead_ms=round(wall - n_lad * lad_ms, 3)))
+    hist = [rw["overhead_ms"] for rw in rows[1:]] or [rows[0]["overhead_ms"]]
+    return {"fourier_clean": {"object": list(obj_d.shape), "ms": round(clean_ms, 4), "achieved": round(clean_gbs, 1),
+                              "unit": "GB/s", "alg_bytes": clean_bytes, "frac": round(clean_gbs / hbm_peak, 4),
+                              "peak_source": peak_src + " (hbm_gbs)", "pass_ms": passes},
+            "lbfgs_epochs": rows,
+            "overhead_ms_per_epoch_with_history": round(float(np.mean(hist)), 3),
+            "lad_ms": round(lad_ms, 3)}
+
+
 def run_reference(args, cfg):
     """--impl reference: the reference algorithm on the host cores, same metric and config."""
     rank = int(os.environ.get("RANK", "0"))
@@ -228,6 +283,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--checkpoint", type=int, default=1,
                     help="256-px windows: keep every k-th slice's wave, recompute the rest")
+    ap.add_argument("--no-optimizer", action="store_true",
+                    help="skip the optimizer-step measurement (fourier_clean, L-BFGS epoch)")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config], name=args.config)
     if args.impl == "reference":
@@ -383,6 +440,11 @@ def main():
         "clocks": {"sm_mhz": cs.get("sm_mhz"), "sm_max_mhz": cs.get("sm_max_mhz"), "reasons": cs.get("reasons")},
         "loss": loss_val,
     }
+    if not args.no_optimizer:
+        try:
+            line["optimizer"] = optimizer_step(eng, prob, geo, meas_d, obj_d, probe_d, wl, ms, hbm_peak, peak_src)
+        except (ValueError, RuntimeError) as exc:      # a diverging trial point: report, keep the line
+            line["optimizer"] = {"error": str(exc)}
     if not args.no_cpu_baseline:
         cb = cpu_baseline(cfg, wl, cfg["algorithm"])
         cb.pop("seconds", None)

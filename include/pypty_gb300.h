@@ -218,6 +218,13 @@ int pty_fourier_clean_workspace_bytes(int32_t ny, int32_t nx, size_t* bytes);
 int pty_fourier_clean(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx,
                       int64_t k, float cutoff, float rolloff, const float* mask_shifted,
                       void* workspace, size_t workspace_bytes, void* stream);
+/* pty_fourier_clean in two halves, for repeated cleans with one band limit: _prepare writes
+ * the twiddle and mask tables into the workspace, _apply uses them (the workspace must hold
+ * the tables of the same ny, nx and band limit, unmodified since _prepare). */
+int pty_fourier_clean_prepare(int32_t ny, int32_t nx, float cutoff, float rolloff, const float* mask_shifted,
+                              void* workspace, size_t workspace_bytes, void* stream);
+int pty_fourier_clean_apply(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx,
+                            int64_t k, const void* workspace, size_t workspace_bytes, void* stream);
 
 /*
  * The optimizer's vector space: up to three float32 segments (the object, the probe and the

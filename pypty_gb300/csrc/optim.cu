@@ -191,33 +191,31 @@ __global__ void twiddle_kernel(float2* tw, int n) {
   tw[m] = make_float2((float)cs, (float)-sn);
 }
 
-// numpy.fft.fftfreq(n)[k] = k_signed * (1.0 / n)
-__device__ __forceinline__ double fftfreq(int k, int n) {
-  const int ks = k < (n + 1) / 2 ? k : k - n;
-  return (double)ks * (1.0 / (double)n);
-}
-
 // Band limit of utils.fourier_clean (pypty/utils.py:128-138), in unshifted order:
 //   r = fx^2 + fy^2 (float64), max_r = 0.5 cutoff, mask = r <= max_r^2 (float32 cutoff
 //   arithmetic promoted to float64 for the comparison), and with a roll-off the cosine taper
 //   0.5 (1 + cos(3.141592654 (r - r0) / (max_r^2 - r0))) for r > r0 = (0.5 (cutoff - rolloff))^2.
 // A caller-given mask (fftshifted order, as utils.fourier_clean(mask=...) receives it) is
 // copied into unshifted order instead.
-__global__ void mask_kernel(float* mask, int ny, int nx, float cutoff, float rolloff, const float* given) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)ny * nx) return;
-  const int ky = (int)(idx / nx), kx = (int)(idx % nx);
+__global__ void mask_kernel(float* mask, int ny, int nx, double inv_ny, double inv_nx, float cutoff, float rolloff,
+                            const float* given) {
+  const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ky = blockIdx.y;
+  if (kx >= nx) return;
+  const long long idx = (long long)ky * nx + kx;
   if (given) {
     mask[idx] = given[(long long)((ky + ny / 2) % ny) * nx + (kx + nx / 2) % nx];
     return;
   }
-  const double fy = fftfreq(ky, ny), fx = fftfreq(kx, nx);
+  // numpy.fft.fftfreq(n)[k] = k_signed * (1.0 / n)
+  const double fy = (double)(ky < (ny + 1) / 2 ? ky : ky - ny) * inv_ny;
+  const double fx = (double)(kx < (nx + 1) / 2 ? kx : kx - nx) * inv_nx;
   const double r = fx * fx + fy * fy;
   const float max_r = __fmul_rn(0.5f, cutoff);
   const float thr = __fmul_rn(max_r, max_r);
   float m = r <= (double)thr ? 1.0f : 0.0f;
   if (rolloff != 0.0f) {
-    float h = __fmul_rn(0.5f, __fsub_rn(cutoff, rolloff));
+    const float h = __fmul_rn(0.5f, __fsub_rn(cutoff, rolloff));
     const float r0 = __fmul_rn(h, h);
     if (r > (double)r0) {
       const double t = 0.5 * (1.0 + cos(3.141592654 * (r - (double)r0) / (double)__fsub_rn(thr, r0)));
@@ -624,25 +622,36 @@ int pty_fourier_clean_workspace_bytes(int32_t ny, int32_t nx, size_t* bytes) {
   return PTY_OK;
 }
 
-int pty_fourier_clean(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx, int64_t k,
-                      float cutoff, float rolloff, const float* mask_shifted, void* workspace,
-                      size_t workspace_bytes, void* stream) {
+int pty_fourier_clean_prepare(int32_t ny, int32_t nx, float cutoff, float rolloff, const float* mask_shifted,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  if (!workspace || ny <= 0 || nx <= 0) return PTY_ERR_INVALID;
+  if (!pow2_in_range(ny) || !pow2_in_range(nx)) return PTY_ERR_UNSUPPORTED;
+  const CleanWs w = clean_ws(ny, nx);
+  if (workspace_bytes < w.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  prof_mark(st, KID_CLEAN_TABLES);
+  twiddle_kernel<<<(nx + 255) / 256, 256, 0, st>>>(at<float2>(workspace, w.o_twx), nx);
+  prof_mark(st, KID_CLEAN_TABLES);
+  twiddle_kernel<<<(ny + 255) / 256, 256, 0, st>>>(at<float2>(workspace, w.o_twy), ny);
+  prof_mark(st, KID_CLEAN_TABLES);
+  mask_kernel<<<dim3((nx + 255) / 256, ny), 256, 0, st>>>(at<float>(workspace, w.o_mask), ny, nx, 1.0 / (double)ny,
+                                                          1.0 / (double)nx, cutoff, rolloff, mask_shifted);
+  prof_mark(st, -1);
+  return cudaGetLastError() == cudaSuccess ? PTY_OK : PTY_ERR_CUDA;
+}
+
+int pty_fourier_clean_apply(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx, int64_t k,
+                            const void* workspace, size_t workspace_bytes, void* stream) {
   if (!out || !workspace || ny <= 0 || nx <= 0 || k <= 0) return PTY_ERR_INVALID;
   if (!pow2_in_range(ny) || !pow2_in_range(nx)) return PTY_ERR_UNSUPPORTED;
   const CleanWs w = clean_ws(ny, nx);
   if (workspace_bytes < w.total) return PTY_ERR_WORKSPACE;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  float2* twx = at<float2>(workspace, w.o_twx);
-  float2* twy = at<float2>(workspace, w.o_twy);
-  float* mask = at<float>(workspace, w.o_mask);
-  prof_mark(st, KID_CLEAN_TABLES);
-  twiddle_kernel<<<(nx + 255) / 256, 256, 0, st>>>(twx, nx);
-  prof_mark(st, KID_CLEAN_TABLES);
-  twiddle_kernel<<<(ny + 255) / 256, 256, 0, st>>>(twy, ny);
+  void* ws = const_cast<void*>(workspace);
+  const float2* twx = at<float2>(ws, w.o_twx);
+  const float2* twy = at<float2>(ws, w.o_twy);
+  const float* mask = at<float>(ws, w.o_mask);
   const long long npix = (long long)ny * nx;
-  prof_mark(st, KID_CLEAN_TABLES);
-  mask_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(mask, ny, nx, cutoff, rolloff, mask_shifted);
-  if (cudaGetLastError() != cudaSuccess) return PTY_ERR_CUDA;
   PassArgs A{};
   A.out = static_cast<float2*>(out);
   // pass X: lines (y, k), element stride K
@@ -672,6 +681,15 @@ int pty_fourier_clean(const void* x, const void* dx, double step, void* out, int
   if (dispatch_pass<2>(nx, A, st) != cudaSuccess) return PTY_ERR_CUDA;
   prof_mark(st, -1);
   return PTY_OK;
+}
+
+int pty_fourier_clean(const void* x, const void* dx, double step, void* out, int32_t ny, int32_t nx, int64_t k,
+                      float cutoff, float rolloff, const float* mask_shifted, void* workspace,
+                      size_t workspace_bytes, void* stream) {
+  if (!out || k <= 0) return PTY_ERR_INVALID;
+  int rc = pty_fourier_clean_prepare(ny, nx, cutoff, rolloff, mask_shifted, workspace, workspace_bytes, stream);
+  if (rc) return rc;
+  return pty_fourier_clean_apply(x, dx, step, out, ny, nx, k, workspace, workspace_bytes, stream);
 }
 
 int pty_lbfgs_state_bytes(size_t* bytes) {

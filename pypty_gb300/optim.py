@@ -63,23 +63,36 @@ def fourier_clean_(x: torch.Tensor, cutoff=None, rolloff=0.0, mask=None, out: to
         out = torch.empty_like(x)
     if dx is not None and (dx.shape != x.shape or dx.dtype != x.dtype or not dx.is_contiguous()):
         raise ValueError("dx must match x")
+    ws = _clean_tables(eng, ny, nx, cutoff, rolloff, mask)
+    _lib.check(_lib.lib().pty_fourier_clean_apply(
+        x.data_ptr(), dx.data_ptr() if dx is not None else None, float(step), out.data_ptr(), ny, nx, k,
+        ws.data_ptr(), ws.numel(), _stream(eng)), "pty_fourier_clean_apply")
+    return out
+
+
+def _clean_tables(eng: Engine, ny, nx, cutoff, rolloff, mask):
+    """Twiddle and band-limit tables of one (ny, nx, cutoff, rolloff), prepared once per
+    engine (``pty_fourier_clean_prepare``); a caller-given mask is prepared every call."""
     n = ctypes.c_size_t(0)
     _lib.check(_lib.lib().pty_fourier_clean_workspace_bytes(ny, nx, ctypes.byref(n)),
                "pty_fourier_clean_workspace_bytes (object extents must be powers of two in [64, 8192])")
-    ws = eng.aux("fourier_clean", int(n.value))
-    mask_ptr = None
     if mask is not None:
         m = mask if isinstance(mask, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(
             np.asarray(mask.get() if hasattr(mask, "get") else mask, dtype=np.float32)))
-        m = m.to(device=x.device, dtype=torch.float32).reshape(ny, nx).contiguous()
-        eng._aux["fourier_clean_mask"] = m     # alive until the kernels have read it
-        mask_ptr = m.data_ptr()
-        cutoff, rolloff = 0.0, 0.0
-    _lib.check(_lib.lib().pty_fourier_clean(
-        x.data_ptr(), dx.data_ptr() if dx is not None else None, float(step), out.data_ptr(), ny, nx, k,
-        float(np.float32(cutoff)), float(np.float32(rolloff)), mask_ptr, ws.data_ptr(), ws.numel(),
-        _stream(eng)), "pty_fourier_clean")
-    return out
+        m = m.to(device=eng.device, dtype=torch.float32).reshape(ny, nx).contiguous()
+        ws = eng.aux("fourier_clean_given_mask", int(n.value))
+        eng._aux["fourier_clean_mask_src"] = m     # alive until the kernels have read it
+        _lib.check(_lib.lib().pty_fourier_clean_prepare(ny, nx, 0.0, 0.0, m.data_ptr(), ws.data_ptr(), ws.numel(),
+                                                        _stream(eng)), "pty_fourier_clean_prepare")
+        return ws
+    c32, r32 = np.float32(cutoff), np.float32(rolloff)
+    key = "fourier_clean:%d:%d:%08x:%08x" % (ny, nx, c32.view(np.uint32), r32.view(np.uint32))
+    ws = eng._aux.get(key)
+    if ws is None:
+        ws = eng.aux(key, int(n.value))
+        _lib.check(_lib.lib().pty_fourier_clean_prepare(ny, nx, float(c32), float(r32), None, ws.data_ptr(),
+                                                        ws.numel(), _stream(eng)), "pty_fourier_clean_prepare")
+    return ws
 
 
 def orthogonalize_modes_(probe: torch.Tensor, engine: Engine | None = None) -> torch.Tensor:
