@@ -179,6 +179,19 @@ int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t i
 int pty_fft2_workspace_bytes(int32_t window, size_t* bytes);
 
 /*
+ * The same batched 2D DFT of `batch` contiguous W x W complex64 windows (W = 64, 128, 256) as
+ * dense GEMMs on the tensor cores (tcgen05, BF16x3 split precision: every FP32 operand is
+ * hi + lo in BF16 and the three significant products accumulate in FP32 in tensor memory).
+ * inverse = 1: scaled by 1/W^2. No shift. in and out must not alias. Relative error ~1e-5
+ * against an FP64 DFT (the FP32 register FFT, pty_fft2, is ~1e-7). Replaces pypty.fft.fft2 /
+ * ifft2 over axes (1, 2) (pypty/fft.py:114-156) in the precision sweep; no counterpart in
+ * the reference.
+ */
+int pty_fft2_bf16x3_workspace_bytes(int32_t batch, int32_t window, size_t* bytes);
+int pty_fft2_bf16x3(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * pty_fft2 without a workspace argument; it allocates nothing. No counterpart in the
  * reference: it exists for callers that cannot allocate device memory -- an application
  * whose own memory pool owns every device allocation, code running while a CUDA graph is

@@ -91,6 +91,8 @@ SIGNATURES = {
     "pty_fourier_clean": ([_VP, _VP, _F64, _VP, _I32, _I32, _I64, _F32, _F32, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fourier_clean_prepare": ([_I32, _I32, _F32, _F32, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fourier_clean_apply": ([_VP, _VP, _F64, _VP, _I32, _I32, _I64, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_fft2_bf16x3_workspace_bytes": ([_I32, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_fft2_bf16x3": ([_VP, _VP, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
     "pty_lbfgs_state_bytes": ([ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_lbfgs_reset": ([_VS, _VP, _VP], ctypes.c_int),
     "pty_lbfgs_first_direction": ([_VS, _PPV, _PPV, _VP, _VP], ctypes.c_int),

@@ -216,6 +216,26 @@ class Engine:
         _lib.check(st, "pty_fft2")
         return out
 
+    def fft2_bf16x3(self, x: torch.Tensor, inverse: bool = False, out=None, stream=None):
+        """Batched 2D DFT over the last two axes of a (..., W, W) complex64 device tensor on the
+        tensor cores in BF16x3 split precision (``pty_fft2_bf16x3``; W = 64, 128, 256)."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        if x.dtype != torch.complex64 or not x.is_cuda:
+            raise TypeError("fft2_bf16x3 needs a complex64 CUDA tensor")
+        W = x.shape[-1]
+        if x.shape[-2] != W:
+            raise ValueError("fft2_bf16x3 needs square windows")
+        x = x.contiguous()
+        out = torch.empty_like(x) if out is None else out
+        batch = x.numel() // (W * W)
+        n = ctypes.c_size_t(0)
+        _lib.check(_lib.lib().pty_fft2_bf16x3_workspace_bytes(batch, W, ctypes.byref(n)),
+                   "pty_fft2_bf16x3_workspace_bytes")
+        ws = self.aux("fft2_bf16x3", int(n.value))
+        _lib.check(_lib.lib().pty_fft2_bf16x3(_ptr(x), _ptr(out), batch, W, int(inverse), _ptr(ws), ws.numel(),
+                                              stream.cuda_stream), "pty_fft2_bf16x3")
+        return out
+
     @staticmethod
     def _check_inputs(problem, obj, probe, measured):
         W = problem.window
