@@ -191,6 +191,33 @@ int pty_fft2_bf16x3_workspace_bytes(int32_t batch, int32_t window, size_t* bytes
 int pty_fft2_bf16x3(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
                     void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same with three BF16 terms per FP32 operand and the six significant products (BF16x6):
+ * twice the tensor work of BF16x3, FP32-level error (~2e-7 relative against an FP64 DFT). */
+int pty_fft2_bf16x6_workspace_bytes(int32_t batch, int32_t window, size_t* bytes);
+int pty_fft2_bf16x6(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* window-DFT engines of the precision sweep */
+#define PTY_DFT_FP32_FFT 0 /* the FP32 register FFT (pty_fft2) */
+#define PTY_DFT_BF16X3 1   /* tensor-core GEMMs in BF16x3 split precision (pty_fft2_bf16x3) */
+#define PTY_DFT_BF16X6 2   /* tensor-core GEMMs in BF16x6 split precision (pty_fft2_bf16x6) */
+
+/*
+ * pty_loss_and_direction computed as batched passes over natural-layout windows with every
+ * window DFT on the chosen engine: the precision sweep of pypty.objective.loss_and_direction
+ * (pypty/objective.py:47-967, same flag set, same arguments and outputs; pos_correction may be
+ * host or device memory). Its own workspace: pty_layered_workspace_bytes. Batches are limited
+ * to compute_batch * max(Z * Mo, Mp * Mo) <= 65535 windows (else PTY_ERR_UNSUPPORTED).
+ * No counterpart in the reference (which has one FFT precision per dtype).
+ */
+int pty_layered_workspace_bytes(const pty_problem_t* problem, int32_t engine, size_t* bytes);
+int pty_loss_and_direction_layered(const pty_problem_t* problem, int32_t engine, const void* obj,
+                                   const void* probe, const int32_t* positions_host,
+                                   const float* pos_correction, const int32_t* sequence_host,
+                                   const float* measured, double* loss_sse, void* object_grad,
+                                   void* probe_grad, float* pos_grad, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
 /*
  * pty_fft2 without a workspace argument; it allocates nothing. No counterpart in the
  * reference: it exists for callers that cannot allocate device memory -- an application

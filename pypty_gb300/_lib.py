@@ -18,6 +18,7 @@ PTY_ERR_WORKSPACE = -4
 PTY_ERR_CUDA = -5
 
 ALGORITHMS = {"lsq_sqrt": 0, "ml": 1, "lsq": 2, "lsq_sqrt_2": 3}
+DFT_ENGINES = {"fp32_fft": 0, "bf16x3": 1, "bf16x6": 2}
 
 
 class Problem(ctypes.Structure):
@@ -93,6 +94,10 @@ SIGNATURES = {
     "pty_fourier_clean_apply": ([_VP, _VP, _F64, _VP, _I32, _I32, _I64, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fft2_bf16x3_workspace_bytes": ([_I32, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_fft2_bf16x3": ([_VP, _VP, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_fft2_bf16x6_workspace_bytes": ([_I32, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_fft2_bf16x6": ([_VP, _VP, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
+    "pty_layered_workspace_bytes": ([_PP, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_loss_and_direction_layered": ([_PP, _I32] + [_VP] * 11 + [_SZ, _VP], ctypes.c_int),
     "pty_lbfgs_state_bytes": ([ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_lbfgs_reset": ([_VS, _VP, _VP], ctypes.c_int),
     "pty_lbfgs_first_direction": ([_VS, _PPV, _PPV, _VP, _VP], ctypes.c_int),

@@ -1,5 +1,5 @@
-// Window DFTs as dense GEMMs on the tensor cores (tcgen05), in BF16x3 split precision with
-// FP32 accumulation: the tensor-core counterpart of the FP32 register FFT for windows of
+// Window DFTs as dense GEMMs on the tensor cores (tcgen05), in BF16x3 (or BF16x6) split
+// precision with FP32 accumulation: the tensor-core counterpart of the FP32 register FFT for windows of
 // 64, 128 and 256 px (the precision sweep of pypty.fft.fft2 / ifft2, pypty/fft.py:114-156).
 //
 // One pass transforms every row of every window and writes the result transposed:
@@ -7,19 +7,23 @@
 // so two passes give the 2D DFT in natural (ky, kx) order. As a real GEMM the rows of all
 // windows are the M dimension (M = windows * W), the interleaved real/imaginary parts of a
 // row are K (= 2W) and of the output N (= 2W); the constant real matrix B^T (N x K) holds
-// the 2x2 blocks [[Re w, -Im w], [Im w, Re w]]. Split precision: every FP32 value x is
-// hi + lo with hi = bf16(x), lo = bf16(x - hi), and D = A_hi B_hi + A_hi B_lo + A_lo B_hi
-// (the lo*lo term, ~2^-18 relative, is dropped) accumulates in FP32 in tensor memory.
+// the 2x2 blocks [[Re w, -Im w], [Im w, Re w]]. Split precision: every FP32 value x is a sum
+// of S BF16 terms t0 = bf16(x), t1 = bf16(x - t0), ...; D = sum over products of terms
+// (i, j) with i + j < S accumulates in FP32 in tensor memory. S = 2 (BF16x3: 3 products,
+// ~2^-17 relative error per product) or S = 3 (BF16x6: 6 products, FP32-level error).
 //
-// Per CTA: a 128-row x BN-column tile of D (BN = min(2W, 256)), K in blocks of 64 through a
+// Per CTA: a 128-row x BN-column tile of D (BN = min(2W, 256 / 128)), K in blocks of 64 through a
 // two-stage shared-memory ring. B blocks are pre-split and pre-swizzled images in global
 // memory (L2-resident, shared by all CTAs) moved by one-dimensional bulk copies; A blocks
 // are loaded as FP32, split in registers and stored in the 128B-swizzled K-major layout by
-// all threads. One thread issues the 12 MMAs (3 products x 4 K-steps of 16) of a stage and
-// commits them to the stage's "empty" mbarrier; every wait is bounded and a wait that runs
-// out sets the error word instead of spinning. The epilogue reads the accumulator with
-// 32-lane TMEM loads (warp w: lanes 32 (w % 4), column half w / 4) and stores the transposed
-// window with 256-byte coalesced warp stores.
+// all threads. One thread issues the MMAs of a stage (products x 4 K-steps of 16) into one of
+// two TMEM accumulators (ping-pong by K block) and commits them to the stage's "empty" and the
+// buffer's "drain" mbarriers. The tensor core's FP32 accumulation is biased (its error grows
+// linearly with the number of accumulated MMAs, ~2^-24 each), so every K block's partial
+// product is drained into registers with 32-lane TMEM loads (warp w: lanes 32 (w % 4), column
+// half w / 4) and added there with round-to-nearest FP32 adds, while the tensor core works on
+// the next block. Every wait is bounded; a wait that runs out sets the error word instead of
+// spinning. The epilogue stores the transposed window with 256-byte coalesced warp stores.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -33,23 +37,32 @@ namespace dg {
 
 constexpr int BM = 128, BK = 64, THREADS = 256, STAGES = 2;
 
-template <int W>
+// S = number of BF16 terms per FP32 operand: 2 (BF16x3: products hh, hl, lh) or 3 (BF16x6:
+// products with term indices i + j <= 2, ~FP32 accuracy); BN shrinks to 128 for S = 3 so that
+// two stages fit in shared memory.
+template <int W, int S>
 struct Cfg {
   static constexpr int NTOT = 2 * W;
-  static constexpr int BN = NTOT < 256 ? NTOT : 256;
+  static constexpr int BNMAX = S == 2 ? 256 : 128;
+  static constexpr int BN = NTOT < BNMAX ? NTOT : BNMAX;
   static constexpr int NT = NTOT / BN;
   static constexpr int KC = (2 * W) / BK;
-  static constexpr int A_BYTES = BM * BK * 2;          // one of hi / lo
+  static constexpr int A_BYTES = BM * BK * 2;          // one term
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int STAGE = S * A_BYTES + S * B_BYTES;
   static constexpr int SMEM = STAGES * STAGE + 1024;   // + slack for 1024-byte alignment
-  static constexpr size_t IMG_BYTES = (size_t)2 * NT * KC * B_BYTES;   // hi and lo images of one direction
+  static constexpr size_t IMG_BYTES = (size_t)S * NT * KC * B_BYTES;   // every term's image, one direction
+  // TMEM: two K-block buffers (ping-pong); with S = 3 each holds the main product hi*hi and,
+  // separately, the correction products (2^-8 smaller, so their accumulation error is too)
+  static constexpr int ACCS = S == 3 ? 2 : 1;
+  static constexpr int TMEM_COLS = 2 * ACCS * BN;
+  static_assert(TMEM_COLS <= 512, "TMEM holds 512 columns");
 };
 
-// Pre-split, pre-swizzled images of B^T for one direction: [hl][nt][kc][BN x 64 block].
-template <int W>
+// Pre-split, pre-swizzled images of B^T for one direction: [term][nt][kc][BN x 64 block].
+template <int W, int S>
 __global__ void dft_matrix_kernel(uint8_t* img, int inverse) {
-  using C = Cfg<W>;
+  using C = Cfg<W, S>;
   const long long total = (long long)C::NT * C::KC * C::BN * BK;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(i % BK);
@@ -64,22 +77,25 @@ __global__ void dft_matrix_kernel(uint8_t* img, int inverse) {
     const double wr = cs, wi = inverse ? sn : -sn;   // w^(c k) = exp(-+ 2 pi i c k / W)
     const int so = n & 1, si = kk & 1;
     const double v = so == 0 ? (si == 0 ? wr : -wi) : (si == 0 ? wi : wr);
-    const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
-    const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
     const size_t blk = ((size_t)nt * C::KC + kc) * C::B_BYTES + umma::sw128_offset(r, k);
-    *reinterpret_cast<__nv_bfloat16*>(img + blk) = hi;
-    *reinterpret_cast<__nv_bfloat16*>(img + (size_t)C::NT * C::KC * C::B_BYTES + blk) = lo;
+    double rest = v;
+#pragma unroll
+    for (int term = 0; term < S; ++term) {
+      const __nv_bfloat16 t = __float2bfloat16_rn((float)rest);
+      rest -= (double)__bfloat162float(t);
+      *reinterpret_cast<__nv_bfloat16*>(img + (size_t)term * C::NT * C::KC * C::B_BYTES + blk) = t;
+    }
   }
 }
 
-template <int W>
+template <int W, int S>
 __global__ void __launch_bounds__(THREADS, 1)
     dft_pass_kernel(const float2* __restrict__ in, float2* __restrict__ out, const uint8_t* __restrict__ img,
                     long long n_rows, float scale, int* err) {
-  using C = Cfg<W>;
+  using C = Cfg<W, S>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], done_bar;
+  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], drain_bar[2];
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long row0 = (long long)blockIdx.x * BM;
@@ -90,124 +106,156 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&done_bar, 1);
+    mbar_init(&drain_bar[0], 1);
+    mbar_init(&drain_bar[1], 1);
     fence_async_shared();
   }
-  if (warp == 0) umma::tmem_alloc(&tmem_base, C::BN);
+  if (warp == 0) umma::tmem_alloc(&tmem_base, C::TMEM_COLS);
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = tmem_base;
-  const uint8_t* img_hi = img + (size_t)nt * C::KC * C::B_BYTES;
-  const uint8_t* img_lo = img + (size_t)C::NT * C::KC * C::B_BYTES + (size_t)nt * C::KC * C::B_BYTES;
+  const uint8_t* img_nt = img + (size_t)nt * C::KC * C::B_BYTES;
+  constexpr size_t TERM = (size_t)C::NT * C::KC * C::B_BYTES;
   constexpr uint32_t idesc = umma::idesc_bf16_f32(BM, C::BN);
-  uint32_t full_par[STAGES] = {0, 0}, empty_par[STAGES] = {0, 0};
+  uint32_t full_par[STAGES] = {0, 0}, empty_par[STAGES] = {0, 0}, drain_par[2] = {0, 0};
+  // this thread's accumulator slice: TMEM lanes 32 (w % 4) + lane (tile rows), column half w / 4
+  const int q = warp & 3, h = warp >> 2;
+  constexpr int HALF = C::BN / 2;
+  float acc[HALF];
+#pragma unroll
+  for (int j = 0; j < HALF; ++j) acc[j] = 0.0f;
+  // add the partial product of K block kc (TMEM buffer kc & 1) to the registers: FP32 adds with
+  // round-to-nearest, so the tensor core's accumulation runs over one K block only
+  auto drain = [&](int kc) {
+    const int buf = kc & 1;
+    mbar_wait(&drain_bar[buf], drain_par[buf], &e);
+    umma::fence_after_sync();
+#pragma unroll
+    for (int c0 = 0; c0 < HALF; c0 += 32) {
+      const uint32_t col = (uint32_t)(buf * C::ACCS * C::BN + h * HALF + c0);
+      float v[32];
+      umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+      if constexpr (C::ACCS == 2) {
+        float w[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col + C::BN, w);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] += w[j];
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[c0 + j] += v[j];
+    }
+    umma::fence_before_sync();
+  };
 
   for (int kc = 0; kc < C::KC; ++kc) {
     const int s = kc % STAGES;
-    uint8_t* sAh = base + s * C::STAGE;
-    uint8_t* sAl = sAh + C::A_BYTES;
-    uint8_t* sBh = sAl + C::A_BYTES;
-    uint8_t* sBl = sBh + C::B_BYTES;
+    uint8_t* sA = base + s * C::STAGE;            // S terms of A, then S terms of B
+    uint8_t* sB = sA + S * C::A_BYTES;
     if (kc >= STAGES) mbar_wait(&empty_bar[s], empty_par[s], &e);   // the MMAs of kc - STAGES are done
     if (tid == 0) {
-      mbar_expect_tx(&full_bar[s], 2 * C::B_BYTES);
-      bulk_copy_g2s(sBh, img_hi + (size_t)kc * C::B_BYTES, C::B_BYTES, &full_bar[s]);
-      bulk_copy_g2s(sBl, img_lo + (size_t)kc * C::B_BYTES, C::B_BYTES, &full_bar[s]);
+      mbar_expect_tx(&full_bar[s], S * C::B_BYTES);
+#pragma unroll
+      for (int term = 0; term < S; ++term)
+        bulk_copy_g2s(sB + term * C::B_BYTES, img_nt + term * TERM + (size_t)kc * C::B_BYTES, C::B_BYTES,
+                      &full_bar[s]);
     }
     // A block: rows row0 .. row0+127, real columns kc*64 .. kc*64+63 (16 float4 per row)
 #pragma unroll
     for (int i = 0; i < (BM * BK / 4) / THREADS; ++i) {
-      const int q = tid + THREADS * i;
-      const int r = q >> 4, c4 = q & 15;
+      const int qq = tid + THREADS * i;
+      const int r = qq >> 4, c4 = qq & 15;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       const long long row = row0 + r;
       if (row < n_rows) v = reinterpret_cast<const float4*>(in + row * W)[kc * 16 + c4];
-      uint16_t h0, l0, h1, l1, h2, l2, h3, l3;
-      umma::split_bf16(v.x, h0, l0);
-      umma::split_bf16(v.y, h1, l1);
-      umma::split_bf16(v.z, h2, l2);
-      umma::split_bf16(v.w, h3, l3);
       const uint32_t off = umma::sw128_offset(r, 4 * c4);
-      *reinterpret_cast<uint2*>(sAh + off) = make_uint2(h0 | ((uint32_t)h1 << 16), h2 | ((uint32_t)h3 << 16));
-      *reinterpret_cast<uint2*>(sAl + off) = make_uint2(l0 | ((uint32_t)l1 << 16), l2 | ((uint32_t)l3 << 16));
+      float4 rest = v;
+#pragma unroll
+      for (int term = 0; term < S; ++term) {
+        // successive BF16 terms; every residual x - bf16(x) is exact in FP32
+        const uint16_t t0 = umma::bf16_bits(rest.x), t1 = umma::bf16_bits(rest.y);
+        const uint16_t t2 = umma::bf16_bits(rest.z), t3 = umma::bf16_bits(rest.w);
+        *reinterpret_cast<uint2*>(sA + term * C::A_BYTES + off) =
+            make_uint2(t0 | ((uint32_t)t1 << 16), t2 | ((uint32_t)t3 << 16));
+        if (term + 1 < S) {
+          rest.x -= umma::bf16_value(t0);
+          rest.y -= umma::bf16_value(t1);
+          rest.z -= umma::bf16_value(t2);
+          rest.w -= umma::bf16_value(t3);
+        }
+      }
     }
     fence_async_shared();
     umma::fence_before_sync();
-    __syncthreads();
+    __syncthreads();   // A is written; every thread has drained TMEM buffer kc & 1 (block kc - 2)
     if (tid == 0) {
       mbar_wait(&full_bar[s], full_par[s], &e);
       umma::fence_after_sync();
-      const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
+      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      const uint32_t d = tmem + (uint32_t)((kc & 1) * C::ACCS * C::BN);
+      const uint32_t dc = d + (C::ACCS == 2 ? (uint32_t)C::BN : 0u);   // accumulator of the correction products
 #pragma unroll
       for (int k = 0; k < BK / 16; ++k) {
         const uint32_t o = 32u * k;
-        umma::mma_bf16(tmem, umma::desc_sw128(ah + o), umma::desc_sw128(bh + o), idesc, (kc | k) != 0);
-        umma::mma_bf16(tmem, umma::desc_sw128(ah + o), umma::desc_sw128(bl + o), idesc, 1);
-        umma::mma_bf16(tmem, umma::desc_sw128(al + o), umma::desc_sw128(bh + o), idesc, 1);
+        // every product of terms (i, j) with i + j < S, largest first
+#pragma unroll
+        for (int sum = 0; sum < S; ++sum)
+#pragma unroll
+          for (int i = 0; i <= sum; ++i) {
+            const bool main = sum == 0 || C::ACCS == 1;
+            const bool first = C::ACCS == 1 ? (k | sum) == 0 : (k == 0 && i == 0 && sum <= 1);
+            umma::mma_bf16(main ? d : dc, umma::desc_sw128(a0 + i * C::A_BYTES + o),
+                           umma::desc_sw128(b0 + (sum - i) * C::B_BYTES + o), idesc, !first);
+          }
       }
       umma::mma_commit(&empty_bar[s]);
+      umma::mma_commit(&drain_bar[kc & 1]);
     }
+    if (kc > 0) drain(kc - 1);   // overlaps the MMAs of block kc
   }
-  if (tid == 0) umma::mma_commit(&done_bar);
-  uint32_t done_par = 0;
-  mbar_wait(&done_bar, done_par, &e);
-  umma::fence_after_sync();
-  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows), column half w / 4
-  const int q = warp & 3, h = warp >> 2;
+  drain(C::KC - 1);
+  // epilogue: out[window][k][row in window] = scale * acc (transposed, coalesced over rows)
   const long long row = row0 + 32 * q + lane;
   const long long win = row / W;
   const int r = (int)(row % W);
-  constexpr int HALF = C::BN / 2;
-#pragma unroll 1
-  for (int c0 = 0; c0 < HALF; c0 += 32) {
-    float v[32];
-    umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(h * HALF + c0), v);
-    if (row < n_rows) {
-      const int k0 = (nt * C::BN + h * HALF + c0) >> 1;
-      float2* o = out + win * (long long)W * W + r;
+  if (row < n_rows) {
+    float2* o = out + win * (long long)W * W + r;
+    const int k0 = (nt * C::BN + h * HALF) >> 1;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) o[(long long)(k0 + j) * W] = make_float2(v[2 * j] * scale, v[2 * j + 1] * scale);
-    }
+    for (int j = 0; j < HALF / 2; ++j) o[(long long)(k0 + j) * W] = make_float2(acc[2 * j] * scale, acc[2 * j + 1] * scale);
   }
-  umma::fence_before_sync();
   __syncthreads();
-  if (warp == 0) umma::tmem_dealloc(tmem, C::BN);
+  if (warp == 0) umma::tmem_dealloc(tmem, C::TMEM_COLS);
   if (e && lane == 0 && err) atomicExch(err, 1);
-}
-
-template <int W>
-size_t img_bytes() {
-  return Cfg<W>::IMG_BYTES;
 }
 
 struct Ws {
   size_t o_fwd, o_inv, o_tmp, o_err, total;
 };
 
-template <int W>
+template <int W, int S>
 Ws make_ws(long long batch) {
   Ws w;
   w.o_fwd = 0;
-  w.o_inv = align_up(w.o_fwd + Cfg<W>::IMG_BYTES);
-  w.o_err = align_up(w.o_inv + Cfg<W>::IMG_BYTES);
+  w.o_inv = align_up(w.o_fwd + Cfg<W, S>::IMG_BYTES);
+  w.o_err = align_up(w.o_inv + Cfg<W, S>::IMG_BYTES);
   w.o_tmp = align_up(w.o_err + 256);
   w.total = align_up(w.o_tmp + (size_t)batch * W * W * sizeof(float2));
   return w;
 }
 
-template <int W>
+template <int W, int S>
 int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* ws, size_t ws_bytes, cudaStream_t st) {
-  using C = Cfg<W>;
-  const Ws w = make_ws<W>(batch);
+  using C = Cfg<W, S>;
+  const Ws w = make_ws<W, S>(batch);
   if (ws_bytes < w.total) return PTY_ERR_WORKSPACE;
   uint8_t* img = at<uint8_t>(ws, inverse ? w.o_inv : w.o_fwd);
   int* err = at<int>(ws, w.o_err);
   float2* tmp = at<float2>(ws, w.o_tmp);
   prof_mark(st, KID_DFT_TABLES);
-  dft_matrix_kernel<W><<<256, 256, 0, st>>>(img, inverse);
+  dft_matrix_kernel<W, S><<<256, 256, 0, st>>>(img, inverse);
   if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
-  auto k = dft_pass_kernel<W>;
+  auto k = dft_pass_kernel<W, S>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess) return PTY_ERR_CUDA;
   const long long rows = batch * W;
   const dim3 grid((unsigned)((rows + BM - 1) / BM), C::NT);
@@ -227,29 +275,54 @@ using namespace pty;
 
 extern "C" {
 
-int pty_fft2_bf16x3_workspace_bytes(int32_t batch, int32_t window, size_t* bytes) {
+static int ws_bytes_for(int32_t batch, int32_t window, int terms, size_t* bytes) {
   if (!bytes || batch <= 0) return PTY_ERR_INVALID;
-  switch (window) {
-    case 64: *bytes = dg::make_ws<64>(batch).total; return PTY_OK;
-    case 128: *bytes = dg::make_ws<128>(batch).total; return PTY_OK;
-    case 256: *bytes = dg::make_ws<256>(batch).total; return PTY_OK;
+  const int key = window * 10 + terms;
+  switch (key) {
+    case 642: *bytes = dg::make_ws<64, 2>(batch).total; return PTY_OK;
+    case 1282: *bytes = dg::make_ws<128, 2>(batch).total; return PTY_OK;
+    case 2562: *bytes = dg::make_ws<256, 2>(batch).total; return PTY_OK;
+    case 643: *bytes = dg::make_ws<64, 3>(batch).total; return PTY_OK;
+    case 1283: *bytes = dg::make_ws<128, 3>(batch).total; return PTY_OK;
+    case 2563: *bytes = dg::make_ws<256, 3>(batch).total; return PTY_OK;
     default: return PTY_ERR_UNSUPPORTED;
   }
 }
 
-int pty_fft2_bf16x3(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, void* workspace,
-                    size_t workspace_bytes, void* stream) {
+static int fft2_tc(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, int terms,
+                   void* workspace, size_t workspace_bytes, void* stream) {
   if (!in || !out || !workspace || batch <= 0) return PTY_ERR_INVALID;
   if (in == out) return PTY_ERR_INVALID;
   const float2* i = static_cast<const float2*>(in);
   float2* o = static_cast<float2*>(out);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  switch (window) {
-    case 64: return dg::run_fft2<64>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 128: return dg::run_fft2<128>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 256: return dg::run_fft2<256>(i, o, batch, inverse, workspace, workspace_bytes, st);
+  switch (window * 10 + terms) {
+    case 642: return dg::run_fft2<64, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 1282: return dg::run_fft2<128, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 2562: return dg::run_fft2<256, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 643: return dg::run_fft2<64, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 1283: return dg::run_fft2<128, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 2563: return dg::run_fft2<256, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
     default: return PTY_ERR_UNSUPPORTED;
   }
+}
+
+int pty_fft2_bf16x3_workspace_bytes(int32_t batch, int32_t window, size_t* bytes) {
+  return ws_bytes_for(batch, window, 2, bytes);
+}
+
+int pty_fft2_bf16x3(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+  return fft2_tc(in, out, batch, window, inverse, 2, workspace, workspace_bytes, stream);
+}
+
+int pty_fft2_bf16x6_workspace_bytes(int32_t batch, int32_t window, size_t* bytes) {
+  return ws_bytes_for(batch, window, 3, bytes);
+}
+
+int pty_fft2_bf16x6(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+  return fft2_tc(in, out, batch, window, inverse, 3, workspace, workspace_bytes, stream);
 }
 
 }  // extern "C"

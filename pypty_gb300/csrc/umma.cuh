@@ -89,6 +89,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// FP32 -> BF16 bits (round to nearest even) and back
+__device__ __forceinline__ uint16_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
 // FP32 -> BF16 hi/lo split (round to nearest even): x ~= hi + lo with |x - hi - lo| <= 2^-16 |x|
 __device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) {
   const __nv_bfloat16 h = __float2bfloat16_rn(x);

@@ -151,6 +151,29 @@ class Engine:
         _lib.check(st, "pty_loss_and_direction")
         return loss_sse, og, pg, posg
 
+    def loss_and_direction_layered(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor,
+                                   geo: Geometry, measured: torch.Tensor, engine: str = "bf16x3", stream=None):
+        """loss_and_direction with every window DFT on `engine` ("fp32_fft" or "bf16x3",
+        ``pty_loss_and_direction_layered``): the precision sweep. Same outputs as
+        ``loss_and_direction``."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        self._check_inputs(problem, obj, probe, measured)
+        eid = _lib.DFT_ENGINES[engine]
+        n = ctypes.c_size_t(0)
+        _lib.check(_lib.lib().pty_layered_workspace_bytes(ctypes.byref(problem), eid, ctypes.byref(n)),
+                   "pty_layered_workspace_bytes")
+        ws = self.workspace(int(n.value))
+        out = (torch.empty(2, dtype=torch.float64, device=self.device), torch.empty_like(obj),
+               torch.empty_like(probe), torch.zeros((problem.n_positions, 2), dtype=torch.float32, device=self.device))
+        loss_sse, og, pg, posg = out
+        pp, pc, ps = self._staging(geo)
+        st = _lib.lib().pty_loss_and_direction_layered(
+            ctypes.byref(problem), eid, _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured), _ptr(loss_sse),
+            _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)
+        self._mark_staging(stream)
+        _lib.check(st, "pty_loss_and_direction_layered")
+        return loss_sse, og, pg, posg
+
     def forward(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
                 measured: torch.Tensor, stream=None):
         """Forward half (pty_forward): returns (loss_sse, workspace). The workspace holds the
@@ -216,9 +239,10 @@ class Engine:
         _lib.check(st, "pty_fft2")
         return out
 
-    def fft2_bf16x3(self, x: torch.Tensor, inverse: bool = False, out=None, stream=None):
+    def fft2_bf16x3(self, x: torch.Tensor, inverse: bool = False, out=None, stream=None, terms: int = 2):
         """Batched 2D DFT over the last two axes of a (..., W, W) complex64 device tensor on the
-        tensor cores in BF16x3 split precision (``pty_fft2_bf16x3``; W = 64, 128, 256)."""
+        tensor cores in BF16x3 split precision (``pty_fft2_bf16x3``; W = 64, 128, 256); with
+        terms=3 in BF16x6 (``pty_fft2_bf16x6``)."""
         stream = stream or torch.cuda.current_stream(self.device)
         if x.dtype != torch.complex64 or not x.is_cuda:
             raise TypeError("fft2_bf16x3 needs a complex64 CUDA tensor")
@@ -229,11 +253,11 @@ class Engine:
         out = torch.empty_like(x) if out is None else out
         batch = x.numel() // (W * W)
         n = ctypes.c_size_t(0)
-        _lib.check(_lib.lib().pty_fft2_bf16x3_workspace_bytes(batch, W, ctypes.byref(n)),
-                   "pty_fft2_bf16x3_workspace_bytes")
-        ws = self.aux("fft2_bf16x3", int(n.value))
-        _lib.check(_lib.lib().pty_fft2_bf16x3(_ptr(x), _ptr(out), batch, W, int(inverse), _ptr(ws), ws.numel(),
-                                              stream.cuda_stream), "pty_fft2_bf16x3")
+        name = "pty_fft2_bf16x3" if terms == 2 else "pty_fft2_bf16x6"
+        _lib.check(getattr(_lib.lib(), name + "_workspace_bytes")(batch, W, ctypes.byref(n)), name + "_workspace_bytes")
+        ws = self.aux("fft2_tensor_core", int(n.value))
+        _lib.check(getattr(_lib.lib(), name)(_ptr(x), _ptr(out), batch, W, int(inverse), _ptr(ws), ws.numel(),
+                                             stream.cuda_stream), name)
         return out
 
     @staticmethod

@@ -1,0 +1,116 @@
+"""The precision sweep: loss_and_direction with every window DFT on one engine.
+
+* FP32 register FFT engine: the same tolerances as the fused path against the reference's
+  own outputs (loss relative error <= 1e-5, gradients relative L2 <= 1e-4).
+* BF16x3 tensor-core engine: the error against the FP64 oracle (complex128 run of the oracle
+  on the same inputs) is printed and bounded: loss <= 5e-5 relative, gradients <= 2e-3
+  relative L2 (each BF16x3 window DFT carries ~5e-6 relative error; the adjoint amplifies
+  it ~25x, as it does the FP32 FFT's ~1e-7).
+* BF16x6 tensor-core engine: within the path's complex64 tolerances of the FP64 oracle
+  (loss <= 1e-5, gradients <= 1e-4).
+"""
+import numpy as np
+import pytest
+
+from golden_io import load_case, loss_case_names, rel_l2
+from oracle import ptycho_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+BF16X3_LOSS_TOL = 5e-5
+BF16X3_GRAD_TOL = 2e-3
+BF16X6_LOSS_TOL = 1e-5
+BF16X6_GRAD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import torch
+    from pypty_gb300.engine import Engine
+    return Engine(torch.device("cuda", 0))
+
+
+def run_layered(eng, c, dft, compute_batch=None):
+    import torch
+    from pypty_gb300.engine import Geometry, make_problem
+    obj = np.ascontiguousarray(c["obj"]).astype(np.complex64)
+    probe = np.ascontiguousarray(c["probe"]).astype(np.complex64)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    W = probe.shape[0]
+    prob = make_problem(W, obj.shape, probe.shape[2], geo, algorithm=c["algorithm"],
+                        wavelength=float(np.float32(c["wavelength"])), pixel_size_x=float(np.float32(c["px"])),
+                        pixel_size_y=float(np.float32(c["px"])), slice_distance=c["distance"],
+                        edge_mult=c["edge_mult"], damping_cutoff=float(np.float32(c["cutoff"])),
+                        smooth_rolloff=float(np.float32(c["rolloff"])), loss_weight=c["loss_weight"],
+                        compute_batch=compute_batch or c["batch"], step_obj=c["step_obj"],
+                        step_probe=c["step_probe"], step_pos=c["step_pos"])
+    ls, og, pg, posg = eng.loss_and_direction_layered(
+        prob, torch.from_numpy(obj).cuda(), torch.from_numpy(probe).cuda(), geo,
+        torch.from_numpy(np.ascontiguousarray(c["measured"]).astype(np.float32)).cuda(), engine=dft)
+    torch.cuda.synchronize()
+    ls = ls.cpu().numpy()
+    return float(ls[0]), float(ls[1]), og.cpu().numpy(), pg.cpu().numpy(), posg.cpu().numpy()
+
+
+def fp64_oracle(c):
+    return orc.loss_and_direction(
+        c["obj"].astype(np.complex128), c["probe"].astype(np.complex128), c["positions"],
+        c["pos_correction"].astype(np.float64), c["distance"], c["edge_mult"], c["measured"].astype(np.float64),
+        c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"], c["step_pos"], c["px"], c["px"],
+        c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"], float_dtype=np.float64,
+        complex_dtype=np.complex128)
+
+
+@pytest.mark.parametrize("name", [n for n in loss_case_names() if not n.endswith("c128")])
+def test_layered_fp32_matches_reference(engine, name):
+    c = load_case(name)
+    loss, sse, og, pg, posg = run_layered(engine, c, "fp32_fft")
+    assert abs(loss - float(c["ref_loss"])) <= 1e-5 * abs(float(c["ref_loss"]))
+    assert rel_l2(og, c["ref_object_grad"]) <= 1e-4
+    if c["step_probe"]:
+        assert rel_l2(pg, np.asarray(c["ref_probe_grad"]).reshape(pg.shape)) <= 1e-4
+    if c["step_pos"]:
+        assert rel_l2(posg, c["ref_pos_grad"]) <= 1e-4
+
+
+@pytest.mark.parametrize("name", ["single_slice_c64", "multislice_ml_c64", "modes_lsq_c64", "w128_modes_c64"])
+def test_layered_bf16x3_error_against_fp64(engine, name):
+    c = load_case(name)
+    loss64, _, og64, pg64, posg64 = fp64_oracle(c)
+    res = {}
+    for dft in ("bf16x3", "bf16x6", "fp32_fft"):
+        loss, _, og, pg, posg = run_layered(engine, c, dft)
+        res[dft] = (abs(loss - loss64) / abs(loss64), rel_l2(og, og64),
+                    rel_l2(pg, pg64) if c["step_probe"] else 0.0, rel_l2(posg, posg64) if c["step_pos"] else 0.0)
+    for k in res:
+        print("%s %-8s loss %.1e obj %.1e probe %.1e pos %.1e" % ((name, k) + res[k]))
+    le, oe, pe, se = res["bf16x3"]
+    assert le <= BF16X3_LOSS_TOL and oe <= BF16X3_GRAD_TOL and pe <= BF16X3_GRAD_TOL and se <= BF16X3_GRAD_TOL
+    le, oe, pe, se = res["bf16x6"]
+    assert le <= BF16X6_LOSS_TOL and oe <= BF16X6_GRAD_TOL and pe <= BF16X6_GRAD_TOL and se <= BF16X6_GRAD_TOL
+
+
+def test_layered_bf16x3_w256_against_fp64(engine):
+    """A 256-px window with five probe modes (the precision-sweep shape, few positions)."""
+    from pypty_gb300 import synth
+    rng = np.random.default_rng(17)
+    W, Z, Mp, px = 256, 3, 5, 0.1
+    obj = synth.gaussian_phase_object(320, 320, Z, 60, 0.3, px, 0.2, 1.0, rng, dtype=np.complex64)
+    probe = synth.make_probe(W, px, 300.0, 30.0, 60.0, Mp, [0.5, 0.2, 0.15, 0.1, 0.05], 1e5, dtype=np.complex64)
+    pos = synth.raster_positions(3, 3, 20.0, 1.0, rng)
+    ipos, corr = synth.split_positions(pos, int_dtype=np.int32, float_dtype=np.float32)
+    lam = synth.wavelength_A(300.0)
+    sim = orc.loss_and_direction(obj, probe, ipos, corr, 1.0, 1.0, None, "ml", lam, 1, 1, 0, px, px, 2 / 3, 0.0,
+                                 np.arange(len(ipos)), 1, 9, simulate=True)
+    meas = synth.poisson_patterns(sim, 1.0, rng).astype(np.float32)
+    obj0 = np.exp(0.7j * np.angle(obj)).astype(np.complex64)
+    c = dict(obj=obj0, probe=probe, positions=ipos, pos_correction=corr, measured=meas, sequence=np.arange(len(ipos)),
+             distance=1.0, edge_mult=1.0, algorithm="ml", wavelength=lam, step_probe=1, step_obj=1, step_pos=1,
+             px=px, cutoff=2 / 3, rolloff=0.0, loss_weight=1.0, batch=9)
+    loss64, _, og64, pg64, posg64 = fp64_oracle(c)
+    for dft, lt, gt in (("bf16x3", BF16X3_LOSS_TOL, BF16X3_GRAD_TOL), ("bf16x6", BF16X6_LOSS_TOL, BF16X6_GRAD_TOL),
+                        ("fp32_fft", 1e-5, 1e-4)):
+        loss, _, og, pg, posg = run_layered(engine, c, dft)
+        le, oe, pe, se = abs(loss - loss64) / abs(loss64), rel_l2(og, og64), rel_l2(pg, pg64), rel_l2(posg, posg64)
+        print("W=256 Z=3 Mp=5 %-8s loss %.1e obj %.1e probe %.1e pos %.1e" % (dft, le, oe, pe, se))
+        assert le <= lt and oe <= gt and pe <= gt and se <= gt
