@@ -49,8 +49,12 @@ CONFIGS = {
     "multislice-small": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=8, algorithm="ml", batch=64,
                              desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 8x8 jittered scan, ml, batch 64"),
     # 256-px windows, 5 modes, 40 slices over a 1024^2 object, 64x64 scan (FP32 FFT path)
-    "precision-sweep": dict(W=256, N_obj=1024, Z=40, Mp=5, n_scan=64, algorithm="lsq_sqrt", batch=512,
+    "precision-sweep": dict(W=256, N_obj=1024, Z=40, Mp=5, n_scan=64, algorithm="lsq_sqrt", batch=512, sweep=True,
                             desc="precision sweep W256 Z40 Mp5 Mo1, 1024x1024 object, 64x64 scan, lsq_sqrt, batch 512"),
+    # the precision sweep's shapes per position on 8x8 positions and 8 slices: for ncu captures
+    "precision-sweep-small": dict(W=256, N_obj=1024, Z=8, Mp=5, n_scan=8, algorithm="lsq_sqrt", batch=64,
+                                  sweep=True, desc="precision sweep W256 Z8 Mp5 Mo1, 1024x1024 object, 8x8 scan, "
+                                                   "lsq_sqrt, batch 64"),
     # 256-px windows, 8 modes, 60 slices over a 2048^2 object, 128x128 scan, batch 512
     "large-adjoint": dict(W=256, N_obj=2048, Z=60, Mp=8, n_scan=128, algorithm="lsq_sqrt", batch=512,
                           desc="large adjoint W256 Z60 Mp8 Mo1, 2048x2048 object, 128x128 scan, lsq_sqrt, batch 512"),
@@ -190,6 +194,53 @@ def cpu_baseline(cfg, wl, algorithm, budget_s=15.0):
     return {"value": n / dt, "unit": "positions/s", "cores": cores, "kind": "port",
             "sample": "%d positions of the %s workload (NumPy/SciPy oracle, complex64, %.1f s)" % (
                 n, cfg["name"], dt), "seconds": dt, "positions": n}
+
+
+def precision_sweep(eng, wl, geo, meas_d, obj_d, probe_d, cfg, common, n_sub=512, batch=256):
+    """The same loss-and-gradient call with every window DFT on each engine of the layered
+    path (pty_loss_and_direction_layered: FP32 register FFT, BF16x3 and BF16x6 tensor-core
+    GEMMs) and on the fused FP32 path, over the first n_sub positions: device-timed positions/s
+    (one warm-up call, one timed call each). Their errors against the FP64 oracle are measured
+    by tests/test_gpu_layered.py and tests/test_gpu_dft_gemm.py."""
+    import torch
+    from pypty_gb300 import _lib
+    from pypty_gb300.engine import Geometry, make_problem
+    dev = obj_d.device
+    stream = torch.cuda.current_stream(dev)
+    W, Z, Mp = cfg["W"], cfg["Z"], cfg["Mp"]
+    sub = Geometry.make(geo.positions, geo.pos_correction, np.arange(n_sub))
+    kw = dict(common, compute_batch=batch)
+    prob = make_problem(W, tuple(obj_d.shape), Mp, sub, step_pos=True, **kw)
+    out = {"positions": n_sub, "batch": batch}
+    # 2D DFTs per position on the layered path: object and gradient-window band limits, probe
+    # shift, forward and adjoint propagation, far field and its adjoint, probe-gradient spectrum
+    n_dft = 4 * Z + 4 * (Z - 1) * Mp + 2 * Mp + 2 * Mp
+    for name in ("fused_fp32", "fp32_fft", "bf16x3", "bf16x6"):
+        def call():
+            if name == "fused_fp32":
+                return eng.loss_and_direction(prob, obj_d, probe_d, sub, meas_d)
+            return eng.loss_and_direction_layered(prob, obj_d, probe_d, sub, meas_d, engine=name)
+        call()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with _lib.LaunchProfiler(1 << 16) as prof:
+            e0.record(stream)
+            res = call()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        row = {"positions_per_s": round(n_sub / (ms / 1e3), 1), "ms": round(ms, 1),
+               "loss": float(res[0][0].item())}
+        gemm_ms = prof.ms.get("dft_gemm_bf16x3", 0.0)
+        if gemm_ms > 0:
+            terms = 2 if name == "bf16x3" else 3
+            products = 3 if terms == 2 else 6
+            flops = n_sub * n_dft * 2 * products * W * (2 * W) * (2 * W) * 2
+            row["dft_gemm_share"] = round(gemm_ms / ms, 3)
+            row["tensor_tflops"] = round(flops / (gemm_ms / 1e3) / 1e12, 1)
+        out[name] = row
+        torch.cuda.empty_cache()
+    return out
 
 
 def optimizer_step(eng, prob, geo, meas_d, obj_d, probe_d, wl, lad_ms, hbm_peak, peak_src, epochs=4):
@@ -440,6 +491,9 @@ def main():
         "clocks": {"sm_mhz": cs.get("sm_mhz"), "sm_max_mhz": cs.get("sm_max_mhz"), "reasons": cs.get("reasons")},
         "loss": loss_val,
     }
+    if cfg.get("sweep"):
+        line["precision_sweep"] = precision_sweep(eng, wl, geo, meas_d, obj_d, probe_d, cfg, common,
+                                                  n_sub=min(512, n_pos), batch=min(256, cfg["batch"]))
     if not args.no_optimizer:
         try:
             line["optimizer"] = optimizer_step(eng, prob, geo, meas_d, obj_d, probe_d, wl, ms, hbm_peak, peak_src)

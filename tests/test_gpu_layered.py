@@ -114,3 +114,41 @@ def test_layered_bf16x3_w256_against_fp64(engine):
         le, oe, pe, se = abs(loss - loss64) / abs(loss64), rel_l2(og, og64), rel_l2(pg, pg64), rel_l2(posg, posg64)
         print("W=256 Z=3 Mp=5 %-8s loss %.1e obj %.1e probe %.1e pos %.1e" % (dft, le, oe, pe, se))
         assert le <= lt and oe <= gt and pe <= gt and se <= gt
+
+
+def test_precision_sweep_depth_40_slices(engine):
+    """The precision-sweep shape per position (256-px window, 40 slices of 1 A, 5 probe modes)
+    on two positions: the fused FP32 path and the three layered engines against FP64."""
+    import torch
+    from pypty_gb300 import synth
+    from pypty_gb300.engine import Geometry, make_problem
+    rng = np.random.default_rng(23)
+    W, Z, Mp, px = 256, 40, 5, 0.1
+    obj = synth.gaussian_phase_object(288, 288, Z, 40, 0.3, px, 0.2, 1.0, rng, dtype=np.complex64)
+    probe = synth.make_probe(W, px, 300.0, 30.0, 80.0, Mp, 0.6 ** np.arange(Mp), 1e5, dtype=np.complex64)
+    pos = np.array([[10.3, 12.6], [25.8, 20.1]])
+    ipos, corr = synth.split_positions(pos, int_dtype=np.int32, float_dtype=np.float32)
+    lam = synth.wavelength_A(300.0)
+    sim = orc.loss_and_direction(obj, probe, ipos, corr, 1.0, 1.0, None, "lsq_sqrt", lam, 1, 1, 0, px, px, 2 / 3,
+                                 0.0, np.arange(2), 1, 2, simulate=True)
+    meas = synth.poisson_patterns(sim, 1.0, rng).astype(np.float32)
+    obj0 = np.exp(0.5j * np.angle(obj)).astype(np.complex64)
+    c = dict(obj=obj0, probe=probe, positions=ipos, pos_correction=corr, measured=meas, sequence=np.arange(2),
+             distance=1.0, edge_mult=1.0, algorithm="lsq_sqrt", wavelength=lam, step_probe=1, step_obj=1,
+             step_pos=1, px=px, cutoff=2 / 3, rolloff=0.0, loss_weight=1.0, batch=2)
+    loss64, _, og64, pg64, posg64 = fp64_oracle(c)
+
+    def errs(loss, og, pg, posg):
+        return abs(loss - loss64) / abs(loss64), rel_l2(og, og64), rel_l2(pg, pg64), rel_l2(posg, posg64)
+
+    from gpu_helpers import run_gpu
+    res = {"fused_fp32": errs(*(lambda r: (r[0], r[2], r[3], r[4]))(run_gpu(c, engine=engine)))}
+    for dft in ("fp32_fft", "bf16x3", "bf16x6"):
+        r = run_layered(engine, c, dft)
+        res[dft] = errs(r[0], r[2], r[3], r[4])
+    for k, v in res.items():
+        print("W=256 Z=40 Mp=5 %-10s loss %.1e obj %.1e probe %.1e pos %.1e" % ((k,) + v))
+    for k, (lt, gt) in {"fused_fp32": (1e-5, 1e-4), "fp32_fft": (1e-5, 1e-4), "bf16x6": (1e-5, 1e-4),
+                        "bf16x3": (BF16X3_LOSS_TOL, 5 * BF16X3_GRAD_TOL)}.items():
+        le, oe, pe, se = res[k]
+        assert le <= lt and oe <= gt and pe <= gt and se <= gt, k
