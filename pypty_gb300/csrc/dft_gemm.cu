@@ -98,8 +98,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], drain_bar[2];
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long row0 = (long long)blockIdx.x * BM;
-  const int nt = blockIdx.y;
+  // the N tiles of one row tile are adjacent in the grid: the second read of A hits L2
+  const long long row0 = (long long)blockIdx.y * BM;
+  const int nt = blockIdx.x;
   int e = 0;
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -257,13 +258,19 @@ int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* 
   if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
   auto k = dft_pass_kernel<W, S>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess) return PTY_ERR_CUDA;
-  const long long rows = batch * W;
-  const dim3 grid((unsigned)((rows + BM - 1) / BM), C::NT);
   const float sc = inverse ? 1.0f / (float)W : 1.0f;   // 1/W per pass: exact
-  prof_mark(st, KID_DFT_GEMM);
-  k<<<grid, THREADS, C::SMEM, st>>>(in, tmp, img, rows, sc, err);
-  prof_mark(st, KID_DFT_GEMM);
-  k<<<grid, THREADS, C::SMEM, st>>>(tmp, out, img, rows, sc, err);
+  // at most 32768 row tiles per launch (grid.y <= 65535)
+  const long long max_win = 32768LL * BM / W;
+  for (long long b0 = 0; b0 < batch; b0 += max_win) {
+    const long long nb = batch - b0 < max_win ? batch - b0 : max_win;
+    const long long rows = nb * W;
+    const dim3 grid(C::NT, (unsigned)((rows + BM - 1) / BM));
+    const size_t off = (size_t)b0 * W * W;
+    prof_mark(st, KID_DFT_GEMM);
+    k<<<grid, THREADS, C::SMEM, st>>>(in + off, tmp + off, img, rows, sc, err);
+    prof_mark(st, KID_DFT_GEMM);
+    k<<<grid, THREADS, C::SMEM, st>>>(tmp + off, out + off, img, rows, sc, err);
+  }
   prof_mark(st, -1);
   return cudaGetLastError() == cudaSuccess ? PTY_OK : PTY_ERR_CUDA;
 }
