@@ -58,6 +58,11 @@ CONFIGS = {
     # 256-px windows, 8 modes, 60 slices over a 2048^2 object, 128x128 scan, batch 512
     "large-adjoint": dict(W=256, N_obj=2048, Z=60, Mp=8, n_scan=128, algorithm="lsq_sqrt", batch=512,
                           desc="large adjoint W256 Z60 Mp8 Mo1, 2048x2048 object, 128x128 scan, lsq_sqrt, batch 512"),
+    # learned warm start: train the U-Net on simulated specimens of the 128-px / 20-slice / 3-mode
+    # experiment, then time the reconstruction to 0.02 rad phase RMSE from the learned and the flat start
+    "warm-start": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=32, algorithm="ml", batch=256, warm_start=True,
+                       desc="learned warm start: U-Net (4 levels, base 32, BF16) on CoM-x/CoM-y/vBF maps of a "
+                            "32x32 scan, 512x512x20 specimens, W128 Mp3"),
     "single-slice": dict(W=64, N_obj=128, Z=1, Mp=1, n_scan=16, algorithm="lsq_sqrt", batch=256,
                          desc="single-slice W64 Z1 Mp1, 128x128 object, 16x16 scan, lsq_sqrt, batch 256"),
 }
@@ -194,6 +199,82 @@ def cpu_baseline(cfg, wl, algorithm, budget_s=15.0):
     return {"value": n / dt, "unit": "positions/s", "cores": cores, "kind": "port",
             "sample": "%d positions of the %s workload (NumPy/SciPy oracle, complex64, %.1f s)" % (
                 n, cfg["name"], dt), "seconds": dt, "positions": n}
+
+
+def run_warm_start(args, cfg):
+    """Learned vs flat start (the warm-start configuration): train on simulated specimens, then
+    reconstruct held-out specimens with the GPU-resident L-BFGS from both starts and report the
+    wall time to 0.02 rad phase RMSE (inference included for the learned start)."""
+    import torch
+    from pypty_gb300 import warmstart as ws
+    from pypty_gb300.engine import Engine
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    eng = Engine(dev)
+    scene = ws.make_scene(eng, W=cfg["W"], Z=cfg["Z"], Mp=cfg["Mp"], obj_n=cfg["N_obj"], n_scan=cfg["n_scan"])
+    t0 = time.perf_counter()
+    xs, ys = ws.make_dataset(scene, args.train, eng, seed=100)
+    torch.cuda.synchronize(dev)
+    t_data = time.perf_counter() - t0
+    stats = (xs.mean(dim=(0, 2, 3)), xs.std(dim=(0, 2, 3)) + 1e-6)
+    net = ws.UNet(in_ch=3, out_ch=cfg["Z"], base=32, levels=4, device=dev, seed=0)
+    t0 = time.perf_counter()
+    hist = ws.train(net, scene, xs, ys, stats, epochs=args.epochs, batch=4, lr=1e-3)
+    torch.cuda.synchronize(dev)
+    t_train = time.perf_counter() - t0
+    del xs, ys
+    rng = np.random.default_rng(999)
+    gen = torch.Generator(device=dev).manual_seed(999)
+    F = scene.frame
+    c0, c1 = int(scene.W / 2), int(scene.geometry.positions.max() + scene.W / 2)
+    region = (c0, c1, c0, c1)          # the probe centres' square: every pixel well illuminated
+    rows = []
+    for k in range(args.test):
+        phase, obj = ws.specimen(scene, rng, eng)
+        meas = ws.measure(scene, obj, eng, gen)
+        flat = torch.ones_like(obj)
+        torch.cuda.synchronize(dev)
+        t_inf0 = time.perf_counter()
+        m = ws.maps(scene, meas, eng)
+        pred = ws.predict(net, scene, m, stats)                      # (Z, F, F)
+        start = torch.ones_like(obj)
+        start[:F, :F, :, 0] = torch.exp(1j * pred.permute(1, 2, 0).to(torch.complex64))
+        torch.cuda.synchronize(dev)
+        t_inf = time.perf_counter() - t_inf0
+        row = {"inference_s": round(t_inf, 4)}
+        for proj in (False, True):
+            key = "projected" if proj else "slices"
+            cf, _ = ws.reconstruct(scene, meas, phase, flat, eng, epochs=args.recon_epochs, region=region,
+                                   projected=proj, target=-1.0)
+            cl, _ = ws.reconstruct(scene, meas, phase, start, eng, epochs=args.recon_epochs, region=region,
+                                   projected=proj, target=-1.0)
+            r0f = ws.phase_rmse(flat, phase, region, proj)
+            r0l = ws.phase_rmse(start, phase, region, proj)
+            levels = {"0.02": 0.02, "0.9_flat0": 0.9 * r0f, "0.75_flat0": 0.75 * r0f, "0.5_flat0": 0.5 * r0f}
+            row[key] = {"rmse0": {"flat": round(r0f, 4), "learned": round(r0l, 4)},
+                        "final": {"flat": round(cf[-1][1], 4), "learned": round(cl[-1][1], 4)},
+                        "time_to": {name: {"flat": ws.time_to(cf, lv), "learned": ws.time_to(cl, lv, t_inf)}
+                                    for name, lv in levels.items()},
+                        "flat_curve": [(round(a, 3), round(b, 4)) for a, b in cf[::5]],
+                        "learned_curve": [(round(a, 3), round(b, 4)) for a, b in cl[::5]]}
+        rows.append(row)
+
+    def mean_time(key, level, who):
+        v = [r[key]["time_to"][level][who] for r in rows]
+        return float(np.mean(v)) if all(x is not None for x in v) else None
+
+    summary = {key: {lv: {"flat_s": mean_time(key, lv, "flat"), "learned_s": mean_time(key, lv, "learned")}
+                     for lv in ("0.02", "0.9_flat0", "0.75_flat0", "0.5_flat0")} for key in ("slices", "projected")}
+    v_l, v_f = summary["slices"]["0.02"]["learned_s"], summary["slices"]["0.02"]["flat_s"]
+    line = {"metric": "time to 0.02 rad phase RMSE, learned vs plain init", "impl": "ours",
+            "value": v_l, "unit": "s", "higher_is_better": False, "plain_s": v_f,
+            "ratio_learned_over_plain": (v_l / v_f) if v_l and v_f else None,
+            "summary": summary, "n_gpus": 1, "data": "synthetic", "dtype": "bf16 network, c64 reconstruction",
+            "config": {"workload": cfg["desc"], "train_specimens": args.train, "test_specimens": args.test,
+                       "epochs": args.epochs, "recon_epochs": args.recon_epochs, "frame_px": F, "region": region},
+            "train": {"dataset_s": round(t_data, 2), "train_s": round(t_train, 2), "loss": [round(h, 5) for h in hist]},
+            "specimens": rows}
+    print(json.dumps(line))
 
 
 def precision_sweep(eng, wl, geo, meas_d, obj_d, probe_d, cfg, common, n_sub=512, batch=256):
@@ -336,10 +417,16 @@ def main():
                     help="256-px windows: keep every k-th slice's wave, recompute the rest")
     ap.add_argument("--no-optimizer", action="store_true",
                     help="skip the optimizer-step measurement (fourier_clean, L-BFGS epoch)")
+    ap.add_argument("--train", type=int, default=256, help="warm-start: training specimens")
+    ap.add_argument("--test", type=int, default=4, help="warm-start: held-out specimens")
+    ap.add_argument("--epochs", type=int, default=8, help="warm-start: training epochs")
+    ap.add_argument("--recon-epochs", type=int, default=80, help="warm-start: L-BFGS epochs per reconstruction")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config], name=args.config)
     if args.impl == "reference":
         return run_reference(args, cfg)
+    if cfg.get("warm_start"):
+        return run_warm_start(args, cfg)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

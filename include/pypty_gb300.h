@@ -317,6 +317,57 @@ int pty_lbfgs_read(const void* state, double* out, void* stream);
 int pty_orthogonalize_modes(void* probe, int64_t n_pixels, int32_t n_modes, void* stream);
 
 /*
+ * ---------------------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference, whose warm starts are non-learned,
+ * pypty/initialize.py:629): the kernels of a small U-Net that maps per-position
+ * centre-of-mass / virtual-bright-field maps to an object phase stack, and of its training.
+ * Tensors are NCHW; activations and their gradients BF16 (void*), weights and their gradients
+ * FP32. 3x3 convolutions need H and W multiples of 32; 1x1 convolutions at most 64 channels.
+ */
+/* out = act(conv3x3(x, w) + b), zero padding 1; transpose = 1: the data gradient
+ * (x = dL/d(layer output) with Ci = the layer's Co, out = dL/d(layer input), Co = the layer's Ci). */
+int pty_nn_conv3x3(const void* x, const float* w, const float* bias, void* out, int32_t N, int32_t Ci,
+                   int32_t Co, int32_t H, int32_t W, int32_t relu, int32_t transpose, void* stream);
+/* dw (Co, Ci, 3, 3) and db (Co) of a 3x3 convolution, deterministic (fixed-order block sums). */
+int pty_nn_conv3x3_wgrad_workspace_floats(int32_t N, int32_t Ci, int32_t Co, int32_t H, int32_t W, int64_t* n);
+int pty_nn_conv3x3_wgrad(const void* dy, const void* x, float* dw, float* db, int32_t N, int32_t Ci, int32_t Co,
+                         int32_t H, int32_t W, float* workspace, void* stream);
+int pty_nn_conv1x1(const void* x, const float* w, const float* b, void* out, int32_t N, int32_t Ci, int32_t Co,
+                   int64_t plane, void* stream);
+int pty_nn_conv1x1_workspace_floats(int32_t N, int32_t Ci, int32_t Co, int64_t plane, int64_t* n);
+int pty_nn_conv1x1_backward(const void* dy, const void* x, const float* w, void* dx, float* dw, float* db,
+                            int32_t N, int32_t Ci, int32_t Co, int64_t plane, float* workspace, void* stream);
+/* dst += src (BF16) */
+int pty_nn_add(void* dst, const void* src, int64_t n, void* stream);
+/* dy *= (y > 0) */
+int pty_nn_relu_mask(void* dy, const void* y, int64_t n, void* stream);
+/* 2x2 average pooling (backward = 1: its adjoint, x = dL/dy of size H/2 x W/2, y = dL/dx of H x W) */
+int pty_nn_avgpool2(const void* x, void* y, int64_t nplanes, int32_t H, int32_t W, int32_t backward, void* stream);
+/* nearest 2x upsampling of x (N, C, H, W) into channels [c_off, c_off + C) of y (N, Ct, 2H, 2W); backward: adjoint */
+int pty_nn_upsample2(const void* x, void* y, int32_t N, int32_t C, int32_t Ct, int32_t c_off, int32_t H, int32_t W,
+                     int32_t backward, void* stream);
+/* copy (N, C, plane) into (into = 1) or out of channels [c_off, c_off + C) of (N, Ct, plane) */
+int pty_nn_channel_copy(const void* src, void* dst, int32_t N, int32_t C, int32_t Ct, int32_t c_off, int64_t plane,
+                        int32_t into, void* stream);
+/* bilinear float (N, C, h, w) -> BF16 (N, Cd, H, W): output pixel (Y, X) samples the map at
+ * ((Y - oy) / sy, (X - ox) / sx), zero outside it; channels >= C zero */
+int pty_nn_bilinear(const float* src, void* dst, int32_t N, int32_t C, int32_t Cd, int32_t h, int32_t w, int32_t H,
+                    int32_t W, float oy, float ox, float sy, float sx, void* stream);
+/* mean squared error: 256 FP64 partial sums (sum them for n * loss) and dL/dpred */
+int pty_nn_mse(const void* pred, const float* target, void* dpred, double* partials, int64_t n, void* stream);
+/* Adam step with the bias-corrected learning rate lr_t */
+int pty_nn_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr_t, float b1, float b2, float eps,
+                void* stream);
+/* per pattern (detector order): centre of mass x, y (pixels from the centre) and the bright-field
+ * disk sum within r_bf pixels (pypty/dpc.py:137-151); out (n_patterns, 3) */
+int pty_virtual_detectors(const float* patterns, int32_t n_patterns, int32_t window, float r_bf, float* out,
+                          void* stream);
+/* Gaussian-atom phase slices (atoms: (n_slices, n_atoms, 3) = y, x [px], peak phase [rad]) into
+ * phase (n_slices, ny, nx) float and, if obj != NULL, exp(i phase) into obj (ny, nx, n_slices, 1) complex64 */
+int pty_atom_slices(const float* atoms, int32_t n_atoms, int32_t ny, int32_t nx, int32_t n_slices, float sigma_px,
+                    float* phase, void* obj, void* stream);
+
+/*
  * Launch profiler (no counterpart in the reference, which only logs wall time,
  * pypty/utils.py:1894). While enabled, every kernel launch of the library records a CUDA
  * event on its stream just before the launch, and every call records one when its last

@@ -98,6 +98,22 @@ SIGNATURES = {
     "pty_fft2_bf16x6": ([_VP, _VP, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
     "pty_layered_workspace_bytes": ([_PP, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_loss_and_direction_layered": ([_PP, _I32] + [_VP] * 11 + [_SZ, _VP], ctypes.c_int),
+    "pty_nn_conv3x3": ([_VP, _VP, _VP, _VP] + [_I32] * 7 + [_VP], ctypes.c_int),
+    "pty_nn_conv3x3_wgrad_workspace_floats": ([_I32] * 5 + [ctypes.POINTER(_I64)], ctypes.c_int),
+    "pty_nn_conv3x3_wgrad": ([_VP] * 4 + [_I32] * 5 + [_VP, _VP], ctypes.c_int),
+    "pty_nn_conv1x1": ([_VP] * 4 + [_I32] * 3 + [_I64, _VP], ctypes.c_int),
+    "pty_nn_conv1x1_workspace_floats": ([_I32] * 3 + [_I64, ctypes.POINTER(_I64)], ctypes.c_int),
+    "pty_nn_conv1x1_backward": ([_VP] * 6 + [_I32] * 3 + [_I64, _VP, _VP], ctypes.c_int),
+    "pty_nn_relu_mask": ([_VP, _VP, _I64, _VP], ctypes.c_int),
+    "pty_nn_add": ([_VP, _VP, _I64, _VP], ctypes.c_int),
+    "pty_nn_avgpool2": ([_VP, _VP, _I64, _I32, _I32, _I32, _VP], ctypes.c_int),
+    "pty_nn_upsample2": ([_VP, _VP] + [_I32] * 7 + [_VP], ctypes.c_int),
+    "pty_nn_channel_copy": ([_VP, _VP] + [_I32] * 4 + [_I64, _I32, _VP], ctypes.c_int),
+    "pty_nn_bilinear": ([_VP, _VP] + [_I32] * 7 + [_F32] * 4 + [_VP], ctypes.c_int),
+    "pty_nn_mse": ([_VP, _VP, _VP, _VP, _I64, _VP], ctypes.c_int),
+    "pty_nn_adam": ([_VP] * 4 + [_I64, _F32, _F32, _F32, _F32, _VP], ctypes.c_int),
+    "pty_virtual_detectors": ([_VP, _I32, _I32, _F32, _VP, _VP], ctypes.c_int),
+    "pty_atom_slices": ([_VP, _I32, _I32, _I32, _I32, _F32, _VP, _VP, _VP], ctypes.c_int),
     "pty_lbfgs_state_bytes": ([ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_lbfgs_reset": ([_VS, _VP, _VP], ctypes.c_int),
     "pty_lbfgs_first_direction": ([_VS, _PPV, _PPV, _VP, _VP], ctypes.c_int),

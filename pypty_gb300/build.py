@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBNAME = "libpypty_gb300.so"
-UNITS = ["capi.cu", "path_w64.cu", "path_w128.cu", "path_w256.cu", "noalloc.cu", "optim.cu", "dft_gemm.cu", "layered.cu"]
+UNITS = ["capi.cu", "path_w64.cu", "path_w128.cu", "path_w256.cu", "noalloc.cu", "optim.cu", "dft_gemm.cu", "layered.cu", "unet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

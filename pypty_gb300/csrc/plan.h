@@ -183,7 +183,7 @@ enum KernelId : int {
   KID_TWIDDLES = 0, KID_TABLES, KID_PROBE_FFT, KID_OBJ_TO_SLICES, KID_OBJECT_WINDOWS, KID_FUSED,
   KID_GRAD_WINDOWS, KID_TILE_LISTS, KID_SCATTER, KID_PROBE_PARTIAL, KID_SLICES_TO_OBJ, KID_PROBE_FINAL,
   KID_FINALIZE, KID_FFT2, KID_LAYOUT, KID_CLEAN_TABLES, KID_CLEAN_X, KID_CLEAN_Y, KID_CLEAN_XI,
-  KID_VEC, KID_SCALAR, KID_ACCEPT, KID_ORTHO, KID_DFT_TABLES, KID_DFT_GEMM, KID_ELEMENTWISE, KID_COUNT
+  KID_VEC, KID_SCALAR, KID_ACCEPT, KID_ORTHO, KID_DFT_TABLES, KID_DFT_GEMM, KID_ELEMENTWISE, KID_NN, KID_COUNT
 };
 
 // Records an event on `st` before a launch of kernel class `id` while profiling is on

@@ -1,0 +1,228 @@
+"""Warm-start network kernels against a plain PyTorch CPU FP64 reference of the same ops.
+
+Activations are BF16 in the kernels, so inputs are drawn BF16-exact and forward outputs are
+compared after BF16 rounding (relative L2 <= 1e-2); weight gradients (FP32 accumulation of
+BF16-exact products) to relative L2 <= 1e-4. The whole U-Net's parameter gradients are
+checked against the same network in PyTorch FP32 autograd (relative L2 <= 5e-2: the kernels
+round every activation to BF16).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from golden_io import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_exact(rng, shape, scale=1.0):
+    import torch
+    return (torch.from_numpy(rng.normal(size=shape) * scale).float().to(torch.bfloat16))
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+@pytest.mark.parametrize("N,Ci,Co,H", [(2, 8, 16, 32), (1, 24, 32, 64)])
+def test_conv3x3_forward_data_and_weight_gradients(N, Ci, Co, H):
+    import torch
+    import torch.nn.functional as F
+    from pypty_gb300 import _lib
+    lib = _lib.lib()
+    rng = np.random.default_rng(Ci + Co)
+    x = _bf16_exact(rng, (N, Ci, H, H))
+    w = torch.from_numpy(rng.normal(size=(Co, Ci, 3, 3)) * 0.2).float()
+    b = torch.from_numpy(rng.normal(size=Co) * 0.1).float()
+    dy = _bf16_exact(rng, (N, Co, H, H))
+    xd, wd, bd, dyd = x.cuda(), w.cuda(), b.cuda(), dy.cuda()
+    out = torch.empty((N, Co, H, H), dtype=torch.bfloat16, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.pty_nn_conv3x3(_p(xd), _p(wd), _p(bd), _p(out), N, Ci, Co, H, H, 1, 0, st) == 0
+    ref = F.relu(F.conv2d(x.double(), w.double(), b.double(), padding=1))
+    assert rel_l2(out.float().cpu().numpy(), ref.numpy()) <= 1e-2
+    # data gradient: the transposed, flipped weights with the same kernel
+    dx = torch.empty((N, Ci, H, H), dtype=torch.bfloat16, device="cuda")
+    assert lib.pty_nn_conv3x3(_p(dyd), _p(wd), None, _p(dx), N, Co, Ci, H, H, 0, 1, st) == 0
+    xr = x.double().requires_grad_(True)
+    yr = F.conv2d(xr, w.double(), b.double(), padding=1)
+    yr.backward(dy.double())
+    assert rel_l2(dx.float().cpu().numpy(), xr.grad.numpy()) <= 1e-2
+    # weight and bias gradients (deterministic block sums)
+    n = ctypes.c_int64(0)
+    lib.pty_nn_conv3x3_wgrad_workspace_floats(N, Ci, Co, H, H, ctypes.byref(n))
+    ws = torch.empty(n.value, dtype=torch.float32, device="cuda")
+    gw, gb = torch.empty_like(wd), torch.empty_like(bd)
+    assert lib.pty_nn_conv3x3_wgrad(_p(dyd), _p(xd), _p(gw), _p(gb), N, Ci, Co, H, H, _p(ws), st) == 0
+    wr = w.double().requires_grad_(True)
+    br = b.double().requires_grad_(True)
+    F.conv2d(x.double(), wr, br, padding=1).backward(dy.double())
+    assert rel_l2(gw.cpu().numpy(), wr.grad.numpy()) <= 1e-4
+    assert rel_l2(gb.cpu().numpy(), br.grad.numpy()) <= 1e-4
+    gw2 = torch.empty_like(wd)
+    lib.pty_nn_conv3x3_wgrad(_p(dyd), _p(xd), _p(gw2), _p(gb), N, Ci, Co, H, H, _p(ws), st)
+    assert torch.equal(gw, gw2)
+
+
+def test_pool_upsample_concat_1x1_mse_adam_bilinear():
+    import torch
+    import torch.nn.functional as F
+    from pypty_gb300 import _lib
+    lib = _lib.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(5)
+    x = _bf16_exact(rng, (2, 16, 64, 64))
+    xd = x.cuda()
+    y = torch.empty((2, 16, 32, 32), dtype=torch.bfloat16, device="cuda")
+    lib.pty_nn_avgpool2(_p(xd), _p(y), 32, 64, 64, 0, st)
+    assert rel_l2(y.float().cpu().numpy(), F.avg_pool2d(x.double(), 2).numpy()) <= 1e-2
+    g = torch.empty_like(xd)
+    lib.pty_nn_avgpool2(_p(y), _p(g), 32, 64, 64, 1, st)
+    assert rel_l2(g.float().cpu().numpy(), np.repeat(np.repeat(y.float().cpu().numpy(), 2, 2), 2, 3) / 4) <= 1e-2
+    # upsample into channels [8, 24) of a 24-channel tensor, concat channels [0, 8)
+    small = _bf16_exact(rng, (2, 16, 32, 32)).cuda()
+    skip = _bf16_exact(rng, (2, 8, 64, 64)).cuda()
+    cat = torch.empty((2, 24, 64, 64), dtype=torch.bfloat16, device="cuda")
+    lib.pty_nn_channel_copy(_p(skip), _p(cat), 2, 8, 24, 0, 64 * 64, 1, st)
+    lib.pty_nn_upsample2(_p(small), _p(cat), 2, 16, 24, 8, 32, 32, 0, st)
+    ref = torch.cat([skip.cpu(), F.interpolate(small.cpu().float(), scale_factor=2, mode="nearest").bfloat16()], 1)
+    assert torch.equal(cat.cpu(), ref)
+    back = torch.empty((2, 16, 32, 32), dtype=torch.bfloat16, device="cuda")
+    lib.pty_nn_upsample2(_p(cat), _p(back), 2, 16, 24, 8, 32, 32, 1, st)
+    refb = F.avg_pool2d(cat[:, 8:].cpu().double(), 2) * 4
+    assert rel_l2(back.float().cpu().numpy(), refb.numpy()) <= 1e-2
+    # 1x1 convolution and its gradients
+    w = torch.from_numpy(rng.normal(size=(20, 16)) * 0.3).float()
+    b = torch.from_numpy(rng.normal(size=20) * 0.1).float()
+    o = torch.empty((2, 20, 64, 64), dtype=torch.bfloat16, device="cuda")
+    wd, bd = w.cuda(), b.cuda()          # kept alive until the asynchronous launches have read them
+    lib.pty_nn_conv1x1(_p(xd), _p(wd), _p(bd), _p(o), 2, 16, 20, 64 * 64, st)
+    refo = F.conv2d(x.double(), w.double()[:, :, None, None], b.double())
+    assert rel_l2(o.float().cpu().numpy(), refo.numpy()) <= 1e-2
+    dy = _bf16_exact(rng, (2, 20, 64, 64))
+    n = ctypes.c_int64(0)
+    lib.pty_nn_conv1x1_workspace_floats(2, 16, 20, 64 * 64, ctypes.byref(n))
+    ws = torch.empty(n.value, device="cuda")
+    dx = torch.empty_like(xd)
+    gw, gb = torch.empty(20, 16, device="cuda"), torch.empty(20, device="cuda")
+    dyd = dy.cuda()
+    lib.pty_nn_conv1x1_backward(_p(dyd), _p(xd), _p(wd), _p(dx), _p(gw), _p(gb), 2, 16, 20, 64 * 64, _p(ws), st)
+    wr = w.double().requires_grad_(True)
+    br = b.double().requires_grad_(True)
+    xr = x.double().requires_grad_(True)
+    F.conv2d(xr, wr[:, :, None, None], br).backward(dy.double())
+    assert rel_l2(gw.cpu().numpy(), wr.grad.numpy()) <= 1e-4
+    assert rel_l2(gb.cpu().numpy(), br.grad.numpy()) <= 1e-4
+    assert rel_l2(dx.float().cpu().numpy(), xr.grad.numpy()) <= 1e-2
+    # mean squared error
+    t = torch.from_numpy(rng.normal(size=(2, 20, 64, 64))).float()
+    part = torch.empty(256, dtype=torch.float64, device="cuda")
+    dp = torch.empty_like(o)
+    td = t.cuda()
+    lib.pty_nn_mse(_p(o), _p(td), _p(dp), _p(part), o.numel(), st)
+    refl = float(((o.float().cpu().double() - t.double()) ** 2).sum())
+    assert abs(float(part.sum()) - refl) <= 1e-9 * refl
+    # bilinear placement of a map in a frame
+    m = torch.from_numpy(rng.normal(size=(1, 3, 8, 8))).float().cuda()
+    fr = torch.empty((1, 8, 64, 64), dtype=torch.bfloat16, device="cuda")
+    lib.pty_nn_bilinear(_p(m), _p(fr), 1, 3, 8, 8, 8, 64, 64, ctypes.c_float(4.0), ctypes.c_float(4.0),
+                        ctypes.c_float(4.0), ctypes.c_float(4.0), st)
+    frc = fr.float().cpu().numpy()
+    assert abs(frc[0, 1, 8, 12] - m.cpu().numpy()[0, 1, 1, 2]) <= 1e-2 * (1 + abs(frc[0, 1, 8, 12]))
+    assert frc[0, 0, 0, 0] == 0.0 and np.all(frc[0, 3:] == 0.0)
+    # Adam against the textbook update
+    p = torch.randn(1000, device="cuda")
+    gr = torch.randn(1000, device="cuda")
+    mm, vv = torch.zeros_like(p), torch.zeros_like(p)
+    p0 = p.clone()
+    lib.pty_nn_adam(_p(p), _p(gr), _p(mm), _p(vv), 1000, ctypes.c_float(1e-3), ctypes.c_float(0.9),
+                    ctypes.c_float(0.999), ctypes.c_float(1e-8), st)
+    m_ref, v_ref = 0.1 * gr, 0.001 * gr * gr
+    assert torch.allclose(p, p0 - 1e-3 * m_ref / (v_ref.sqrt() + 1e-8), rtol=1e-5, atol=1e-6)
+
+
+def test_virtual_detectors_match_numpy():
+    import torch
+    from pypty_gb300 import _lib
+    rng = np.random.default_rng(2)
+    pat = rng.uniform(0, 10, (5, 64, 64)).astype(np.float32)
+    out = torch.empty((5, 3), device="cuda")
+    pd = torch.from_numpy(pat).cuda()
+    _lib.lib().pty_virtual_detectors(_p(pd), 5, 64, ctypes.c_float(10.0), _p(out),
+                                     torch.cuda.current_stream().cuda_stream)
+    ky, kx = np.mgrid[:64, :64] - 32
+    tot = pat.sum((1, 2))
+    ref = np.stack([(pat * kx).sum((1, 2)) / tot, (pat * ky).sum((1, 2)) / tot,
+                    (pat * (kx ** 2 + ky ** 2 <= 100)).sum((1, 2))], 1)
+    assert np.allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-4)
+
+
+def test_unet_gradients_match_torch_autograd():
+    """The whole network (3 levels, base 16) against the same network in PyTorch FP32."""
+    import torch
+    import torch.nn.functional as F
+    from pypty_gb300.warmstart import UNet, mse
+    net = UNet(in_ch=3, out_ch=4, base=16, levels=3, device="cuda", seed=3)
+    rng = np.random.default_rng(7)
+    x = _bf16_exact(rng, (2, 8, 128, 128))
+    t = torch.from_numpy(rng.normal(size=(2, 4, 128, 128)) * 0.5).float()
+    pred = net.forward(x.cuda())
+    loss, d = mse(pred, t.cuda())
+    net.backward(d)
+    # reference network
+    P = {}
+
+    def conv(h, c, relu=True):
+        y = F.conv2d(h, c.w.cpu().requires_grad_(True) if id(c) not in P else P[id(c)][0], None, padding=1)
+        return y
+
+    params = []
+
+    def mk(c):
+        w = c.w.detach().cpu().clone().requires_grad_(True)
+        b = c.b.detach().cpu().clone().requires_grad_(True)
+        params.append((c, w, b))
+        return w, b
+
+    def block(h, c):
+        w, b = mk(c)
+        return F.relu(F.conv2d(h, w, b, padding=1))
+
+    h = x.float()
+    skips = []
+    for lvl, (a, b) in enumerate(net.enc):
+        if lvl > 0:
+            h = F.avg_pool2d(h, 2)
+        h = block(block(h, a), b)
+        skips.append(h)
+    for lvl in range(net.levels - 2, -1, -1):
+        a, b = net.dec[lvl]
+        h = torch.cat([skips[lvl], F.interpolate(h, scale_factor=2, mode="nearest")], 1)
+        h = block(block(h, a), b)
+    wo = net.wout.detach().cpu().clone().requires_grad_(True)
+    bo = net.bout.detach().cpu().clone().requires_grad_(True)
+    out = F.conv2d(h, wo[:, :, None, None], bo)
+    lref = ((out - t) ** 2).mean()
+    lref.backward()
+    assert abs(float(loss) - float(lref)) <= 5e-2 * float(lref)
+    assert rel_l2(net.gwout.cpu().numpy(), wo.grad.numpy()) <= 5e-2
+    for c, w, b in params:
+        assert rel_l2(c.gw.cpu().numpy(), w.grad.numpy()) <= 5e-2
+
+
+def test_training_reduces_the_loss():
+    """A few Adam steps on one fixed batch lower the mean squared error."""
+    import torch
+    from pypty_gb300.warmstart import UNet, mse
+    net = UNet(in_ch=3, out_ch=4, base=16, levels=3, device="cuda", seed=1)
+    rng = np.random.default_rng(11)
+    x = _bf16_exact(rng, (2, 8, 128, 128)).cuda()
+    t = torch.from_numpy(rng.normal(size=(2, 4, 128, 128)) * 0.3).float().cuda()
+    losses = []
+    for _ in range(30):
+        loss, d = mse(net.forward(x), t)
+        losses.append(float(loss))
+        net.backward(d)
+        net.step(3e-3)
+    assert losses[-1] < 0.7 * losses[0]
