@@ -219,7 +219,7 @@ def run_warm_start(args, cfg):
     stats = (xs.mean(dim=(0, 2, 3)), xs.std(dim=(0, 2, 3)) + 1e-6)
     net = ws.UNet(in_ch=3, out_ch=cfg["Z"], base=32, levels=4, device=dev, seed=0)
     t0 = time.perf_counter()
-    hist = ws.train(net, scene, xs, ys, stats, epochs=args.epochs, batch=4, lr=1e-3)
+    hist = ws.train(net, scene, xs, ys, stats, epochs=args.epochs, batch=4, lr=args.lr)
     torch.cuda.synchronize(dev)
     t_train = time.perf_counter() - t0
     del xs, ys
@@ -229,6 +229,7 @@ def run_warm_start(args, cfg):
     c0, c1 = int(scene.W / 2), int(scene.geometry.positions.max() + scene.W / 2)
     region = (c0, c1, c0, c1)          # the probe centres' square: every pixel well illuminated
     rows = []
+    ws.predict(net, scene, torch.zeros((3, scene.n_scan, scene.n_scan), device=dev), stats)   # warm the path up
     for k in range(args.test):
         phase, obj = ws.specimen(scene, rng, eng)
         meas = ws.measure(scene, obj, eng, gen)
@@ -241,7 +242,10 @@ def run_warm_start(args, cfg):
         start[:F, :F, :, 0] = torch.exp(1j * pred.permute(1, 2, 0).to(torch.complex64))
         torch.cuda.synchronize(dev)
         t_inf = time.perf_counter() - t_inf0
-        row = {"inference_s": round(t_inf, 4)}
+        tgt = ws.predictable_target(phase[:, :F, :F], 0.1, eng)
+        row = {"inference_s": round(t_inf, 4), "pred_std": round(float(pred.std()), 5),
+               "target_std": round(float(tgt.std()), 5),
+               "pred_target_corr": round(float(torch.corrcoef(torch.stack([pred.flatten(), tgt.flatten()]))[0, 1]), 4)}
         for proj in (False, True):
             key = "projected" if proj else "slices"
             cf, _ = ws.reconstruct(scene, meas, phase, flat, eng, epochs=args.recon_epochs, region=region,
@@ -421,6 +425,7 @@ def main():
     ap.add_argument("--test", type=int, default=4, help="warm-start: held-out specimens")
     ap.add_argument("--epochs", type=int, default=8, help="warm-start: training epochs")
     ap.add_argument("--recon-epochs", type=int, default=80, help="warm-start: L-BFGS epochs per reconstruction")
+    ap.add_argument("--lr", type=float, default=3e-4, help="warm-start: Adam learning rate")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config], name=args.config)
     if args.impl == "reference":

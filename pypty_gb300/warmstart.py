@@ -303,8 +303,27 @@ def network_input(scene: Scene, m, stats, dev):
     return out
 
 
-def make_dataset(scene: Scene, n, eng: Engine, seed):
-    """n specimens: input maps (n, 3, s, s) and target phases (n, Z, F, F) on the frame."""
+def lowpass_target(phase_frame, cutoff, eng: Engine):
+    """The part of a (Z, F, F) phase stack the maps can predict: each slice band-limited to
+    ``cutoff`` (fraction of Nyquist) with the library's fourier_clean kernel."""
+    from .optim import fourier_clean_
+    z = phase_frame.permute(1, 2, 0).contiguous().to(torch.complex64)      # (F, F, Z)
+    fourier_clean_(z, cutoff, 0.0, out=z, engine=eng)
+    return z.real.permute(2, 0, 1).contiguous()
+
+
+def predictable_target(phase_frame, cutoff, eng: Engine):
+    """E[phase_z | maps]: the maps see the depth-integrated phase blurred by the probe, and the
+    slices of a random specimen are independent, so the predictable part of every slice is the
+    band-limited depth average (each slice's own deviation from it is not predictable)."""
+    lp = lowpass_target(phase_frame, cutoff, eng)
+    return lp.mean(dim=0, keepdim=True).expand_as(lp).contiguous()
+
+
+def make_dataset(scene: Scene, n, eng: Engine, seed, target_cutoff=0.1):
+    """n specimens: input maps (n, 3, s, s) and target phases (n, Z, F, F) on the frame: the
+    conditional-mean target ``predictable_target`` (the scan samples every ``step`` pixels and
+    the probe blurs the depth-integrated phase)."""
     rng = np.random.default_rng(seed)
     gen = torch.Generator(device=eng.device).manual_seed(seed)
     F = scene.frame
@@ -314,13 +333,17 @@ def make_dataset(scene: Scene, n, eng: Engine, seed):
         phase, obj = specimen(scene, rng, eng)
         pat = measure(scene, obj, eng, gen)
         xs[i] = maps(scene, pat, eng)
-        ys[i] = phase[:, :F, :F]
+        ys[i] = predictable_target(phase[:, :F, :F], target_cutoff, eng)
     return xs, ys
 
 
 def train(net: UNet, scene: Scene, xs, ys, stats, epochs=10, batch=4, lr=1e-3, seed=0, log=None):
-    """Adam on the mean squared phase error; returns the per-epoch mean loss."""
+    """Adam on the mean squared error of the standardised target phase (the target's mean and
+    standard deviation are kept in ``net.target_stats`` and undone by ``predict``); returns the
+    per-epoch mean loss (in units of the target variance)."""
     n = xs.shape[0]
+    t_mean, t_std = float(ys.mean()), float(ys.std()) + 1e-12
+    net.target_stats = (t_mean, t_std)
     rng = np.random.default_rng(seed)
     hist = []
     for ep in range(epochs):
@@ -330,7 +353,7 @@ def train(net: UNet, scene: Scene, xs, ys, stats, epochs=10, batch=4, lr=1e-3, s
             idx = torch.from_numpy(order[b0:b0 + batch]).to(xs.device)
             x = network_input(scene, xs[idx], stats, net.dev)
             pred = net.forward(x)
-            loss, d = mse(pred, ys[idx].contiguous())
+            loss, d = mse(pred, ((ys[idx] - t_mean) / t_std).contiguous())
             net.backward(d)
             net.step(lr)
             tot += float(loss)
@@ -341,8 +364,10 @@ def train(net: UNet, scene: Scene, xs, ys, stats, epochs=10, batch=4, lr=1e-3, s
 
 
 def predict(net: UNet, scene: Scene, m, stats):
+    """Phase stack (Z, F, F) predicted from the maps m (3, s, s)."""
     x = network_input(scene, m[None], stats, net.dev)
-    return net.forward(x)[0].float()
+    t_mean, t_std = getattr(net, "target_stats", (0.0, 1.0))
+    return net.forward(x)[0].float() * t_std + t_mean
 
 
 def phase_rmse(obj, truth_phase, region, projected=False):

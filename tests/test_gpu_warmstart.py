@@ -158,15 +158,16 @@ def test_virtual_detectors_match_numpy():
     assert np.allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-4)
 
 
-def test_unet_gradients_match_torch_autograd():
-    """The whole network (3 levels, base 16) against the same network in PyTorch FP32."""
+@pytest.mark.parametrize("levels,base,size,out_ch,batch", [(3, 16, 128, 4, 2), (4, 32, 256, 20, 1)])
+def test_unet_gradients_match_torch_autograd(levels, base, size, out_ch, batch):
+    """The whole network against the same network in PyTorch FP32 (the warm-start shape last)."""
     import torch
     import torch.nn.functional as F
     from pypty_gb300.warmstart import UNet, mse
-    net = UNet(in_ch=3, out_ch=4, base=16, levels=3, device="cuda", seed=3)
+    net = UNet(in_ch=3, out_ch=out_ch, base=base, levels=levels, device="cuda", seed=3)
     rng = np.random.default_rng(7)
-    x = _bf16_exact(rng, (2, 8, 128, 128))
-    t = torch.from_numpy(rng.normal(size=(2, 4, 128, 128)) * 0.5).float()
+    x = _bf16_exact(rng, (batch, 8, size, size))
+    t = torch.from_numpy(rng.normal(size=(batch, out_ch, size, size)) * 0.5).float()
     pred = net.forward(x.cuda())
     loss, d = mse(pred, t.cuda())
     net.backward(d)
@@ -207,8 +208,9 @@ def test_unet_gradients_match_torch_autograd():
     lref.backward()
     assert abs(float(loss) - float(lref)) <= 5e-2 * float(lref)
     assert rel_l2(net.gwout.cpu().numpy(), wo.grad.numpy()) <= 5e-2
-    for c, w, b in params:
-        assert rel_l2(c.gw.cpu().numpy(), w.grad.numpy()) <= 5e-2
+    errs = [rel_l2(c.gw.cpu().numpy(), w.grad.numpy()) for c, w, b in params]
+    print("layer weight-gradient errors:", ["%.1e" % e for e in errs])
+    assert max(errs) <= 5e-2
 
 
 def test_training_reduces_the_loss():
