@@ -50,7 +50,8 @@ struct Path {
     const size_t smem = Smem<W>::bytes;
     int rc;
     if ((rc = set_smem(probe_fft_kernel<W>, smem)) || (rc = set_smem(object_windows_kernel<W>, smem)) ||
-        (rc = set_smem(fused_multislice_kernel<W>, FusedSmem<W>::bytes)) ||
+        (rc = set_smem(fused_multislice_kernel<W, 0>, FusedSmem<W>::bytes)) ||
+        (rc = set_smem(fused_multislice_kernel<W, 1>, FusedSmem<W>::bytes)) ||
         (rc = set_smem(grad_windows_kernel<W>, smem)) || (rc = set_smem(probe_final_kernel<W>, smem)))
       return rc;
     return PTY_OK;
@@ -148,7 +149,9 @@ struct Path {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     prof_mark(st, KID_FUSED);
-    if (cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W>, fa) != cudaSuccess) return PTY_ERR_CUDA;
+    const cudaError_t e = fa.phase == 0 ? cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W, 0>, fa)
+                                        : cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W, 1>, fa);
+    if (e != cudaSuccess) return PTY_ERR_CUDA;
     return cuda_status();
   }
 
@@ -251,6 +254,7 @@ int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2
 template <int W>
 int ms_fused(const MsPlan& q, int phase, int step_obj, int step_probe, int use_edge, void* ws, cudaStream_t st) {
   const size_t WW = (size_t)W * W;
+  if (set_smem(fused_multislice_kernel<W, 1>, FusedSmem<W>::bytes)) return PTY_ERR_CUDA;
   FusedArgs fa{};
   fa.Z = q.Z;
   fa.Mp = q.Mp;
@@ -298,7 +302,7 @@ int ms_fused(const MsPlan& q, int phase, int step_obj, int step_probe, int use_e
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   prof_mark(st, KID_FUSED);
-  if (cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W>, fa) != cudaSuccess) return PTY_ERR_CUDA;
+  if (cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W, 1>, fa) != cudaSuccess) return PTY_ERR_CUDA;
   return cuda_status();
 }
 

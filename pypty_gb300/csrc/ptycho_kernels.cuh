@@ -342,7 +342,9 @@ struct FusedSmem {
 // Operands are prefetched by TMA bulk copies: the next step's window (O_z, or conj(psi_z) in
 // the adjoint) lands in the exchange buffer while the inverse transform finishes its last
 // register-only round; the adjoint's O_z arrives in the side buffer one step ahead.
-template <int W>
+// PH = 0: the whole pass (phase 0) with every phase branch compiled out; PH = 1: a.phase at
+// run time (the split halves and the multislice_core phases).
+template <int W, int PH>
 __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kernel(FusedArgs a) {
   using G = Geo<W>;
   using F = WinFFT<W>;
@@ -371,6 +373,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
   const int Z = a.Z;
   const bool adj_stack = a.step_obj && !a.simulate;   // the adjoint reads conj(psi_z)
+  const int phase = PH == 0 ? 0 : a.phase;
   if (t == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
@@ -411,9 +414,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 
   float2 v[32];
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
-  const bool adjoint_only = (a.phase == 2 || a.phase == 4);
+  const bool adjoint_only = (phase == 2 || phase == 4);
   const int s_begin = adjoint_only ? Z + 1 : 0;
-  const int s_end = (a.simulate || a.phase == 1 || a.phase == 3) ? Z + 1 : 2 * Z + 1;
+  const int s_end = (a.simulate || phase == 1 || phase == 3) ? Z + 1 : 2 * Z + 1;
   if (adjoint_only) {
     // adjoint half: resume from dL/d(exit wave) kept by the forward half
     ld_native<W>(gb, v);
@@ -428,7 +431,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 
     // ------------------------------------------------ real-space op
     if (s == 0) {
-      if (a.probe_b) {
+      if (PH != 0 && a.probe_b) {
         ld_native<W>(a.probe_b + ((size_t)b * a.Mp + p) * WW, v);
       } else if (!a.probe_shift) {
 #pragma unroll
@@ -442,7 +445,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         st_native<W>(stack_ptr(z), c);
         fence_async_global();   // these stores are read back by TMA in the adjoint
       }
-      if (z == Z - 1 && adj_stack && a.phase == 0) issue_side(Z - 1);
+      if (z == Z - 1 && adj_stack && phase == 0) issue_side(Z - 1);
       mbar_wait(&bars[0], ph_x, a.err);
       {
         const float4* ob = reinterpret_cast<const float4*>(xbuf);
@@ -453,7 +456,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
         }
       }
-      if (a.phase == 3 && z == Z - 1) {
+      if (phase == 3 && z == Z - 1) {
         st_native<W>(a.exit_out + (((size_t)b * a.Mp + p) * a.Mo + m) * WW, v);   // the exit wave
         break;
       }
@@ -553,7 +556,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           cluster.sync();
           if (m != 0) break;
         }
-        if (a.phase == 4) {   // interm_probe_grad of multislice_core.py:193-197, real space
+        if (phase == 4) {   // interm_probe_grad of multislice_core.py:193-197, real space
           if (a.step_probe) st_native<W>(a.fprobe + ((size_t)b * a.Mp + p) * WW, v);
           break;
         }
@@ -689,7 +692,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     }
     F::inverse_tail(v, tw1);
   }
-  if (a.phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
+  if (phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
 }
 
 // ------------------------------------------------------------------ reference-layout windows
