@@ -21,7 +21,7 @@
 // buffer's "drain" mbarriers. The tensor core's FP32 accumulation is biased (its error grows
 // linearly with the number of accumulated MMAs, ~2^-24 each), so every K block's partial
 // product is drained into registers with 32-lane TMEM loads (warp w: lanes 32 (w % 4), column
-// half w / 4) and added there with round-to-nearest FP32 adds, while the tensor core works on
+// part w / 4 of four) and added there with round-to-nearest FP32 adds, while the tensor core works on
 // the next block. Every wait is bounded; a wait that runs out sets the error word instead of
 // spinning. The epilogue stores the transposed window with 256-byte coalesced warp stores.
 #include <cuda_bf16.h>
@@ -35,7 +35,8 @@
 namespace pty {
 namespace dg {
 
-constexpr int BM = 128, BK = 64, THREADS = 256, STAGES = 2;
+constexpr int BM = 128, BK = 64, THREADS = 512, STAGES = 2;
+constexpr int NPART = THREADS / 128;   // warps per TMEM lane quadrant: each drains BN / NPART columns
 
 // S = number of BF16 terms per FP32 operand: 2 (BF16x3: products hh, hl, lh) or 3 (BF16x6:
 // products with term indices i + j <= 2, ~FP32 accuracy); BN shrinks to 128 for S = 3 so that
@@ -120,9 +121,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   constexpr size_t TERM = (size_t)C::NT * C::KC * C::B_BYTES;
   constexpr uint32_t idesc = umma::idesc_bf16_f32(BM, C::BN);
   uint32_t full_par[STAGES] = {0, 0}, empty_par[STAGES] = {0, 0}, drain_par[2] = {0, 0};
-  // this thread's accumulator slice: TMEM lanes 32 (w % 4) + lane (tile rows), column half w / 4
+  // this thread's accumulator slice: TMEM lanes 32 (w % 4) + lane (tile rows), column part w / 4
   const int q = warp & 3, h = warp >> 2;
-  constexpr int HALF = C::BN / 2;
+  constexpr int HALF = C::BN / NPART;   // columns this warp drains
   float acc[HALF];
 #pragma unroll
   for (int j = 0; j < HALF; ++j) acc[j] = 0.0f;
@@ -149,6 +150,21 @@ __global__ void __launch_bounds__(THREADS, 1)
     umma::fence_before_sync();
   };
 
+  // A blocks: rows row0 .. row0+127, real columns kc*64 .. kc*64+63 (16 float4 per row); the next
+  // block's FP32 values are loaded into registers while the current block's MMAs run
+  constexpr int APT = (BM * BK / 4) / THREADS;   // float4 per thread per block
+  float4 pre[APT];
+  auto load_a = [&](int kc) {
+#pragma unroll
+    for (int i = 0; i < APT; ++i) {
+      const int qq = tid + THREADS * i;
+      const int r = qq >> 4, c4 = qq & 15;
+      const long long row = row0 + r;
+      pre[i] = row < n_rows ? reinterpret_cast<const float4*>(in + row * W)[kc * 16 + c4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  load_a(0);
+
   for (int kc = 0; kc < C::KC; ++kc) {
     const int s = kc % STAGES;
     uint8_t* sA = base + s * C::STAGE;            // S terms of A, then S terms of B
@@ -161,16 +177,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         bulk_copy_g2s(sB + term * C::B_BYTES, img_nt + term * TERM + (size_t)kc * C::B_BYTES, C::B_BYTES,
                       &full_bar[s]);
     }
-    // A block: rows row0 .. row0+127, real columns kc*64 .. kc*64+63 (16 float4 per row)
 #pragma unroll
-    for (int i = 0; i < (BM * BK / 4) / THREADS; ++i) {
+    for (int i = 0; i < APT; ++i) {
       const int qq = tid + THREADS * i;
       const int r = qq >> 4, c4 = qq & 15;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      const long long row = row0 + r;
-      if (row < n_rows) v = reinterpret_cast<const float4*>(in + row * W)[kc * 16 + c4];
       const uint32_t off = umma::sw128_offset(r, 4 * c4);
-      float4 rest = v;
+      float4 rest = pre[i];
 #pragma unroll
       for (int term = 0; term < S; ++term) {
         // successive BF16 terms; every residual x - bf16(x) is exact in FP32
@@ -186,6 +198,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
     }
+    if (kc + 1 < C::KC) load_a(kc + 1);
     fence_async_shared();
     umma::fence_before_sync();
     __syncthreads();   // A is written; every thread has drained TMEM buffer kc & 1 (block kc - 2)
