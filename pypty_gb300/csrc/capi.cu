@@ -76,7 +76,7 @@ const char* kKernelNames[KID_COUNT] = {
     "grad_windows", "tile_lists", "scatter_tiles", "probe_partial", "slices_to_obj", "probe_final",
     "finalize_scalars", "fft2_batch", "layout", "clean_tables", "clean_pass_x", "clean_pass_y",
     "clean_pass_x_inverse", "opt_vector", "opt_scalar", "opt_accept", "orthogonalize_modes", "dft_tables",
-    "dft_gemm_bf16x3", "layered_elementwise", "warm_start_net"};
+    "dft_gemm_bf16x3", "layered_elementwise", "warm_start_net", "probe_spectrum", "shifted_probes"};
 
 }  // namespace
 

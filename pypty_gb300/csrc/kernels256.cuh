@@ -75,7 +75,7 @@ struct Smem256 {
   static constexpr size_t small = red_off + sizeof(double) * 72;              // FFT-only kernels
   static constexpr size_t pyx_off = small;
   static constexpr size_t bits_off = pyx_off + sizeof(float2) * 512;
-  static constexpr size_t acc_off = bits_off + sizeof(uint32_t) * G::T;
+  static constexpr size_t acc_off = bits_off + sizeof(uint32_t) * G::T * 4;
   static constexpr size_t fused = acc_off + sizeof(float) * G::XBUF;         // the fused kernel
 };
 
@@ -129,10 +129,7 @@ __global__ void __launch_bounds__(512, 1) object_windows256_kernel(WindowArgs a)
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = src[G::rx(c, t, i)];
   __syncthreads();
-  WinFFT256::forward(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], a.mask_sc[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
-  WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
+  WinFFT256::band_limit(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl, a.mask_sc);
   st_native<128>(a.out + (size_t)win * 65536 + c * G::PART, v);
 }
 
@@ -152,10 +149,7 @@ __global__ void __launch_bounds__(512, 1) grad_windows256_kernel(float2* buf, co
   ld_native<128>(win + c * G::PART, v);
   __syncthreads();
   // the cluster barriers inside the transforms order every block's reads before any write
-  WinFFT256::forward(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], mask_sc[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
-  WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
+  WinFFT256::band_limit(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl, mask_sc);
 #pragma unroll
   for (int i = 0; i < 32; ++i) win[G::ry(c, t) * 256 + G::rx(c, t, i)] = v[i];
 }
@@ -233,12 +227,22 @@ __global__ void __launch_bounds__(512, 1) fft2_batch256_kernel(const float2* __r
 //
 // Steps form a small state machine, each "real-space op -> FFT -> frequency op -> inverse
 // FFT" with the two transforms inlined once:
-//   F_START  probe spectrum -> IFFT           F_SLICE  * O_z, FFT, * P (or far field), IFFT
+//   F_START  load the shifted probe           F_SLICE  * O_z, FFT, * P (or far field), IFFT
 //   LOSS     dL/dI (no transform)             A_START  dL/dI * Psi_k -> IFFT
 //   A_RECOMP segment recomputation            A_SLICE  gradient, * conj O_z, FFT, * conj P, IFFT
+//
+// The kernel is compiled twice: PH = 1 runs the forward stages and the loss and leaves dL/dI
+// in dldi; PH = 2 starts from dldi and runs the adjoint stages. Each instance carries only
+// its own stages' code and live state (the one-kernel state machine spilled ~400 B per
+// thread; the two instances spill under 100 B). Propagation steps fold the forward cross
+// butterfly, the propagator and the inverse cross butterfly into one cluster exchange
+// (WinFFT256::cross_propagate).
 enum Stage256 : int { F_START = 0, F_SLICE, S_LOSS, A_START, A_RECOMP, A_SLICE, S_DONE };
 
+template <int PH>
 __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
+  static_assert(PH == 1 || PH == 2, "phase 1: forward + loss, phase 2: adjoint");
+  constexpr bool FWD = PH == 1, ADJ = PH == 2;
   using G = Geo256;
   constexpr int T = G::T;
   constexpr size_t WW = 65536;
@@ -260,11 +264,11 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
   load_twiddles<128>(s.tw1, s.tw2, a.tw);
   load_tw256(s.tw256);
   for (int i = t; i < 512; i += T) spy[i] = a.pyx[i];
-  {
+  for (int q = 0; q < 4; ++q) {   // band-limit bits of this thread's elements in every quadrant
     uint32_t mb = 0;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) mb |= (a.mask[G::fky(c, t, i) * 256 + G::fkx(c, t, i)] != 0.0f ? 1u : 0u) << i;
-    sbits[t] = mb;
+    for (int i = 0; i < 32; ++i) mb |= (a.mask[G::fky(q, t, i) * 256 + G::fkx(q, t, i)] != 0.0f ? 1u : 0u) << i;
+    sbits[q * T + t] = mb;
   }
   for (int i = 0; i < 32; ++i) facc[i * T + t] = 0.0f;
   const bool want_probe = a.step_probe || a.step_pos;
@@ -272,21 +276,20 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
   auto wpart = [&](float2* base, size_t win) { return base + win * WW + c * PART; };
   auto stack_win = [&](int z, int p, int m) { return (((size_t)b * nck + z / K) * Mp + p) * Mo + m; };
 
-  int stage = F_START, k = 0, z = 0, z0 = 0, zl = 0;
-  if (a.phase == 2) {
-    stage = A_START;
+  int stage = FWD ? F_START : A_START, k = 0, z = 0, z0 = 0, zl = 0;
+  if (ADJ) {
     for (int i = 0; i < 32; ++i) facc[i * T + t] = a.dldi[(size_t)b * WW + c * PART + i * T + t];
   }
   __syncthreads();
 
   float2 v[32];
   while (stage != S_DONE) {
-    const bool fwd_stage = stage == F_START || stage == F_SLICE;
+    const bool fwd_stage = FWD;
     const int p = fwd_stage ? k % Mp : k / Mo;
     const int m = fwd_stage ? k / Mp : k % Mo;
     const int kidx = m * Mp + p;
 
-    if (stage == S_LOSS) {
+    if (FWD && stage == S_LOSS) {
       // ------------------------------------------------ loss and dL/dI of this quadrant
       const int gi = a.seq[b];
       const float inv_modes = 1.0f / (float)nmodes;
@@ -324,20 +327,38 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
         a.loss_part[2 * b + 1] = q;
       }
       cl.sync();
-      if (a.phase == 1) {
-        for (int i = 0; i < 32; ++i) a.dldi[(size_t)b * WW + c * PART + i * T + t] = facc[i * T + t];
-        return;
+      for (int i = 0; i < 32; ++i) a.dldi[(size_t)b * WW + c * PART + i * T + t] = facc[i * T + t];
+      return;
+    }
+
+    // ------------------------------------------------ L2 prefetch of the next step's operands
+    // (this block's part of each window), one FFT pair ahead of their loads
+    if (t == 0) {
+      constexpr uint32_t PB = (uint32_t)(PART * sizeof(float2));
+      if (FWD) {
+        const int zn = stage == F_START ? 0 : z + 1;
+        if (zn < Z) prefetch_l2(part(a.obl, ((size_t)b * Z + zn) * Mo + m), PB);
+      } else if (stage == A_SLICE || (stage == A_START && K == 1)) {
+        const int zn = stage == A_START ? Z - 1 : z - 1;
+        if (zn >= 0 && (K == 1 || zn >= z0)) {   // the next step stays in this segment
+          prefetch_l2(part(a.obl, ((size_t)b * Z + zn) * Mo + m), PB);
+          if (store_stack) {
+            prefetch_l2(K == 1 ? part(a.stack, stack_win(zn, p, m)) : part(a.seg, (size_t)b * K + (zn - z0)), PB);
+            if (p > 0) prefetch_l2(part(a.gsum, ((size_t)b * Z + zn) * Mo + m), PB);
+          }
+        }
+      } else if (stage == A_RECOMP && z < zl) {
+        prefetch_l2(part(a.obl, ((size_t)b * Z + z + 1) * Mo + m), PB);
       }
-      stage = A_START;
-      k = 0;
-      continue;
     }
 
     // ------------------------------------------------ real-space op
-    bool do_fwd = false, do_inv = false, epilogue = false, skip = false;
-    if (stage == F_START || stage == A_START) {
+    bool do_fwd = false, do_inv = false, skip = false;
+    if (FWD && stage == F_START) {
+      ld_native<128>(part(a.fprobe, (size_t)b * Mp + p), v);   // the shifted incoming probe
+    } else if (ADJ && stage == A_START) {
       do_inv = true;
-    } else if (stage == F_SLICE) {
+    } else if (FWD) {   // F_SLICE
       if (store_stack && z % K == 0) st_native128_conj(wpart(a.stack, stack_win(z, p, m)), v);
       mul_native128(v, part(a.obl, ((size_t)b * Z + z) * Mo + m), false);
       do_fwd = true;
@@ -377,123 +398,61 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
             skip = true;
           }
         }
-        if (!skip) {
-          do_fwd = true;   // probe-gradient spectrum
-          epilogue = true;
-        }
+        // the probe-gradient wave; probe_spectrum256_kernel takes its spectrum
+        if (!skip) st_native<128>(wpart(a.fprobe, (size_t)b * Mp + p), v);
       }
     }
 
-    // ------------------------------------------------ forward FFT
-    if (do_fwd) WinFFT256::forward(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
-
-    // ------------------------------------------------ frequency op
-    if (stage == F_START) {
-      // incoming probe: FFT(P) * shift ramp * mask / W^2 (objective.py:469-476); without a
-      // shift the probe is taken back unchanged (FFT(P) / W^2)
-      const float2* pf = part(a.probe_f, p);
-      const float inv = 1.0f / (float)WW;
-      const int gi = a.seq[b];
-      const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        float2 w = make_float2(inv, 0.f);
-        if (a.probe_shift) {
-          const int ky = G::fky(c, t, i), kx = G::fkx(c, t, i);
-          const float mk = a.mask[ky * 256 + kx];
-          const float th = __fadd_rn(__fmul_rn(__fmul_rn(a.sx[kx], mk), dx), __fmul_rn(__fmul_rn(a.sy[ky], mk), dy));
-          float sn, cs;
-          sincosf(th, &sn, &cs);
-          w = make_float2(cs * mk * inv, sn * mk * inv);
-        }
-        v[i] = cmul(pf[nidx<128>(i, t)], w);
-      }
-    } else if (stage == A_START) {
-      // dL/dPsi = dL/dI * Psi * w (objective.py:595-597)
-      ld_native<128>(part(a.psi, (size_t)b * nmodes + kidx), v);
-#pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cscale(cscale(v[i], facc[i * T + t]), a.loss_weight);
-    } else if (stage == F_SLICE && z == Z - 1) {
-      // far field of this mode: Psi = FFT(exit) * mask; accumulate |Psi|^2
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        v[i] = cscale(v[i], a.mask[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
-        facc[i * T + t] += cabs2(v[i]);
-      }
-      if (!a.simulate) st_native<128>(wpart(a.psi, (size_t)b * nmodes + kidx), v);
-    } else if (do_inv) {
+    // ------------------------------------------------ transforms and frequency op
+    // forward: twiddled sub-transform, then either the full cross butterfly or (propagation
+    // steps) the folded butterfly-propagator-butterfly exchange; inverse: conjugate twiddle
+    // and sub-transform. Each sub-transform is inlined once.
+    const bool prop_step = do_fwd && do_inv;
+    if (do_fwd) {
+      WinFFT<128>::forward(v, s.xbuf, s.tw1, s.tw2);
+      WinFFT256::twiddle(v, s.tw256, c, false);
+    }
+    if (prop_step) {
       // propagator (conjugated in the adjoint); the thick first slice uses the table
-      const bool adjoint = stage == A_SLICE;
+      const bool adjoint = ADJ && stage == A_SLICE;
       const int zstep = adjoint ? z - 1 : z;
       const bool edge = a.use_edge && zstep == 0;
-      if (a.use_sep && !edge) {
-        const uint32_t mb = sbits[t];
+      const bool tab = !a.use_sep || edge;
+      const float2* pr = edge ? a.prop_edge : a.prop;
+      WinFFT256::cross_propagate(v, s.xbuf, cl, c, adjoint, [&](int i, int q) {
+        const int ky = G::fky(q, t, i), kx = G::fkx(q, t, i);
+        if (tab) return pr[ky * 256 + kx];
+        return ((sbits[q * T + t] >> i) & 1u) ? cmul(spy[ky], spx[kx]) : make_float2(0.f, 0.f);
+      });
+    } else {
+      if (do_fwd) WinFFT256::cross(v, s.xbuf, cl, c);
+      if (ADJ && stage == A_START) {
+        // dL/dPsi = dL/dI * Psi * w (objective.py:595-597)
+        ld_native<128>(part(a.psi, (size_t)b * nmodes + kidx), v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = cscale(cscale(v[i], facc[i * T + t]), a.loss_weight);
+      } else if (FWD && stage == F_SLICE && z == Z - 1) {   // the exit plane
+        // far field of this mode: Psi = FFT(exit) * mask; accumulate |Psi|^2
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-          const float2 P = cmul(spy[G::fky(c, t, i)], spx[G::fkx(c, t, i)]);
-          v[i] = ((mb >> i) & 1u) ? (adjoint ? cmulc(v[i], P) : cmul(v[i], P)) : make_float2(0.f, 0.f);
+          v[i] = cscale(v[i], a.mask[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
+          facc[i * T + t] += cabs2(v[i]);
         }
-      } else {
-        const float2* pr = edge ? a.prop_edge : a.prop;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const float2 P = pr[G::fky(c, t, i) * 256 + G::fkx(c, t, i)];
-          v[i] = adjoint ? cmulc(v[i], P) : cmul(v[i], P);
-        }
+        if (!a.simulate) st_native<128>(wpart(a.psi, (size_t)b * nmodes + kidx), v);
       }
-    } else if (epilogue) {
-      // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
-      double gy = 0.0, gx = 0.0;
-      if (a.probe_shift) {
-        const float2* pf = part(a.probe_f, p);
-        const int gi = a.seq[b];
-        const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int ky = G::fky(c, t, i), kx = G::fkx(c, t, i);
-          const float mk = a.mask[ky * 256 + kx];
-          const float th = __fadd_rn(__fmul_rn(__fmul_rn(a.sx[kx], mk), dx), __fmul_rn(__fmul_rn(a.sy[ky], mk), dy));
-          float sn, cs;
-          sincosf(th, &sn, &cs);
-          v[i] = cmulc(v[i], make_float2(cs * mk, sn * mk));
-          if (a.step_pos) {
-            const float im = cmulc(v[i], pf[nidx<128>(i, t)]).y;
-            gy += (double)(-(a.sy[ky] * mk) * im);
-            gx += (double)(-(a.sx[kx] * mk) * im);
-          }
-        }
-      }
-      if (a.step_probe) st_native<128>(wpart(a.fprobe, (size_t)b * Mp + p), v);
-      if (a.step_pos) {
-        block_sum2(gy, gx, s.red);
-        if (t == 0) {
-          xch[2] = gy;
-          xch[3] = gx;
-        }
-        cl.sync();
-        if (c == 0 && t == 0) {
-          double sy_ = 0.0, sx_ = 0.0;
-          for (int rr = 0; rr < 4; ++rr) {
-            const double* rx = cl.map_shared_rank(xch, rr);
-            sy_ += rx[2];
-            sx_ += rx[3];
-          }
-          a.pos_part[((size_t)b * Mp + p) * 2] = sy_;
-          a.pos_part[((size_t)b * Mp + p) * 2 + 1] = sx_;
-        }
-        cl.sync();
-      }
+      if (do_inv) WinFFT256::cross(v, s.xbuf, cl, c);
+    }
+    if (do_inv) {
+      WinFFT256::twiddle(v, s.tw256, c, true);
+      WinFFT<128>::inverse(v, s.xbuf, s.tw1, s.tw2);
     }
 
-    // ------------------------------------------------ inverse FFT
-    if (do_inv) WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
-
     // ------------------------------------------------ next step
-    if (stage == F_START) {
-      stage = F_SLICE;
-      z = 0;
-    } else if (stage == F_SLICE) {
-      if (z < Z - 1) {
+    if (FWD) {
+      if (stage == F_START) {
+        stage = F_SLICE;
+        z = 0;
+      } else if (z < Z - 1) {
         ++z;
       } else if (++k < nmodes) {
         stage = F_START;
@@ -526,6 +485,106 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
         stage = S_DONE;
       }
     }
+  }
+}
+
+
+// ------------------------------------------------------------------ shifted incoming probes
+// Real-space probe of every (position, probe mode): IFFT(FFT(P) * shift ramp * mask) / W^2
+// (objective.py:469-476); without a shift the probe comes back unchanged (FFT(P) / W^2).
+// Written to fprobe in native order for the forward stages; grid = Bn * Mp clusters of 4.
+__global__ void __launch_bounds__(512, 1) shifted_probes256_kernel(FusedArgs a) {
+  using G = Geo256;
+  constexpr size_t WW = 65536;
+  extern __shared__ __align__(16) unsigned char smem[];
+  Carve256 s(smem);
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank(), t = threadIdx.x;
+  const int win = blockIdx.x / 4, b = win / a.Mp, p = win % a.Mp;
+  load_twiddles<128>(s.tw1, s.tw2, a.tw);
+  load_tw256(s.tw256);
+  __syncthreads();
+  const float2* pf = a.probe_f + (size_t)p * WW + c * G::PART;
+  const float inv = 1.0f / (float)WW;
+  const int gi = a.seq[b];
+  const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    float2 w = make_float2(inv, 0.f);
+    if (a.probe_shift) {
+      const int ky = G::fky(c, t, i), kx = G::fkx(c, t, i);
+      const float mk = a.mask[ky * 256 + kx];
+      const float th = __fadd_rn(__fmul_rn(__fmul_rn(a.sx[kx], mk), dx), __fmul_rn(__fmul_rn(a.sy[ky], mk), dy));
+      float sn, cs;
+      sincosf(th, &sn, &cs);
+      w = make_float2(cs * mk * inv, sn * mk * inv);
+    }
+    v[i] = cmul(pf[nidx<128>(i, t)], w);
+  }
+  WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
+  st_native<128>(a.fprobe + (size_t)win * WW + c * G::PART, v);
+}
+
+// ------------------------------------------------------------------ probe-gradient spectrum
+// Spectrum of the probe-gradient wave of every (position, probe mode) that the adjoint left
+// in fprobe (real space, native order), in place, with the shift adjoint and the position
+// gradient (objective.py:641-656); grid = Bn * Mp clusters of 4.
+__global__ void __launch_bounds__(512, 1) probe_spectrum256_kernel(FusedArgs a) {
+  using G = Geo256;
+  constexpr size_t WW = 65536;
+  extern __shared__ __align__(16) unsigned char smem[];
+  Carve256 s(smem);
+  double* xch = s.red + 64;
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank(), t = threadIdx.x;
+  const int win = blockIdx.x / 4, b = win / a.Mp, p = win % a.Mp;
+  load_twiddles<128>(s.tw1, s.tw2, a.tw);
+  load_tw256(s.tw256);
+  float2* dst = a.fprobe + (size_t)win * WW + c * G::PART;
+  float2 v[32];
+  ld_native<128>(dst, v);
+  __syncthreads();
+  WinFFT256::forward(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
+  double gy = 0.0, gx = 0.0;
+  if (a.probe_shift) {
+    const float2* pf = a.probe_f + (size_t)p * WW + c * G::PART;
+    const int gi = a.seq[b];
+    const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int ky = G::fky(c, t, i), kx = G::fkx(c, t, i);
+      const float mk = a.mask[ky * 256 + kx];
+      const float th = __fadd_rn(__fmul_rn(__fmul_rn(a.sx[kx], mk), dx), __fmul_rn(__fmul_rn(a.sy[ky], mk), dy));
+      float sn, cs;
+      sincosf(th, &sn, &cs);
+      v[i] = cmulc(v[i], make_float2(cs * mk, sn * mk));
+      if (a.step_pos) {
+        const float im = cmulc(v[i], pf[nidx<128>(i, t)]).y;
+        gy += (double)(-(a.sy[ky] * mk) * im);
+        gx += (double)(-(a.sx[kx] * mk) * im);
+      }
+    }
+  }
+  if (a.step_probe) st_native<128>(dst, v);
+  if (a.step_pos) {
+    block_sum2(gy, gx, s.red);
+    if (t == 0) {
+      xch[2] = gy;
+      xch[3] = gx;
+    }
+    cl.sync();
+    if (c == 0 && t == 0) {
+      double sy_ = 0.0, sx_ = 0.0;
+      for (int rr = 0; rr < 4; ++rr) {
+        const double* rx = cl.map_shared_rank(xch, rr);
+        sy_ += rx[2];
+        sx_ += rx[3];
+      }
+      a.pos_part[(size_t)win * 2] = sy_;
+      a.pos_part[(size_t)win * 2 + 1] = sx_;
+    }
+    cl.sync();
   }
 }
 

@@ -10,7 +10,10 @@ int set_attrs256() {
   int rc;
   if ((rc = set_smem(probe_fft256_kernel, Smem256::small)) || (rc = set_smem(object_windows256_kernel, Smem256::small)) ||
       (rc = set_smem(grad_windows256_kernel, Smem256::small)) || (rc = set_smem(probe_final256_kernel, Smem256::small)) ||
-      (rc = set_smem(fused256_kernel, Smem256::fused)) || (rc = set_smem(fft2_batch256_kernel, Smem256::small)))
+      (rc = set_smem(fused256_kernel<1>, Smem256::fused)) ||
+      (rc = set_smem(fused256_kernel<2>, Smem256::fused)) ||
+      (rc = set_smem(probe_spectrum256_kernel, Smem256::small)) ||
+      (rc = set_smem(shifted_probes256_kernel, Smem256::small)) || (rc = set_smem(fft2_batch256_kernel, Smem256::small)))
     return rc;
   return PTY_OK;
 }
@@ -143,8 +146,22 @@ struct Path256 {
     fa.pos_part = at<double>(ws, q.o_pos_part) + 2 * (size_t)s0 * q.Mp;
     fa.sim_out = simulate ? patterns + (size_t)s0 * WW : nullptr;
     fa.err = at<int>(ws, q.o_err);
+    // phase 0 = forward + loss (phase 1) then the adjoint (phase 2), through dldi
+    int rc = PTY_OK;
+    if (phase != 2) {
+      prof_mark(st, KID_PROBE_SHIFT);
+      rc = launch4(shifted_probes256_kernel, (unsigned)(Bn * q.Mp), Smem256::small, st, fa);
+      prof_mark(st, KID_FUSED);
+      if (!rc) rc = launch4(fused256_kernel<1>, (unsigned)Bn, Smem256::fused, st, fa);
+    }
     prof_mark(st, KID_FUSED);
-    int rc = launch4(fused256_kernel, (unsigned)Bn, Smem256::fused, st, fa);
+    if (!rc && phase != 1 && !simulate) {
+      rc = launch4(fused256_kernel<2>, (unsigned)Bn, Smem256::fused, st, fa);
+      if (!rc && (fa.step_probe || fa.step_pos)) {
+        prof_mark(st, KID_PROBE_SPECTRUM);
+        rc = launch4(probe_spectrum256_kernel, (unsigned)(Bn * q.Mp), Smem256::small, st, fa);
+      }
+    }
     return rc ? rc : cuda_status();
   }
 

@@ -99,7 +99,7 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   const bool w256 = q.W == 256;
   q.o_gbuf = take(split && !w256 ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
   q.o_psi = take(w256 ? (size_t)q.Bb * q.Mp * q.Mo * WW * c8 : 0);
-  q.o_dldi = take(w256 && split ? (size_t)q.Bb * WW * f4 : 0);
+  q.o_dldi = take(w256 ? (size_t)q.Bb * WW * f4 : 0);
   q.o_pgr = take(w256 && q.Mo > 1 ? (size_t)q.Bb * q.Mp * WW * c8 : 0);
   q.o_seg = take(q.ckpt > 1 ? (size_t)q.Bb * q.ckpt * WW * c8 : 0);
   q.o_gpark = take(q.ckpt > 1 ? (size_t)q.Bb * WW * c8 : 0);
@@ -183,7 +183,7 @@ enum KernelId : int {
   KID_TWIDDLES = 0, KID_TABLES, KID_PROBE_FFT, KID_OBJ_TO_SLICES, KID_OBJECT_WINDOWS, KID_FUSED,
   KID_GRAD_WINDOWS, KID_TILE_LISTS, KID_SCATTER, KID_PROBE_PARTIAL, KID_SLICES_TO_OBJ, KID_PROBE_FINAL,
   KID_FINALIZE, KID_FFT2, KID_LAYOUT, KID_CLEAN_TABLES, KID_CLEAN_X, KID_CLEAN_Y, KID_CLEAN_XI,
-  KID_VEC, KID_SCALAR, KID_ACCEPT, KID_ORTHO, KID_DFT_TABLES, KID_DFT_GEMM, KID_ELEMENTWISE, KID_NN, KID_COUNT
+  KID_VEC, KID_SCALAR, KID_ACCEPT, KID_ORTHO, KID_DFT_TABLES, KID_DFT_GEMM, KID_ELEMENTWISE, KID_NN, KID_PROBE_SPECTRUM, KID_PROBE_SHIFT, KID_COUNT
 };
 
 // Records an event on `st` before a launch of kernel class `id` while profiling is on

@@ -382,6 +382,17 @@ __device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t& parity, int* 
   parity ^= 1u;
 }
 
+// Issue (one thread) an L2 prefetch of `bytes` at `src` (16-byte aligned, a multiple of 16
+// bytes) in chunks of at most 64 KiB; nothing waits on it.
+__device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
+  constexpr uint32_t kChunk = 64u * 1024u;
+  for (uint32_t o = 0; o < bytes; o += kChunk) {
+    const uint32_t n = bytes - o < kChunk ? bytes - o : kChunk;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(static_cast<const char*>(src) + o), "r"(n)
+                 : "memory");
+  }
+}
+
 // Issue (one thread) a copy of `bytes` from global `src` into shared `dst` in chunks of at
 // most 64 KiB, all completing on `bar`.
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

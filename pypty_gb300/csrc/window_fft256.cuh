@@ -6,7 +6,8 @@
 //   1. the register-resident 128 x 128 FFT of the block's component (WinFFT<128>),
 //   2. the twiddle w_256^(ky' cy + kx' cx),
 //   3. a radix-2 x 2 butterfly across the four blocks through distributed shared memory:
-//      X_q = sum_r (-1)^(qy ry + qx rx) T_r  (block q keeps quadrant q);
+//      X_q = sum_r (-1)^(qy ry + qx rx) T_r  (block q keeps quadrant q), one exchange in
+//      which every block publishes its values and pulls the three partners' values;
 // the inverse runs the same steps backwards with conjugate twiddles (unnormalised).
 // Each block's part of a window is stored in the 128 native order (window_fft.cuh) at
 // offset c * 128^2 of the window.
@@ -31,11 +32,6 @@ struct Geo256 {
   static __device__ __forceinline__ int fkx(int c, int t, int i) { return G::fkx(t, i) + H * (c & 1); }
 };
 
-// sign (-1)^(qy*ry + qx*rx) of the cross-block butterfly
-__device__ __forceinline__ float quad_sign(int q, int r) {
-  return (((q >> 1) & (r >> 1)) ^ ((q & 1) & (r & 1))) ? -1.0f : 1.0f;
-}
-
 // tw256[k] = exp(-2 pi i k / 256) into shared memory (256 entries)
 __device__ __forceinline__ void load_tw256(float2* tw256) {
   for (int k = threadIdx.x; k < 256; k += blockDim.x) {
@@ -45,62 +41,144 @@ __device__ __forceinline__ void load_tw256(float2* tw256) {
   }
 }
 
+// shared::cluster address of `p` (this block's shared memory) in block `rank` of the cluster
+__device__ __forceinline__ uint32_t cluster_map(const void* p, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ float4 ld_cluster_f4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+
 struct WinFFT256 {
   using G = Geo<128>;
   static constexpr int T = G::T;
 
-  // Radix-2 x 2 butterfly across the four blocks, block `me` keeping output quadrant `me`:
-  //   out_me = sum_r (-1)^(me_y r_y + me_x r_x) in_r.
-  // It is separable: a stage with the x partner (me ^ 1) then a stage with the y partner
-  // (me ^ 2). In each stage every block stores its values into the partner's exchange
-  // buffer (remote shared-memory stores, which do not wait), the cluster synchronises, and
-  // the block combines its own values with the partner's from its local buffer:
-  //   bit of me clear: out = own + partner,  bit set: out = partner - own.
-  static __device__ __forceinline__ void cross_stage(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl,
-                                                     int me, int bit) {
+  // Every block stores its 32 values (element pairs as 16-byte words, native order) into its
+  // own exchange buffer; after the cluster barrier the partners pull them with
+  // ld.shared::cluster. The caller ends the exchange with end_exchange.
+  static __device__ __forceinline__ void publish(const float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl) {
     const int t = threadIdx.x;
-    cl.sync();   // the partner has finished with its exchange buffer
-    float2* dst = cl.map_shared_rank(xbuf, me ^ bit);
+    __syncthreads();   // this block's own transform has finished reading xbuf
+    float4* p = reinterpret_cast<float4*>(xbuf);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) dst[nidx<128>(i, t)] = v[i];
-    cl.sync();   // the partner's values have arrived
-    const bool upper = (me & bit) != 0;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const float2 o = xbuf[nidx<128>(i, t)];
-      v[i] = upper ? csub(o, v[i]) : cadd(v[i], o);
-    }
+    for (int j = 0; j < 16; ++j) p[j * T + t] = make_float4(v[2 * j].x, v[2 * j].y, v[2 * j + 1].x, v[2 * j + 1].y);
+    cl.sync();   // every block's values are published
+  }
+  static __device__ __forceinline__ void end_exchange(cg256::cluster_group& cl) {
+    cl.sync();   // every partner has read this block's buffer before it is reused
   }
 
+  // Radix-2 x 2 butterfly across the four blocks, block `me` keeping output quadrant `me`:
+  //   out_me = sum_r (-1)^(me_y r_y + me_x r_x) in_r.
+  // With R_d = in_(me ^ d) (R_0 the block's own value) and s_x, s_y = -1 where bit x / y of
+  // `me` is set: out_me = R_3 + s_x R_2 + s_y R_1 + s_x s_y R_0. One exchange: the block
+  // publishes its values and pulls those of the three partners.
   static __device__ __forceinline__ void cross(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl, int me) {
-    cross_stage(v, xbuf, cl, me, 1);
-    cross_stage(v, xbuf, cl, me, 2);
-    cl.sync();   // every block is done with the exchange buffers
+    const int t = threadIdx.x;
+    publish(v, xbuf, cl);
+    const uint32_t a1 = cluster_map(xbuf, me ^ 1), a2 = cluster_map(xbuf, me ^ 2), a3 = cluster_map(xbuf, me ^ 3);
+    const float sx = (me & 1) ? -1.0f : 1.0f, sy = (me & 2) ? -1.0f : 1.0f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const uint32_t off = (uint32_t)(j * T + t) * 16u;
+      const float4 q1 = ld_cluster_f4(a1 + off), q2 = ld_cluster_f4(a2 + off), q3 = ld_cluster_f4(a3 + off);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float2 r0 = v[2 * j + h];
+        const float2 r1 = h ? make_float2(q1.z, q1.w) : make_float2(q1.x, q1.y);
+        const float2 r2 = h ? make_float2(q2.z, q2.w) : make_float2(q2.x, q2.y);
+        const float2 r3 = h ? make_float2(q3.z, q3.w) : make_float2(q3.x, q3.y);
+        // (R_3 + s_x R_2) + s_y (R_1 + s_x R_0)
+        const float2 u = make_float2(fmaf(sx, r2.x, r3.x), fmaf(sx, r2.y, r3.y));
+        const float2 w = make_float2(fmaf(sx, r0.x, r1.x), fmaf(sx, r0.y, r1.y));
+        v[2 * j + h] = make_float2(fmaf(sy, w.x, u.x), fmaf(sy, w.y, u.y));
+      }
+    }
+    end_exchange(cl);
+  }
+
+  static __device__ __forceinline__ void twiddle(float2 (&v)[32], const float2* tw256, int c, bool conj) {
+    if (c == 0) return;
+    const int t = threadIdx.x;
+    const int cy = c >> 1, cx = c & 1;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const float2 w = tw256[G::fky(t, i) * cy + G::fkx(t, i) * cx];
+      v[i] = conj ? cmulc(v[i], w) : cmul(v[i], w);
+    }
   }
 
   static __device__ __forceinline__ void forward(float2 (&v)[32], float2* xbuf, const float2* tw1, const float2* tw2,
                                                  const float2* tw256, cg256::cluster_group& cl) {
     const int c = (int)cl.block_rank();
-    const int t = threadIdx.x;
     WinFFT<128>::forward(v, xbuf, tw1, tw2);
-    if (c != 0) {
-      const int cy = c >> 1, cx = c & 1;
-#pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], tw256[G::fky(t, i) * cy + G::fkx(t, i) * cx]);
-    }
+    twiddle(v, tw256, c, false);
     cross(v, xbuf, cl, c);
   }
 
   static __device__ __forceinline__ void inverse(float2 (&v)[32], float2* xbuf, const float2* tw1, const float2* tw2,
                                                  const float2* tw256, cg256::cluster_group& cl) {
     const int c = (int)cl.block_rank();
-    const int t = threadIdx.x;
     cross(v, xbuf, cl, c);
-    if (c != 0) {
-      const int cy = c >> 1, cx = c & 1;
+    twiddle(v, tw256, c, true);
+    WinFFT<128>::inverse(v, xbuf, tw1, tw2);
+  }
+
+  // The middle of one propagation step x -> IFFT(FFT(x) * P) (conj(P) if `adjoint`): the
+  // forward cross butterfly, the multiply and the inverse cross butterfly folded into one
+  // exchange, between the twiddled forward sub-transform and the conjugate twiddle of the
+  // inverse. With T_r the twiddled sub-transform of block r and R_d = T_(me ^ d):
+  //   X_q = sum_r s(q, r) T_r = s(q, me) Z_q,  Z_q = sum_d s(q, d) R_d,
+  //   U_me = sum_q s(me, q) P_q X_q = sum_q P_q Z_q        (s(me, q) s(q, me) = 1),
+  // where P_q is the propagator at frequency (ky + 128 q_y, kx + 128 q_x) of this thread's
+  // element; pq(i, q) returns it (zero outside the band).
+  template <typename PQ>
+  static __device__ __forceinline__ void cross_propagate(float2 (&v)[32], float2* xbuf, cg256::cluster_group& cl,
+                                                         int me, bool adjoint, PQ&& pq) {
+    const int t = threadIdx.x;
+    publish(v, xbuf, cl);
+    const uint32_t a1 = cluster_map(xbuf, me ^ 1), a2 = cluster_map(xbuf, me ^ 2), a3 = cluster_map(xbuf, me ^ 3);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], tw256[G::fky(t, i) * cy + G::fkx(t, i) * cx]);
+    for (int j = 0; j < 16; ++j) {
+      const uint32_t off = (uint32_t)(j * T + t) * 16u;
+      const float4 q1 = ld_cluster_f4(a1 + off), q2 = ld_cluster_f4(a2 + off), q3 = ld_cluster_f4(a3 + off);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = 2 * j + h;
+        const float2 r0 = v[i];
+        const float2 r1 = h ? make_float2(q1.z, q1.w) : make_float2(q1.x, q1.y);
+        const float2 r2 = h ? make_float2(q2.z, q2.w) : make_float2(q2.x, q2.y);
+        const float2 r3 = h ? make_float2(q3.z, q3.w) : make_float2(q3.x, q3.y);
+        const float2 e0 = cadd(r0, r1), e1 = csub(r0, r1), e2 = cadd(r2, r3), e3 = csub(r2, r3);
+        const float2 z0 = cadd(e0, e2), z1 = cadd(e1, e3), z2 = csub(e0, e2), z3 = csub(e1, e3);
+        const float2 p0 = pq(i, 0), p1 = pq(i, 1), p2 = pq(i, 2), p3 = pq(i, 3);
+        v[i] = adjoint ? cadd(cadd(cmulc(z0, p0), cmulc(z1, p1)), cadd(cmulc(z2, p2), cmulc(z3, p3)))
+                       : cadd(cadd(cmul(z0, p0), cmul(z1, p1)), cadd(cmul(z2, p2), cmul(z3, p3)));
+      }
     }
+    end_exchange(cl);
+  }
+
+  // x -> IFFT(FFT(x) * m) for a real multiplier m (256 x 256, unshifted frequency order)
+  static __device__ __forceinline__ void band_limit(float2 (&v)[32], float2* xbuf, const float2* tw1,
+                                                    const float2* tw2, const float2* tw256, cg256::cluster_group& cl,
+                                                    const float* __restrict__ m) {
+    const int c = (int)cl.block_rank();
+    const int t = threadIdx.x;
+    WinFFT<128>::forward(v, xbuf, tw1, tw2);
+    twiddle(v, tw256, c, false);
+    cross_propagate(v, xbuf, cl, c, false, [&](int i, int q) {
+      return make_float2(m[(G::fky(t, i) + 128 * (q >> 1)) * 256 + G::fkx(t, i) + 128 * (q & 1)], 0.0f);
+    });
+    twiddle(v, tw256, c, true);
     WinFFT<128>::inverse(v, xbuf, tw1, tw2);
   }
 };
