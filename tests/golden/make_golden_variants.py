@@ -1,0 +1,176 @@
+"""Golden vectors for the near-field, compressed-detector, beam-current, aberration and
+inside-tilt branches, produced by running the reference's own NumPy path.
+
+Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
+/root/reference)::
+
+    python tests/golden/make_golden_variants.py
+
+Every case builds seeded inputs (``pypty_gb300.synth``), simulates measurements with the
+variants oracle at the true specimen (patterns plus Poisson noise, or detector coefficients
+plus Gaussian noise for the compressed losses), evaluates the reference's
+``pypty.objective.loss_and_direction`` (``pypty/objective.py:47``) at a perturbed
+object/probe and writes inputs and outputs to ``tests/golden/variant_<case>.npz``.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from refimport import import_reference  # noqa: E402
+from pypty_gb300 import synth  # noqa: E402
+from oracle import variants_oracle as vor  # noqa: E402
+
+
+def ref_call(pypty, c):
+    """The reference with every argument spelled out (signature objective.py:47)."""
+    f, cx = (np.float64, np.complex128) if c["double"] else (np.float32, np.complex64)
+    tilts = np.zeros((1, 6), dtype=f)
+    tilts[0, 2], tilts[0, 3] = c["tan_y"], c["tan_x"]
+    masks = None if c["masks"] is None else c["masks"].astype(f)
+    bc = None if c["beam_current"] is None else c["beam_current"].astype(f)
+    ab = None if c["aberrations"] is None else c["aberrations"].astype(f)
+    res = pypty.objective.loss_and_direction(
+        this_obj=c["obj"].astype(cx), full_probe=c["probe"].astype(cx),
+        this_pos_array=c["positions"].copy(), this_pos_correction=c["pos_correction"].astype(f),
+        this_tilt_array=tilts, this_tilts_correction=np.zeros_like(tilts),
+        this_distances=np.array([c["distance"]], dtype=f), edge_slice_thickness_multiplier=c["edge_mult"],
+        measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
+        this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
+        this_step_tilts=0, masks=masks, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+        recon_type=c["recon_type"], Cs=f(c["cs"]), defocus_array=np.array([c["defocus"]], dtype=f),
+        alpha_near_field=f(c["alpha"]), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
+        propmethod="multislice", this_chopped_sequence=c["sequence"], load_one_by_one=False,
+        data_multiplier=f(1), data_pad=0, phase_plate_in_h5=None, this_loss_weight=c["loss_weight"], data_bin=1,
+        data_shift_vector=[0, 0], upsample_pattern=1, static_background=None, this_step_static_background=0,
+        tilt_mode=0, aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
+        compute_batch=c["batch"], phase_only_obj=False, beam_current=bc,
+        this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], default_float=f,
+        default_complex=cx, xp=np, is_first_epoch=True, scan_size=None, scan_step_A=1,
+        fast_axis_reg_weight_positions=0, slow_axis_reg_weight_positions=0, slow_axis_reg_weight_tilts=0,
+        current_deformation_reg_weight_positions=0, current_deformation_reg_weight_tilts=0,
+        fast_axis_reg_weight_tilts=0, aperture_mask=None, probe_reg_weight=0, current_window_weight=0,
+        current_window=None, phase_norm_weight=0, abs_norm_weight=0, atv_weight=0, atv_q=1, atv_p=2,
+        mixed_variance_weight=0, mixed_variance_sigma=0.5, wedge_mu=0, beta_wedge=0, probe_mod_reg_weight=0,
+        probe_mod_tol=0.05, smart_memory=False, print_flag=0, data_simulation_flag=False,
+        data_simulation_exitwave=False, use_padded_intensity=True)
+    # outer return order (objective.py:967): aberrations gradient before beam-current gradient
+    return res[0], res[1], res[2], res[3], res[4], res[8], res[7]
+
+
+def detector_masks(W, n, rng):
+    """Segmented annular virtual detectors in detector (fftshifted) order, float32."""
+    y, x = np.mgrid[:W, :W] - W // 2
+    r = np.hypot(y, x)
+    th = np.arctan2(y, x)
+    out = []
+    for i in range(n):
+        r0, r1 = (i // 2) * W / (2 * n) * 1.5, (i // 2 + 1) * W / (2 * n) * 1.5 + 2
+        half = (th >= 0) if i % 2 == 0 else (th < 0)
+        out.append(((r >= r0) & (r < r1) & half).astype(np.float32) * rng.uniform(0.5, 1.0))
+    return np.array(out, dtype=np.float32)
+
+
+def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorithm, batch, px=0.2, kV=200.0,
+               alpha=25.0, probe_defocus=80.0, distance=2.0, edge_mult=1.0, cutoff=2 / 3, rolloff=0.0,
+               loss_weight=1.0, step_probe=1, step_obj=1, step_pos=0, dose=1e4, double=False, recon_type="far_field",
+               defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
+               n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False):
+    rng = np.random.default_rng(seed)
+    cx, f = np.complex64, np.float32
+    truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
+    probe_true = synth.make_probe(W, px, kV, alpha, probe_defocus, Mp, [0.6, 0.3, 0.1][:Mp], dose, dtype=cx)
+    pos = synth.raster_positions(n_scan, n_scan, step_px, jitter_px, rng)
+    if integer_positions:
+        pos = np.round(pos)
+    ipos, corr = synth.split_positions(pos, int_dtype=np.int32, float_dtype=f)
+    assert ipos.max() + W <= min(ny, nx), "object too small for the scan"
+    lam = synth.wavelength_A(kV)
+    N = ipos.shape[0]
+    masks = detector_masks(W, n_masks, rng) if n_masks else None
+    bc = (1.0 + 0.1 * rng.normal(size=N)).astype(f) if beam_current else None
+    ab = (rng.normal(size=(n_ab_sets, n_abs)) * 20.0).astype(f) if n_ab_sets else None
+    marker = (np.arange(N) % n_ab_sets).astype(np.int64) if n_ab_sets else None
+    kw = dict(recon_type=recon_type, defocus=defocus, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
+              masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker)
+    sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, distance, edge_mult, None, algorithm, lam,
+                                          1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
+    if n_masks:
+        measured = (sim * (1.0 + 0.02 * rng.normal(size=sim.shape))).astype(f)
+    else:
+        measured = synth.poisson_patterns(sim, 1.0, rng).astype(f)
+    obj0 = np.exp(0.5j * np.angle(truth)).astype(cx)
+    probe0 = synth.make_probe(W, px, kV, alpha, probe_defocus + 15.0, Mp, [0.5, 0.3, 0.2][:Mp], dose, dtype=cx)
+    if double:
+        measured, corr = measured.astype(np.float64), corr.astype(np.float64)
+        obj0, probe0 = obj0.astype(np.complex128), probe0.astype(np.complex128)
+    return dict(name=name, double=double, positions=ipos, pos_correction=corr, distance=distance,
+                edge_mult=edge_mult, measured=measured, algorithm=algorithm, wavelength=lam, step_probe=step_probe,
+                step_obj=step_obj, step_pos=step_pos, px=px, cutoff=cutoff, rolloff=rolloff,
+                sequence=np.arange(N), loss_weight=loss_weight, batch=batch, obj=obj0, probe=probe0,
+                recon_type=recon_type, defocus=defocus, cs=cs, alpha=alpha_nf, tan_x=tan_x, tan_y=tan_y, masks=masks,
+                beam_current=bc, step_bc=step_bc, aberrations=ab, aberration_marker=marker, step_ab=step_ab)
+
+
+BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
+            alpha=30.0, probe_defocus=40.0, dose=1e5)
+CASES = [
+    # near field: CTF with defocus, Cs and an inside tilt; position gradient
+    dict(BASE, name="near_c64", seed=31, algorithm="lsq_sqrt", recon_type="near_field", defocus=60.0, cs=2e5,
+         tan_x=2e-3, tan_y=-1e-3, step_pos=1),
+    dict(BASE, name="near_c128", seed=31, algorithm="lsq_sqrt", recon_type="near_field", defocus=60.0, cs=2e5,
+         tan_x=2e-3, tan_y=-1e-3, step_pos=1, double=True),
+    # near field, Poisson loss, integer positions, thick first slice
+    dict(BASE, name="near_ml_c64", seed=32, algorithm="ml", recon_type="near_field", defocus=80.0, Z=3,
+         edge_mult=1.4, integer_positions=True),
+    # compressed detectors (far field, inside tilt)
+    dict(BASE, name="lsq_compressed_c64", seed=33, algorithm="lsq_compressed", n_masks=6, tan_x=1e-3, step_pos=1),
+    dict(BASE, name="gauss_compressed_c64", seed=34, algorithm="gauss_compressed", n_masks=6),
+    dict(BASE, name="poisson_compressed_c64", seed=35, algorithm="poisson_compressed", n_masks=6, loss_weight=0.5),
+    # beam current and aberration plates, integer positions (the plates act in the forward model)
+    dict(BASE, name="current_aberr_c64", seed=36, algorithm="ml", beam_current=True, step_bc=1, n_ab_sets=3,
+         n_abs=7, step_ab=1, integer_positions=True),
+    dict(BASE, name="current_aberr_c128", seed=36, algorithm="ml", beam_current=True, step_bc=1, n_ab_sets=3,
+         n_abs=7, step_ab=1, integer_positions=True, double=True),
+    # the same with sub-pixel shifts: the shift spectrum excludes the plates (objective.py:461, 471)
+    dict(BASE, name="current_aberr_shift_c64", seed=37, algorithm="lsq_sqrt", beam_current=True, step_bc=1,
+         n_ab_sets=2, n_abs=4, step_ab=1, step_pos=1),
+]
+
+
+def main():
+    pypty = import_reference()
+    for spec in CASES:
+        spec = dict(spec)
+        name = spec.pop("name")
+        c = build_case(name, **spec)
+        loss, sse, og, pg, posg, bcg, abg = ref_call(pypty, c)
+        out = os.path.join(HERE, "variant_" + name + ".npz")
+        none = np.zeros(0, np.float32)
+        np.savez_compressed(
+            out, obj=c["obj"], probe=c["probe"], positions=c["positions"], pos_correction=c["pos_correction"],
+            measured=c["measured"], sequence=c["sequence"],
+            scalars=np.array([c["distance"], c["edge_mult"], c["wavelength"], c["px"], c["cutoff"], c["rolloff"],
+                              c["loss_weight"], c["batch"], c["step_probe"], c["step_obj"], c["step_pos"],
+                              c["defocus"], c["cs"], c["alpha"], c["tan_x"], c["tan_y"], c["step_bc"], c["step_ab"]],
+                             dtype=np.float64),
+            algorithm=np.array(c["algorithm"]), recon_type=np.array(c["recon_type"]), double=np.array(c["double"]),
+            masks=none if c["masks"] is None else c["masks"],
+            beam_current=none if c["beam_current"] is None else c["beam_current"],
+            aberrations=none if c["aberrations"] is None else c["aberrations"],
+            aberration_marker=np.zeros(0, np.int64) if c["aberration_marker"] is None else c["aberration_marker"],
+            ref_loss=np.array(loss, dtype=np.float64), ref_sse=np.array(sse, dtype=np.float64),
+            ref_object_grad=og, ref_probe_grad=np.asarray(pg), ref_pos_grad=posg,
+            ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg))
+        print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
+            name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
+            np.linalg.norm(np.asarray(abg)), os.path.basename(out)))
+
+
+if __name__ == "__main__":
+    main()

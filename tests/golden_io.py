@@ -11,7 +11,7 @@ def loss_case_names():
     names = []
     for p in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
         n = os.path.basename(p)[:-4]
-        if not n.startswith(("core_", "fourier_clean", "lbfgs_")):
+        if not n.startswith(("core_", "fourier_clean", "lbfgs_", "variant_")):
             names.append(n)
     return names
 
@@ -31,3 +31,28 @@ def rel_l2(a, b):
     a = np.asarray(a, dtype=np.complex128)
     b = np.asarray(b, dtype=np.complex128)
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def variant_case_names():
+    return [os.path.basename(p)[len("variant_"):-4]
+            for p in sorted(glob.glob(os.path.join(GOLDEN_DIR, "variant_*.npz")))]
+
+
+def load_variant_case(name):
+    """A near-field / compressed / beam-current / aberration fixture
+    (``tests/golden/make_golden_variants.py``)."""
+    d = dict(np.load(os.path.join(GOLDEN_DIR, "variant_" + name + ".npz")))
+    s = d["scalars"]
+    keys = ["distance", "edge_mult", "wavelength", "px", "cutoff", "rolloff", "loss_weight", "batch", "step_probe",
+            "step_obj", "step_pos", "defocus", "cs", "alpha", "tan_x", "tan_y", "step_bc", "step_ab"]
+    for i, k in enumerate(keys):
+        d[k] = float(s[i])
+    for k in ("batch", "step_probe", "step_obj", "step_pos", "step_bc", "step_ab"):
+        d[k] = int(d[k])
+    d["algorithm"] = str(d["algorithm"])
+    d["recon_type"] = str(d["recon_type"])
+    d["double"] = bool(d["double"])
+    for k in ("masks", "beam_current", "aberrations", "aberration_marker"):
+        if d[k].size == 0:
+            d[k] = None
+    return d
