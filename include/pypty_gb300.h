@@ -41,6 +41,11 @@ extern "C" {
 #define PTY_ML 1         /* "ml"         Poisson negative log-likelihood */
 #define PTY_LSQ 2        /* "lsq"        intensity L2 */
 #define PTY_LSQ_SQRT_2 3 /* "lsq_sqrt_2" */
+/* compressed-detector losses on detector coefficients (pypty/objective.py:560-585); only
+   pty_loss_and_direction_variants accepts them */
+#define PTY_LSQ_COMPRESSED 4     /* "lsq_compressed" */
+#define PTY_GAUSS_COMPRESSED 5   /* "gauss_compressed" */
+#define PTY_POISSON_COMPRESSED 6 /* "poisson_compressed" */
 
 typedef struct pty_problem {
   int32_t window;         /* W, probe window size in px: 64 or 128 */
@@ -217,6 +222,52 @@ int pty_loss_and_direction_layered(const pty_problem_t* problem, int32_t engine,
                                    const float* measured, double* loss_sse, void* object_grad,
                                    void* probe_grad, float* pos_grad, void* workspace,
                                    size_t workspace_bytes, void* stream);
+
+/*
+ * The other propagation, loss and probe branches of pypty.objective.loss_and_direction
+ * (pypty/objective.py:283-742), computed like pty_loss_and_direction_layered on the FP32
+ * FFT engine (pypty/objective.py line numbers below):
+ *   near-field propagation (recon_type "near_field", one defocus, Cs: 504-508, 598-604);
+ *   compressed-detector losses (algorithm PTY_*_COMPRESSED on n_masks detector masks,
+ *     560-585; measured is then (n_positions, n_masks));
+ *   beam-current fluctuations and their gradient (448-452, 687-697);
+ *   per-position aberration phase plates and their gradient (324-329, 459-463, 676-684);
+ *   one inside beam tilt, tilt_mode 0 (337-345, 505).
+ * The variant fields that are off (recon_type 0, n_masks 0, NULL arrays) leave the far-field
+ * path of pty_loss_and_direction_layered. Replaces the same loss_and_direction call
+ * (pypty/objective.py:47) with those arguments set. Device arrays: masks (n_masks, W, W) in
+ * pattern order (fftshifted detector order for the far field, real-space order for the
+ * near field), beam_current / beam_current_grad (n_positions), aberrations /
+ * aberrations_grad (n_aberration_sets, n_aberrations), aberration_marker (n_positions); a
+ * marker outside [0, n_aberration_sets) leaves its position without a plate.
+ * The near-field partial-coherence correction (alpha_near_field > 0) has no counterpart:
+ * the reference raises on it.
+ */
+typedef struct pty_variant {
+  int32_t recon_type;          /* 0: far field, 1: near field */
+  float defocus;               /* near field: defocus_array[0], Angstrom */
+  float cs;                    /* near field: spherical aberration Cs, Angstrom */
+  float tan_x, tan_y;          /* inside tilt (tilts[0, 3], tilts[0, 2]) */
+  int32_t n_masks;             /* compressed losses: number of detector masks */
+  const float* masks;
+  const float* beam_current;   /* NULL: no beam-current fluctuations */
+  int32_t step_beam_current;
+  float* beam_current_grad;
+  int32_t n_aberrations;       /* coefficients per aberration set (Krivanek order) */
+  int32_t n_aberration_sets;
+  const float* aberrations;    /* NULL: no aberration plates */
+  const int32_t* aberration_marker;
+  int32_t step_aberrations;
+  float* aberrations_grad;
+} pty_variant_t;
+
+int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);
+int pty_loss_and_direction_variants(const pty_problem_t* problem, const pty_variant_t* variant,
+                                    const void* obj, const void* probe, const int32_t* positions_host,
+                                    const float* pos_correction, const int32_t* sequence_host,
+                                    const float* measured, double* loss_sse, void* object_grad,
+                                    void* probe_grad, float* pos_grad, void* workspace,
+                                    size_t workspace_bytes, void* stream);
 
 /*
  * pty_fft2 without a workspace argument; it allocates nothing. No counterpart in the

@@ -18,6 +18,9 @@ PTY_ERR_WORKSPACE = -4
 PTY_ERR_CUDA = -5
 
 ALGORITHMS = {"lsq_sqrt": 0, "ml": 1, "lsq": 2, "lsq_sqrt_2": 3}
+# compressed-detector losses: pty_loss_and_direction_variants only
+COMPRESSED_ALGORITHMS = {"lsq_compressed": 4, "gauss_compressed": 5, "poisson_compressed": 6}
+RECON_TYPES = {"far_field": 0, "near_field": 1}
 DFT_ENGINES = {"fp32_fft": 0, "bf16x3": 1, "bf16x6": 2}
 
 
@@ -44,6 +47,18 @@ class VSpace(ctypes.Structure):
                 ("n", ctypes.c_int64 * 3), ("weight", ctypes.c_double * 3)]
 
 
+class Variant(ctypes.Structure):
+    """Mirror of ``pty_variant_t``: near field, compressed detectors, beam current, aberration
+    plates and the inside tilt of ``pty_loss_and_direction_variants``."""
+    _fields_ = [("recon_type", ctypes.c_int32), ("defocus", ctypes.c_float), ("cs", ctypes.c_float),
+                ("tan_x", ctypes.c_float), ("tan_y", ctypes.c_float), ("n_masks", ctypes.c_int32),
+                ("masks", ctypes.c_void_p), ("beam_current", ctypes.c_void_p),
+                ("step_beam_current", ctypes.c_int32), ("beam_current_grad", ctypes.c_void_p),
+                ("n_aberrations", ctypes.c_int32), ("n_aberration_sets", ctypes.c_int32),
+                ("aberrations", ctypes.c_void_p), ("aberration_marker", ctypes.c_void_p),
+                ("step_aberrations", ctypes.c_int32), ("aberrations_grad", ctypes.c_void_p)]
+
+
 class PtyError(RuntimeError):
     """A PTY_ERR_* status returned by the library."""
 
@@ -61,6 +76,7 @@ _F32P = ctypes.POINTER(ctypes.c_float)
 _F64P = ctypes.POINTER(ctypes.c_double)
 _PP = ctypes.POINTER(Problem)
 _VS = ctypes.POINTER(VSpace)
+_VARP = ctypes.POINTER(Variant)
 _PPV = ctypes.POINTER(ctypes.c_void_p)
 _F64 = ctypes.c_double
 _F32 = ctypes.c_float
@@ -98,6 +114,8 @@ SIGNATURES = {
     "pty_fft2_bf16x6": ([_VP, _VP, _I32, _I32, _I32, _VP, _SZ, _VP], ctypes.c_int),
     "pty_layered_workspace_bytes": ([_PP, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_loss_and_direction_layered": ([_PP, _I32] + [_VP] * 11 + [_SZ, _VP], ctypes.c_int),
+    "pty_variants_workspace_bytes": ([_PP, _VARP, ctypes.POINTER(_SZ)], ctypes.c_int),
+    "pty_loss_and_direction_variants": ([_PP, _VARP] + [_VP] * 11 + [_SZ, _VP], ctypes.c_int),
     "pty_nn_conv3x3": ([_VP, _VP, _VP, _VP] + [_I32] * 7 + [_VP], ctypes.c_int),
     "pty_nn_conv3x3_wgrad_workspace_floats": ([_I32] * 5 + [ctypes.POINTER(_I64)], ctypes.c_int),
     "pty_nn_conv3x3_wgrad": ([_VP] * 4 + [_I32] * 5 + [_VP, _VP], ctypes.c_int),

@@ -209,15 +209,375 @@ __global__ void planes_to_probe_kernel(const float2* __restrict__ planes, float2
   ref[(size_t)u * Mp + p] = planes[(size_t)p * WW + u];
 }
 
+// ------------------------------------------------------------------ variants
+// Tables of pty_loss_and_direction_variants (after tables_kernel wrote the mask):
+// propagator with the inside tilt (pypty/objective.py:343) and its edge power, the
+// near-field CTF (objective.py:505) and the aberration basis imag(poly_j) = -A_j
+// (pypty/utils.py:1333-1368 get_ctf_matrix, objective.py:326-327).
+struct VarTableArgs {
+  float2* prop;
+  float2* prop_edge;
+  float2* ctf;
+  float* abasis;          // [n_abs][WW]
+  const float* mask;
+  const int* abn;         // [n_abs] Krivanek n
+  const int* abm;         // [n_abs] Krivanek m
+  const int* abk;         // [n_abs] 0: m = 0, 1: cos (a), 2: sin (b)
+  int W, use_edge, near, n_abs;
+  float px, py, distance, wavelength, edge_mult, tan_x, tan_y, defocus, cs;
+};
+
+__global__ void var_tables_kernel(VarTableArgs a) {
+  const int W = a.W, WW = W * W;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= WW) return;
+  const int ky = u / W, kx = u % W;
+  const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
+  const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
+  const float mk = a.mask[u];
+  // lambda q2 + 2 (qx tan_x + qy tan_y), float32 in the reference's order
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, a.tan_x), __fmul_rn(qy, a.tan_y)));
+  const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
+  const float inv = 1.0f / (float)WW;
+  {
+    const float phase = __fmul_rn(__fmul_rn(-3.141592654f, a.distance), x);
+    float s, c;
+    sincosf(phase, &s, &c);
+    const float2 p = make_float2(c * mk, s * mk);
+    a.prop[u] = make_float2(p.x * inv, p.y * inv);
+    if (a.use_edge) {
+      const float r = sqrtf(p.x * p.x + p.y * p.y);
+      float2 pe = make_float2(0.f, 0.f);
+      if (r > 0.f) {
+        const float ang = atan2f(p.y, p.x) * a.edge_mult;
+        const float re = powf(r, a.edge_mult);
+        float se, ce;
+        sincosf(ang, &se, &ce);
+        pe = make_float2(re * ce, re * se);
+      }
+      a.prop_edge[u] = make_float2(pe.x * inv, pe.y * inv);
+    }
+  }
+  if (a.near) {
+    // exp(-i pi (x defocus + 0.5 Cs lambda^3 q2^2)) * mask
+    const float l3 = __fmul_rn(__fmul_rn(a.wavelength, a.wavelength), a.wavelength);
+    const float sph = __fmul_rn(__fmul_rn(__fmul_rn(0.5f, a.cs), l3), __fmul_rn(q2, q2));
+    const float phase = __fmul_rn(-3.141592654f, __fadd_rn(__fmul_rn(x, a.defocus), sph));
+    float s, c;
+    sincosf(phase, &s, &c);
+    a.ctf[u] = make_float2(c * mk, s * mk);
+  }
+  if (a.n_abs > 0) {
+    // k = lambda q (float32); k_r ** (n + 1) / (n + 1) and cos / sin (m phi) in float64 (the
+    // reference's int64 orders promote), scaled by float32(2 pi / lambda)
+    const float kxv = __fmul_rn(a.wavelength, qx), kyv = __fmul_rn(a.wavelength, qy);
+    const double kr = (double)sqrtf(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)));
+    const double phi = (double)atan2f(kyv, kxv);
+    const double sc = (double)__fdiv_rn(6.2831855f, a.wavelength);
+    for (int j = 0; j < a.n_abs; ++j) {
+      const int n = a.abn[j], m = a.abm[j];
+      double term = pow(kr, (double)(n + 1)) / (double)(n + 1);
+      if (a.abk[j] == 1) term *= cos((double)m * phi);
+      else if (a.abk[j] == 2) term *= sin((double)m * phi);
+      a.abasis[(size_t)j * WW + u] = -(float)(term * sc);
+    }
+  }
+}
+
+// aberration plate of position b at pixel u: exp(i sum_j imag(poly_j) c_j) * mask
+// (objective.py:328; the sum runs over j in order in float32)
+__device__ __forceinline__ float2 plate_at(const float* __restrict__ abasis, const float* __restrict__ coef, int n_abs,
+                                           int WW, int u, float mk) {
+  float th = 0.0f;
+  for (int j = 0; j < n_abs; ++j) th = __fadd_rn(th, __fmul_rn(abasis[(size_t)j * WW + u], coef[j]));
+  float s, c;
+  sincosf(th, &s, &c);
+  return make_float2(c * mk, s * mk);
+}
+
+struct VarProbeArgs {
+  const float2* pf;          // [Mp][WW] probe spectra
+  const float2* planes;      // [Mp][WW] probe planes
+  const float *sx, *sy, *mask, *corr;
+  const int* seq;
+  const float* bc;           // beam current [N] or null
+  const float* abasis;       // [n_abs][WW]
+  const float* coefs;        // aberrations [sets][n_abs] or null
+  const int* marker;         // [N]
+  int W, Mp, shift, n_abs, n_sets;
+};
+
+// aberration coefficients of position gi, or null (no plates, or a marker out of range)
+__device__ __forceinline__ const float* coefs_of(const VarProbeArgs& a, int gi) {
+  if (!a.coefs) return nullptr;
+  const int m = a.marker[gi];
+  return (m >= 0 && m < a.n_sets) ? a.coefs + (size_t)m * a.n_abs : nullptr;
+}
+
+// incoming probe per position (objective.py:448-476): with a shift or aberration plates the
+// spectrum bc * FFT(P) times the shift ramp (the shift takes the spectrum before the plates,
+// objective.py:461, 471) or the plate; else the real-space probe times bc.
+// spec_or_pb[b][p][u]   grid (WW / EB, Mp, Bn)
+__global__ void var_probe_in_kernel(VarProbeArgs a, float2* __restrict__ out) {
+  const int u = blockIdx.x * EB + threadIdx.x, p = blockIdx.y, b = blockIdx.z;
+  const int W = a.W, WW = W * W, gi = a.seq[b];
+  const float bc = a.bc ? fabsf(a.bc[gi]) : 1.0f;
+  float2 v;
+  if (a.shift || a.coefs) {
+    const float mk = a.mask[u];
+    const float* coef = coefs_of(a, gi);
+    const float2 w = a.shift ? ramp(a.sx, a.sy, u / W, u % W, mk, a.corr[2 * gi], a.corr[2 * gi + 1])
+                     : coef  ? plate_at(a.abasis, coef, a.n_abs, WW, u, mk)
+                             : make_float2(mk, 0.0f);
+    v = cmul(a.bc ? cscale(a.pf[(size_t)p * WW + u], bc) : a.pf[(size_t)p * WW + u], w);
+  } else {
+    v = cscale(a.planes[(size_t)p * WW + u], bc);
+  }
+  out[((size_t)b * a.Mp + p) * WW + u] = v;
+}
+
+// pattern of every position (objective.py:509-512): mean over modes of |field|^2; the far
+// field is the unshifted spectrum, masked, stored at the detector (fftshifted) pixel; the
+// near field is the real-space wave.   grid (WW / EB, Bn)
+__global__ void var_intensity_kernel(const float2* __restrict__ field, const float* __restrict__ mask,
+                                     float* __restrict__ ibuf, int W, int nm, int near) {
+  const int u = blockIdx.x * EB + threadIdx.x, b = blockIdx.y;
+  const int WW = W * W;
+  const float2* f = field + (size_t)b * nm * WW;
+  float acc = 0.0f;
+  if (near) {
+    for (int k = 0; k < nm; ++k) acc += cabs2(f[(size_t)k * WW + u]);
+  } else {
+    const float mk = mask[u];
+    for (int k = 0; k < nm; ++k) acc += cabs2(cscale(f[(size_t)k * WW + u], mk));
+  }
+  const float I = nm == 1 ? acc : acc * (1.0f / (float)nm);
+  const int ky = u / W, kx = u % W;
+  const int pix = near ? u : ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
+  ibuf[(size_t)b * WW + pix] = I;
+}
+
+// per-pixel losses (objective.py:527-559) on the pattern: ibuf <- dL/dI / nm, FP64 partial
+// sums per position   grid Bn, block 1024
+__global__ void __launch_bounds__(1024) var_pixel_loss_kernel(float* __restrict__ ibuf, const float* __restrict__ measured,
+                                                              const int* __restrict__ seq, int WW, int nm, int alg,
+                                                              double* __restrict__ loss_part) {
+  __shared__ double red[64];
+  const int b = blockIdx.x;
+  const float* meas = measured + (size_t)seq[b] * WW;
+  float* I = ibuf + (size_t)b * WW;
+  double lsum = 0.0, ssum = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+    float d = loss_pixel(alg, I[u], meas[u], lsum, ssum);
+    if (nm > 1) d = d / (float)nm;
+    I[u] = d;
+  }
+  block_sum2(lsum, ssum, red);
+  if (threadIdx.x == 0) {
+    loss_part[2 * b] = lsum;
+    loss_part[2 * b + 1] = ssum;
+  }
+}
+
+// detector coefficients coef[b][j] = sum_u I[b][u] masks[j][u] (objective.py:561)
+// grid (n_masks, Bn), block 256
+__global__ void var_coef_kernel(const float* __restrict__ ibuf, const float* __restrict__ masks, int WW, int nmask,
+                                float* __restrict__ coef) {
+  __shared__ double red[64];
+  const int j = blockIdx.x, b = blockIdx.y;
+  const float* I = ibuf + (size_t)b * WW;
+  const float* m = masks + (size_t)j * WW;
+  double acc = 0.0, unused = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) acc += (double)(I[u] * m[u]);
+  block_sum2(acc, unused, red);
+  if (threadIdx.x == 0) coef[(size_t)b * nmask + j] = (float)acc;
+}
+
+// compressed losses on the coefficients (objective.py:560-585): dco[b][j] = dL/dcoef,
+// FP64 loss / sse partial sums per position   grid Bn, block 32
+__global__ void var_closs_kernel(const float* __restrict__ coef, const float* __restrict__ measured,
+                                 const int* __restrict__ seq, int nmask, int alg, float* __restrict__ dco,
+                                 double* __restrict__ loss_part) {
+  const int b = blockIdx.x;
+  const float* ms = measured + (size_t)seq[b] * nmask;
+  double lsum = 0.0, ssum = 0.0;
+  for (int j = threadIdx.x; j < nmask; j += blockDim.x) {
+    const float c = coef[(size_t)b * nmask + j], mv = ms[j];
+    float d;
+    if (alg == PTY_LSQ_COMPRESSED) {
+      const float df = c - mv;
+      const float t = df * df;
+      lsum += (double)t;
+      ssum += (double)t;
+      d = 2.0f * df;
+    } else if (alg == PTY_GAUSS_COMPRESSED) {
+      float cs = sqrtf(c);
+      const float dd = cs - sqrtf(mv);
+      const float e = c - mv;
+      ssum += (double)(e * e);
+      lsum += (double)(dd * dd);
+      if (cs == 0.0f) cs = 1.0f;
+      d = dd / cs;
+    } else {   // PTY_POISSON_COMPRESSED
+      const float dd = c - mv;
+      ssum += (double)(dd * dd);
+      const float cz = c == 0.0f ? 1.0f : c;
+      lsum += (double)(cz - mv * logf(cz));
+      d = dd / cz;
+    }
+    dco[(size_t)b * nmask + j] = d;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+    ssum += __shfl_down_sync(0xffffffffu, ssum, o);
+  }
+  if (threadIdx.x == 0) {
+    loss_part[2 * b] = lsum;
+    loss_part[2 * b + 1] = ssum;
+  }
+}
+
+// dL/dI = sum_j masks[j] dco[b][j] (j in order), / nm   grid (WW / EB, Bn)
+__global__ void var_cdldi_kernel(float* __restrict__ ibuf, const float* __restrict__ masks,
+                                 const float* __restrict__ dco, int WW, int nmask, int nm) {
+  const int u = blockIdx.x * EB + threadIdx.x, b = blockIdx.y;
+  float acc = 0.0f;
+  for (int j = 0; j < nmask; ++j) acc += masks[(size_t)j * WW + u] * dco[(size_t)b * nmask + j];
+  if (nm > 1) acc = acc / (float)nm;
+  ibuf[(size_t)b * WW + u] = acc;
+}
+
+// dL/dwave: far field F_k *= mask * dL/dI[detector pixel] * scale (objective.py:595-596);
+// near field wave_k *= dL/dI (objective.py:602)   grid (WW / EB, nm, Bn)
+__global__ void var_apply_kernel(float2* __restrict__ field, const float* __restrict__ ibuf,
+                                 const float* __restrict__ mask, int W, int nm, int near, float scale) {
+  const int u = blockIdx.x * EB + threadIdx.x, k = blockIdx.y, b = blockIdx.z;
+  const int WW = W * W;
+  float2* q = field + ((size_t)b * nm + k) * WW + u;
+  if (near) {
+    *q = cscale(*q, ibuf[(size_t)b * WW + u]);
+  } else {
+    const int ky = u / W, kx = u % W;
+    const int pix = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
+    *q = cscale(cscale(cscale(*q, mask[u]), ibuf[(size_t)b * WW + pix]), scale);
+  }
+}
+
+// probe-gradient spectrum chain of one (probe mode p, position b) (objective.py:641-697):
+// F = FFT(probe gradient); shift adjoint and position gradient partials; plate adjoint and
+// aberration gradient partials against bc * FFT(P); beam-current gradient partial
+// sum Re(F conj(FFT(P))) (Parseval: W^2 times the real-space sum); F *= bc for the probe
+// gradient. Partials: pos_part[s][p][2], bc_part[s][p], ab_part[s][p][n_abs].
+// grid (Mp, Bn), block 1024
+__global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict__ F, VarProbeArgs a, int step_pos,
+                                                             int step_bc, int step_ab, int step_probe,
+                                                             double* __restrict__ pos_part, double* __restrict__ bc_part,
+                                                             double* __restrict__ ab_part) {
+  __shared__ double red[64];
+  const int p = blockIdx.x, b = blockIdx.y, gi = a.seq[b];
+  const int W = a.W, WW = W * W;
+  const float bc = a.bc ? fabsf(a.bc[gi]) : 1.0f;
+  const float* coef = coefs_of(a, gi);
+  const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
+  float2* f = F + ((size_t)b * a.Mp + p) * WW;
+  const float2* pf = a.pf + (size_t)p * WW;
+  double gy = 0.0, gx = 0.0, gb = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+    const int ky = u / W, kx = u % W;
+    const float mk = a.mask[u];
+    const float2 before = a.bc ? cscale(pf[u], bc) : pf[u];
+    float2 v = f[u];
+    if (a.shift) {
+      v = cmulc(v, ramp(a.sx, a.sy, ky, kx, mk, dy, dx));
+      if (step_pos) {
+        const float im = cmulc(v, before).y;
+        gy += (double)(-(a.sy[ky] * mk) * im);
+        gx += (double)(-(a.sx[kx] * mk) * im);
+      }
+    }
+    if (coef) v = cmulc(v, plate_at(a.abasis, coef, a.n_abs, WW, u, mk));
+    if (a.bc && step_bc) gb += (double)cmulc(v, pf[u]).x;
+    f[u] = v;
+  }
+  if (step_pos && a.shift) {
+    double gyy = gy, gxx = gx;
+    block_sum2(gyy, gxx, red);
+    if (threadIdx.x == 0) {
+      pos_part[((size_t)b * a.Mp + p) * 2] = gyy;
+      pos_part[((size_t)b * a.Mp + p) * 2 + 1] = gxx;
+    }
+  }
+  if (a.bc && step_bc) {
+    double unused = 0.0;
+    block_sum2(gb, unused, red);
+    if (threadIdx.x == 0) bc_part[(size_t)b * a.Mp + p] = gb;
+  }
+  if (coef && step_ab) {
+    // sum_u -A_j Im(F conj(bc FFT(P))) for every aberration coefficient j; the plate adjoint
+    // has been applied to f (objective.py:677-681)
+    for (int j = 0; j < a.n_abs; ++j) {
+      __syncthreads();
+      double acc = 0.0, unused = 0.0;
+      for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+        const float2 before = a.bc ? cscale(pf[u], bc) : pf[u];
+        acc += (double)(a.abasis[(size_t)j * WW + u] * cmulc(f[u], before).y);
+      }
+      block_sum2(acc, unused, red);
+      if (threadIdx.x == 0) ab_part[((size_t)b * a.Mp + p) * a.n_abs + j] = acc;
+    }
+  }
+  // probe gradient times the beam current (objective.py:698-699); every thread rescales the
+  // pixels it wrote itself
+  if (a.bc && step_probe)
+    for (int u = threadIdx.x; u < WW; u += blockDim.x) f[u] = cscale(f[u], bc);
+}
+
+// beam-current and aberration gradients from the partials, in sequence order
+// (objective.py:681-682, 693-697)   one block of 256
+__global__ void var_finalize_kernel(const double* __restrict__ bc_part, const double* __restrict__ ab_part,
+                                    const int* __restrict__ seq, int nseq, int Mp, int W, int N,
+                                    const float* __restrict__ bc, float* __restrict__ bc_grad, int n_sets, int n_abs,
+                                    const int* __restrict__ marker, float* __restrict__ ab_grad) {
+  const double sh = 2.0 / ((double)W * (double)W);
+  if (bc_grad) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) bc_grad[i] = 0.0f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int s = 0; s < nseq; ++s) {
+        double g = 0.0;
+        for (int p = 0; p < Mp; ++p) g += bc_part[(size_t)s * Mp + p];
+        const float sgn = bc[seq[s]] != 0.0f ? 1.0f : 0.0f;   // sign(|bc|)
+        bc_grad[seq[s]] = (float)(sh * g) * sgn;
+      }
+    }
+  }
+  if (ab_grad) {
+    for (int t = threadIdx.x; t < n_sets * n_abs; t += blockDim.x) {
+      const int set = t / n_abs, j = t % n_abs;
+      double g = 0.0;
+      for (int s = 0; s < nseq; ++s) {
+        if (marker[seq[s]] != set) continue;
+        double gs = 0.0;
+        for (int p = 0; p < Mp; ++p) gs += ab_part[((size_t)s * Mp + p) * n_abs + j];
+        g += (double)(float)(sh * gs);
+      }
+      ab_grad[t] = (float)g;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ plan
 struct LPlan {
   int W, WW, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, zm, ntx, nty, ntiles, chunk, nchunk, engine;
   size_t o_pos, o_corr, o_seq, o_tab_pyx, o_mask, o_mask_sc, o_prop, o_prop_edge, o_sx, o_sy, o_planes, o_pf;
   size_t o_obj, o_grad, o_ob, o_tmp, o_dob, o_stack, o_psi, o_psi2, o_pb, o_pbs, o_partial, o_lists, o_counts;
   size_t o_loss_part, o_pos_part, o_dft, dft_bytes, total;
+  // variants (pty_loss_and_direction_variants)
+  int near, compressed, nmask, n_abs, n_sets, has_bc;
+  size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part;
 };
 
-inline LPlan make_lplan(const pty_problem_t* p, int engine) {
+inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t* v = nullptr) {
   LPlan q{};
   q.W = p->window;
   q.WW = q.W * q.W;
@@ -271,6 +631,22 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine) {
   q.o_counts = take((size_t)q.ntiles * sizeof(int));
   q.o_loss_part = take((size_t)q.nseq * 2 * sizeof(double));
   q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
+  if (v) {
+    q.near = v->recon_type == 1;
+    q.compressed = p->algorithm >= PTY_LSQ_COMPRESSED;
+    q.nmask = q.compressed ? v->n_masks : 0;
+    q.n_abs = v->aberrations ? v->n_aberrations : 0;
+    q.n_sets = v->aberrations ? v->n_aberration_sets : 0;
+    q.has_bc = v->beam_current != nullptr;
+    q.o_ctf = take(q.near ? WWs * c8 : 0);
+    q.o_abasis = take((size_t)q.n_abs * WWs * sizeof(float));
+    q.o_abidx = take((size_t)3 * q.n_abs * sizeof(int));
+    q.o_ibuf = take((size_t)q.Bb * WWs * sizeof(float));
+    q.o_coef = take((size_t)q.Bb * q.nmask * sizeof(float));
+    q.o_dco = take((size_t)q.Bb * q.nmask * sizeof(float));
+    q.o_bc_part = take(q.has_bc ? (size_t)q.nseq * q.Mp * sizeof(double) : 0);
+    q.o_ab_part = take((size_t)q.nseq * q.Mp * q.n_abs * sizeof(double));
+  }
   size_t db = 0;
   const size_t maxwin = nobw > nwave ? nobw : nwave;
   const int32_t nmax = (int32_t)(maxwin > (size_t)q.Mp ? maxwin : (size_t)q.Mp);
@@ -286,11 +662,27 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine) {
   return q;
 }
 
+// Krivanek (n, m, a/b) order of the first n aberrations (pypty/utils.py:1272-1308):
+// kind 0 for m = 0, 1 for the cos (a) term, 2 for the sin (b) term
+inline void krivanek_order(int n_abs, int* n_out, int* m_out, int* kind_out) {
+  int i = 0;
+  for (int n = 1; i < n_abs; ++n)
+    for (int m = (n + 1) % 2; m <= n + 1 && i < n_abs; m += 2) {
+      if (m == 0) {
+        n_out[i] = n, m_out[i] = 0, kind_out[i] = 0, ++i;
+      } else {
+        n_out[i] = n, m_out[i] = m, kind_out[i] = 1, ++i;
+        if (i < n_abs) n_out[i] = n, m_out[i] = m, kind_out[i] = 2, ++i;
+      }
+    }
+}
+
 struct Run {
   const pty_problem_t* p;
   LPlan q;
   void* ws;
   cudaStream_t st;
+  const pty_variant_t* v = nullptr;
   TableArgs ta{};
 
   int dft(const float2* in, float2* out, long long nwin, int inverse) {
@@ -330,6 +722,39 @@ struct Run {
     if (W == 64) tables_kernel<64><<<(WW + 255) / 256, 256, 0, st>>>(ta);
     else if (W == 128) tables_kernel<128><<<(WW + 255) / 256, 256, 0, st>>>(ta);
     else tables_kernel<256><<<(WW + 255) / 256, 256, 0, st>>>(ta);
+    if (v) {
+      VarTableArgs va{};
+      va.prop = ta.prop;
+      va.prop_edge = ta.prop_edge;
+      va.ctf = at<float2>(ws, q.o_ctf);
+      va.abasis = at<float>(ws, q.o_abasis);
+      va.mask = ta.mask;
+      int* abidx = at<int>(ws, q.o_abidx);
+      if (q.n_abs > 0) {
+        int host[3 * 64];
+        if (q.n_abs > 64) return PTY_ERR_UNSUPPORTED;
+        krivanek_order(q.n_abs, host, host + q.n_abs, host + 2 * q.n_abs);
+        if (cudaMemcpyAsync(abidx, host, (size_t)3 * q.n_abs * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+          return PTY_ERR_CUDA;
+      }
+      va.abn = abidx;
+      va.abm = abidx + q.n_abs;
+      va.abk = abidx + 2 * q.n_abs;
+      va.W = W;
+      va.use_edge = ta.use_edge;
+      va.near = q.near;
+      va.n_abs = q.n_abs;
+      va.px = p->pixel_size_x;
+      va.py = p->pixel_size_y;
+      va.distance = p->slice_distance;
+      va.wavelength = p->wavelength;
+      va.edge_mult = p->edge_mult;
+      va.tan_x = v->tan_x;
+      va.tan_y = v->tan_y;
+      va.defocus = v->defocus;
+      va.cs = v->cs;
+      var_tables_kernel<<<(WW + 255) / 256, 256, 0, st>>>(va);
+    }
     float2* planes = at<float2>(ws, q.o_planes);
     float2* pf = at<float2>(ws, q.o_pf);
     prof_mark(st, KID_LAYOUT);
@@ -344,6 +769,23 @@ struct Run {
     float2 *stack = at<float2>(ws, q.o_stack), *psi = at<float2>(ws, q.o_psi), *psi2 = at<float2>(ws, q.o_psi2);
     float2 *pb = at<float2>(ws, q.o_pb), *pbs = at<float2>(ws, q.o_pbs);
     const int nm = q.Mp * q.Mo;
+    VarProbeArgs pa{};
+    pa.pf = pf;
+    pa.planes = planes;
+    pa.sx = ta.sx;
+    pa.sy = ta.sy;
+    pa.mask = ta.mask;
+    pa.corr = d_corr;
+    pa.bc = v ? v->beam_current : nullptr;
+    pa.abasis = at<float>(ws, q.o_abasis);
+    pa.coefs = v ? v->aberrations : nullptr;
+    pa.marker = v ? v->aberration_marker : nullptr;
+    pa.W = W;
+    pa.Mp = q.Mp;
+    pa.shift = shift ? 1 : 0;
+    pa.n_abs = q.n_abs;
+    pa.n_sets = q.n_sets;
+    const bool var_probe = v && (shift || pa.bc || pa.coefs);
     for (int i0 = 0, ib = 0; i0 < q.nseq; i0 += q.Bb, ++ib) {
       const int Bn = q.nseq - i0 < q.Bb ? q.nseq - i0 : q.Bb;
       const int* seq_b = at<int>(ws, q.o_seq) + i0;
@@ -357,7 +799,15 @@ struct Run {
       // incoming probe per position (objective.py:469-476)
       const float2* pin = planes;
       size_t pin_stride = 0;
-      if (shift) {
+      pa.seq = seq_b;
+      if (var_probe) {
+        prof_mark(st, KID_ELEMENTWISE);
+        const bool spectral = shift || pa.coefs;
+        var_probe_in_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pa, spectral ? pbs : pb);
+        if (spectral && (rc = dft(pbs, pb, (long long)Bn * q.Mp, 1))) return rc;
+        pin = pb;
+        pin_stride = (size_t)q.Mp * WWs;
+      } else if (shift) {
         prof_mark(st, KID_ELEMENTWISE);
         probe_spec_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pbs, pf, ta.sx, ta.sy, ta.mask, d_corr, seq_b, W, q.Mp);
         if ((rc = dft(pbs, pb, (long long)Bn * q.Mp, 1))) return rc;
@@ -378,10 +828,14 @@ struct Run {
       }
       // far field, loss, dL/dPsi (objective.py:501-597)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
-      prof_mark(st, KID_FINALIZE);
-      loss_kernel<<<Bn, 1024, 0, st>>>(psi2, ta.mask, measured, seq_b, W, q.Mp, q.Mo, p->algorithm,
-                                       p->loss_weight * (float)WW, at<double>(ws, q.o_loss_part) + 2 * i0);
-      if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
+      if (!v) {
+        prof_mark(st, KID_FINALIZE);
+        loss_kernel<<<Bn, 1024, 0, st>>>(psi2, ta.mask, measured, seq_b, W, q.Mp, q.Mo, p->algorithm,
+                                         p->loss_weight * (float)WW, at<double>(ws, q.o_loss_part) + 2 * i0);
+        if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
+      } else if ((rc = variant_loss(psi, psi2, measured, seq_b, Bn, i0))) {
+        return rc;
+      }
       // adjoint multislice (multislice_core.py:158-200)
       for (int z = q.Z - 1; z >= 0; --z) {
         prof_mark(st, KID_FUSED);
@@ -408,13 +862,19 @@ struct Run {
         scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, st>>>(
             dob, d_pos, seq_b, lists, counts, at<float2>(ws, q.o_grad), Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0);
       }
-      if (p->step_probe || p->step_pos) {
+      const bool step_bc = v && v->beam_current && v->step_beam_current;
+      const bool step_ab = v && v->aberrations && v->step_aberrations;
+      if (p->step_probe || p->step_pos || step_bc || step_ab) {
         // probe-gradient spectra with the shift adjoint and the position gradient (objective.py:641-703)
         prof_mark(st, KID_PROBE_PARTIAL);
         probe_sum_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(psi, pbs, q.Mp, q.Mo, WW);
         if ((rc = dft(pbs, pb, (long long)Bn * q.Mp, 0))) return rc;
         prof_mark(st, KID_ELEMENTWISE);
-        if (shift)
+        if (var_probe)
+          var_probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(
+              pb, pa, p->step_pos, step_bc, step_ab, p->step_probe, at<double>(ws, q.o_pos_part) + (size_t)i0 * q.Mp * 2,
+              at<double>(ws, q.o_bc_part) + (size_t)i0 * q.Mp, at<double>(ws, q.o_ab_part) + (size_t)i0 * q.Mp * q.n_abs);
+        else if (shift)
           probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(pb, pf, ta.sx, ta.sy, ta.mask, d_corr, seq_b, W, q.Mp,
                                                            p->step_pos, at<double>(ws, q.o_pos_part) + (size_t)i0 * q.Mp * 2);
         if (p->step_probe) {
@@ -443,8 +903,50 @@ struct Run {
     finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
                                                p->step_pos && shift, nullptr, loss_sse, pos_grad);
+    if (v && ((v->beam_current && v->step_beam_current) || (v->aberrations && v->step_aberrations))) {
+      const bool gb = v->beam_current && v->step_beam_current, ga = v->aberrations && v->step_aberrations;
+      var_finalize_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_bc_part), at<double>(ws, q.o_ab_part),
+                                             at<int>(ws, q.o_seq), q.nseq, q.Mp, W, q.N, v->beam_current,
+                                             gb ? v->beam_current_grad : nullptr, q.n_sets, q.n_abs,
+                                             v->aberration_marker, ga ? v->aberrations_grad : nullptr);
+    }
     prof_mark(st, -1);
     return cuda_status();
+  }
+
+  // pattern, loss and dL/d(exit wave) of one batch for the variant branches: psi2 holds the
+  // spectra of the exit waves; on return psi holds dL/d(exit wave) (objective.py:501-604)
+  int variant_loss(float2* psi, float2* psi2, const float* measured, const int* seq_b, int Bn, int i0) {
+    int rc;
+    const int W = q.W, WW = q.WW, nm = q.Mp * q.Mo;
+    float* ibuf = at<float>(ws, q.o_ibuf);
+    double* lpart = at<double>(ws, q.o_loss_part) + 2 * (size_t)i0;
+    const float2* ctf = at<float2>(ws, q.o_ctf);
+    float2* field = psi2;
+    prof_mark(st, KID_FINALIZE);
+    if (q.near) {   // wave = IFFT(FFT(exit) * CTF) (objective.py:506-508)
+      prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 0, 1.0f);
+      if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
+      field = psi;
+    }
+    prof_mark(st, KID_FINALIZE);
+    var_intensity_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(field, ta.mask, ibuf, W, nm, q.near);
+    if (q.compressed) {
+      float* coef = at<float>(ws, q.o_coef);
+      float* dco = at<float>(ws, q.o_dco);
+      var_coef_kernel<<<dim3((unsigned)q.nmask, (unsigned)Bn), 256, 0, st>>>(ibuf, v->masks, WW, q.nmask, coef);
+      var_closs_kernel<<<Bn, 32, 0, st>>>(coef, measured, seq_b, q.nmask, p->algorithm, dco, lpart);
+      var_cdldi_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(ibuf, v->masks, dco, WW, q.nmask, nm);
+    } else {
+      var_pixel_loss_kernel<<<Bn, 1024, 0, st>>>(ibuf, measured, seq_b, WW, nm, p->algorithm, lpart);
+    }
+    var_apply_kernel<<<grid(nm, Bn), EB, 0, st>>>(field, ibuf, ta.mask, W, nm, q.near, p->loss_weight * (float)WW);
+    if (q.near) {   // dL/d(exit) = IFFT(loss_weight FFT(wave dL/dI) conj(CTF)) (objective.py:602-604)
+      if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
+      prof_mark(st, KID_ELEMENTWISE);
+      prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 1, p->loss_weight);
+    }
+    return dft(psi2, psi, (long long)Bn * nm, 1);
   }
 };
 
@@ -494,6 +996,75 @@ int pty_loss_and_direction_layered(const pty_problem_t* problem, int32_t engine,
                       st) != cudaSuccess)
     return PTY_ERR_CUDA;
   lay::Run r{problem, q, workspace, st};
+  return r.run(static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured, loss_sse,
+               static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad);
+}
+
+}  // extern "C"
+
+namespace {
+
+// the problem with a compressed algorithm mapped onto a pixel one for the shared checks
+int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
+  if (!p || !v) return PTY_ERR_INVALID;
+  pty_problem_t base = *p;
+  const bool compressed = p->algorithm >= PTY_LSQ_COMPRESSED && p->algorithm <= PTY_POISSON_COMPRESSED;
+  if (compressed) base.algorithm = PTY_LSQ;
+  int rc = validate(&base);
+  if (rc) return rc;
+  if (v->recon_type != 0 && v->recon_type != 1) return PTY_ERR_UNSUPPORTED;
+  if (compressed && (v->n_masks <= 0 || !v->masks)) return PTY_ERR_INVALID;
+  if (v->beam_current && v->step_beam_current && !v->beam_current_grad) return PTY_ERR_INVALID;
+  if (v->aberrations) {
+    if (v->n_aberrations <= 0 || v->n_aberrations > 64 || v->n_aberration_sets <= 0 || !v->aberration_marker)
+      return PTY_ERR_INVALID;
+    if (v->step_aberrations && !v->aberrations_grad) return PTY_ERR_INVALID;
+  }
+  return PTY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes) {
+  int rc = validate_variant(problem, variant);
+  if (rc) return rc;
+  if (!bytes) return PTY_ERR_INVALID;
+  *bytes = lay::make_lplan(problem, PTY_DFT_FP32_FFT, variant).total;
+  return PTY_OK;
+}
+
+int pty_loss_and_direction_variants(const pty_problem_t* problem, const pty_variant_t* variant, const void* obj,
+                                    const void* probe, const int32_t* positions_host, const float* pos_correction,
+                                    const int32_t* sequence_host, const float* measured, double* loss_sse,
+                                    void* object_grad, void* probe_grad, float* pos_grad, void* workspace,
+                                    size_t workspace_bytes, void* stream) {
+  int rc = validate_variant(problem, variant);
+  if (rc) return rc;
+  if (!obj || !probe || !positions_host || !sequence_host || !measured || !loss_sse || !workspace)
+    return PTY_ERR_INVALID;
+  if ((problem->step_obj && !object_grad) || (problem->step_probe && !probe_grad) || (problem->step_pos && !pos_grad))
+    return PTY_ERR_INVALID;
+  if ((rc = check_geometry(problem, positions_host, sequence_host))) return rc;
+  const lay::LPlan q = lay::make_lplan(problem, PTY_DFT_FP32_FFT, variant);
+  if ((long long)q.Bb * (q.zm > q.Mp * q.Mo ? q.zm : q.Mp * q.Mo) > 65535) return PTY_ERR_UNSUPPORTED;
+  if (workspace_bytes < q.total) return PTY_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(at<int>(workspace, q.o_pos), positions_host, (size_t)q.N * 2 * sizeof(int), cudaMemcpyDefault,
+                      st) != cudaSuccess)
+    return PTY_ERR_CUDA;
+  if (pos_correction) {
+    if (cudaMemcpyAsync(at<float>(workspace, q.o_corr), pos_correction, (size_t)q.N * 2 * sizeof(float),
+                        cudaMemcpyDefault, st) != cudaSuccess)
+      return PTY_ERR_CUDA;
+  } else if (cudaMemsetAsync(at<float>(workspace, q.o_corr), 0, (size_t)q.N * 2 * sizeof(float), st) != cudaSuccess) {
+    return PTY_ERR_CUDA;
+  }
+  if (cudaMemcpyAsync(at<int>(workspace, q.o_seq), sequence_host, (size_t)q.nseq * sizeof(int), cudaMemcpyDefault,
+                      st) != cudaSuccess)
+    return PTY_ERR_CUDA;
+  lay::Run r{problem, q, workspace, st, variant};
   return r.run(static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured, loss_sse,
                static_cast<float2*>(object_grad), static_cast<float2*>(probe_grad), pos_grad);
 }

@@ -43,9 +43,10 @@ def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, 
                  checkpoint_every=1) -> _lib.Problem:
     ny, nx, nz, mo = obj_shape
     if isinstance(algorithm, str):
-        if algorithm not in _lib.ALGORITHMS:
+        codes = dict(_lib.ALGORITHMS, **_lib.COMPRESSED_ALGORITHMS)
+        if algorithm not in codes:
             raise NotImplementedError("loss %r is not implemented on the GPU path" % algorithm)
-        algorithm = _lib.ALGORITHMS[algorithm]
+        algorithm = codes[algorithm]
     if damping_cutoff is None:
         damping_cutoff = 2.0
     if damping_cutoff < 0:
@@ -173,6 +174,83 @@ class Engine:
         self._mark_staging(stream)
         _lib.check(st, "pty_loss_and_direction_layered")
         return loss_sse, og, pg, posg
+
+    def loss_and_direction_variants(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor,
+                                    geo: Geometry, measured: torch.Tensor, *, recon_type: str = "far_field",
+                                    defocus: float = 0.0, cs: float = 0.0, tan_x: float = 0.0, tan_y: float = 0.0,
+                                    masks: torch.Tensor | None = None, beam_current: torch.Tensor | None = None,
+                                    step_beam_current: bool = False, aberrations: torch.Tensor | None = None,
+                                    aberration_marker: torch.Tensor | None = None, step_aberrations: bool = False,
+                                    stream=None):
+        """loss_and_direction with the near-field, compressed-detector, beam-current,
+        aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
+
+        measured is (n_positions, W, W) float32, or (n_positions, n_masks) for the compressed
+        algorithms; masks (n_masks, W, W) float32 in pattern order; beam_current
+        (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
+        (n_positions,) int32. Returns (loss_sse, object_grad, probe_grad, pos_grad,
+        beam_current_grad or None, aberrations_grad or None)."""
+        stream = stream or torch.cuda.current_stream(self.device)
+        compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
+        self._check_inputs(problem, obj, probe, None)
+        want = (problem.n_positions, masks.shape[0]) if compressed else \
+            (problem.n_positions, problem.window, problem.window)
+        if tuple(measured.shape) != want or measured.dtype != torch.float32 or not measured.is_cuda \
+                or not measured.is_contiguous():
+            raise ValueError("measured must be a contiguous float32 CUDA tensor of shape %s" % (want,))
+        if recon_type not in _lib.RECON_TYPES:
+            raise NotImplementedError("recon_type %r" % recon_type)
+        keep = []
+
+        def dev(t, dtype):
+            if t is None:
+                return None
+            t = t.to(device=self.device, dtype=dtype).contiguous()
+            keep.append(t)
+            return t
+
+        if aberrations is not None:
+            mk = np.asarray(aberration_marker.cpu() if torch.is_tensor(aberration_marker) else aberration_marker)
+            if mk.shape != (problem.n_positions,) or mk.min() < 0 or mk.max() >= aberrations.shape[0]:
+                raise ValueError("aberration_marker must hold one set index in [0, %d) per position"
+                                 % aberrations.shape[0])
+        masks_d = dev(masks, torch.float32)
+        bc_d = dev(beam_current, torch.float32)
+        ab_d = dev(aberrations, torch.float32)
+        mk_d = dev(aberration_marker, torch.int32)
+        bc_grad = torch.zeros(problem.n_positions, dtype=torch.float32, device=self.device) \
+            if bc_d is not None and step_beam_current else None
+        ab_grad = torch.zeros(tuple(ab_d.shape), dtype=torch.float32, device=self.device) \
+            if ab_d is not None and step_aberrations else None
+        v = _lib.Variant(recon_type=_lib.RECON_TYPES[recon_type], defocus=float(defocus), cs=float(cs),
+                         tan_x=float(tan_x), tan_y=float(tan_y),
+                         n_masks=0 if masks_d is None else int(masks_d.shape[0]),
+                         masks=None if masks_d is None else masks_d.data_ptr(),
+                         beam_current=None if bc_d is None else bc_d.data_ptr(),
+                         step_beam_current=int(bc_grad is not None),
+                         beam_current_grad=None if bc_grad is None else bc_grad.data_ptr(),
+                         n_aberrations=0 if ab_d is None else int(ab_d.shape[1]),
+                         n_aberration_sets=0 if ab_d is None else int(ab_d.shape[0]),
+                         aberrations=None if ab_d is None else ab_d.data_ptr(),
+                         aberration_marker=None if mk_d is None else mk_d.data_ptr(),
+                         step_aberrations=int(ab_grad is not None),
+                         aberrations_grad=None if ab_grad is None else ab_grad.data_ptr())
+        n = ctypes.c_size_t(0)
+        _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
+                   "pty_variants_workspace_bytes")
+        ws = self.workspace(int(n.value))
+        loss_sse = torch.empty(2, dtype=torch.float64, device=self.device)
+        og, pg = torch.empty_like(obj), torch.empty_like(probe)
+        posg = torch.zeros((problem.n_positions, 2), dtype=torch.float32, device=self.device)
+        pp, pc, ps = self._staging(geo)
+        st = _lib.lib().pty_loss_and_direction_variants(
+            ctypes.byref(problem), ctypes.byref(v), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
+            _ptr(loss_sse), _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)
+        self._mark_staging(stream)
+        for t in keep:
+            t.record_stream(stream)
+        _lib.check(st, "pty_loss_and_direction_variants")
+        return loss_sse, og, pg, posg, bc_grad, ab_grad
 
     def forward(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
                 measured: torch.Tensor, stream=None):

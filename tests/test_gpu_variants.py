@@ -1,0 +1,146 @@
+"""Near-field propagation, compressed-detector losses, beam current, aberration plates and the
+inside tilt on the GPU (``pty_loss_and_direction_variants``) against the reference's own
+results (golden fixtures) and the FP64 variants oracle on the same inputs."""
+import numpy as np
+import pytest
+
+from golden_io import load_variant_case, rel_l2, variant_case_names
+from oracle import variants_oracle as vor
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu_variant(c, engine=None):
+    import torch
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    dev = torch.device("cuda", 0)
+    eng = engine or Engine(dev)
+    obj = np.ascontiguousarray(c["obj"]).astype(np.complex64)
+    probe = np.ascontiguousarray(c["probe"]).astype(np.complex64)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    W = probe.shape[0]
+    prob = make_problem(W, obj.shape, probe.shape[2], geo, algorithm=c["algorithm"],
+                        wavelength=float(np.float32(c["wavelength"])), pixel_size_x=float(np.float32(c["px"])),
+                        pixel_size_y=float(np.float32(c["px"])), slice_distance=c["distance"],
+                        edge_mult=c["edge_mult"], damping_cutoff=float(np.float32(c["cutoff"])),
+                        smooth_rolloff=float(np.float32(c["rolloff"])), loss_weight=c["loss_weight"],
+                        compute_batch=c["batch"], step_obj=c["step_obj"], step_probe=c["step_probe"],
+                        step_pos=c["step_pos"])
+    t = lambda a, dt=None: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
+    ls, og, pg, posg, bcg, abg = eng.loss_and_direction_variants(
+        prob, t(obj), t(probe), geo, t(c["measured"], np.float32), recon_type=c["recon_type"],
+        defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"], masks=t(c["masks"], np.float32),
+        beam_current=t(c["beam_current"], np.float32), step_beam_current=bool(c["step_bc"]),
+        aberrations=t(c["aberrations"], np.float32),
+        aberration_marker=t(c["aberration_marker"], np.int32), step_aberrations=bool(c["step_ab"]))
+    torch.cuda.synchronize()
+    ls = ls.cpu().numpy()
+    cpu = lambda a: None if a is None else a.cpu().numpy()
+    return float(ls[0]), float(ls[1]), og.cpu().numpy(), pg.cpu().numpy(), posg.cpu().numpy(), cpu(bcg), cpu(abg)
+
+
+def fp64_variant_oracle(c):
+    return vor.loss_and_direction_variants(
+        np.asarray(c["obj"], np.complex128), np.asarray(c["probe"], np.complex128), c["positions"],
+        np.asarray(c["pos_correction"], np.float64), c["distance"], c["edge_mult"],
+        np.asarray(c["measured"], np.float64), c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"],
+        c["step_pos"], c["px"], c["px"], c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"],
+        recon_type=c["recon_type"], defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
+        masks=None if c["masks"] is None else np.asarray(c["masks"], np.float64),
+        beam_current=c["beam_current"], step_beam_current=c["step_bc"], aberrations=c["aberrations"],
+        aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], float_dtype=np.float64,
+        complex_dtype=np.complex128)
+
+
+def errors(res, ref):
+    loss, _, og, pg, posg, bcg, abg = res
+    rl, _, rog, rpg, rposg, rbcg, rabg = ref
+    e = dict(loss=abs(loss - float(rl)) / abs(float(rl)), obj=rel_l2(og, rog),
+             probe=rel_l2(pg, np.asarray(rpg).reshape(pg.shape)))
+    if posg is not None and np.linalg.norm(np.asarray(rposg)) > 0:
+        e["pos"] = rel_l2(posg, rposg)
+    if bcg is not None:
+        e["bc"] = rel_l2(bcg, rbcg)
+    if abg is not None:
+        e["ab"] = rel_l2(abg, rabg)
+    return e
+
+
+# complex64 tolerances against FP64 (loss 1e-5, gradients 1e-4). The compressed losses
+# difference coefficients of 4096 pixels against measurements within 2 % of them, which
+# multiplies the relative FP32 error of the coefficients by ~50 in the loss of lsq_compressed
+# and in the gradients of all three: 2e-4 there.
+TOL = {"lsq_compressed": (2e-4, 2e-4), "gauss_compressed": (1e-5, 2e-4), "poisson_compressed": (1e-5, 2e-4)}
+
+
+@pytest.mark.parametrize("name", [n for n in variant_case_names() if not n.endswith("_c128")])
+def test_variants_against_fp64_oracle_and_reference(name):
+    c = load_variant_case(name)
+    res = run_gpu_variant(c)
+    lt, gt = TOL.get(c["algorithm"], (1e-5, 1e-4))
+    e64 = errors(res, fp64_variant_oracle(c))
+    print(name, "vs FP64", {k: "%.1e" % v for k, v in e64.items()})
+    for k, v in e64.items():
+        assert v <= (lt if k == "loss" else gt), (k, v)
+    # the reference's own complex64 result carries its FP32 error too: twice the bound
+    ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
+           c["ref_beam_current_grad"], c["ref_aberrations_grad"])
+    eref = errors(res, ref)
+    print(name, "vs reference c64", {k: "%.1e" % v for k, v in eref.items()})
+    for k, v in eref.items():
+        assert v <= 2 * (lt if k == "loss" else gt), (k, v)
+
+
+@pytest.mark.parametrize("name", [n for n in variant_case_names() if n.endswith("_c128")])
+def test_variants_against_reference_fp64(name):
+    """The complex64 GPU result against the reference run in complex128."""
+    c = load_variant_case(name)
+    res = run_gpu_variant(c)
+    ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
+           c["ref_beam_current_grad"], c["ref_aberrations_grad"])
+    e = errors(res, ref)
+    print(name, {k: "%.1e" % v for k, v in e.items()})
+    for k, v in e.items():
+        assert v <= (1e-5 if k == "loss" else 1e-4), (k, v)
+
+
+def test_variants_without_options_match_layered_far_field():
+    """With every variant off the variants entry is the far-field layered path."""
+    import torch
+    from golden_io import load_case
+    from gpu_helpers import run_gpu
+    c = load_case("multislice_ml_c64")
+    c.update(recon_type="far_field", defocus=0.0, cs=0.0, tan_x=0.0, tan_y=0.0, masks=None, beam_current=None,
+             step_bc=0, aberrations=None, aberration_marker=None, step_ab=0)
+    a = run_gpu_variant(c)
+    b = run_gpu(c)
+    assert abs(a[0] - b[0]) <= 1e-5 * abs(b[0])
+    assert rel_l2(a[2], b[2]) <= 1e-5
+    assert rel_l2(a[3], b[3]) <= 1e-5
+    assert rel_l2(a[4], b[4]) <= 1e-5
+    torch.cuda.synchronize()
+
+
+def test_variants_reject_bad_arguments():
+    import torch
+    from pypty_gb300 import _lib
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    c = load_variant_case("lsq_compressed_c64")
+    dev = torch.device("cuda", 0)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    prob = make_problem(64, c["obj"].shape, c["probe"].shape[2], geo, algorithm="lsq_compressed",
+                        wavelength=float(c["wavelength"]), pixel_size_x=c["px"], pixel_size_y=c["px"],
+                        slice_distance=c["distance"], compute_batch=c["batch"])
+    eng = Engine(dev)
+    obj = torch.from_numpy(c["obj"].astype(np.complex64)).to(dev)
+    probe = torch.from_numpy(c["probe"].astype(np.complex64)).to(dev)
+    meas = torch.from_numpy(c["measured"].astype(np.float32)).to(dev)
+    masks = torch.from_numpy(c["masks"]).to(dev)
+    # the fused entry has no compressed losses
+    with pytest.raises(_lib.PtyError):
+        eng.loss_and_direction(prob, obj, probe, geo, torch.zeros((len(geo.positions), 64, 64), device=dev))
+    # measured must be (n_positions, n_masks)
+    with pytest.raises(ValueError):
+        eng.loss_and_direction_variants(prob, obj, probe, geo, meas[:, :3].contiguous(), masks=masks)
+    with pytest.raises(NotImplementedError):
+        eng.loss_and_direction_variants(prob, obj, probe, geo, meas, masks=masks, recon_type="fresnel")
