@@ -181,15 +181,16 @@ class Engine:
                                     masks: torch.Tensor | None = None, beam_current: torch.Tensor | None = None,
                                     step_beam_current: bool = False, aberrations: torch.Tensor | None = None,
                                     aberration_marker: torch.Tensor | None = None, step_aberrations: bool = False,
-                                    stream=None):
+                                    stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
 
         measured is (n_positions, W, W) float32, or (n_positions, n_masks) for the compressed
         algorithms; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
-        (n_positions,) int32. Returns (loss_sse, object_grad, probe_grad, pos_grad,
-        beam_current_grad or None, aberrations_grad or None)."""
+        (n_positions,) int32; pos_correction as in ``loss_and_direction``. Returns (loss_sse,
+        object_grad, probe_grad, pos_grad, beam_current_grad or None, aberrations_grad or
+        None)."""
         stream = stream or torch.cuda.current_stream(self.device)
         compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
         self._check_inputs(problem, obj, probe, None)
@@ -243,6 +244,12 @@ class Engine:
         og, pg = torch.empty_like(obj), torch.empty_like(probe)
         posg = torch.zeros((problem.n_positions, 2), dtype=torch.float32, device=self.device)
         pp, pc, ps = self._staging(geo)
+        if pos_correction is not None:
+            if (not pos_correction.is_cuda or pos_correction.dtype != torch.float32
+                    or tuple(pos_correction.shape) != (problem.n_positions, 2)
+                    or not pos_correction.is_contiguous()):
+                raise ValueError("pos_correction must be a contiguous (N, 2) float32 CUDA tensor")
+            pc = pos_correction.data_ptr()
         st = _lib.lib().pty_loss_and_direction_variants(
             ctypes.byref(problem), ctypes.byref(v), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
             _ptr(loss_sse), _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)

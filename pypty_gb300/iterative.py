@@ -118,7 +118,7 @@ def _impl(ns, a):
         aperture = ap if not isinstance(ap, (int, float, np.floating)) else np.float32(ap)
         probe_reg_weight = 0
     # the loss-and-gradient call exactly as iterative.py:524 makes it (smooth_rolloff_loss = 0)
-    problem, geo = objective.prepare(
+    problem, geo, variant = objective.prepare(
         ns.obj, ns.probe, ns.positions, ns.positions_correction, ns.tilts, ns.tilts_correction,
         a["this_slice_distances"], a["edge_slice_thickness_multiplier"], a["measured_array"], a["algorithm_type"],
         a["this_wavelength"], update_probe, update_obj, update_pos, a["this_step_tilts"] > 0, a["masks"],
@@ -138,6 +138,11 @@ def _impl(ns, a):
         a["use_padded_intensity"])
     eng = default_engine()
     dev = eng.device
+    if variant is not None:
+        for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
+                      ("aberration_marker", torch.int32)):
+            if variant[k] is not None:
+                variant[k] = _to_device(variant[k], dt, dev)
     st = _STATES.setdefault(id(ns), {"opt": None, "meas_src": None, "meas": None})
     meas_src = a["measured_array"]
     if st["meas_src"] is not meas_src:
@@ -159,9 +164,9 @@ def _impl(ns, a):
     empty = hist is None or bool(hist.get("empty_hist", True))
     if opt is None or tuple(opt.obj.shape) != tuple(obj_d.shape) or tuple(opt.probe.shape) != tuple(probe_d.shape) \
             or tuple(opt.corr.shape) != tuple(corr_d.shape):
-        opt = st["opt"] = LBFGS(problem, geo, st["meas"], obj_d, probe_d, corr_d, cfg, eng)
+        opt = st["opt"] = LBFGS(problem, geo, st["meas"], obj_d, probe_d, corr_d, cfg, eng, variant=variant)
     else:
-        opt.problem, opt.geo, opt.measured, opt.cfg = problem, geo, st["meas"], cfg
+        opt.problem, opt.geo, opt.measured, opt.cfg, opt.variant = problem, geo, st["meas"], cfg, variant
         opt.obj, opt.probe, opt.corr = obj_d, probe_d, corr_d
     if empty:
         opt.reset()

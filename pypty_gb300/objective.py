@@ -5,12 +5,17 @@
 (``pypty/objective.py:967``). Installing it in place of the reference function
 (``pypty_gb300.shim.install``) lets ``pypty.iterative.run`` drive the GB300 kernels.
 
-Supported flag set: far-field propagation, ``propmethod="multislice"``, one slice distance,
-no tilts (``tilt_mode`` 0, zero tilt arrays), no phase plates, aberration arrays, probe
-markers, beam-current fluctuations, static background, data padding / binning / shifting /
-upsampling, compressed detectors or regularisers, algorithms ``lsq_sqrt``, ``ml``, ``lsq``,
-``lsq_sqrt_2``. Any other combination raises ``NotImplementedError`` naming the flag: the
-product path never falls back to a CPU implementation.
+Supported flag set: ``propmethod="multislice"``, one slice distance, algorithms ``lsq_sqrt``,
+``ml``, ``lsq``, ``lsq_sqrt_2`` on the fused path; with any of far-field or near-field
+propagation (one defocus, ``Cs``; ``pypty/objective.py:504-508``), the compressed-detector
+algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations and their
+gradient, aberration arrays with markers and their gradient, or one inside beam tilt
+(``tilt_mode`` 0, one tilt row, no tilt refinement) on the variants path
+(``pty_loss_and_direction_variants``). No phase plates, probe markers, static background,
+data padding / binning / shifting / upsampling, near-field ``alpha_near_field`` (the
+reference raises on it) or regularisers. Any other combination raises
+``NotImplementedError`` naming the flag: the product path never falls back to a CPU
+implementation.
 """
 from __future__ import annotations
 
@@ -70,18 +75,32 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                        wedge_mu, beta_wedge, probe_mod_reg_weight, probe_mod_tol, smart_memory, print_flag,
                        data_simulation_flag, data_simulation_exitwave, use_padded_intensity):
     """Check the arguments of ``loss_and_direction`` against the supported flag set and
-    build the C-ABI problem and scan geometry: returns (problem, geometry).
-    ``NotImplementedError`` names the first unsupported flag."""
-    _unsupported(recon_type != "far_field", "recon_type=%r" % (recon_type,))
+    build the C-ABI problem and scan geometry: returns (problem, geometry, variant) where
+    variant is None for the fused far-field path, else the keyword arguments of
+    ``Engine.loss_and_direction_variants``. ``NotImplementedError`` names the first
+    unsupported flag."""
+    _unsupported(recon_type not in _lib.RECON_TYPES, "recon_type=%r" % (recon_type,))
     _unsupported(propmethod != "multislice", "propmethod=%r" % (propmethod,))
-    _unsupported(algorithm_type not in _lib.ALGORITHMS, "algorithm_type=%r" % (algorithm_type,))
+    compressed = algorithm_type in _lib.COMPRESSED_ALGORITHMS
+    _unsupported(algorithm_type not in _lib.ALGORITHMS and not compressed, "algorithm_type=%r" % (algorithm_type,))
+    _unsupported(compressed and masks is None, "compressed algorithms without masks")
     _unsupported(bool(this_step_tilts) or tilt_mode not in (0, None), "beam tilts (tilt_mode/this_step_tilts)")
-    _unsupported(not _is_zero(this_tilt_array) or not _is_zero(this_tilts_correction), "nonzero beam tilts")
+    tilts = np.asarray(_to_numpy(this_tilt_array), dtype=np.float64)
+    if not _is_zero(this_tilts_correction):
+        tilts = tilts + np.asarray(_to_numpy(this_tilts_correction), dtype=np.float64)
+    _unsupported(tilts.ndim != 2 or (tilts.shape[0] != 1 and not _is_zero(tilts)),
+                 "per-position beam tilts")          # objective.py:339-345: one tilt row only
+    tan_y, tan_x = (float(tilts[0, 2]), float(tilts[0, 3])) if tilts.size else (0.0, 0.0)
     _unsupported(np.asarray(_to_numpy(this_distances)).reshape(-1).shape[0] != 1, "per-slice distances")
     _unsupported(phase_plate_in_h5 is not None, "phase plates")
-    _unsupported(aberration_marker is not None or bool(this_step_aberrations_array), "aberration arrays")
     _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
-    _unsupported(beam_current is not None or bool(this_beam_current_step), "beam-current fluctuations")
+    near = recon_type == "near_field"
+    if near:
+        _unsupported(np.asarray(_to_numpy(defocus_array)).reshape(-1).shape[0] != 1, "per-position defocus")
+        _unsupported(float(alpha_near_field) > 0, "alpha_near_field > 0 (the reference raises on it)")
+    _unsupported(aberrations_array is not None and aberration_marker is None, "aberrations without markers")
+    _unsupported(bool(this_step_aberrations_array) and aberrations_array is None, "aberration steps without arrays")
+    _unsupported(bool(this_beam_current_step) and beam_current is None, "beam-current steps without currents")
     _unsupported(static_background is not None and not _is_zero(static_background), "static background")
     _unsupported(bool(this_step_static_background), "static-background refinement")
     _unsupported(int(data_pad) != 0 or int(data_bin) != 1 or int(upsample_pattern) != 1,
@@ -116,7 +135,18 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         smooth_rolloff=float(smooth_rolloff), loss_weight=float(this_loss_weight),
         compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
         step_pos=bool(this_step_pos_correction))
-    return problem, geo
+    variant = None
+    if near or compressed or beam_current is not None or aberrations_array is not None or tan_x or tan_y:
+        variant = dict(recon_type=recon_type,
+                       defocus=float(np.asarray(_to_numpy(defocus_array)).reshape(-1)[0]) if near else 0.0,
+                       cs=float(Cs) if near else 0.0, tan_x=tan_x, tan_y=tan_y,
+                       masks=None if not compressed else _to_numpy(masks),
+                       beam_current=None if beam_current is None else _to_numpy(beam_current),
+                       step_beam_current=bool(this_beam_current_step),
+                       aberrations=None if aberrations_array is None else _to_numpy(aberrations_array),
+                       aberration_marker=None if aberration_marker is None else _to_numpy(aberration_marker),
+                       step_aberrations=bool(this_step_aberrations_array))
+    return problem, geo, variant
 
 
 def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
@@ -144,7 +174,7 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     when the object was given as a NumPy array, else as CUDA tensors.
     """
     args = dict(locals())
-    problem, geo = prepare(**args)
+    problem, geo, variant = prepare(**args)
     obj_is_numpy = not isinstance(this_obj, torch.Tensor)
     in_dtype = this_obj.dtype
     eng = default_engine()
@@ -152,7 +182,24 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     obj_d = _device_tensor(this_obj, torch.complex64, dev)
     probe_d = _device_tensor(full_probe, torch.complex64, dev)
     meas_d = _device_tensor(measured_array, torch.float32, dev)
-    loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
+    bc_grad, ab_grad = 0, 0
+    if variant is None:
+        loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
+    else:
+        kw = dict(variant)
+        for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
+                      ("aberration_marker", torch.int32)):
+            if kw[k] is not None:
+                kw[k] = _device_tensor(kw[k], dt, dev)
+        loss_sse, og, pg, posg, bcg, abg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo, meas_d,
+                                                                           **kw)
+        # zero-initialised accumulators of the reference (objective.py:381-382)
+        if beam_current is not None:
+            bc_grad = np.zeros_like(_to_numpy(beam_current)) if bcg is None else \
+                bcg.cpu().numpy().astype(_to_numpy(beam_current).dtype, copy=False)
+        if aberrations_array is not None:
+            ab_grad = np.zeros_like(_to_numpy(aberrations_array)) if abg is None else \
+                abg.cpu().numpy().astype(_to_numpy(aberrations_array).dtype, copy=False)
     ls = loss_sse.cpu().numpy()
     loss, sse = float(ls[0]), float(ls[1])
     if loss != loss:
@@ -160,7 +207,6 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     if not this_step_probe:
         pg = torch.zeros((1,) + tuple(pg.shape), dtype=pg.dtype, device=pg.device)  # objective.py:747-751
     tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))
-    aberr_grad = 0 if aberrations_array is None else np.zeros_like(_to_numpy(aberrations_array))
     constraints = np.zeros(N_CONSTRAINTS)
     if obj_is_numpy:
         og_out = og.cpu().numpy().astype(in_dtype, copy=False)
@@ -168,4 +214,4 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         posg_out = posg.cpu().numpy().astype(np.asarray(_to_numpy(this_pos_correction)).dtype, copy=False)
     else:
         og_out, pg_out, posg_out = og, pg, posg
-    return loss, sse, og_out, pg_out, posg_out, tilts_grad, 0, aberr_grad, 0, constraints
+    return loss, sse, og_out, pg_out, posg_out, tilts_grad, 0, ab_grad, bc_grad, constraints

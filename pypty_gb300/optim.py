@@ -151,8 +151,12 @@ class LBFGS:
     HMAX = 64
 
     def __init__(self, problem: _lib.Problem, geometry: Geometry, measured: torch.Tensor, obj: torch.Tensor,
-                 probe: torch.Tensor, corr: torch.Tensor, config: LineSearchConfig, engine: Engine | None = None):
+                 probe: torch.Tensor, corr: torch.Tensor, config: LineSearchConfig, engine: Engine | None = None,
+                 variant: dict | None = None):
         self.eng = engine or default_engine(obj.device)
+        # keyword arguments of Engine.loss_and_direction_variants (near field, compressed
+        # detectors, beam current, aberration plates, inside tilt), or None for the fused path
+        self.variant = variant
         self.problem, self.geo, self.measured = problem, geometry, measured
         self.obj, self.probe, self.corr = obj, probe, corr
         self.cfg = config
@@ -217,6 +221,9 @@ class LBFGS:
         p = self.problem
         out = (torch.empty(2, dtype=torch.float64, device=self.eng.device), torch.empty_like(obj),
                torch.empty_like(probe), torch.empty((p.n_positions, 2), dtype=torch.float32, device=self.eng.device))
+        if self.variant is not None:
+            return self.eng.loss_and_direction_variants(p, obj, probe, self.geo, self.measured, pos_correction=corr,
+                                                        **self.variant)[:4]
         loss_sse, og, pg, posg = self.eng.loss_and_direction(p, obj, probe, self.geo, self.measured, out=out,
                                                              pos_correction=corr)
         return loss_sse, og, pg, posg

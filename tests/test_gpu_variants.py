@@ -144,3 +144,75 @@ def test_variants_reject_bad_arguments():
         eng.loss_and_direction_variants(prob, obj, probe, geo, meas[:, :3].contiguous(), masks=masks)
     with pytest.raises(NotImplementedError):
         eng.loss_and_direction_variants(prob, obj, probe, geo, meas, masks=masks, recon_type="fresnel")
+
+
+@pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64"])
+def test_reference_signature_call_routes_variants(name):
+    """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
+    variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
+    index 7 and of the beam current at index 8 (objective.py:967)."""
+    from pypty_gb300 import objective
+    from test_host_logic import base_kwargs
+    c = load_variant_case(name)
+    tilts = np.zeros((1, 6), np.float32)
+    tilts[0, 2], tilts[0, 3] = c["tan_y"], c["tan_x"]
+    kw = base_kwargs(
+        this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
+        this_pos_correction=c["pos_correction"], this_tilt_array=tilts, this_tilts_correction=np.zeros_like(tilts),
+        this_distances=np.array([c["distance"]], np.float32), edge_slice_thickness_multiplier=c["edge_mult"],
+        measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=np.float32(c["wavelength"]),
+        this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
+        masks=c["masks"], pixel_size_x_A=np.float32(c["px"]), pixel_size_y_A=np.float32(c["px"]),
+        recon_type=c["recon_type"], Cs=np.float32(c["cs"]), defocus_array=np.array([c["defocus"]], np.float32),
+        damping_cutoff_multislice=np.float32(c["cutoff"]), smooth_rolloff=np.float32(c["rolloff"]),
+        this_chopped_sequence=c["sequence"], this_loss_weight=c["loss_weight"], compute_batch=c["batch"],
+        aberration_marker=c["aberration_marker"], aberrations_array=c["aberrations"], beam_current=c["beam_current"],
+        this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"])
+    out = objective.loss_and_direction(**kw)
+    assert len(out) == 10
+    lt, gt = TOL.get(c["algorithm"], (1e-5, 1e-4))
+    assert abs(out[0] - float(c["ref_loss"])) <= 2 * lt * abs(float(c["ref_loss"]))
+    assert rel_l2(out[2], c["ref_object_grad"]) <= 2 * gt
+    assert rel_l2(out[3], np.asarray(c["ref_probe_grad"]).reshape(out[3].shape)) <= 2 * gt
+    if c["step_pos"]:
+        assert rel_l2(out[4], c["ref_pos_grad"]) <= 2 * gt
+    if c["step_ab"]:
+        assert rel_l2(out[7], c["ref_aberrations_grad"]) <= 2 * gt
+    if c["step_bc"]:
+        assert rel_l2(out[8], c["ref_beam_current_grad"]) <= 2 * gt
+
+
+def test_lbfgs_runs_on_the_variants_path():
+    """The device-resident L-BFGS with a variants loss (near field, inside tilt): its first
+    loss is the variants entry's at the pre-cleaned start, and accepted steps lower it."""
+    import torch
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    from pypty_gb300.optim import LBFGS, LineSearchConfig
+    c = load_variant_case("near_c64")
+    # the full-object band limit of the optimizer wants power-of-two extents: pad with vacuum
+    o = np.ones((128, 128) + c["obj"].shape[2:], np.complex64)
+    o[:112, :112] = c["obj"]
+    c["obj"] = o
+    dev = torch.device("cuda", 0)
+    eng = Engine(dev)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    prob = make_problem(64, c["obj"].shape, c["probe"].shape[2], geo, algorithm=c["algorithm"],
+                        wavelength=float(np.float32(c["wavelength"])), pixel_size_x=float(np.float32(c["px"])),
+                        pixel_size_y=float(np.float32(c["px"])), slice_distance=c["distance"],
+                        compute_batch=c["batch"], step_pos=True)
+    variant = dict(recon_type="near_field", defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"])
+    meas = torch.from_numpy(c["measured"].astype(np.float32)).to(dev)
+    obj = torch.from_numpy(c["obj"].astype(np.complex64)).to(dev)
+    probe = torch.from_numpy(c["probe"].astype(np.complex64)).to(dev)
+    corr = torch.from_numpy(c["pos_correction"].astype(np.float32)).to(dev)
+    first = float(eng.loss_and_direction_variants(prob, obj, probe, geo, meas, **variant)[0][0])
+    opt = LBFGS(prob, geo, meas, obj, probe, corr, LineSearchConfig(update_pos=True), eng, variant=variant)
+    losses = []
+    step = 1e-6
+    for _ in range(5):
+        r = opt.step(step)
+        step = r.actual_step
+        losses.append(r.total_loss)
+    # the start point is band-limited first (iterative.py:497-514): a small change of the loss
+    assert abs(losses[0] - first) <= 1e-2 * abs(first)
+    assert all(np.isfinite(losses)) and losses[-1] < losses[0]

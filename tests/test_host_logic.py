@@ -38,10 +38,13 @@ def base_kwargs(**over):
 
 
 @pytest.mark.parametrize("over", [
-    dict(recon_type="near_field"), dict(propmethod="yoshida"), dict(algorithm_type="lsq_compressed"),
-    dict(this_step_tilts=1), dict(tilt_mode=3), dict(this_tilt_array=np.ones((1, 6), np.float32)),
+    dict(recon_type="fresnel"), dict(recon_type="near_field", alpha_near_field=0.1),
+    dict(recon_type="near_field", defocus_array=np.array([1.0, 2.0])), dict(propmethod="yoshida"),
+    dict(algorithm_type="lsq_compressed"), dict(algorithm_type="huber"),
+    dict(this_step_tilts=1), dict(tilt_mode=3), dict(this_tilt_array=np.ones((2, 6), np.float32)),
     dict(this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
-    dict(probe_marker=np.zeros(2, int)), dict(beam_current=np.ones(2)), dict(data_pad=4),
+    dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
+    dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_pad=4),
     dict(upsample_pattern=2), dict(atv_weight=0.1), dict(static_background=np.ones((64, 64))),
     dict(data_simulation_flag="sim.npy"),
 ])
@@ -121,3 +124,27 @@ def test_bfgs_update_unsupported_options_raise_before_any_gpu_work(flag):
     kw[flag] = 1
     with pytest.raises(NotImplementedError):
         iterative.bind(ns)(**kw)
+
+
+def test_variant_flags_route_to_the_variants_path():
+    """Near field, compressed detectors, beam current, aberration plates and one inside tilt
+    select pty_loss_and_direction_variants with the reference's values."""
+    kw = base_kwargs(recon_type="near_field", defocus_array=np.array([55.0], np.float32), Cs=np.float32(2e5))
+    _, _, v = objective.prepare(**kw)
+    assert v["recon_type"] == "near_field" and v["defocus"] == 55.0 and v["cs"] == 2e5
+    tilt = np.zeros((1, 6), np.float32)
+    tilt[0, 2], tilt[0, 3] = -1e-3, 2e-3
+    corr = np.zeros((1, 6), np.float32)
+    corr[0, 3] = 1e-3
+    _, _, v = objective.prepare(**base_kwargs(this_tilt_array=tilt, this_tilts_correction=corr))
+    assert v["tan_y"] == pytest.approx(-1e-3) and v["tan_x"] == pytest.approx(3e-3)   # tilt + correction
+    masks = np.ones((3, 64, 64), np.float32)
+    _, _, v = objective.prepare(**base_kwargs(algorithm_type="poisson_compressed", masks=masks,
+                                              measured_array=np.zeros((2, 3), np.float32)))
+    assert v["masks"].shape == (3, 64, 64)
+    _, _, v = objective.prepare(**base_kwargs(beam_current=np.ones(2, np.float32), this_beam_current_step=1,
+                                              aberrations_array=np.zeros((1, 4), np.float32),
+                                              aberration_marker=np.zeros(2, int), this_step_aberrations_array=1))
+    assert v["step_beam_current"] and v["step_aberrations"] and v["aberrations"].shape == (1, 4)
+    p, _, v = objective.prepare(**base_kwargs())
+    assert v is None and p.algorithm == _lib.ALGORITHMS["lsq_sqrt"]
