@@ -425,7 +425,9 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
         return ((sbits[q * T + t] >> i) & 1u) ? cmul(spy[ky], spx[kx]) : make_float2(0.f, 0.f);
       });
     } else {
-      if (do_fwd) WinFFT256::cross(v, s.xbuf, cl, c);
+      // outside the propagation steps only the far field (forward) transforms forward: the
+      // adjoint instance carries no copy of that butterfly
+      if (FWD && do_fwd) WinFFT256::cross(v, s.xbuf, cl, c);
       if (ADJ && stage == A_START) {
         // dL/dPsi = dL/dI * Psi * w (objective.py:595-597)
         ld_native<128>(part(a.psi, (size_t)b * nmodes + kidx), v);
