@@ -259,6 +259,16 @@ typedef struct pty_variant {
   const int32_t* aberration_marker;
   int32_t step_aberrations;
   float* aberrations_grad;
+  /* per-batch measured-data preprocessing (pypty/utils.py:626-652 as objective.py:411-412
+     calls it; not for the compressed losses): the measured patterns are
+     (W - 2 data_pad)^2, rolled by (shift_y, shift_x) with the reference's zeroed rows and
+     columns, scaled by data_multiplier, then zero-padded to W (use_padded_intensity != 0) or
+     compared with the model pattern cropped by data_pad (use_padded_intensity == 0,
+     objective.py:516-517, 592-593) */
+  int32_t data_pad;
+  int32_t use_padded_intensity;
+  int32_t shift_y, shift_x;
+  float data_multiplier;   /* 0 is read as 1: a zero-initialised struct leaves the data unscaled */
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

@@ -6,7 +6,10 @@ tilt.
 TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): this module checks the CUDA path; it
 is never part of it.
 
-Flag set (beyond ``ptycho_oracle``'s): ``recon_type`` "far_field" or "near_field" with one
+Flag set (beyond ``ptycho_oracle``'s): the per-batch measured-data preprocessing of
+``objective.py:411-412`` (shift vector, multiplier, zero padding by ``data_pad`` with
+``use_padded_intensity``, or the cropped model pattern without it, ``objective.py:516-517,
+592-593``); ``recon_type`` "far_field" or "near_field" with one
 defocus (``is_single_defocus``) and spherical aberration ``Cs`` (``objective.py:504-508,
 598-604``); algorithms
 ``lsq_compressed``, ``gauss_compressed`` and ``poisson_compressed`` with detector masks
@@ -105,12 +108,35 @@ def compressed_terms(pattern, measured, masks, algorithm):
     raise ValueError("unsupported compressed algorithm %r" % algorithm)
 
 
+def preprocess_measured(dataset, data_shift_vector, data_multiplier, data_pad):
+    """``utils.py:626-652`` ``preprocess_dataset`` as ``objective.py:411-412`` calls it per
+    batch (not compressed, ``force_pad``, no binning): roll by the shift vector and zero the
+    rows / columns the reference zeroes, scale, zero-pad."""
+    s0, s1 = int(data_shift_vector[0]), int(data_shift_vector[1])
+    if s0 != 0:
+        dataset = np.roll(dataset, s0, axis=1)
+        if s0 > 0:
+            dataset[:, -s0:, :] = 0
+        else:
+            dataset[:, :-s0, :] = 0
+    if s1 != 0:
+        dataset = np.roll(dataset, s1, axis=2)
+        if s1 > 0:
+            dataset[:, :, -s1:] = 0
+        else:
+            dataset[:, :, :-s1] = 0
+    if data_multiplier != 1:
+        dataset = dataset * data_multiplier
+    return np.pad(dataset, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
+
+
 def loss_and_direction_variants(obj, probe, positions, pos_correction, distance, edge_mult, measured, algorithm,
                                 wavelength, step_probe, step_obj, step_pos, pixel_size_x, pixel_size_y,
                                 damping_cutoff, smooth_rolloff, sequence, loss_weight, compute_batch,
                                 recon_type="far_field", defocus=0.0, cs=0.0, alpha_near_field=0.0, tan_x=0.0,
                                 tan_y=0.0, masks=None, beam_current=None, step_beam_current=0, aberrations=None,
-                                aberration_marker=None, step_aberrations=0, float_dtype=np.float32,
+                                aberration_marker=None, step_aberrations=0, data_pad=0, use_padded_intensity=True,
+                                data_shift_vector=(0, 0), data_multiplier=1.0, float_dtype=np.float32,
                                 complex_dtype=np.complex64, simulate=False):
     """Restatement of ``pypty/objective.py:47-967`` for the flag set in the module docstring.
 
@@ -118,7 +144,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     aberrations_grad); the last two are 0 when the feature is off (as the reference's
     zero-initialised accumulators, ``objective.py:381-382``). ``simulate=True`` returns the
     model patterns (len(sequence), W, W) or, for compressed algorithms, the coefficients
-    (len(sequence), n_masks).
+    (len(sequence), n_masks); with ``data_pad`` the patterns are cropped to the measured
+    (W - 2 data_pad)² detector.
     """
     f = float_dtype
     obj = np.asarray(obj, dtype=complex_dtype)
@@ -144,6 +171,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         aberrations = np.asarray(aberrations, dtype=f)
         polys = aberration_polynomials(qx, qy, aberrations.shape[1], lam, complex_dtype)
         plates = np.exp(np.sum(polys[None] * aberrations[:, :, None, None], 1)) * mask
+    if compressed and data_pad != 0:
+        raise ValueError("data_pad with compressed detectors: the masks would need the cropped shape")
     if near:                                                            # objective.py:505, 516
         dfc = f(defocus)
         ctf = (np.exp(-3.141592654j * (((lam * q2 + 2 * (qx * tx + qy * ty)) * dfc)
@@ -195,13 +224,19 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
             wave = shift_fft2(exit_wave, axes=(1, 2)) * mask_s[None, :, :, None, None]
         pattern = np.abs(wave) ** 2
         pattern = pattern[:, :, :, 0, 0] if coherent else np.mean(pattern, (-1, -2))
+        if data_pad != 0 and not use_padded_intensity:                 # objective.py:516-517
+            pattern = pattern[:, data_pad:-data_pad, data_pad:-data_pad]
         if simulate:
+            if data_pad != 0 and use_padded_intensity:
+                pattern = pattern[:, data_pad:-data_pad, data_pad:-data_pad]
             if compressed:
                 sim.append(np.sum(pattern[:, None] * masks[None], axis=(2, 3)))
             else:
                 sim.append(pattern)
             continue
-        meas = np.array(measured[tcs])
+        meas = 1 * np.asarray(measured)[tcs]
+        if not compressed:                                              # objective.py:411-412
+            meas = preprocess_measured(meas, data_shift_vector, data_multiplier, data_pad * use_padded_intensity)
         if compressed:
             l_b, s_b, dldi = compressed_terms(pattern, meas, masks, algorithm)
         else:
@@ -210,6 +245,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         sse = sse + s_b
         if not coherent:
             dldi = dldi / (Mp * Mo)                                     # objective.py:586-587
+        if not use_padded_intensity and data_pad != 0:                  # objective.py:592-593
+            dldi = np.pad(dldi, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
         if near:                                                        # objective.py:598-604
             dwave = wave * np.expand_dims(dldi, (-1, -2))
             fwg = loss_weight * fft2(dwave, axes=(1, 2)) * np.conjugate(ctf)

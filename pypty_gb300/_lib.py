@@ -56,7 +56,9 @@ class Variant(ctypes.Structure):
                 ("step_beam_current", ctypes.c_int32), ("beam_current_grad", ctypes.c_void_p),
                 ("n_aberrations", ctypes.c_int32), ("n_aberration_sets", ctypes.c_int32),
                 ("aberrations", ctypes.c_void_p), ("aberration_marker", ctypes.c_void_p),
-                ("step_aberrations", ctypes.c_int32), ("aberrations_grad", ctypes.c_void_p)]
+                ("step_aberrations", ctypes.c_int32), ("aberrations_grad", ctypes.c_void_p),
+                ("data_pad", ctypes.c_int32), ("use_padded_intensity", ctypes.c_int32),
+                ("shift_y", ctypes.c_int32), ("shift_x", ctypes.c_int32), ("data_multiplier", ctypes.c_float)]
 
 
 class PtyError(RuntimeError):

@@ -357,18 +357,48 @@ __global__ void var_intensity_kernel(const float2* __restrict__ field, const flo
   ibuf[(size_t)b * WW + pix] = I;
 }
 
-// per-pixel losses (objective.py:527-559) on the pattern: ibuf <- dL/dI / nm, FP64 partial
-// sums per position   grid Bn, block 1024
+// measured-data preprocessing applied on the fly (pypty/utils.py:626-652): the measured
+// patterns are Wm x Wm (Wm = W - 2 pad), rolled by (sy, sx) with the rows / columns the
+// reference zeroes, scaled by mult, then either zero-padded to W (padded) or compared with
+// the model pattern cropped by pad
+struct MeasPrep {
+  int W, pad, padded, sy, sx;
+  float mult;
+};
+
+// source index along one axis of the rolled Wm-long measured axis, or -1 for a zeroed entry
+// (np.roll then a[-s:] = 0 for s > 0, a[:-s] = 0 for s < 0)
+__device__ __forceinline__ int rolled(int i, int s, int n) {
+  if ((s > 0 && i >= n - s) || (s < 0 && i < -s)) return -1;
+  int j = (i - s) % n;
+  return j < 0 ? j + n : j;
+}
+
+// per-pixel losses (objective.py:527-559) on the pattern: ibuf <- dL/dI / nm (zero outside a
+// cropped pattern), FP64 partial sums per position   grid Bn, block 1024
 __global__ void __launch_bounds__(1024) var_pixel_loss_kernel(float* __restrict__ ibuf, const float* __restrict__ measured,
-                                                              const int* __restrict__ seq, int WW, int nm, int alg,
+                                                              const int* __restrict__ seq, MeasPrep mp, int nm, int alg,
                                                               double* __restrict__ loss_part) {
   __shared__ double red[64];
   const int b = blockIdx.x;
-  const float* meas = measured + (size_t)seq[b] * WW;
+  const int W = mp.W, WW = W * W, Wm = W - 2 * mp.pad;
+  const float* meas = measured + (size_t)seq[b] * Wm * Wm;
   float* I = ibuf + (size_t)b * WW;
   double lsum = 0.0, ssum = 0.0;
   for (int u = threadIdx.x; u < WW; u += blockDim.x) {
-    float d = loss_pixel(alg, I[u], meas[u], lsum, ssum);
+    const int y = u / W - mp.pad, x = u % W - mp.pad;
+    const bool inside = y >= 0 && y < Wm && x >= 0 && x < Wm;
+    if (!inside && !mp.padded) {   // cropped model pattern: no loss, dL/dI padded with zeros
+      I[u] = 0.0f;
+      continue;
+    }
+    float Mv = 0.0f;
+    if (inside) {
+      const int ry = rolled(y, mp.sy, Wm), rx = rolled(x, mp.sx, Wm);
+      if (ry >= 0 && rx >= 0) Mv = meas[ry * Wm + rx];
+      if (mp.mult != 1.0f) Mv = Mv * mp.mult;
+    }
+    float d = loss_pixel(alg, I[u], Mv, lsum, ssum);
     if (nm > 1) d = d / (float)nm;
     I[u] = d;
   }
@@ -938,7 +968,9 @@ struct Run {
       var_closs_kernel<<<Bn, 32, 0, st>>>(coef, measured, seq_b, q.nmask, p->algorithm, dco, lpart);
       var_cdldi_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(ibuf, v->masks, dco, WW, q.nmask, nm);
     } else {
-      var_pixel_loss_kernel<<<Bn, 1024, 0, st>>>(ibuf, measured, seq_b, WW, nm, p->algorithm, lpart);
+      MeasPrep mp{W, v->data_pad, v->use_padded_intensity != 0, v->shift_y, v->shift_x,
+                  v->data_multiplier == 0.0f ? 1.0f : v->data_multiplier};
+      var_pixel_loss_kernel<<<Bn, 1024, 0, st>>>(ibuf, measured, seq_b, mp, nm, p->algorithm, lpart);
     }
     var_apply_kernel<<<grid(nm, Bn), EB, 0, st>>>(field, ibuf, ta.mask, W, nm, q.near, p->loss_weight * (float)WW);
     if (q.near) {   // dL/d(exit) = IFFT(loss_weight FFT(wave dL/dI) conj(CTF)) (objective.py:602-604)
@@ -1013,6 +1045,8 @@ int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
   int rc = validate(&base);
   if (rc) return rc;
   if (v->recon_type != 0 && v->recon_type != 1) return PTY_ERR_UNSUPPORTED;
+  if (v->data_pad < 0 || 2 * v->data_pad >= p->window) return PTY_ERR_INVALID;
+  if (compressed && v->data_pad != 0) return PTY_ERR_UNSUPPORTED;
   if (compressed && (v->n_masks <= 0 || !v->masks)) return PTY_ERR_INVALID;
   if (v->beam_current && v->step_beam_current && !v->beam_current_grad) return PTY_ERR_INVALID;
   if (v->aberrations) {

@@ -181,12 +181,16 @@ class Engine:
                                     masks: torch.Tensor | None = None, beam_current: torch.Tensor | None = None,
                                     step_beam_current: bool = False, aberrations: torch.Tensor | None = None,
                                     aberration_marker: torch.Tensor | None = None, step_aberrations: bool = False,
+                                    data_pad: int = 0, use_padded_intensity: bool = True,
+                                    data_shift_vector=(0, 0), data_multiplier: float = 1.0,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
 
-        measured is (n_positions, W, W) float32, or (n_positions, n_masks) for the compressed
-        algorithms; masks (n_masks, W, W) float32 in pattern order; beam_current
+        measured is (n_positions, W - 2 data_pad, W - 2 data_pad) float32 (device memory, or
+        pinned host memory read in place), or (n_positions, n_masks) for the compressed
+        algorithms; data_pad / use_padded_intensity / data_shift_vector / data_multiplier are
+        the reference's per-batch measured-data preprocessing, applied on the fly; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
         (n_positions,) int32; pos_correction as in ``loss_and_direction``. Returns (loss_sse,
         object_grad, probe_grad, pos_grad, beam_current_grad or None, aberrations_grad or
@@ -194,11 +198,12 @@ class Engine:
         stream = stream or torch.cuda.current_stream(self.device)
         compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
         self._check_inputs(problem, obj, probe, None)
-        want = (problem.n_positions, masks.shape[0]) if compressed else \
-            (problem.n_positions, problem.window, problem.window)
-        if tuple(measured.shape) != want or measured.dtype != torch.float32 or not measured.is_cuda \
+        wm = problem.window - 2 * int(data_pad)
+        want = (problem.n_positions, masks.shape[0]) if compressed else (problem.n_positions, wm, wm)
+        if tuple(measured.shape) != want or measured.dtype != torch.float32 or not _readable(measured) \
                 or not measured.is_contiguous():
-            raise ValueError("measured must be a contiguous float32 CUDA tensor of shape %s" % (want,))
+            raise ValueError("measured must be a contiguous float32 CUDA or pinned host tensor of shape %s"
+                             % (want,))
         if recon_type not in _lib.RECON_TYPES:
             raise NotImplementedError("recon_type %r" % recon_type)
         keep = []
@@ -235,7 +240,10 @@ class Engine:
                          aberrations=None if ab_d is None else ab_d.data_ptr(),
                          aberration_marker=None if mk_d is None else mk_d.data_ptr(),
                          step_aberrations=int(ab_grad is not None),
-                         aberrations_grad=None if ab_grad is None else ab_grad.data_ptr())
+                         aberrations_grad=None if ab_grad is None else ab_grad.data_ptr(),
+                         data_pad=int(data_pad), use_padded_intensity=int(bool(use_padded_intensity)),
+                         shift_y=int(data_shift_vector[0]), shift_x=int(data_shift_vector[1]),
+                         data_multiplier=float(data_multiplier))
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")
@@ -359,9 +367,18 @@ class Engine:
                                      measured.dtype != torch.float32 or not measured.is_contiguous()):
             raise ValueError("measured must be a contiguous float32 tensor of shape %s" %
                              ((problem.n_positions, W, W),))
-        for t in (obj, probe) + ((measured,) if measured is not None else ()):
+        for t in (obj, probe):
             if not t.is_cuda:
                 raise ValueError("inputs must be CUDA tensors")
+        if measured is not None and not _readable(measured):
+            raise ValueError("measured must be a CUDA tensor or a pinned host tensor (read in place over "
+                             "the host link)")
+
+
+def _readable(t: torch.Tensor) -> bool:
+    """Device memory, or pinned host memory that the kernels read in place (the patterns of a
+    dataset larger than HBM streamed over the host link, no staging copy)."""
+    return t.is_cuda or (t.device.type == "cpu" and t.is_pinned())
 
 
 _ENGINES = {}

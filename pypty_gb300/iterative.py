@@ -146,7 +146,7 @@ def _impl(ns, a):
     st = _STATES.setdefault(id(ns), {"opt": None, "meas_src": None, "meas": None})
     meas_src = a["measured_array"]
     if st["meas_src"] is not meas_src:
-        st["meas"] = _to_device(meas_src, torch.float32, dev)
+        st["meas"] = objective.measured_tensor(meas_src, dev, bool(a["load_one_by_one"]))
         st["meas_src"] = meas_src
     obj_d = _to_device(ns.obj, torch.complex64, dev)
     probe_d = _to_device(ns.probe, torch.complex64, dev)

@@ -12,8 +12,11 @@ algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations 
 gradient, aberration arrays with markers and their gradient, or one inside beam tilt
 (``tilt_mode`` 0, one tilt row, no tilt refinement) on the variants path
 (``pty_loss_and_direction_variants``). No phase plates, probe markers, static background,
-data padding / binning / shifting / upsampling, near-field ``alpha_near_field`` (the
-reference raises on it) or regularisers. Any other combination raises
+data binning (the reference raises on it) or upsampling, near-field ``alpha_near_field``
+(the reference raises on it) or regularisers. The per-batch measured-data preprocessing
+(``data_pad`` with or without ``use_padded_intensity``, ``data_shift_vector``,
+``data_multiplier``) runs on the fly on the variants path; with ``load_one_by_one`` the
+patterns stay in pinned host memory and the kernels read them in place. Any other combination raises
 ``NotImplementedError`` naming the flag: the product path never falls back to a CPU
 implementation.
 """
@@ -54,6 +57,27 @@ def _device_tensor(a, dtype, device):
     if isinstance(a, torch.Tensor):
         return a.to(device=device, dtype=dtype).contiguous()
     return torch.from_numpy(np.ascontiguousarray(_to_numpy(a))).to(device=device, dtype=dtype)
+
+
+_PINNED = {}
+
+
+def measured_tensor(measured_array, device, load_one_by_one):
+    """The measured patterns as the kernels read them. With ``load_one_by_one`` (the
+    reference keeps the dataset in host memory and copies each batch, ``objective.py:398-409``)
+    a host array is pinned once and read in place by the kernels over the host link, so a
+    dataset larger than HBM needs no device copy; otherwise it is copied to the device."""
+    if isinstance(measured_array, torch.Tensor) and (measured_array.is_cuda or measured_array.is_pinned()):
+        return measured_array.to(torch.float32).contiguous()
+    if not load_one_by_one:
+        return _device_tensor(measured_array, torch.float32, device)
+    key = id(measured_array)
+    hit = _PINNED.get(key)
+    if hit is None or hit[0] is not measured_array:
+        host = np.ascontiguousarray(_to_numpy(measured_array), dtype=np.float32)
+        _PINNED.clear()                      # one dataset pinned at a time
+        _PINNED[key] = hit = (measured_array, torch.from_numpy(host).pin_memory())
+    return hit[1]
 
 
 def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt_array,
@@ -103,10 +127,11 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     _unsupported(bool(this_beam_current_step) and beam_current is None, "beam-current steps without currents")
     _unsupported(static_background is not None and not _is_zero(static_background), "static background")
     _unsupported(bool(this_step_static_background), "static-background refinement")
-    _unsupported(int(data_pad) != 0 or int(data_bin) != 1 or int(upsample_pattern) != 1,
-                 "data padding / binning / upsampling")
-    _unsupported(not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0,
-                 "data shift vectors or multipliers")
+    # the reference's binning loop indexes an undefined name (utils.py:643: i2), so it raises
+    _unsupported(int(data_bin) != 1, "data binning (the reference raises NameError on it)")
+    _unsupported(int(upsample_pattern) != 1, "upsample_pattern")
+    _unsupported(compressed and int(data_pad) != 0, "data_pad with compressed detectors")
+    prep = not compressed and (int(data_pad) != 0 or not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0)
     _unsupported(bool(data_simulation_flag), "data simulation output files")
     for name, w in [("fast_axis_reg_weight_positions", fast_axis_reg_weight_positions),
                     ("slow_axis_reg_weight_positions", slow_axis_reg_weight_positions),
@@ -136,7 +161,7 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
         step_pos=bool(this_step_pos_correction))
     variant = None
-    if near or compressed or beam_current is not None or aberrations_array is not None or tan_x or tan_y:
+    if near or compressed or prep or beam_current is not None or aberrations_array is not None or tan_x or tan_y:
         variant = dict(recon_type=recon_type,
                        defocus=float(np.asarray(_to_numpy(defocus_array)).reshape(-1)[0]) if near else 0.0,
                        cs=float(Cs) if near else 0.0, tan_x=tan_x, tan_y=tan_y,
@@ -145,7 +170,11 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                        step_beam_current=bool(this_beam_current_step),
                        aberrations=None if aberrations_array is None else _to_numpy(aberrations_array),
                        aberration_marker=None if aberration_marker is None else _to_numpy(aberration_marker),
-                       step_aberrations=bool(this_step_aberrations_array))
+                       step_aberrations=bool(this_step_aberrations_array),
+                       data_pad=0 if compressed else int(data_pad),
+                       use_padded_intensity=True if use_padded_intensity is None else bool(use_padded_intensity),
+                       data_shift_vector=(0, 0) if compressed else tuple(int(x) for x in data_shift_vector),
+                       data_multiplier=1.0 if compressed else float(data_multiplier))
     return problem, geo, variant
 
 
@@ -181,7 +210,7 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     dev = eng.device
     obj_d = _device_tensor(this_obj, torch.complex64, dev)
     probe_d = _device_tensor(full_probe, torch.complex64, dev)
-    meas_d = _device_tensor(measured_array, torch.float32, dev)
+    meas_d = measured_tensor(measured_array, dev, bool(load_one_by_one))
     bc_grad, ab_grad = 0, 0
     if variant is None:
         loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)

@@ -46,8 +46,9 @@ def ref_call(pypty, c):
         recon_type=c["recon_type"], Cs=f(c["cs"]), defocus_array=np.array([c["defocus"]], dtype=f),
         alpha_near_field=f(c["alpha"]), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
         propmethod="multislice", this_chopped_sequence=c["sequence"], load_one_by_one=False,
-        data_multiplier=f(1), data_pad=0, phase_plate_in_h5=None, this_loss_weight=c["loss_weight"], data_bin=1,
-        data_shift_vector=[0, 0], upsample_pattern=1, static_background=None, this_step_static_background=0,
+        data_multiplier=f(c["mult"]), data_pad=c["data_pad"], phase_plate_in_h5=None, this_loss_weight=c["loss_weight"],
+        data_bin=1, data_shift_vector=[c["shift0"], c["shift1"]], upsample_pattern=1, static_background=None,
+        this_step_static_background=0,
         tilt_mode=0, aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
         compute_batch=c["batch"], phase_only_obj=False, beam_current=bc,
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], default_float=f,
@@ -58,7 +59,7 @@ def ref_call(pypty, c):
         current_window=None, phase_norm_weight=0, abs_norm_weight=0, atv_weight=0, atv_q=1, atv_p=2,
         mixed_variance_weight=0, mixed_variance_sigma=0.5, wedge_mu=0, beta_wedge=0, probe_mod_reg_weight=0,
         probe_mod_tol=0.05, smart_memory=False, print_flag=0, data_simulation_flag=False,
-        data_simulation_exitwave=False, use_padded_intensity=True)
+        data_simulation_exitwave=False, use_padded_intensity=bool(c["use_padded"]))
     # outer return order (objective.py:967): aberrations gradient before beam-current gradient
     return res[0], res[1], res[2], res[3], res[4], res[8], res[7]
 
@@ -80,7 +81,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                alpha=25.0, probe_defocus=80.0, distance=2.0, edge_mult=1.0, cutoff=2 / 3, rolloff=0.0,
                loss_weight=1.0, step_probe=1, step_obj=1, step_pos=0, dose=1e4, double=False, recon_type="far_field",
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
-               n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False):
+               n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
+               mult=1.0):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
@@ -97,13 +99,17 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
     ab = (rng.normal(size=(n_ab_sets, n_abs)) * 20.0).astype(f) if n_ab_sets else None
     marker = (np.arange(N) % n_ab_sets).astype(np.int64) if n_ab_sets else None
     kw = dict(recon_type=recon_type, defocus=defocus, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
-              masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker)
+              masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
+              use_padded_intensity=use_padded)
     sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, distance, edge_mult, None, algorithm, lam,
                                           1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
     if n_masks:
         measured = (sim * (1.0 + 0.02 * rng.normal(size=sim.shape))).astype(f)
     else:
         measured = synth.poisson_patterns(sim, 1.0, rng).astype(f)
+        # stored so that the reference's per-batch shift and multiplier (objective.py:411)
+        # bring it back near the model
+        measured = (np.roll(measured, (-shift[0], -shift[1]), axis=(1, 2)) / mult).astype(f)
     obj0 = np.exp(0.5j * np.angle(truth)).astype(cx)
     probe0 = synth.make_probe(W, px, kV, alpha, probe_defocus + 15.0, Mp, [0.5, 0.3, 0.2][:Mp], dose, dtype=cx)
     if double:
@@ -114,7 +120,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 step_obj=step_obj, step_pos=step_pos, px=px, cutoff=cutoff, rolloff=rolloff,
                 sequence=np.arange(N), loss_weight=loss_weight, batch=batch, obj=obj0, probe=probe0,
                 recon_type=recon_type, defocus=defocus, cs=cs, alpha=alpha_nf, tan_x=tan_x, tan_y=tan_y, masks=masks,
-                beam_current=bc, step_bc=step_bc, aberrations=ab, aberration_marker=marker, step_ab=step_ab)
+                beam_current=bc, step_bc=step_bc, aberrations=ab, aberration_marker=marker, step_ab=step_ab,
+                data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult)
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -137,6 +144,12 @@ CASES = [
          n_abs=7, step_ab=1, integer_positions=True),
     dict(BASE, name="current_aberr_c128", seed=36, algorithm="ml", beam_current=True, step_bc=1, n_ab_sets=3,
          n_abs=7, step_ab=1, integer_positions=True, double=True),
+    # measured detector smaller than the window: zero-padded measurements, or the cropped model
+    # pattern (objective.py:411, 516-517, 592-593)
+    dict(BASE, name="pad_c64", seed=38, algorithm="ml", data_pad=6, step_pos=1),
+    dict(BASE, name="crop_c64", seed=39, algorithm="lsq_sqrt", data_pad=6, use_padded=0),
+    # the per-batch shift vector and multiplier of the measured patterns (utils.py:626-647)
+    dict(BASE, name="shift_mult_c64", seed=40, algorithm="lsq", shift=(2, -3), mult=1.5, Mp=1),
     # the same with sub-pixel shifts: the shift spectrum excludes the plates (objective.py:461, 471)
     dict(BASE, name="current_aberr_shift_c64", seed=37, algorithm="lsq_sqrt", beam_current=True, step_bc=1,
          n_ab_sets=2, n_abs=4, step_ab=1, step_pos=1),
@@ -157,7 +170,8 @@ def main():
             measured=c["measured"], sequence=c["sequence"],
             scalars=np.array([c["distance"], c["edge_mult"], c["wavelength"], c["px"], c["cutoff"], c["rolloff"],
                               c["loss_weight"], c["batch"], c["step_probe"], c["step_obj"], c["step_pos"],
-                              c["defocus"], c["cs"], c["alpha"], c["tan_x"], c["tan_y"], c["step_bc"], c["step_ab"]],
+                              c["defocus"], c["cs"], c["alpha"], c["tan_x"], c["tan_y"], c["step_bc"], c["step_ab"],
+                              c["data_pad"], c["use_padded"], c["shift0"], c["shift1"], c["mult"]],
                              dtype=np.float64),
             algorithm=np.array(c["algorithm"]), recon_type=np.array(c["recon_type"]), double=np.array(c["double"]),
             masks=none if c["masks"] is None else c["masks"],

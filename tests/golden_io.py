@@ -44,10 +44,12 @@ def load_variant_case(name):
     d = dict(np.load(os.path.join(GOLDEN_DIR, "variant_" + name + ".npz")))
     s = d["scalars"]
     keys = ["distance", "edge_mult", "wavelength", "px", "cutoff", "rolloff", "loss_weight", "batch", "step_probe",
-            "step_obj", "step_pos", "defocus", "cs", "alpha", "tan_x", "tan_y", "step_bc", "step_ab"]
+            "step_obj", "step_pos", "defocus", "cs", "alpha", "tan_x", "tan_y", "step_bc", "step_ab", "data_pad",
+            "use_padded", "shift0", "shift1", "mult"]
     for i, k in enumerate(keys):
         d[k] = float(s[i])
-    for k in ("batch", "step_probe", "step_obj", "step_pos", "step_bc", "step_ab"):
+    for k in ("batch", "step_probe", "step_obj", "step_pos", "step_bc", "step_ab", "data_pad", "use_padded", "shift0",
+              "shift1"):
         d[k] = int(d[k])
     d["algorithm"] = str(d["algorithm"])
     d["recon_type"] = str(d["recon_type"])

@@ -32,7 +32,9 @@ def run_gpu_variant(c, engine=None):
         defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"], masks=t(c["masks"], np.float32),
         beam_current=t(c["beam_current"], np.float32), step_beam_current=bool(c["step_bc"]),
         aberrations=t(c["aberrations"], np.float32),
-        aberration_marker=t(c["aberration_marker"], np.int32), step_aberrations=bool(c["step_ab"]))
+        aberration_marker=t(c["aberration_marker"], np.int32), step_aberrations=bool(c["step_ab"]),
+        data_pad=c.get("data_pad", 0), use_padded_intensity=bool(c.get("use_padded", 1)),
+        data_shift_vector=(c.get("shift0", 0), c.get("shift1", 0)), data_multiplier=c.get("mult", 1.0))
     torch.cuda.synchronize()
     ls = ls.cpu().numpy()
     cpu = lambda a: None if a is None else a.cpu().numpy()
@@ -48,8 +50,9 @@ def fp64_variant_oracle(c):
         recon_type=c["recon_type"], defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
         masks=None if c["masks"] is None else np.asarray(c["masks"], np.float64),
         beam_current=c["beam_current"], step_beam_current=c["step_bc"], aberrations=c["aberrations"],
-        aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], float_dtype=np.float64,
-        complex_dtype=np.complex128)
+        aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], data_pad=c["data_pad"],
+        use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]), data_multiplier=c["mult"],
+        float_dtype=np.float64, complex_dtype=np.complex128)
 
 
 def errors(res, ref):
@@ -146,7 +149,8 @@ def test_variants_reject_bad_arguments():
         eng.loss_and_direction_variants(prob, obj, probe, geo, meas, masks=masks, recon_type="fresnel")
 
 
-@pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64"])
+@pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64", "crop_c64",
+                                  "shift_mult_c64"])
 def test_reference_signature_call_routes_variants(name):
     """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
     variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
@@ -166,6 +170,8 @@ def test_reference_signature_call_routes_variants(name):
         recon_type=c["recon_type"], Cs=np.float32(c["cs"]), defocus_array=np.array([c["defocus"]], np.float32),
         damping_cutoff_multislice=np.float32(c["cutoff"]), smooth_rolloff=np.float32(c["rolloff"]),
         this_chopped_sequence=c["sequence"], this_loss_weight=c["loss_weight"], compute_batch=c["batch"],
+        data_pad=c["data_pad"], use_padded_intensity=bool(c["use_padded"]),
+        data_shift_vector=[c["shift0"], c["shift1"]], data_multiplier=np.float32(c["mult"]), load_one_by_one=True,
         aberration_marker=c["aberration_marker"], aberrations_array=c["aberrations"], beam_current=c["beam_current"],
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"])
     out = objective.loss_and_direction(**kw)
@@ -216,3 +222,35 @@ def test_lbfgs_runs_on_the_variants_path():
     # the start point is band-limited first (iterative.py:497-514): a small change of the loss
     assert abs(losses[0] - first) <= 1e-2 * abs(first)
     assert all(np.isfinite(losses)) and losses[-1] < losses[0]
+
+
+def test_pinned_host_measured_is_read_in_place():
+    """Patterns left in pinned host memory (a dataset larger than HBM) give the same result as
+    device-resident ones, on the fused and the variants paths."""
+    import torch
+    from golden_io import load_case
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    dev = torch.device("cuda", 0)
+    eng = Engine(dev)
+    for name in ("multislice_ml_c64", "w128_modes_c64"):
+        c = load_case(name)
+        geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+        W = c["probe"].shape[0]
+        prob = make_problem(W, c["obj"].shape, c["probe"].shape[2], geo, algorithm=c["algorithm"],
+                            wavelength=float(np.float32(c["wavelength"])), pixel_size_x=float(np.float32(c["px"])),
+                            pixel_size_y=float(np.float32(c["px"])), slice_distance=c["distance"],
+                            edge_mult=c["edge_mult"], compute_batch=c["batch"], step_pos=c["step_pos"])
+        obj = torch.from_numpy(c["obj"].astype(np.complex64)).to(dev)
+        probe = torch.from_numpy(c["probe"].astype(np.complex64)).to(dev)
+        host = torch.from_numpy(c["measured"].astype(np.float32)).pin_memory()
+        devm = host.to(dev)
+        a = [x.cpu().numpy() for x in eng.loss_and_direction(prob, obj, probe, geo, devm)]
+        b = [x.cpu().numpy() for x in eng.loss_and_direction(prob, obj, probe, geo, host)]
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+        a = eng.loss_and_direction_variants(prob, obj, probe, geo, devm, data_multiplier=1.25)
+        b = eng.loss_and_direction_variants(prob, obj, probe, geo, host, data_multiplier=1.25)
+        for x, y in zip(a[:4], b[:4]):
+            assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+    with pytest.raises(ValueError):   # pageable host memory is not readable by the kernels
+        eng.loss_and_direction(prob, obj, probe, geo, host.clone())

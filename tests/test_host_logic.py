@@ -44,7 +44,8 @@ def base_kwargs(**over):
     dict(this_step_tilts=1), dict(tilt_mode=3), dict(this_tilt_array=np.ones((2, 6), np.float32)),
     dict(this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
     dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
-    dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_pad=4),
+    dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_bin=2),
+    dict(algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32), data_pad=4),
     dict(upsample_pattern=2), dict(atv_weight=0.1), dict(static_background=np.ones((64, 64))),
     dict(data_simulation_flag="sim.npy"),
 ])
@@ -148,3 +149,11 @@ def test_variant_flags_route_to_the_variants_path():
     assert v["step_beam_current"] and v["step_aberrations"] and v["aberrations"].shape == (1, 4)
     p, _, v = objective.prepare(**base_kwargs())
     assert v is None and p.algorithm == _lib.ALGORITHMS["lsq_sqrt"]
+
+
+def test_measured_preprocessing_routes_to_the_variants_path():
+    _, _, v = objective.prepare(**base_kwargs(data_pad=4, use_padded_intensity=False,
+                                              measured_array=np.zeros((2, 56, 56), np.float32)))
+    assert v["data_pad"] == 4 and v["use_padded_intensity"] is False
+    _, _, v = objective.prepare(**base_kwargs(data_shift_vector=[1, -2], data_multiplier=2.0))
+    assert v["data_shift_vector"] == (1, -2) and v["data_multiplier"] == 2.0

@@ -16,7 +16,8 @@ def run_variant_oracle(c):
         defocus=c["defocus"], cs=c["cs"], alpha_near_field=c["alpha"], tan_x=c["tan_x"], tan_y=c["tan_y"],
         masks=c["masks"], beam_current=c["beam_current"], step_beam_current=c["step_bc"],
         aberrations=c["aberrations"], aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"],
-        float_dtype=f, complex_dtype=cx)
+        data_pad=c["data_pad"], use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]),
+        data_multiplier=f(c["mult"]), float_dtype=f, complex_dtype=cx)
 
 
 @pytest.mark.parametrize("name", variant_case_names())
