@@ -11,7 +11,7 @@ own multislice forward (``pty_simulate_patterns``) with Poisson noise.
 
 The network covers the object region the scan illuminates (``frame`` x ``frame`` pixels from the
 origin: scan extent plus one window); outside it the start stays flat. The flat start
-(``obj = ones``, ``pypty/iterative.py:131``) stays the fallback and the judge:
+(``obj = ones``, ``pypty/iterative.py:131``) stays the fallback and the yardstick:
 ``reconstruct`` runs the same GPU-resident L-BFGS loop (``optim.LBFGS``) from either start and
 records the phase RMSE against the ground truth after every epoch.
 """
