@@ -33,6 +33,7 @@ the plate's conjugate; and the gradient arrays come back in the reference's orde
 from __future__ import annotations
 
 import numpy as np
+import scipy.fft as sfft
 
 from .ptycho_oracle import (fft2, ifft2, ifft2_ishift, loss_terms, multislice, multislice_grads, propagator,
                             scatteradd, shift_fft2, shift_ramp_tables, spatial_frequencies)
@@ -130,22 +131,35 @@ def preprocess_measured(dataset, data_shift_vector, data_multiplier, data_pad):
     return np.pad(dataset, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
 
 
+def tilt_grids(W, pixel_size_x, pixel_size_y, wavelength, complex_dtype):
+    """Real-space tilt ramps of ``objective.py:303-307``: (y_grid, x_grid), each (W, W)
+    purely imaginary, 2*pi*i*W*px/lambda times the fftshifted frequencies (complex128, then the
+    complex dtype)."""
+    fx, fy = np.meshgrid(sfft.fftshift(sfft.fftfreq(W)), sfft.fftshift(sfft.fftfreq(W)), indexing="xy")
+    xg = (fx * 6.2831855j * W * pixel_size_x / wavelength).astype(complex_dtype)
+    yg = (fy * 6.2831855j * W * pixel_size_y / wavelength).astype(complex_dtype)
+    return yg, xg
+
+
 def loss_and_direction_variants(obj, probe, positions, pos_correction, distance, edge_mult, measured, algorithm,
                                 wavelength, step_probe, step_obj, step_pos, pixel_size_x, pixel_size_y,
                                 damping_cutoff, smooth_rolloff, sequence, loss_weight, compute_batch,
                                 recon_type="far_field", defocus=0.0, cs=0.0, alpha_near_field=0.0, tan_x=0.0,
                                 tan_y=0.0, masks=None, beam_current=None, step_beam_current=0, aberrations=None,
                                 aberration_marker=None, step_aberrations=0, data_pad=0, use_padded_intensity=True,
-                                data_shift_vector=(0, 0), data_multiplier=1.0, float_dtype=np.float32,
-                                complex_dtype=np.complex64, simulate=False):
+                                data_shift_vector=(0, 0), data_multiplier=1.0, tilts=None, tilt_mode=0,
+                                step_tilts=0, float_dtype=np.float32, complex_dtype=np.complex64, simulate=False):
     """Restatement of ``pypty/objective.py:47-967`` for the flag set in the module docstring.
 
-    Returns (loss, sse, object_grad, probe_grad, pos_grad, beam_current_grad,
-    aberrations_grad); the last two are 0 when the feature is off (as the reference's
-    zero-initialised accumulators, ``objective.py:381-382``). ``simulate=True`` returns the
-    model patterns (len(sequence), W, W) or, for compressed algorithms, the coefficients
-    (len(sequence), n_masks); with ``data_pad`` the patterns are cropped to the measured
-    (W - 2 data_pad)² detector.
+    tilts: (N_tilts, 6) rows [tan_y, tan_x] before / inside / after the specimen (the
+    reference's tilt array plus its correction; one row for all positions or one per position),
+    used by ``tilt_mode`` 0-4 (``objective.py:302-345, 464-499``); without it one inside tilt
+    (tan_x, tan_y). Returns (loss, sse, object_grad, probe_grad, pos_grad, beam_current_grad,
+    aberrations_grad, tilts_grad); the beam-current and aberration gradients are 0 when the
+    feature is off (the reference's zero-initialised accumulators, ``objective.py:381-382``).
+    ``simulate=True`` returns the model patterns (len(sequence), W, W) or, for compressed
+    algorithms, the coefficients (len(sequence), n_masks); with ``data_pad`` the patterns are
+    cropped to the measured (W - 2 data_pad)² detector.
     """
     f = float_dtype
     obj = np.asarray(obj, dtype=complex_dtype)
@@ -159,9 +173,23 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     lam = f(wavelength)
     q2, qx, qy, mask_s, mask = spatial_frequencies(px, py, W, f(damping_cutoff), f(smooth_rolloff), f)
     smy, smx = shift_ramp_tables(W, mask, complex_dtype)
-    # the reference's tilt arrays are (1, 6, 1, 1) default_float rows (objective.py:343, 434-435)
-    tx, ty = np.full((1, 1), tan_x, dtype=f), np.full((1, 1), tan_y, dtype=f)
-    prop = propagator(f(distance), lam, q2, qx, qy, mask, complex_dtype, tx, ty)
+    if tilts is None:
+        tilts = np.zeros((1, 6), dtype=f)
+        tilts[0, 2], tilts[0, 3] = tan_y, tan_x
+    tilts = np.asarray(tilts, dtype=f)
+    single_tilt = tilts.shape[0] == 1
+    inside_grad = bool(step_tilts) and tilt_mode in (0, 3, 4)
+    before = tilt_mode in (2, 4)
+    after = tilt_mode in (1, 3, 4)
+    if before or after:
+        yg, xg = tilt_grids(W, px, py, lam, complex_dtype)
+        yx = np.stack((yg[None, :, :, None], xg[None, :, :, None]), axis=1)   # (1, 2, W, W, 1), objective.py:307
+    # one propagator for all positions unless per-position inside tilts (objective.py:330-345)
+    same_prop = single_tilt or tilt_mode in (1, 2)
+    d = f(distance)
+    if same_prop:
+        t0 = tilts[0]
+        prop = propagator(d, lam, q2, qx, qy, mask, complex_dtype, t0[3], t0[2])
     probe_shift = bool(np.sum(np.asarray(pos_correction, np.float64) ** 2) != 0.0) or bool(step_pos)
     fluct = beam_current is not None
     morph = aberrations is not None
@@ -173,26 +201,30 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         plates = np.exp(np.sum(polys[None] * aberrations[:, :, None, None], 1)) * mask
     if compressed and data_pad != 0:
         raise ValueError("data_pad with compressed detectors: the masks would need the cropped shape")
-    if near:                                                            # objective.py:505, 516
+    if near:
         dfc = f(defocus)
-        ctf = (np.exp(-3.141592654j * (((lam * q2 + 2 * (qx * tx + qy * ty)) * dfc)
-                                      + (0.5 * f(cs) * lam ** 3 * q2 ** 2))) * mask)[None, :, :, None, None]
         if alpha_near_field > 0:
             raise ValueError("near-field alpha_near_field > 0: the reference raises (objective.py:600)")
     runx, runy = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
     object_grad = np.zeros_like(obj)
     probe_grad = np.zeros((W, W, Mp), dtype=complex_dtype)
     pos_grad = np.zeros_like(pos_correction)
+    tilts_grad = np.zeros_like(tilts)
     bc_grad = np.zeros_like(beam_current) if fluct else 0
     ab_grad = np.zeros_like(aberrations) if morph else 0
     helper2 = step_probe or step_beam_current or step_aberrations
-    helper4 = helper2 or step_pos
+    helper3 = helper2 or (bool(step_tilts) and before)
+    helper4 = helper3 or step_pos
     loss, sse = 0, 0
     sim = []
     seq = np.asarray(sequence)
     for i in range(0, len(seq), compute_batch):
         tcs = seq[i:i + compute_batch]
         B = len(tcs)
+        tind = [0] if single_tilt else tcs
+        tl = tilts[tind][:, :, None, None]                              # (n, 6, 1, 1)
+        ty_b, tx_b, ty_i, tx_i, ty_a, tx_a = np.split(tl, 6, axis=1)    # each (n, 1, 1, 1)
+        ty_i, tx_i = ty_i[:, :, :, 0], tx_i[:, :, :, 0]                 # (n, 1, 1)
         my = positions[tcs, 0][:, None, None] + runy[None]
         mx = positions[tcs, 1][:, None, None] + runx[None]
         ob = obj[my, mx, :, :]                                          # objective.py:436-441
@@ -208,6 +240,10 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
             probe_f = fft2(this_probe, axes=(1, 2))
             before_ab = probe_f * 1
             this_probe = ifft2(before_ab * plate[:, :, :, None], axes=(1, 2))
+        if before:                                                      # objective.py:464-467
+            tmask_b = np.exp(xg[None, :, :, None] * tx_b + yg[None, :, :, None] * ty_b)
+            probe_before_tilt = this_probe
+            this_probe = probe_before_tilt * tmask_b
         if probe_shift:                                                 # objective.py:470-476
             if probe_f is None:
                 probe_f = fft2(this_probe, axes=(1, 2))
@@ -217,9 +253,23 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         if this_probe.shape[0] == 1 and B > 1:
             this_probe = np.repeat(this_probe, B, axis=0)
         this_probe = this_probe.astype(complex_dtype)
-        stack, exit_wave = multislice(this_probe, ob, prop, edge_mult)
-        if near:                                                        # objective.py:506-508
-            wave = ifft2(fft2(exit_wave, axes=(1, 2)) * ctf, axes=(1, 2))
+        if same_prop:
+            prop_b = prop[None]
+        else:                                                           # objective.py:482-484
+            prop_b = (np.exp(-3.141592654j * d * (lam * q2 + 2 * (qx * tx_i + qy * ty_i))) * mask)
+            prop_b = prop_b.astype(complex_dtype)
+        stack, exit_wave, spec_stack = multislice_tilted(this_probe, ob, prop_b, edge_mult, inside_grad)
+        if after:                                                       # objective.py:490-499
+            tmask_a = np.exp(xg[None, :, :, None] * tx_a + yg[None, :, :, None] * ty_a)[:, :, :, :, None]
+            if Z == 1:
+                exit_wave = ifft2(fft2(exit_wave, axes=(1, 2)) * mask[None, :, :, None, None], axes=(1, 2))
+            exit_before_tilt = exit_wave
+            exit_wave = exit_before_tilt * tmask_a
+        if near:                                                        # objective.py:504-508
+            ctf = (np.exp(-3.141592654j * (((lam * q2 + 2 * (qx * tx_i + qy * ty_i)) * dfc)
+                                          + (0.5 * f(cs) * lam ** 3 * q2 ** 2))) * mask)[:, :, :, None, None]
+            fourier_exit = fft2(exit_wave, axes=(1, 2))
+            wave = ifft2(fourier_exit * ctf, axes=(1, 2))
         else:                                                           # objective.py:502-503
             wave = shift_fft2(exit_wave, axes=(1, 2)) * mask_s[None, :, :, None, None]
         pattern = np.abs(wave) ** 2
@@ -247,15 +297,46 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
             dldi = dldi / (Mp * Mo)                                     # objective.py:586-587
         if not use_padded_intensity and data_pad != 0:                  # objective.py:592-593
             dldi = np.pad(dldi, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
-        if near:                                                        # objective.py:598-604
+        if near:                                                        # objective.py:598-619
             dwave = wave * np.expand_dims(dldi, (-1, -2))
             fwg = loss_weight * fft2(dwave, axes=(1, 2)) * np.conjugate(ctf)
             g = ifft2(fwg, axes=(1, 2))
+            if inside_grad:
+                rsc = -12.566370614359172 / (W * W)
+                fwg = fwg * np.conjugate(fourier_exit)
+                if coherent:
+                    gx = np.sum(np.imag(fwg[:, :, :, 0, 0] * qx * dfc), (1, 2))
+                    gy = np.sum(np.imag(fwg[:, :, :, 0, 0] * qy * dfc), (1, 2))
+                else:
+                    gx = np.sum(np.imag(fwg * qx[None, :, :, None, None] * dfc), (1, 2, 3, 4))
+                    gy = np.sum(np.imag(fwg * qy[None, :, :, None, None] * dfc), (1, 2, 3, 4))
+                if single_tilt:
+                    gx, gy = np.sum(gx), np.sum(gy)
+                tilts_grad[tind, 2] += gy * rsc
+                tilts_grad[tind, 3] += gx * rsc
         else:                                                           # objective.py:595-597
             dwave = dldi[:, :, :, None, None] * wave * (loss_weight * W * W)
             g = ifft2_ishift(dwave, axes=(1, 2))
+        if after:                                                       # objective.py:620-639
+            g = g * np.conjugate(tmask_a)
+            if step_tilts:
+                kern = -2 * g * np.conjugate(exit_before_tilt)
+                if coherent:
+                    dt = np.sum(np.real(kern[:, None, :, :, 0, 0] * yx[:, :, :, :, 0]), (2, 3), dtype=f)
+                else:
+                    dt = np.sum(np.real(kern[:, None] * yx[:, :, :, :, :, None]), (2, 3, 4, 5), dtype=f)
+                if single_tilt:
+                    tilts_grad[0, 4:] += np.sum(dt, 0)
+                else:
+                    tilts_grad[tind, 4:] = dt
+            if Z == 1:
+                g = ifft2(fft2(g, axes=(1, 2)) * mask[None, :, :, None, None], axes=(1, 2))
         g = g.astype(complex_dtype)
-        grad_w, pgrad = multislice_grads(g, stack, ob, prop, edge_mult, mask)
+        # a single tilt row with more than one position per batch makes the reference add a
+        # (B,) vector into one row of tilts_grad (multislice_core.py:180-182): NumPy raises
+        # ValueError there, as the reference does
+        grad_w, pgrad = multislice_grads_tilted(g, stack, spec_stack, ob, prop_b, edge_mult, mask, d, qx, qy,
+                                                tilts_grad if inside_grad else None, tind)
         if step_obj:
             scatteradd(object_grad, my, mx, grad_w.astype(complex_dtype))
         if not helper4:
@@ -269,27 +350,41 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                 sh = -2 / (W * W)
                 pos_grad[tcs, 0] = sh * np.sum(np.real(smy[None, :, :, None] * smg), (1, 2, 3))
                 pos_grad[tcs, 1] = sh * np.sum(np.real(smx[None, :, :, None] * smg), (1, 2, 3))
-        if helper2:
-            if morph:                                                   # objective.py:676-684
-                if fpg is None:
+        if helper3:
+            if before:                                                  # objective.py:660-673
+                pgrad = pgrad * np.conjugate(tmask_b)
+                if step_tilts:
+                    kern = -2 * pgrad * np.conjugate(probe_before_tilt)
+                    if Mp == 1:
+                        # yx[:, :, :, 0] selects x = 0 (shape (1, 2, W, 1)): the x component uses
+                        # the grid's first column for every x, as the reference computes it
+                        dt = np.sum(np.real(kern[:, None, :, :, 0] * yx[:, :, :, 0]), (2, 3), dtype=f)
+                    else:
+                        dt = np.sum(np.real(kern[:, None] * yx), (2, 3, 4), dtype=f)
+                    if single_tilt:
+                        tilts_grad[0, :2] += np.sum(dt, 0)
+                    else:
+                        tilts_grad[tind, :2] = dt
+            if helper2:
+                if morph:                                               # objective.py:676-684
                     fpg = fft2(pgrad, axes=(1, 2))
-                fpg = fpg * np.conjugate(plate[:, :, :, None])
-                pgrad = ifft2(fpg, axes=(1, 2))
-                if step_aberrations:
-                    sh = 2 / (W * W)
-                    defgr = sh * np.sum(np.real((fpg * np.conjugate(before_ab))[:, None]
-                                                * np.conjugate(polys[None, :, :, :, None])), axis=(2, 3, 4),
-                                        dtype=f)
-                    np.add.at(ab_grad, np.asarray(aberration_marker)[tcs], defgr)
-            if step_probe or step_beam_current:
-                if fluct:                                               # objective.py:687-697
-                    if step_beam_current:
-                        bc_grad[tcs] = 2 * np.sign(bc) * np.sum(np.real(pgrad * np.conjugate(before_fluct)),
-                                                                (1, 2, 3))
+                    fpg = fpg * np.conjugate(plate[:, :, :, None])
+                    pgrad = ifft2(fpg, axes=(1, 2))
+                    if step_aberrations:
+                        sh = 2 / (W * W)
+                        defgr = sh * np.sum(np.real((fpg * np.conjugate(before_ab))[:, None]
+                                                    * np.conjugate(polys[None, :, :, :, None])), axis=(2, 3, 4),
+                                            dtype=f)
+                        np.add.at(ab_grad, np.asarray(aberration_marker)[tcs], defgr)
+                if step_probe or step_beam_current:
+                    if fluct:                                           # objective.py:687-697
+                        if step_beam_current:
+                            bc_grad[tcs] = 2 * np.sign(bc) * np.sum(np.real(pgrad * np.conjugate(before_fluct)),
+                                                                    (1, 2, 3))
+                        if step_probe:
+                            pgrad = pgrad * bc[:, None, None, None]
                     if step_probe:
-                        pgrad = pgrad * bc[:, None, None, None]
-                if step_probe:
-                    probe_grad = probe_grad + np.sum(pgrad, 0)          # objective.py:703
+                        probe_grad = probe_grad + np.sum(pgrad, 0)      # objective.py:703
     if simulate:
         return np.concatenate(sim, 0)
     loss = loss * loss_weight                                           # objective.py:742
@@ -297,4 +392,63 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         raise ValueError('A very specific bad thing. Loss is Nan.')
     if step_probe:                                                      # objective.py:927-933
         probe_grad = ifft2(fft2(probe_grad) * mask[:, :, None])
-    return (loss, sse, object_grad, np.asarray(probe_grad).astype(complex_dtype), pos_grad, bc_grad, ab_grad)
+    return (loss, sse, object_grad, np.asarray(probe_grad).astype(complex_dtype), pos_grad, bc_grad, ab_grad,
+            tilts_grad)
+
+
+def multislice_tilted(probe_b, obj_b, prop_b, edge_mult, keep_spectra):
+    """Forward multislice with one propagator per position (prop_b (n, W, W), n = 1 or B),
+    ``multislice_core.py:61-82``; with ``keep_spectra`` also the conjugated spectra
+    FFT(psi_z O_z) of every propagated slice (the second stack channel, ``:76-77``)."""
+    B, W, _, Z, Mo = obj_b.shape
+    Mp = probe_b.shape[-1]
+    stack = np.empty((B, W, W, Z, Mp, Mo), dtype=obj_b.dtype)
+    spec = np.zeros((B, W, W, Z, Mp, Mo), dtype=obj_b.dtype) if keep_spectra else None
+    wave = np.repeat(probe_b[:, :, :, :, None], Mo, axis=-1)
+    for z in range(Z):
+        stack[:, :, :, z] = wave
+        wave = wave * obj_b[:, :, :, z:z + 1, :]
+        if z < Z - 1:
+            p = prop_b
+            if edge_mult > 1 and z == 0:
+                p = p ** edge_mult
+            wave = fft2(wave, axes=(1, 2))
+            if keep_spectra:
+                spec[:, :, :, z] = wave
+            wave = wave * p[:, :, :, None, None]
+            wave = ifft2(wave, axes=(1, 2))
+    return np.conjugate(stack), wave, (None if spec is None else np.conjugate(spec))
+
+
+def multislice_grads_tilted(g, stack_conj, spec_conj, obj_b, prop_b, edge_mult, mask, distance, qx, qy,
+                            tilts_grad, tind):
+    """Adjoint multislice with per-position propagators, ``multislice_core.py:158-200``; with
+    ``tilts_grad`` it adds the inside-tilt gradient terms of every step into rows ``tind``
+    (``:178-182``). Returns (gradient windows, probe gradient)."""
+    Z = obj_b.shape[3]
+    W = obj_b.shape[1]
+    obj_c = np.conjugate(obj_b)
+    contrib = np.empty_like(stack_conj)
+    for z in range(Z - 1, -1, -1):
+        contrib[:, :, :, z] = stack_conj[:, :, :, z] * g
+        g = g * obj_c[:, :, :, z:z + 1, :]
+        if z > 0:
+            p = np.conjugate(prop_b)
+            dist = 1 * distance
+            if edge_mult > 1 and z == 1:
+                p = p ** edge_mult
+                dist *= edge_mult
+            g = fft2(g, axes=(1, 2))
+            g = g * p[:, :, :, None, None]
+            if tilts_grad is not None:
+                sh = -12.566370614359172 * dist / (W * W)
+                dldp = np.sum(spec_conj[:, :, :, z - 1] * g, (3, 4))
+                tilts_grad[tind, 3] += sh * np.sum(np.imag(dldp * qx), (1, 2))
+                tilts_grad[tind, 2] += sh * np.sum(np.imag(dldp * qy), (1, 2))
+            g = ifft2(g, axes=(1, 2))
+    grad = contrib.sum(axis=4)
+    grad = fft2(grad, axes=(1, 2))
+    grad = grad * mask[None, :, :, None, None]
+    grad = ifft2(grad, axes=(1, 2))
+    probe_grad = g.sum(axis=-1)
+    return grad, probe_grad

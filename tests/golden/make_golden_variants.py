@@ -30,8 +30,11 @@ from oracle import variants_oracle as vor  # noqa: E402
 def ref_call(pypty, c):
     """The reference with every argument spelled out (signature objective.py:47)."""
     f, cx = (np.float64, np.complex128) if c["double"] else (np.float32, np.complex64)
-    tilts = np.zeros((1, 6), dtype=f)
-    tilts[0, 2], tilts[0, 3] = c["tan_y"], c["tan_x"]
+    if c["tilts"] is not None:
+        tilts = c["tilts"].astype(f)
+    else:
+        tilts = np.zeros((1, 6), dtype=f)
+        tilts[0, 2], tilts[0, 3] = c["tan_y"], c["tan_x"]
     masks = None if c["masks"] is None else c["masks"].astype(f)
     bc = None if c["beam_current"] is None else c["beam_current"].astype(f)
     ab = None if c["aberrations"] is None else c["aberrations"].astype(f)
@@ -42,14 +45,14 @@ def ref_call(pypty, c):
         this_distances=np.array([c["distance"]], dtype=f), edge_slice_thickness_multiplier=c["edge_mult"],
         measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
-        this_step_tilts=0, masks=masks, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+        this_step_tilts=c["step_tilts"], masks=masks, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
         recon_type=c["recon_type"], Cs=f(c["cs"]), defocus_array=np.array([c["defocus"]], dtype=f),
         alpha_near_field=f(c["alpha"]), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
         propmethod="multislice", this_chopped_sequence=c["sequence"], load_one_by_one=False,
         data_multiplier=f(c["mult"]), data_pad=c["data_pad"], phase_plate_in_h5=None, this_loss_weight=c["loss_weight"],
         data_bin=1, data_shift_vector=[c["shift0"], c["shift1"]], upsample_pattern=1, static_background=None,
         this_step_static_background=0,
-        tilt_mode=0, aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
+        tilt_mode=c["tilt_mode"], aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
         compute_batch=c["batch"], phase_only_obj=False, beam_current=bc,
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], default_float=f,
         default_complex=cx, xp=np, is_first_epoch=True, scan_size=None, scan_step_A=1,
@@ -61,7 +64,7 @@ def ref_call(pypty, c):
         probe_mod_tol=0.05, smart_memory=False, print_flag=0, data_simulation_flag=False,
         data_simulation_exitwave=False, use_padded_intensity=bool(c["use_padded"]))
     # outer return order (objective.py:967): aberrations gradient before beam-current gradient
-    return res[0], res[1], res[2], res[3], res[4], res[8], res[7]
+    return res[0], res[1], res[2], res[3], res[4], res[8], res[7], res[5]
 
 
 def detector_masks(W, n, rng):
@@ -82,7 +85,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                loss_weight=1.0, step_probe=1, step_obj=1, step_pos=0, dose=1e4, double=False, recon_type="far_field",
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
                n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
-               mult=1.0):
+               mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
@@ -98,9 +101,12 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
     bc = (1.0 + 0.1 * rng.normal(size=N)).astype(f) if beam_current else None
     ab = (rng.normal(size=(n_ab_sets, n_abs)) * 20.0).astype(f) if n_ab_sets else None
     marker = (np.arange(N) % n_ab_sets).astype(np.int64) if n_ab_sets else None
+    # tilt rows [tan_y, tan_x] before / inside / after: one row, or one per position
+    tilts = (rng.normal(size=(N if tilt_rows == "per_position" else 1, 6)) * tilt_scale).astype(f) \
+        if tilt_rows else None
     kw = dict(recon_type=recon_type, defocus=defocus, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
               masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
-              use_padded_intensity=use_padded)
+              use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode)
     sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, distance, edge_mult, None, algorithm, lam,
                                           1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
     if n_masks:
@@ -121,7 +127,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 sequence=np.arange(N), loss_weight=loss_weight, batch=batch, obj=obj0, probe=probe0,
                 recon_type=recon_type, defocus=defocus, cs=cs, alpha=alpha_nf, tan_x=tan_x, tan_y=tan_y, masks=masks,
                 beam_current=bc, step_bc=step_bc, aberrations=ab, aberration_marker=marker, step_ab=step_ab,
-                data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult)
+                data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult,
+                tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts)
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -150,6 +157,29 @@ CASES = [
     dict(BASE, name="crop_c64", seed=39, algorithm="lsq_sqrt", data_pad=6, use_padded=0),
     # the per-batch shift vector and multiplier of the measured patterns (utils.py:626-647)
     dict(BASE, name="shift_mult_c64", seed=40, algorithm="lsq", shift=(2, -3), mult=1.5, Mp=1),
+    # beam tilts (objective.py:302-345, 464-499, 605-673; multislice_core.py:76-77, 178-182):
+    # per-position inside tilts with their gradient
+    dict(BASE, name="tilt0_rows_c64", seed=41, algorithm="ml", tilt_mode=0, tilt_rows="per_position",
+         step_tilts=1),
+    # one inside tilt row: batches of one position (the reference raises for more)
+    dict(BASE, name="tilt0_single_c64", seed=42, algorithm="lsq_sqrt", tilt_mode=0, tilt_rows="single",
+         step_tilts=1, batch=1, n_scan=3),
+    # after the specimen, per position; one slice (the exit wave is band-limited first)
+    dict(BASE, name="tilt1_rows_z1_c64", seed=43, algorithm="lsq_sqrt", tilt_mode=1, tilt_rows="per_position",
+         step_tilts=1, Z=1),
+    # before the specimen, one row, one probe mode (the reference's x grid quirk), shifts; the
+    # amplitude loss (a Poisson loss on one coherent mode divides by near-zero intensities at the
+    # pattern's dark pixels, where any two FP32 evaluations differ)
+    dict(BASE, name="tilt2_single_c64", seed=44, algorithm="lsq_sqrt", tilt_mode=2, tilt_rows="single",
+         step_tilts=1, Mp=1, step_pos=1),
+    # inside and after, near field, per position
+    dict(BASE, name="tilt3_near_rows_c64", seed=45, algorithm="lsq_sqrt", tilt_mode=3, tilt_rows="per_position",
+         step_tilts=1, recon_type="near_field", defocus=60.0, cs=2e5),
+    # before, inside and after, per position, with shifts, and its FP64 twin
+    dict(BASE, name="tilt4_rows_c64", seed=46, algorithm="ml", tilt_mode=4, tilt_rows="per_position", step_tilts=1,
+         step_pos=1),
+    dict(BASE, name="tilt4_rows_c128", seed=46, algorithm="ml", tilt_mode=4, tilt_rows="per_position",
+         step_tilts=1, step_pos=1, double=True),
     # the same with sub-pixel shifts: the shift spectrum excludes the plates (objective.py:461, 471)
     dict(BASE, name="current_aberr_shift_c64", seed=37, algorithm="lsq_sqrt", beam_current=True, step_bc=1,
          n_ab_sets=2, n_abs=4, step_ab=1, step_pos=1),
@@ -162,7 +192,7 @@ def main():
         spec = dict(spec)
         name = spec.pop("name")
         c = build_case(name, **spec)
-        loss, sse, og, pg, posg, bcg, abg = ref_call(pypty, c)
+        loss, sse, og, pg, posg, bcg, abg, tg = ref_call(pypty, c)
         out = os.path.join(HERE, "variant_" + name + ".npz")
         none = np.zeros(0, np.float32)
         np.savez_compressed(
@@ -171,7 +201,8 @@ def main():
             scalars=np.array([c["distance"], c["edge_mult"], c["wavelength"], c["px"], c["cutoff"], c["rolloff"],
                               c["loss_weight"], c["batch"], c["step_probe"], c["step_obj"], c["step_pos"],
                               c["defocus"], c["cs"], c["alpha"], c["tan_x"], c["tan_y"], c["step_bc"], c["step_ab"],
-                              c["data_pad"], c["use_padded"], c["shift0"], c["shift1"], c["mult"]],
+                              c["data_pad"], c["use_padded"], c["shift0"], c["shift1"], c["mult"], c["tilt_mode"],
+                              c["step_tilts"]],
                              dtype=np.float64),
             algorithm=np.array(c["algorithm"]), recon_type=np.array(c["recon_type"]), double=np.array(c["double"]),
             masks=none if c["masks"] is None else c["masks"],
@@ -180,7 +211,8 @@ def main():
             aberration_marker=np.zeros(0, np.int64) if c["aberration_marker"] is None else c["aberration_marker"],
             ref_loss=np.array(loss, dtype=np.float64), ref_sse=np.array(sse, dtype=np.float64),
             ref_object_grad=og, ref_probe_grad=np.asarray(pg), ref_pos_grad=posg,
-            ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg))
+            ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg),
+            tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg))
         print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
             np.linalg.norm(np.asarray(abg)), os.path.basename(out)))

@@ -45,16 +45,16 @@ def load_variant_case(name):
     s = d["scalars"]
     keys = ["distance", "edge_mult", "wavelength", "px", "cutoff", "rolloff", "loss_weight", "batch", "step_probe",
             "step_obj", "step_pos", "defocus", "cs", "alpha", "tan_x", "tan_y", "step_bc", "step_ab", "data_pad",
-            "use_padded", "shift0", "shift1", "mult"]
+            "use_padded", "shift0", "shift1", "mult", "tilt_mode", "step_tilts"]
     for i, k in enumerate(keys):
         d[k] = float(s[i])
     for k in ("batch", "step_probe", "step_obj", "step_pos", "step_bc", "step_ab", "data_pad", "use_padded", "shift0",
-              "shift1"):
+              "shift1", "tilt_mode", "step_tilts"):
         d[k] = int(d[k])
     d["algorithm"] = str(d["algorithm"])
     d["recon_type"] = str(d["recon_type"])
     d["double"] = bool(d["double"])
-    for k in ("masks", "beam_current", "aberrations", "aberration_marker"):
+    for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts"):
         if d[k].size == 0:
             d[k] = None
     return d

@@ -17,13 +17,14 @@ def run_variant_oracle(c):
         masks=c["masks"], beam_current=c["beam_current"], step_beam_current=c["step_bc"],
         aberrations=c["aberrations"], aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"],
         data_pad=c["data_pad"], use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]),
-        data_multiplier=f(c["mult"]), float_dtype=f, complex_dtype=cx)
+        data_multiplier=f(c["mult"]), tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"],
+        float_dtype=f, complex_dtype=cx)
 
 
 @pytest.mark.parametrize("name", variant_case_names())
 def test_variants_oracle_matches_reference(name):
     c = load_variant_case(name)
-    loss, sse, og, pg, posg, bcg, abg = run_variant_oracle(c)
+    loss, sse, og, pg, posg, bcg, abg, tg = run_variant_oracle(c)
     tol = 1e-12 if c["double"] else 5e-6
     assert abs(float(loss) - float(c["ref_loss"])) <= tol * abs(float(c["ref_loss"]))
     assert abs(float(sse) - float(c["ref_sse"])) <= tol * abs(float(c["ref_sse"]))
@@ -36,6 +37,8 @@ def test_variants_oracle_matches_reference(name):
         assert rel_l2(bcg, c["ref_beam_current_grad"]) <= (1e-12 if c["double"] else 1e-5)
     if c["step_ab"]:
         assert rel_l2(abg, c["ref_aberrations_grad"]) <= (1e-12 if c["double"] else 1e-5)
+    if c["step_tilts"]:
+        assert rel_l2(tg, c["ref_tilts_grad"]) <= (1e-12 if c["double"] else 1e-5)
 
 
 def test_near_field_alpha_is_rejected():
@@ -53,3 +56,12 @@ def test_aberration_basis_order():
     assert n == [1, 1, 1, 2, 2, 2, 2, 3]
     assert m == [0, 2, 2, 1, 1, 3, 3, 0]
     assert ab == ["", "a", "b", "a", "b", "a", "b", ""]
+
+
+def test_single_tilt_inside_gradient_with_batches_raises_like_the_reference():
+    """One tilt row, inside-tilt refinement and several positions per batch: the reference adds
+    a (B,) vector into one row (multislice_core.py:180-182) and raises; so does the oracle."""
+    c = load_variant_case("tilt0_single_c64")
+    c = dict(c, batch=3)
+    with pytest.raises(ValueError):
+        run_variant_oracle(c)
