@@ -269,6 +269,18 @@ typedef struct pty_variant {
   int32_t use_padded_intensity;
   int32_t shift_y, shift_x;
   float data_multiplier;   /* 0 is read as 1: a zero-initialised struct leaves the data unscaled */
+  /* beam tilts (pypty/objective.py:302-345, 464-499, 605-673; multislice_core.py:76-77,
+     178-182): n_tilts rows (1, or one per position) of [tan_y, tan_x] before / inside / after
+     the specimen in HOST memory (the reference's tilt array plus its correction); tilt_mode
+     0-4 as the reference's; with step_tilts the gradient (n_tilts, 6) goes to tilts_grad
+     (device). n_tilts = 0: one inside tilt (tan_x, tan_y) and no tilt gradient. One row with
+     step_tilts and tilt_mode 0, 3 or 4 returns the sum over positions of the inside-tilt
+     gradient (the reference raises there unless compute_batch is 1). */
+  int32_t n_tilts;
+  const float* tilts_host;
+  int32_t tilt_mode;
+  int32_t step_tilts;
+  float* tilts_grad;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

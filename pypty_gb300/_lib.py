@@ -58,7 +58,9 @@ class Variant(ctypes.Structure):
                 ("aberrations", ctypes.c_void_p), ("aberration_marker", ctypes.c_void_p),
                 ("step_aberrations", ctypes.c_int32), ("aberrations_grad", ctypes.c_void_p),
                 ("data_pad", ctypes.c_int32), ("use_padded_intensity", ctypes.c_int32),
-                ("shift_y", ctypes.c_int32), ("shift_x", ctypes.c_int32), ("data_multiplier", ctypes.c_float)]
+                ("shift_y", ctypes.c_int32), ("shift_x", ctypes.c_int32), ("data_multiplier", ctypes.c_float),
+                ("n_tilts", ctypes.c_int32), ("tilts_host", ctypes.c_void_p), ("tilt_mode", ctypes.c_int32),
+                ("step_tilts", ctypes.c_int32), ("tilts_grad", ctypes.c_void_p)]
 
 
 class PtyError(RuntimeError):

@@ -218,6 +218,7 @@ struct VarTableArgs {
   float2* prop;
   float2* prop_edge;
   float2* ctf;
+  float* tgrid;           // [2][W] real-space tilt ramps (x, y)
   float* abasis;          // [n_abs][WW]
   const float* mask;
   const int* abn;         // [n_abs] Krivanek n
@@ -231,6 +232,13 @@ __global__ void var_tables_kernel(VarTableArgs a) {
   const int W = a.W, WW = W * W;
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= WW) return;
+  if (u < W) {
+    // x_real_grid_tilt / y_real_grid_tilt (objective.py:303-307): fftshift(fftfreq(W)) *
+    // 6.2831855 i * W * pixel size / lambda in float64, rounded to complex64
+    const double f = (double)(u - W / 2) / (double)W;
+    a.tgrid[u] = (float)(f * 6.2831855 * (double)W * (double)a.px / (double)a.wavelength);
+    a.tgrid[W + u] = (float)(f * 6.2831855 * (double)W * (double)a.py / (double)a.wavelength);
+  }
   const int ky = u / W, kx = u % W;
   const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
   const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
@@ -304,6 +312,7 @@ struct VarProbeArgs {
   const float* abasis;       // [n_abs][WW]
   const float* coefs;        // aberrations [sets][n_abs] or null
   const int* marker;         // [N]
+  const float2* pspec;       // [Bn][Mp][WW] per-position probe spectra the shift was applied to, or null (bc FFT(P))
   int W, Mp, shift, n_abs, n_sets;
 };
 
@@ -499,15 +508,19 @@ __global__ void var_apply_kernel(float2* __restrict__ field, const float* __rest
 // sum Re(F conj(FFT(P))) (Parseval: W^2 times the real-space sum); F *= bc for the probe
 // gradient. Partials: pos_part[s][p][2], bc_part[s][p], ab_part[s][p][n_abs].
 // grid (Mp, Bn), block 1024
+// do_shift / do_rest split the chain around the adjoint of a tilt before the specimen, which
+// the caller applies in real space between the two parts (objective.py:660-673).
 __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict__ F, VarProbeArgs a, int step_pos,
-                                                             int step_bc, int step_ab, int step_probe,
-                                                             double* __restrict__ pos_part, double* __restrict__ bc_part,
+                                                             int step_bc, int step_ab, int step_probe, int do_shift,
+                                                             int do_rest, double* __restrict__ pos_part,
+                                                             double* __restrict__ bc_part,
                                                              double* __restrict__ ab_part) {
   __shared__ double red[64];
   const int p = blockIdx.x, b = blockIdx.y, gi = a.seq[b];
   const int W = a.W, WW = W * W;
   const float bc = a.bc ? fabsf(a.bc[gi]) : 1.0f;
-  const float* coef = coefs_of(a, gi);
+  const float* coef = do_rest ? coefs_of(a, gi) : nullptr;
+  const bool sh = a.shift && do_shift, bcr = a.bc && do_rest;
   const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
   float2* f = F + ((size_t)b * a.Mp + p) * WW;
   const float2* pf = a.pf + (size_t)p * WW;
@@ -515,9 +528,9 @@ __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict_
   for (int u = threadIdx.x; u < WW; u += blockDim.x) {
     const int ky = u / W, kx = u % W;
     const float mk = a.mask[u];
-    const float2 before = a.bc ? cscale(pf[u], bc) : pf[u];
+    const float2 before = a.pspec ? a.pspec[((size_t)b * a.Mp + p) * WW + u] : (a.bc ? cscale(pf[u], bc) : pf[u]);
     float2 v = f[u];
-    if (a.shift) {
+    if (sh) {
       v = cmulc(v, ramp(a.sx, a.sy, ky, kx, mk, dy, dx));
       if (step_pos) {
         const float im = cmulc(v, before).y;
@@ -526,10 +539,10 @@ __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict_
       }
     }
     if (coef) v = cmulc(v, plate_at(a.abasis, coef, a.n_abs, WW, u, mk));
-    if (a.bc && step_bc) gb += (double)cmulc(v, pf[u]).x;
+    if (bcr && step_bc) gb += (double)cmulc(v, pf[u]).x;
     f[u] = v;
   }
-  if (step_pos && a.shift) {
+  if (step_pos && sh) {
     double gyy = gy, gxx = gx;
     block_sum2(gyy, gxx, red);
     if (threadIdx.x == 0) {
@@ -537,7 +550,7 @@ __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict_
       pos_part[((size_t)b * a.Mp + p) * 2 + 1] = gxx;
     }
   }
-  if (a.bc && step_bc) {
+  if (bcr && step_bc) {
     double unused = 0.0;
     block_sum2(gb, unused, red);
     if (threadIdx.x == 0) bc_part[(size_t)b * a.Mp + p] = gb;
@@ -558,7 +571,7 @@ __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict_
   }
   // probe gradient times the beam current (objective.py:698-699); every thread rescales the
   // pixels it wrote itself
-  if (a.bc && step_probe)
+  if (bcr && step_probe)
     for (int u = threadIdx.x; u < WW; u += blockDim.x) f[u] = cscale(f[u], bc);
 }
 
@@ -596,6 +609,220 @@ __global__ void var_finalize_kernel(const double* __restrict__ bc_part, const do
   }
 }
 
+// ------------------------------------------------------------------ beam tilts
+// Tilt rows [tan_y, tan_x] before (0, 1), inside (2, 3) and after (4, 5) the specimen; row 0
+// for every position with one row, else the row of the position (objective.py:420-435).
+struct TiltArgs {
+  const float* rows;     // [n_tilts][6]
+  const float* grid;     // [2][W]: x ramp, y ramp (imaginary parts of objective.py:303-307)
+  const int* seq;
+  int single, W;
+};
+
+__device__ __forceinline__ const float* tilt_row(const TiltArgs& t, int b) {
+  return t.rows + (t.single ? 0 : (size_t)t.seq[b] * 6);
+}
+
+// real-space tilt mask exp(x_grid tan_x + y_grid tan_y) at pixel u, columns c, c + 1 of the
+// row (objective.py:465, 491): the purely imaginary complex64 grids times float32 tangents,
+// summed in float32
+__device__ __forceinline__ float2 tilt_mask_at(const TiltArgs& t, const float* row, int col, int u) {
+  const int y = u / t.W, x = u % t.W;
+  const float th = __fadd_rn(__fmul_rn(t.grid[x], row[col + 1]), __fmul_rn(t.grid[t.W + y], row[col]));
+  float s, c;
+  sincosf(th, &s, &c);
+  return make_float2(c, s);
+}
+
+// x[b][k] *= mask (conj(mask)) with the tilt columns col (0 before, 4 after)
+// grid (WW / EB, nper, Bn)
+__global__ void var_tilt_mul_kernel(float2* __restrict__ x, TiltArgs t, int nper, int col, int conj) {
+  const int u = blockIdx.x * EB + threadIdx.x, k = blockIdx.y, b = blockIdx.z;
+  const int WW = t.W * t.W;
+  const float2 m = tilt_mask_at(t, tilt_row(t, b), col, u);
+  float2* q = x + ((size_t)b * nper + k) * WW + u;
+  *q = conj ? cmulc(*q, m) : cmul(*q, m);
+}
+
+struct PropArgs {
+  const float* mask;
+  float distance, wavelength, px, py, edge_mult, defocus, cs;
+  int W;
+};
+
+// propagator of the position's inside tilt (objective.py:482-484), or its edge power
+// (multislice_core.py:72-73), computed as tables_kernel / var_tables_kernel do
+__device__ __forceinline__ float2 tilted_prop(const PropArgs& a, const float* row, int u, bool edge) {
+  const int W = a.W, ky = u / W, kx = u % W;
+  const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
+  const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, row[3]), __fmul_rn(qy, row[2])));
+  const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
+  const float phase = __fmul_rn(__fmul_rn(-3.141592654f, a.distance), x);
+  const float mk = a.mask[u];
+  float s, c;
+  sincosf(phase, &s, &c);
+  float2 p = make_float2(c * mk, s * mk);
+  if (edge) {
+    const float r = sqrtf(p.x * p.x + p.y * p.y);
+    float2 pe = make_float2(0.f, 0.f);
+    if (r > 0.f) {
+      const float ang = atan2f(p.y, p.x) * a.edge_mult;
+      const float re = powf(r, a.edge_mult);
+      float se, ce;
+      sincosf(ang, &se, &ce);
+      pe = make_float2(re * ce, re * se);
+    }
+    p = pe;
+  }
+  return p;
+}
+
+// near-field CTF of the position's inside tilt (objective.py:505)
+__device__ __forceinline__ float2 tilted_ctf(const PropArgs& a, const float* row, int u) {
+  const int W = a.W, ky = u / W, kx = u % W;
+  const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
+  const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, row[3]), __fmul_rn(qy, row[2])));
+  const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
+  const float l3 = __fmul_rn(__fmul_rn(a.wavelength, a.wavelength), a.wavelength);
+  const float sph = __fmul_rn(__fmul_rn(__fmul_rn(0.5f, a.cs), l3), __fmul_rn(q2, q2));
+  const float phase = __fmul_rn(-3.141592654f, __fadd_rn(__fmul_rn(x, a.defocus), sph));
+  const float mk = a.mask[u];
+  float s, c;
+  sincosf(phase, &s, &c);
+  return make_float2(c * mk, s * mk);
+}
+
+// x[b][k] *= P_b (conj: conj(P_b)) * scale; ctf selects the near-field CTF instead of the
+// propagator   grid (WW / EB, nper, Bn)
+__global__ void var_tilted_mul_kernel(float2* __restrict__ x, TiltArgs t, PropArgs a, int nper, int edge, int ctf,
+                                      int conj, float scale) {
+  const int u = blockIdx.x * EB + threadIdx.x, k = blockIdx.y, b = blockIdx.z;
+  const int WW = a.W * a.W;
+  const float* row = tilt_row(t, b);
+  const float2 P = cscale(ctf ? tilted_ctf(a, row, u) : tilted_prop(a, row, u, edge != 0), scale);
+  float2* q = x + ((size_t)b * nper + k) * WW + u;
+  *q = conj ? cmulc(*q, P) : cmul(*q, P);
+}
+
+// spec[b][p][u] *= the position's shift ramp   grid (WW / EB, Mp, Bn)
+__global__ void var_ramp_mul_kernel(float2* __restrict__ spec, const float* __restrict__ sx, const float* __restrict__ sy,
+                                    const float* __restrict__ mask, const float* __restrict__ corr,
+                                    const int* __restrict__ seq, int W, int Mp) {
+  const int u = blockIdx.x * EB + threadIdx.x, p = blockIdx.y, b = blockIdx.z;
+  const int gi = seq[b];
+  float2* q = spec + ((size_t)b * Mp + p) * W * W + u;
+  *q = cmul(*q, ramp(sx, sy, u / W, u % W, mask[u], corr[2 * gi], corr[2 * gi + 1]));
+}
+
+// inside-tilt gradient terms of one propagation step (multislice_core.py:178-182):
+// part[b] += sh * sum_u (qy, qx) Im(sum_k conj(F_k) G_k), F = FFT(psi O) of the forward step,
+// G = the adjoint wave's spectrum times conj(P)   grid Bn, block 1024
+__global__ void __launch_bounds__(1024) var_inside_tilt_kernel(const float2* __restrict__ G, const float2* __restrict__ F,
+                                                               int nm, int W, float px, float py, double sh,
+                                                               double* __restrict__ part) {
+  __shared__ double red[64];
+  const int b = blockIdx.x, WW = W * W;
+  double gy = 0.0, gx = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = 0; k < nm; ++k) {
+      const size_t i = ((size_t)b * nm + k) * WW + u;
+      acc = cadd(acc, cmulc(G[i], F[i]));   // conj(F) G
+    }
+    const float qx = fftfreq_f32(u % W, W, px), qy = fftfreq_f32(u / W, W, py);
+    gy += (double)(qy * acc.y);
+    gx += (double)(qx * acc.y);
+  }
+  block_sum2(gy, gx, red);
+  if (threadIdx.x == 0) {
+    part[(size_t)b * 6 + 2] += sh * gy;
+    part[(size_t)b * 6 + 3] += sh * gx;
+  }
+}
+
+// near-field inside-tilt gradient (objective.py:605-619): rsc * defocus * sum (qy, qx)
+// Im(FWG conj(FFT(exit)))   grid Bn, block 1024
+__global__ void __launch_bounds__(1024) var_near_tilt_kernel(const float2* __restrict__ FWG, const float2* __restrict__ FE,
+                                                             int nm, int W, float px, float py, float defocus,
+                                                             double rsc, double* __restrict__ part) {
+  __shared__ double red[64];
+  const int b = blockIdx.x, WW = W * W;
+  double gy = 0.0, gx = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+    float im = 0.0f;
+    for (int k = 0; k < nm; ++k) {
+      const size_t i = ((size_t)b * nm + k) * WW + u;
+      im += cmulc(FWG[i], FE[i]).y;
+    }
+    const float qx = fftfreq_f32(u % W, W, px), qy = fftfreq_f32(u / W, W, py);
+    gy += (double)(im * qy * defocus);
+    gx += (double)(im * qx * defocus);
+  }
+  block_sum2(gy, gx, red);
+  if (threadIdx.x == 0) {
+    part[(size_t)b * 6 + 2] += rsc * gy;
+    part[(size_t)b * 6 + 3] += rsc * gx;
+  }
+}
+
+// adjoint of a real-space tilt mask and its gradient (objective.py:620-634 after the
+// specimen, 660-673 before it): x *= conj(mask); with grad, sum over modes and pixels of
+// Re(-2 x conj(ref) * i grid) into part[b][col], part[b][col + 1] (y, x). xcol0: the x grid's
+// first column for every x (the reference's indexing for one probe mode before the specimen)
+// grid Bn, block 1024
+__global__ void __launch_bounds__(1024) var_tilt_adj_kernel(float2* __restrict__ x, const float2* __restrict__ ref,
+                                                            TiltArgs t, int nper, int col, int grad, int xcol0,
+                                                            double* __restrict__ part) {
+  __shared__ double red[64];
+  const int b = blockIdx.x, W = t.W, WW = W * W;
+  const float* row = tilt_row(t, b);
+  double gy = 0.0, gx = 0.0;
+  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+    const float2 m = tilt_mask_at(t, row, col, u);
+    const float yg = t.grid[W + u / W], xg = t.grid[xcol0 ? 0 : u % W];
+    for (int k = 0; k < nper; ++k) {
+      const size_t i = ((size_t)b * nper + k) * WW + u;
+      const float2 v = cmulc(x[i], m);
+      x[i] = v;
+      if (grad) {
+        // kern = -2 v conj(ref); Re(kern * i g) = -g Im(kern) = 2 g Im(v conj(ref))
+        const float im = cmulc(v, ref[i]).y;
+        gy += (double)(2.0f * yg * im);
+        gx += (double)(2.0f * xg * im);
+      }
+    }
+  }
+  if (!grad) return;
+  block_sum2(gy, gx, red);
+  if (threadIdx.x == 0) {
+    part[(size_t)b * 6 + col] = gy;
+    part[(size_t)b * 6 + col + 1] = gx;
+  }
+}
+
+// tilt gradient rows from the per-position partials, in sequence order
+// (objective.py:616-619, 635-639, 668-673; multislice_core.py:181-182)   one block
+__global__ void var_tilt_finalize_kernel(const double* __restrict__ part, const int* __restrict__ seq, int nseq,
+                                         int n_rows, int single, int use_before, int use_inside, int use_after,
+                                         float* __restrict__ grad) {
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < n_rows * 6; ++i) grad[i] = 0.0f;
+  for (int s = 0; s < nseq; ++s) {
+    float* g = grad + (single ? 0 : (size_t)seq[s] * 6);
+    const double* pp = part + (size_t)s * 6;
+    for (int c = 0; c < 6; ++c) {
+      const bool on = c < 2 ? use_before : (c < 4 ? use_inside : use_after);
+      if (!on) continue;
+      // before / after: one row sums the positions, per-position rows are assigned; inside
+      // terms accumulate
+      if (single || (c >= 2 && c < 4)) g[c] += (float)pp[c];
+      else g[c] = (float)pp[c];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ plan
 struct LPlan {
   int W, WW, Ny, Nx, Z, Mo, Mp, N, nseq, Bb, zm, ntx, nty, ntiles, chunk, nchunk, engine;
@@ -605,6 +832,9 @@ struct LPlan {
   // variants (pty_loss_and_direction_variants)
   int near, compressed, nmask, n_abs, n_sets, has_bc;
   size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part;
+  // beam tilts
+  int n_rows, single_tilt, same_prop, before, after, inside_grad, step_tilts;
+  size_t o_tilts, o_tgrid, o_spec, o_fexit, o_exitb, o_pbt, o_pft, o_tpart;
 };
 
 inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t* v = nullptr) {
@@ -676,6 +906,24 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
     q.o_dco = take((size_t)q.Bb * q.nmask * sizeof(float));
     q.o_bc_part = take(q.has_bc ? (size_t)q.nseq * q.Mp * sizeof(double) : 0);
     q.o_ab_part = take((size_t)q.nseq * q.Mp * q.n_abs * sizeof(double));
+    const int tm = v->n_tilts > 0 ? v->tilt_mode : 0;
+    q.n_rows = v->n_tilts > 0 ? v->n_tilts : 1;
+    q.single_tilt = q.n_rows == 1;
+    q.same_prop = q.single_tilt || tm == 1 || tm == 2;   // objective.py:330, 482
+    q.before = tm == 2 || tm == 4;
+    q.after = tm == 1 || tm == 3 || tm == 4;
+    q.step_tilts = v->n_tilts > 0 && v->step_tilts && v->tilts_grad;
+    q.inside_grad = q.step_tilts && (tm == 0 || tm == 3 || tm == 4);
+    q.o_tilts = take((size_t)q.n_rows * 6 * sizeof(float));
+    q.o_tgrid = take((size_t)2 * q.W * sizeof(float));
+    q.o_spec = take(q.inside_grad && q.Z > 1 ? (size_t)(q.Z - 1) * nwave * WWs * c8 : 0);
+    q.o_fexit = take(q.inside_grad && q.near ? nwave * WWs * c8 : 0);
+    q.o_exitb = take(q.after ? nwave * WWs * c8 : 0);
+    q.o_pbt = take(q.before ? (size_t)q.Bb * q.Mp * WWs * c8 : 0);
+    // spectra of the tilted probes the shift is applied to (no plates): the position gradient's
+    // probe spectrum (objective.py:471, 651)
+    q.o_pft = take(q.before && p->probe_shift && !q.n_abs ? (size_t)q.Bb * q.Mp * WWs * c8 : 0);
+    q.o_tpart = take((size_t)q.nseq * 6 * sizeof(double));
   }
   size_t db = 0;
   const size_t maxwin = nobw > nwave ? nobw : nwave;
@@ -690,6 +938,12 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
   q.o_dft = take(db);
   q.total = o;
   return q;
+}
+
+// float32 division on the host (IEEE round to nearest, as the reference's float32 arithmetic)
+inline float fdiv_host(float a, float b) {
+  volatile float r = a / b;
+  return r;
 }
 
 // Krivanek (n, m, a/b) order of the first n aberrations (pypty/utils.py:1272-1308):
@@ -781,6 +1035,16 @@ struct Run {
       va.edge_mult = p->edge_mult;
       va.tan_x = v->tan_x;
       va.tan_y = v->tan_y;
+      va.tgrid = at<float>(ws, q.o_tgrid);
+      if (v->n_tilts > 0) {   // the shared propagator / CTF take row 0's inside tilt (objective.py:339-345)
+        va.tan_y = v->tilts_host[2];
+        va.tan_x = v->tilts_host[3];
+        if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), v->tilts_host, (size_t)q.n_rows * 6 * sizeof(float),
+                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+          return PTY_ERR_CUDA;
+      }
+      if (cudaMemsetAsync(at<double>(ws, q.o_tpart), 0, (size_t)q.nseq * 6 * sizeof(double), st) != cudaSuccess)
+        return PTY_ERR_CUDA;
       va.defocus = v->defocus;
       va.cs = v->cs;
       var_tables_kernel<<<(WW + 255) / 256, 256, 0, st>>>(va);
@@ -815,7 +1079,25 @@ struct Run {
     pa.shift = shift ? 1 : 0;
     pa.n_abs = q.n_abs;
     pa.n_sets = q.n_sets;
-    const bool var_probe = v && (shift || pa.bc || pa.coefs);
+    const bool var_probe = v && (shift || pa.bc || pa.coefs || q.before);
+    TiltArgs tg{};
+    tg.rows = at<float>(ws, q.o_tilts);
+    tg.grid = at<float>(ws, q.o_tgrid);
+    tg.single = q.single_tilt;
+    tg.W = W;
+    PropArgs pr{};
+    pr.mask = ta.mask;
+    pr.distance = p->slice_distance;
+    pr.wavelength = p->wavelength;
+    pr.px = p->pixel_size_x;
+    pr.py = p->pixel_size_y;
+    pr.edge_mult = p->edge_mult;
+    pr.defocus = v ? v->defocus : 0.0f;
+    pr.cs = v ? v->cs : 0.0f;
+    pr.W = W;
+    const bool tilted_prop = v && !q.same_prop;
+    float2* spec = at<float2>(ws, q.o_spec);
+    const size_t spec_stride = (size_t)q.Bb * nm * WWs;   // one forward step of the batch
     for (int i0 = 0, ib = 0; i0 < q.nseq; i0 += q.Bb, ++ib) {
       const int Bn = q.nseq - i0 < q.Bb ? q.nseq - i0 : q.Bb;
       const int* seq_b = at<int>(ws, q.o_seq) + i0;
@@ -830,7 +1112,36 @@ struct Run {
       const float2* pin = planes;
       size_t pin_stride = 0;
       pa.seq = seq_b;
-      if (var_probe) {
+      tg.seq = seq_b;
+      if (var_probe && q.before) {
+        // the probe before the tilt (after beam current and plates), then the tilt mask, then
+        // the shift: from the pre-plate spectrum with plates, else the tilted probe's
+        // (objective.py:448-476)
+        prof_mark(st, KID_ELEMENTWISE);
+        float2* pbt = at<float2>(ws, q.o_pbt);
+        VarProbeArgs p0 = pa;
+        p0.shift = 0;
+        var_probe_in_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(p0, p0.coefs ? pbs : pbt);
+        if (p0.coefs && (rc = dft(pbs, pbt, (long long)Bn * q.Mp, 1))) return rc;
+        if (cudaMemcpyAsync(pb, pbt, (size_t)Bn * q.Mp * WWs * sizeof(float2), cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess)
+          return PTY_ERR_CUDA;
+        var_tilt_mul_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pb, tg, q.Mp, 0, 0);
+        if (shift) {
+          if (pa.coefs) {
+            var_probe_in_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pa, pbs);
+          } else {
+            if ((rc = dft(pb, pbs, (long long)Bn * q.Mp, 0))) return rc;
+            if (cudaMemcpyAsync(at<float2>(ws, q.o_pft), pbs, (size_t)Bn * q.Mp * WWs * sizeof(float2),
+                                cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+              return PTY_ERR_CUDA;
+            var_ramp_mul_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pbs, ta.sx, ta.sy, ta.mask, d_corr, seq_b, W, q.Mp);
+          }
+          if ((rc = dft(pbs, pb, (long long)Bn * q.Mp, 1))) return rc;
+        }
+        pin = pb;
+        pin_stride = (size_t)q.Mp * WWs;
+      } else if (var_probe) {
         prof_mark(st, KID_ELEMENTWISE);
         const bool spectral = shift || pa.coefs;
         var_probe_in_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(pa, spectral ? pbs : pb);
@@ -850,21 +1161,56 @@ struct Run {
         fwd_slice_kernel<<<grid(nm, Bn), EB, 0, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp, q.Mo, WW);
         if (z < q.Z - 1) {
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
+          if (v && q.inside_grad &&   // FFT(psi O) of the step, for the inside-tilt gradient
+              cudaMemcpyAsync(spec + z * spec_stride, psi2, (size_t)Bn * nm * WWs * sizeof(float2),
+                              cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            return PTY_ERR_CUDA;
           prof_mark(st, KID_ELEMENTWISE);
-          prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? ta.prop_edge : ta.prop, WW,
-                                                       0, unfold);
+          if (tilted_prop)
+            var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, z == 0 && ta.use_edge, 0, 0, 1.0f);
+          else
+            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? ta.prop_edge : ta.prop, WW,
+                                                         0, unfold);
           if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
         }
       }
+      if (v && q.after) {
+        // tilt after the specimen (objective.py:490-499): one slice band-limits the exit first
+        prof_mark(st, KID_ELEMENTWISE);
+        if (q.Z == 1) {
+          if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
+          mask_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ta.mask, WW);
+          if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
+        }
+        if (cudaMemcpyAsync(at<float2>(ws, q.o_exitb), psi, (size_t)Bn * nm * WWs * sizeof(float2),
+                            cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+          return PTY_ERR_CUDA;
+        var_tilt_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi, tg, nm, 4, 0);
+      }
       // far field, loss, dL/dPsi (objective.py:501-597)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
+      if (v && q.inside_grad && q.near &&   // FFT(exit) for the near-field inside-tilt gradient
+          cudaMemcpyAsync(at<float2>(ws, q.o_fexit), psi2, (size_t)Bn * nm * WWs * sizeof(float2),
+                          cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return PTY_ERR_CUDA;
       if (!v) {
         prof_mark(st, KID_FINALIZE);
         loss_kernel<<<Bn, 1024, 0, st>>>(psi2, ta.mask, measured, seq_b, W, q.Mp, q.Mo, p->algorithm,
                                          p->loss_weight * (float)WW, at<double>(ws, q.o_loss_part) + 2 * i0);
         if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
-      } else if ((rc = variant_loss(psi, psi2, measured, seq_b, Bn, i0))) {
+      } else if ((rc = variant_loss(psi, psi2, measured, seq_b, Bn, i0, tg, pr))) {
         return rc;
+      }
+      double* tpart = at<double>(ws, q.o_tpart) + (size_t)i0 * 6;
+      if (v && q.after) {
+        // adjoint of the tilt after the specimen and its gradient (objective.py:620-639)
+        prof_mark(st, KID_ELEMENTWISE);
+        var_tilt_adj_kernel<<<Bn, 1024, 0, st>>>(psi, at<float2>(ws, q.o_exitb), tg, nm, 4, q.step_tilts, 0, tpart);
+        if (q.Z == 1) {
+          if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
+          mask_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ta.mask, WW);
+          if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
+        }
       }
       // adjoint multislice (multislice_core.py:158-200)
       for (int z = q.Z - 1; z >= 0; --z) {
@@ -873,8 +1219,19 @@ struct Run {
         if (z > 0) {
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
           prof_mark(st, KID_ELEMENTWISE);
-          prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, (z == 1 && ta.use_edge) ? ta.prop_edge : ta.prop, WW,
-                                                       1, unfold);
+          const bool edge = z == 1 && ta.use_edge;
+          if (tilted_prop)
+            var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, edge, 0, 1, 1.0f);
+          else
+            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, edge ? ta.prop_edge : ta.prop, WW, 1, unfold);
+          if (v && q.inside_grad) {
+            // sh = -4 pi d / W^2 in float32, d times the edge multiplier on the thick step
+            // (multislice_core.py:171-180)
+            const float dist = edge ? p->slice_distance * p->edge_mult : p->slice_distance;
+            const float shf = fdiv_host((float)-12.566370614359172 * dist, (float)WW);
+            var_inside_tilt_kernel<<<Bn, 1024, 0, st>>>(psi2, spec + (size_t)(z - 1) * spec_stride, nm, W,
+                                                        p->pixel_size_x, p->pixel_size_y, (double)shf, tpart);
+          }
           if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
         }
       }
@@ -894,16 +1251,32 @@ struct Run {
       }
       const bool step_bc = v && v->beam_current && v->step_beam_current;
       const bool step_ab = v && v->aberrations && v->step_aberrations;
-      if (p->step_probe || p->step_pos || step_bc || step_ab) {
+      const bool step_tb = v && q.before && q.step_tilts;
+      if (p->step_probe || p->step_pos || step_bc || step_ab || step_tb) {
         // probe-gradient spectra with the shift adjoint and the position gradient (objective.py:641-703)
         prof_mark(st, KID_PROBE_PARTIAL);
         probe_sum_kernel<<<grid(q.Mp, Bn), EB, 0, st>>>(psi, pbs, q.Mp, q.Mo, WW);
         if ((rc = dft(pbs, pb, (long long)Bn * q.Mp, 0))) return rc;
         prof_mark(st, KID_ELEMENTWISE);
-        if (var_probe)
-          var_probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(
-              pb, pa, p->step_pos, step_bc, step_ab, p->step_probe, at<double>(ws, q.o_pos_part) + (size_t)i0 * q.Mp * 2,
-              at<double>(ws, q.o_bc_part) + (size_t)i0 * q.Mp, at<double>(ws, q.o_ab_part) + (size_t)i0 * q.Mp * q.n_abs);
+        double* pos_part = at<double>(ws, q.o_pos_part) + (size_t)i0 * q.Mp * 2;
+        double* bc_part = at<double>(ws, q.o_bc_part) + (size_t)i0 * q.Mp;
+        double* ab_part = at<double>(ws, q.o_ab_part) + (size_t)i0 * q.Mp * q.n_abs;
+        if (var_probe && q.before) {
+          // shift adjoint, then the tilt adjoint in real space (objective.py:660-673), then
+          // plates and beam current
+          VarProbeArgs p1 = pa;
+          if (shift && !pa.coefs) p1.pspec = at<float2>(ws, q.o_pft);
+          var_probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(pb, p1, p->step_pos, step_bc, step_ab,
+                                                                p->step_probe, 1, 0, pos_part, bc_part, ab_part);
+          if ((rc = dft(pb, pbs, (long long)Bn * q.Mp, 1))) return rc;
+          var_tilt_adj_kernel<<<Bn, 1024, 0, st>>>(pbs, at<float2>(ws, q.o_pbt), tg, q.Mp, 0, q.step_tilts,
+                                                   q.Mp == 1, tpart);
+          if ((rc = dft(pbs, pb, (long long)Bn * q.Mp, 0))) return rc;
+          var_probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(pb, pa, p->step_pos, step_bc, step_ab,
+                                                                p->step_probe, 0, 1, pos_part, bc_part, ab_part);
+        } else if (var_probe)
+          var_probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(pb, pa, p->step_pos, step_bc, step_ab,
+                                                                p->step_probe, 1, 1, pos_part, bc_part, ab_part);
         else if (shift)
           probe_adj_kernel<<<dim3(q.Mp, Bn), 1024, 0, st>>>(pb, pf, ta.sx, ta.sy, ta.mask, d_corr, seq_b, W, q.Mp,
                                                            p->step_pos, at<double>(ws, q.o_pos_part) + (size_t)i0 * q.Mp * 2);
@@ -933,6 +1306,9 @@ struct Run {
     finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
                                                p->step_pos && shift, nullptr, loss_sse, pos_grad);
+    if (v && q.step_tilts)
+      var_tilt_finalize_kernel<<<1, 32, 0, st>>>(at<double>(ws, q.o_tpart), at<int>(ws, q.o_seq), q.nseq, q.n_rows,
+                                                 q.single_tilt, q.before, q.inside_grad, q.after, v->tilts_grad);
     if (v && ((v->beam_current && v->step_beam_current) || (v->aberrations && v->step_aberrations))) {
       const bool gb = v->beam_current && v->step_beam_current, ga = v->aberrations && v->step_aberrations;
       var_finalize_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_bc_part), at<double>(ws, q.o_ab_part),
@@ -946,7 +1322,8 @@ struct Run {
 
   // pattern, loss and dL/d(exit wave) of one batch for the variant branches: psi2 holds the
   // spectra of the exit waves; on return psi holds dL/d(exit wave) (objective.py:501-604)
-  int variant_loss(float2* psi, float2* psi2, const float* measured, const int* seq_b, int Bn, int i0) {
+  int variant_loss(float2* psi, float2* psi2, const float* measured, const int* seq_b, int Bn, int i0,
+                   const TiltArgs& tg, const PropArgs& pr) {
     int rc;
     const int W = q.W, WW = q.WW, nm = q.Mp * q.Mo;
     float* ibuf = at<float>(ws, q.o_ibuf);
@@ -955,7 +1332,10 @@ struct Run {
     float2* field = psi2;
     prof_mark(st, KID_FINALIZE);
     if (q.near) {   // wave = IFFT(FFT(exit) * CTF) (objective.py:506-508)
-      prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 0, 1.0f);
+      if (q.single_tilt)
+        prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 0, 1.0f);
+      else   // the position's inside tilt
+        var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, 0, 1, 0, 1.0f);
       if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
       field = psi;
     }
@@ -976,7 +1356,14 @@ struct Run {
     if (q.near) {   // dL/d(exit) = IFFT(loss_weight FFT(wave dL/dI) conj(CTF)) (objective.py:602-604)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
       prof_mark(st, KID_ELEMENTWISE);
-      prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 1, p->loss_weight);
+      if (q.single_tilt)
+        prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 1, p->loss_weight);
+      else
+        var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, 0, 1, 1, p->loss_weight);
+      if (q.inside_grad)   // near-field inside-tilt gradient (objective.py:605-619)
+        var_near_tilt_kernel<<<Bn, 1024, 0, st>>>(psi2, at<float2>(ws, q.o_fexit), nm, W, p->pixel_size_x,
+                                                  p->pixel_size_y, v->defocus, -12.566370614359172 / (double)WW,
+                                                  at<double>(ws, q.o_tpart) + (size_t)i0 * 6);
     }
     return dft(psi2, psi, (long long)Bn * nm, 1);
   }
@@ -1047,6 +1434,9 @@ int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
   if (v->recon_type != 0 && v->recon_type != 1) return PTY_ERR_UNSUPPORTED;
   if (v->data_pad < 0 || 2 * v->data_pad >= p->window) return PTY_ERR_INVALID;
   if (compressed && v->data_pad != 0) return PTY_ERR_UNSUPPORTED;
+  if (v->n_tilts < 0 || (v->n_tilts > 0 && (!v->tilts_host || (v->n_tilts != 1 && v->n_tilts != p->n_positions))))
+    return PTY_ERR_INVALID;
+  if (v->n_tilts > 0 && (v->tilt_mode < 0 || v->tilt_mode > 4)) return PTY_ERR_UNSUPPORTED;
   if (compressed && (v->n_masks <= 0 || !v->masks)) return PTY_ERR_INVALID;
   if (v->beam_current && v->step_beam_current && !v->beam_current_grad) return PTY_ERR_INVALID;
   if (v->aberrations) {

@@ -183,6 +183,7 @@ class Engine:
                                     aberration_marker: torch.Tensor | None = None, step_aberrations: bool = False,
                                     data_pad: int = 0, use_padded_intensity: bool = True,
                                     data_shift_vector=(0, 0), data_multiplier: float = 1.0,
+                                    tilts=None, tilt_mode: int = 0, step_tilts: bool = False,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
@@ -190,11 +191,13 @@ class Engine:
         measured is (n_positions, W - 2 data_pad, W - 2 data_pad) float32 (device memory, or
         pinned host memory read in place), or (n_positions, n_masks) for the compressed
         algorithms; data_pad / use_padded_intensity / data_shift_vector / data_multiplier are
-        the reference's per-batch measured-data preprocessing, applied on the fly; masks (n_masks, W, W) float32 in pattern order; beam_current
+        the reference's per-batch measured-data preprocessing, applied on the fly; tilts
+        (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
+        one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
         (n_positions,) int32; pos_correction as in ``loss_and_direction``. Returns (loss_sse,
         object_grad, probe_grad, pos_grad, beam_current_grad or None, aberrations_grad or
-        None)."""
+        None, tilts_grad or None)."""
         stream = stream or torch.cuda.current_stream(self.device)
         compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
         self._check_inputs(problem, obj, probe, None)
@@ -228,6 +231,15 @@ class Engine:
             if bc_d is not None and step_beam_current else None
         ab_grad = torch.zeros(tuple(ab_d.shape), dtype=torch.float32, device=self.device) \
             if ab_d is not None and step_aberrations else None
+        tilts_h = None
+        tilts_grad = None
+        if tilts is not None:
+            tilts_h = np.ascontiguousarray(np.asarray(tilts.cpu() if torch.is_tensor(tilts) else tilts,
+                                                      dtype=np.float32).reshape(-1, 6))
+            if tilts_h.shape[0] not in (1, problem.n_positions):
+                raise ValueError("tilts must have one row or one row per position")
+            if step_tilts:
+                tilts_grad = torch.zeros(tuple(tilts_h.shape), dtype=torch.float32, device=self.device)
         v = _lib.Variant(recon_type=_lib.RECON_TYPES[recon_type], defocus=float(defocus), cs=float(cs),
                          tan_x=float(tan_x), tan_y=float(tan_y),
                          n_masks=0 if masks_d is None else int(masks_d.shape[0]),
@@ -243,7 +255,11 @@ class Engine:
                          aberrations_grad=None if ab_grad is None else ab_grad.data_ptr(),
                          data_pad=int(data_pad), use_padded_intensity=int(bool(use_padded_intensity)),
                          shift_y=int(data_shift_vector[0]), shift_x=int(data_shift_vector[1]),
-                         data_multiplier=float(data_multiplier))
+                         data_multiplier=float(data_multiplier),
+                         n_tilts=0 if tilts_h is None else int(tilts_h.shape[0]),
+                         tilts_host=None if tilts_h is None else tilts_h.ctypes.data,
+                         tilt_mode=int(tilt_mode), step_tilts=int(tilts_grad is not None),
+                         tilts_grad=None if tilts_grad is None else tilts_grad.data_ptr())
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")
@@ -265,7 +281,7 @@ class Engine:
         for t in keep:
             t.record_stream(stream)
         _lib.check(st, "pty_loss_and_direction_variants")
-        return loss_sse, og, pg, posg, bc_grad, ab_grad
+        return loss_sse, og, pg, posg, bc_grad, ab_grad, tilts_grad
 
     def forward(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
                 measured: torch.Tensor, stream=None):

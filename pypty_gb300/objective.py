@@ -9,8 +9,8 @@ Supported flag set: ``propmethod="multislice"``, one slice distance, algorithms 
 ``ml``, ``lsq``, ``lsq_sqrt_2`` on the fused path; with any of far-field or near-field
 propagation (one defocus, ``Cs``; ``pypty/objective.py:504-508``), the compressed-detector
 algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations and their
-gradient, aberration arrays with markers and their gradient, or one inside beam tilt
-(``tilt_mode`` 0, one tilt row, no tilt refinement) on the variants path
+gradient, aberration arrays with markers and their gradient, or beam tilts (``tilt_mode``
+0-4, one tilt row or one per position, with the tilt gradient) on the variants path
 (``pty_loss_and_direction_variants``). No phase plates, probe markers, static background,
 data binning (the reference raises on it) or upsampling, near-field ``alpha_near_field``
 (the reference raises on it) or regularisers. The per-batch measured-data preprocessing
@@ -108,13 +108,15 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     compressed = algorithm_type in _lib.COMPRESSED_ALGORITHMS
     _unsupported(algorithm_type not in _lib.ALGORITHMS and not compressed, "algorithm_type=%r" % (algorithm_type,))
     _unsupported(compressed and masks is None, "compressed algorithms without masks")
-    _unsupported(bool(this_step_tilts) or tilt_mode not in (0, None), "beam tilts (tilt_mode/this_step_tilts)")
-    tilts = np.asarray(_to_numpy(this_tilt_array), dtype=np.float64)
-    if not _is_zero(this_tilts_correction):
-        tilts = tilts + np.asarray(_to_numpy(this_tilts_correction), dtype=np.float64)
-    _unsupported(tilts.ndim != 2 or (tilts.shape[0] != 1 and not _is_zero(tilts)),
-                 "per-position beam tilts")          # objective.py:339-345: one tilt row only
-    tan_y, tan_x = (float(tilts[0, 2]), float(tilts[0, 3])) if tilts.size else (0.0, 0.0)
+    tmode = 0 if tilt_mode is None else int(tilt_mode)
+    _unsupported(tmode not in (0, 1, 2, 3, 4), "tilt_mode=%r" % (tilt_mode,))
+    # the reference adds the correction in the default float type (objective.py:343, 348)
+    tilts = np.asarray(_to_numpy(this_tilt_array), dtype=np.float32) + \
+        np.asarray(_to_numpy(this_tilts_correction), dtype=np.float32)
+    n_pos = int(np.asarray(_to_numpy(this_pos_array)).shape[0])
+    _unsupported(tilts.ndim != 2 or tilts.shape[1] != 6 or tilts.shape[0] not in (1, n_pos),
+                 "tilt arrays that are not one row or one row per position")
+    tilted = tmode != 0 or bool(this_step_tilts) or not _is_zero(tilts)
     _unsupported(np.asarray(_to_numpy(this_distances)).reshape(-1).shape[0] != 1, "per-slice distances")
     _unsupported(phase_plate_in_h5 is not None, "phase plates")
     _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
@@ -161,10 +163,11 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
         step_pos=bool(this_step_pos_correction))
     variant = None
-    if near or compressed or prep or beam_current is not None or aberrations_array is not None or tan_x or tan_y:
+    if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted:
         variant = dict(recon_type=recon_type,
                        defocus=float(np.asarray(_to_numpy(defocus_array)).reshape(-1)[0]) if near else 0.0,
-                       cs=float(Cs) if near else 0.0, tan_x=tan_x, tan_y=tan_y,
+                       cs=float(Cs) if near else 0.0, tilts=tilts, tilt_mode=tmode,
+                       step_tilts=bool(this_step_tilts),
                        masks=None if not compressed else _to_numpy(masks),
                        beam_current=None if beam_current is None else _to_numpy(beam_current),
                        step_beam_current=bool(this_beam_current_step),
@@ -212,6 +215,7 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     probe_d = _device_tensor(full_probe, torch.complex64, dev)
     meas_d = measured_tensor(measured_array, dev, bool(load_one_by_one))
     bc_grad, ab_grad = 0, 0
+    tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))    # objective.py:380
     if variant is None:
         loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
     else:
@@ -220,8 +224,10 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
                       ("aberration_marker", torch.int32)):
             if kw[k] is not None:
                 kw[k] = _device_tensor(kw[k], dt, dev)
-        loss_sse, og, pg, posg, bcg, abg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo, meas_d,
-                                                                           **kw)
+        loss_sse, og, pg, posg, bcg, abg, tg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo,
+                                                                               meas_d, **kw)
+        if tg is not None:
+            tilts_grad = tg.cpu().numpy().astype(_to_numpy(this_tilts_correction).dtype, copy=False)
         # zero-initialised accumulators of the reference (objective.py:381-382)
         if beam_current is not None:
             bc_grad = np.zeros_like(_to_numpy(beam_current)) if bcg is None else \
@@ -235,7 +241,6 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         raise ValueError('A very specific bad thing. Loss is Nan.')   # objective.py:925-926
     if not this_step_probe:
         pg = torch.zeros((1,) + tuple(pg.shape), dtype=pg.dtype, device=pg.device)  # objective.py:747-751
-    tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))
     constraints = np.zeros(N_CONSTRAINTS)
     if obj_is_numpy:
         og_out = og.cpu().numpy().astype(in_dtype, copy=False)

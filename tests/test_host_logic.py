@@ -41,7 +41,7 @@ def base_kwargs(**over):
     dict(recon_type="fresnel"), dict(recon_type="near_field", alpha_near_field=0.1),
     dict(recon_type="near_field", defocus_array=np.array([1.0, 2.0])), dict(propmethod="yoshida"),
     dict(algorithm_type="lsq_compressed"), dict(algorithm_type="huber"),
-    dict(this_step_tilts=1), dict(tilt_mode=3), dict(this_tilt_array=np.ones((2, 6), np.float32)),
+    dict(tilt_mode=7), dict(this_tilt_array=np.ones((3, 6), np.float32)),
     dict(this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
     dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
     dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_bin=2),
@@ -138,7 +138,11 @@ def test_variant_flags_route_to_the_variants_path():
     corr = np.zeros((1, 6), np.float32)
     corr[0, 3] = 1e-3
     _, _, v = objective.prepare(**base_kwargs(this_tilt_array=tilt, this_tilts_correction=corr))
-    assert v["tan_y"] == pytest.approx(-1e-3) and v["tan_x"] == pytest.approx(3e-3)   # tilt + correction
+    assert v["tilts"][0, 2] == pytest.approx(-1e-3) and v["tilts"][0, 3] == pytest.approx(3e-3)   # + correction
+    rows = np.full((2, 6), 1e-3, np.float32)
+    _, _, v = objective.prepare(**base_kwargs(this_tilt_array=rows, this_tilts_correction=np.zeros_like(rows),
+                                              tilt_mode=4, this_step_tilts=1))
+    assert v["tilt_mode"] == 4 and v["step_tilts"] and v["tilts"].shape == (2, 6)
     masks = np.ones((3, 64, 64), np.float32)
     _, _, v = objective.prepare(**base_kwargs(algorithm_type="poisson_compressed", masks=masks,
                                               measured_array=np.zeros((2, 3), np.float32)))
