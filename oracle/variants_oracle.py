@@ -1,7 +1,7 @@
 """NumPy restatement of the other propagation / loss / probe branches of pypty's
 ``objective.loss_and_direction``: near-field propagation, compressed-detector losses,
-beam-current fluctuations, per-position aberration phase plates and a single inside beam
-tilt.
+beam-current fluctuations, per-position aberration phase plates, beam tilts and the
+per-batch measured-data preprocessing.
 
 TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): this module checks the CUDA path; it
 is never part of it.
@@ -15,9 +15,10 @@ defocus (``is_single_defocus``) and spherical aberration ``Cs`` (``objective.py:
 ``lsq_compressed``, ``gauss_compressed`` and ``poisson_compressed`` with detector masks
 (``objective.py:560-585``); ``beam_current`` with its gradient (``objective.py:448-452,
 687-697``); ``aberrations_array`` / ``aberration_marker`` with their gradient
-(``objective.py:324-329, 459-463, 676-684``); one inside tilt (``tilt_mode`` 0, a single tilt
-row, ``objective.py:337-345, 505``) without tilt gradients. Every step cites the reference
-line it restates; dtypes follow the reference in single or double precision.
+(``objective.py:324-329, 459-463, 676-684``); beam tilts (``tilt_mode`` 0-4, one tilt row or
+one per position, with the tilt gradient: ``objective.py:302-345, 464-499, 605-673``,
+``multislice_core.py:76-77, 178-182``). Every step cites the reference line it restates;
+dtypes follow the reference in single or double precision.
 
 The near-field partial-coherence correction (``alpha_near_field > 0``) is not restated: the
 reference's envelope has shape (1, 1, W, W) (``objective.py:514``, ``q2`` already carries a
@@ -25,10 +26,12 @@ leading axis), its forward transforms the wrong axes and its adjoint raises a br
 error (``objective.py:600`` into ``multislice_core.py:161``), so the branch has no reference
 result to match; this function raises ValueError for it, as the reference raises.
 
-Two reference behaviours are restated as they are: with a probe shift active, the forward
-probe is built from the spectrum taken before the aberration plate (``objective.py:461,
-471-476``: ``this_probe_fourier`` is not updated by the plate) while the adjoint still applies
-the plate's conjugate; and the gradient arrays come back in the reference's order.
+Reference behaviours restated as they are: with a probe shift active, the forward probe is
+built from the spectrum taken before the aberration plate (``objective.py:461, 471-476``:
+``this_probe_fourier`` is not updated by the plate or a tilt after it) while the adjoint
+still applies their conjugates; with one probe mode the before-tilt gradient's x component
+uses the x grid's first column (``objective.py:664``); one tilt row with inside-tilt
+refinement raises for batches of more than one position (``multislice_core.py:181``).
 """
 from __future__ import annotations
 
