@@ -86,6 +86,14 @@ def fused_bytes_per_position(W, Z, Mp, Mo=1):
     return W * W * (16 * Z * Mo + 16 * Z * Mp * Mo + 8 * Z * Mo + 4 + 8 * Mp)
 
 
+# DRAM bytes (read + write) per position of the fused kernel(s), from one ncu capture each
+# (dram__bytes_read.sum + dram__bytes_write.sum of the launch / positions in it); a launch of
+# the same shape moves the same bytes per position, so traffic per launch scales by positions:
+#   (128, 20, 3): fused_multislice_kernel<128>, multislice-small, 64 positions, 1.3708 GB
+#   (256, 8, 5):  fused256_kernel<1> + <2>, precision-sweep-small, 64 positions, 10.674 GB
+TRAFFIC_PER_POSITION = {(128, 20, 3): 1.3708e9 / 64, (256, 8, 5): 10.674e9 / 64}
+
+
 def fft_flops_per_position(W, Z, Mp, Mo=1):
     """5 W^2 log2(W^2) flops per 2D FFT; FFTs per position of the reference algorithm:
     4 Z Mo (object and gradient band limits) + 4 (Z-1) Mp Mo (propagation both ways)
@@ -599,7 +607,11 @@ def main():
                               "note": "measured patterns read in place from pinned host memory"},
         "roofline": {"bound": "hbm", "kernel": "fused_multislice", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src + " (hbm_gbs)",
-                     "traffic": None, "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3},
+                     "traffic": (TRAFFIC_PER_POSITION[(W, Z, Mp)] * per_launch_pos
+                                 if (W, Z, Mp) in TRAFFIC_PER_POSITION else None),
+                     "traffic_source": "ncu dram bytes of a 64-position capture of the same shape, scaled by "
+                                       "positions per launch (profiles/)",
+                     "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3},
         "path_roofline": {"alg_bytes_per_position": alg_bytes_per_position(W, Z, Mp),
                           "achieved_gbs": path_bytes / (ms / 1000.0) / 1e9,
                           "frac": path_bytes / (ms / 1000.0) / 1e9 / hbm_peak,

@@ -340,18 +340,21 @@ int pty_fourier_clean_apply(const void* x, const void* dx, double step, void* ou
                             int64_t k, const void* workspace, size_t workspace_bytes, void* stream);
 
 /*
- * The optimizer's vector space: up to three float32 segments (the object, the probe and the
- * position corrections of pypty/iterative.py:583-606; a complex64 element counts as two
- * floats). Every inner product is sum_seg weight[seg] * <a_seg, b_seg>; the reference's
- * weights are 2 for the complex segments and 1 for the positions (iterative.py:597-606).
- * obj_seg names the object segment for the first step's normalisation (-1: none).
- * Vectors are passed as arrays of n_seg device pointers.
+ * The optimizer's vector space: up to PTY_VSPACE_MAX_SEG float32 segments (the object, the
+ * probe, the position corrections, the tilt corrections, the aberration arrays and the beam
+ * currents of pypty/iterative.py:583-672; a complex64 element counts as two floats). Every
+ * inner product is sum_seg weight[seg] * <a_seg, b_seg>; the reference's weights are 2 for
+ * the complex segments and 1 for the real ones (iterative.py:597-609). Each segment has its
+ * own Barzilai-Borwein gamma (iterative.py:626-647, 869-916). obj_seg names the object
+ * segment for the first step's normalisation (-1: none). Vectors are passed as arrays of
+ * n_seg device pointers.
  */
+#define PTY_VSPACE_MAX_SEG 6
 typedef struct pty_vspace {
   int32_t n_seg;
   int32_t obj_seg;
-  int64_t n[3];
-  double weight[3];
+  int64_t n[PTY_VSPACE_MAX_SEG];
+  double weight[PTY_VSPACE_MAX_SEG];
 } pty_vspace_t;
 
 /* Device bytes of the optimizer state (FP64 scalars, partial sums); caller-allocated. */
@@ -383,7 +386,8 @@ int pty_lbfgs_axpy(const pty_vspace_t* vs, float* const* out, float* const* a, f
 int pty_lbfgs_accept(const pty_vspace_t* vs, double step, float* const* dir, float* const* grad,
                      float* const* new_grad, float* const* s_out, float* const* y_out, int32_t slot,
                      void* state, void* stream);
-/* Synchronising read of 8 doubles: d_value, new_d_value, gamma[3], last reduced dots[3]. */
+/* Synchronising read of 2 + 2 * PTY_VSPACE_MAX_SEG doubles: d_value, new_d_value,
+ * gamma[PTY_VSPACE_MAX_SEG], last reduced dots[PTY_VSPACE_MAX_SEG]. */
 int pty_lbfgs_read(const void* state, double* out, void* stream);
 /* Gram-Schmidt over the modes of a (n_pixels, n_modes) complex64 probe, in place
  * (pypty/objective.py:1119-1141, keep_probe_states_orthogonal). */

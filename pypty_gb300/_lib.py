@@ -41,10 +41,14 @@ class Problem(ctypes.Structure):
     ]
 
 
+VSPACE_MAX_SEG = 6
+
+
 class VSpace(ctypes.Structure):
-    """Mirror of ``pty_vspace_t``: the optimizer's (object, probe, positions) segments."""
+    """Mirror of ``pty_vspace_t``: the optimizer's segments (object, probe, positions, tilts,
+    aberrations, beam current)."""
     _fields_ = [("n_seg", ctypes.c_int32), ("obj_seg", ctypes.c_int32),
-                ("n", ctypes.c_int64 * 3), ("weight", ctypes.c_double * 3)]
+                ("n", ctypes.c_int64 * VSPACE_MAX_SEG), ("weight", ctypes.c_double * VSPACE_MAX_SEG)]
 
 
 class Variant(ctypes.Structure):

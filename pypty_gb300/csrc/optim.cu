@@ -272,16 +272,17 @@ CleanWs clean_ws(int ny, int nx) {
 constexpr int VB = 608;    // fixed reduction grid: 4 blocks per SM of a 152-SM GB300
 constexpr int VT = 256;
 constexpr int HMAX = 64;   // history slots
+constexpr int NSEG = PTY_VSPACE_MAX_SEG;   // object, probe, positions, tilts, aberrations, beam current
 
 struct OptState {
-  double w[3];              // inner-product weight of each segment
-  double coef[6];           // a-coefficients, b-coefficients of the next vector pass
-  double dot[3];            // last reduced inner products, per segment (unweighted)
-  double dot2[3];           // second reduced product (accept: y.s)
-  double gamma[3];          // Barzilai-Borwein scaling per segment
-  double dval, dval_new;    // directional derivatives at the start point and at the trial
+  double w[NSEG];              // inner-product weight of each segment
+  double coef[2 * NSEG];       // a-coefficients, b-coefficients of the next vector pass
+  double dot[NSEG];            // last reduced inner products, per segment (unweighted)
+  double dot2[NSEG];           // second reduced product (accept: y.s)
+  double gamma[NSEG];          // Barzilai-Borwein scaling per segment
+  double dval, dval_new;       // directional derivatives at the start point and at the trial
   double rho[HMAX], alpha[HMAX];
-  double part[2][3][VB];    // per-block partial sums of the last reduction
+  double part[2][NSEG][VB];    // per-block partial sums of the last reduction
 };
 
 struct VSeg {
@@ -294,12 +295,12 @@ struct VSeg {
 };
 
 struct VecArgs {
-  VSeg seg[3];
+  VSeg seg[NSEG];
   int nseg;
-  const double* coef;   // device coefficients [a0 a1 a2 b0 b1 b2], or nullptr: use hc
-  double hc[6];
+  const double* coef;   // device coefficients [a_0 .. a_NSEG-1, b_0 .. b_NSEG-1], or nullptr: use hc
+  double hc[2 * NSEG];
   int dot_out;          // 1: the inner product's left operand is the value just written
-  double* part;         // [3][VB] partial sums (a dot is taken where seg.dy != nullptr)
+  double* part;         // [NSEG][VB] partial sums (a dot is taken where seg.dy != nullptr)
 };
 
 __device__ __forceinline__ float lin(float ca, float a, float cb, const float* b, long long i, bool hb) {
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(VT) vec_kernel(VecArgs A) {
   for (int sg = 0; sg < A.nseg; ++sg) {
     const VSeg S = A.seg[sg];
     const float ca = (float)(A.coef ? A.coef[sg] : A.hc[sg]);
-    const float cb = (float)(A.coef ? A.coef[3 + sg] : A.hc[3 + sg]);
+    const float cb = (float)(A.coef ? A.coef[NSEG + sg] : A.hc[NSEG + sg]);
     const bool hb = S.b != nullptr, dot = S.dy != nullptr, wr = S.out != nullptr;
     double acc = 0.0;
     const bool v4 = (S.n % 4 == 0) && al16(S.out) && al16(S.a) && al16(S.b) && al16(S.dx) && al16(S.dy);
@@ -377,15 +378,15 @@ __global__ void __launch_bounds__(VT) vec_kernel(VecArgs A) {
 // History pair of an accepted step: s = step * q, y = new_g - g, and the partial sums of
 // <y, y> (buffer 0) and <y, s> (buffer 1) per segment (pypty/iterative.py:849-856, 869-916).
 struct AcceptArgs {
-  const float* q[3];
-  const float* g[3];
-  const float* ng[3];
-  float* s[3];
-  float* y[3];
-  long long n[3];
+  const float* q[NSEG];
+  const float* g[NSEG];
+  const float* ng[NSEG];
+  float* s[NSEG];
+  float* y[NSEG];
+  long long n[NSEG];
   int nseg;
   float step;
-  double* part;   // [2][3][VB]
+  double* part;   // [2][NSEG][VB]
 };
 
 __global__ void __launch_bounds__(VT) accept_kernel(AcceptArgs A) {
@@ -402,9 +403,9 @@ __global__ void __launch_bounds__(VT) accept_kernel(AcceptArgs A) {
       ays += (double)(yv * sv);
     }
     const double tyy = block_sum(ayy, red);
-    if (threadIdx.x == 0) A.part[(0 * 3 + sg) * VB + blockIdx.x] = tyy;
+    if (threadIdx.x == 0) A.part[(0 * NSEG + sg) * VB + blockIdx.x] = tyy;
     const double tys = block_sum(ays, red);
-    if (threadIdx.x == 0) A.part[(1 * 3 + sg) * VB + blockIdx.x] = tys;
+    if (threadIdx.x == 0) A.part[(1 * NSEG + sg) * VB + blockIdx.x] = tys;
   }
 }
 
@@ -425,7 +426,7 @@ enum ScalarOp {
 __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int slot, int final_beta) {
   const int lane = threadIdx.x;
   const int nbuf = op == OP_ACCEPT ? 2 : 1;
-  double d[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  double d[2][NSEG] = {};
   if (op != OP_GAMMA && op != OP_STEEPEST) {
     for (int b = 0; b < nbuf; ++b)
       for (int sg = 0; sg < nseg; ++sg) {
@@ -449,7 +450,7 @@ __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int sl
       if (dvo == 0.0) dvo = 1.0;
       for (int sg = 0; sg < nseg; ++sg) {
         S->coef[sg] = sg == obj_seg ? -1.0 : -dvo / (S->w[sg] * d[0][sg]);
-        S->coef[3 + sg] = 0.0;
+        S->coef[NSEG + sg] = 0.0;
       }
       break;
     }
@@ -457,7 +458,7 @@ __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int sl
       for (int sg = 0; sg < nseg; ++sg) {
         const double gm = S->gamma[sg];
         S->coef[sg] = (gm > 0.0 && gm == gm) ? -gm : -1.0;
-        S->coef[3 + sg] = 0.0;
+        S->coef[NSEG + sg] = 0.0;
       }
       break;
     case OP_ALPHA: {
@@ -465,7 +466,7 @@ __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int sl
       S->alpha[slot] = a;
       for (int sg = 0; sg < nseg; ++sg) {
         S->coef[sg] = 1.0;
-        S->coef[3 + sg] = -a;
+        S->coef[NSEG + sg] = -a;
       }
       break;
     }
@@ -473,14 +474,14 @@ __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int sl
       for (int sg = 0; sg < nseg; ++sg) {
         const double gm = S->gamma[sg];
         S->coef[sg] = (gm != 0.0 && gm == gm) ? gm : 1.0;
-        S->coef[3 + sg] = 0.0;
+        S->coef[NSEG + sg] = 0.0;
       }
       break;
     case OP_BETA: {
       const double beta = S->alpha[slot] - S->rho[slot] * wsum;
       for (int sg = 0; sg < nseg; ++sg) {
         S->coef[sg] = final_beta ? -1.0 : 1.0;
-        S->coef[3 + sg] = final_beta ? -beta : beta;
+        S->coef[NSEG + sg] = final_beta ? -beta : beta;
       }
       break;
     }
@@ -501,16 +502,18 @@ __global__ void scalar_kernel(OptState* S, int op, int nseg, int obj_seg, int sl
   }
 }
 
-__global__ void reset_kernel(OptState* S, double w0, double w1, double w2) {
+struct SegWeights {
+  double w[NSEG];
+};
+
+__global__ void reset_kernel(OptState* S, SegWeights W) {
   if (threadIdx.x != 0) return;
-  S->w[0] = w0;
-  S->w[1] = w1;
-  S->w[2] = w2;
-  for (int i = 0; i < 3; ++i) {
+  for (int i = 0; i < NSEG; ++i) {
+    S->w[i] = W.w[i];
     S->gamma[i] = 1.0;
     S->dot[i] = S->dot2[i] = 0.0;
   }
-  for (int i = 0; i < 6; ++i) S->coef[i] = 0.0;
+  for (int i = 0; i < 2 * NSEG; ++i) S->coef[i] = 0.0;
   S->dval = S->dval_new = 0.0;
   for (int i = 0; i < HMAX; ++i) S->rho[i] = S->alpha[i] = 0.0;
 }
@@ -570,7 +573,7 @@ __global__ void __launch_bounds__(1024) orthogonalize_kernel(float2* p, long lon
 
 // ------------------------------------------------------------------ host helpers
 int check_vspace(const pty_vspace_t* vs) {
-  if (!vs || vs->n_seg < 1 || vs->n_seg > 3) return PTY_ERR_INVALID;
+  if (!vs || vs->n_seg < 1 || vs->n_seg > NSEG) return PTY_ERR_INVALID;
   if (vs->obj_seg < -1 || vs->obj_seg >= vs->n_seg) return PTY_ERR_INVALID;
   for (int i = 0; i < vs->n_seg; ++i)
     if (vs->n[i] <= 0) return PTY_ERR_INVALID;
@@ -592,7 +595,7 @@ int run_vec(const pty_vspace_t* vs, float* const* out, float* const* a, float* c
     if (A.seg[i].dy && !dot_out && !A.seg[i].dx) return PTY_ERR_INVALID;
   }
   A.coef = coef;
-  for (int i = 0; i < 6; ++i) A.hc[i] = hc ? hc[i] : 0.0;
+  for (int i = 0; i < 2 * NSEG; ++i) A.hc[i] = hc ? hc[i] : 0.0;
   A.dot_out = dot_out;
   A.part = &S->part[0][0][0];
   prof_mark(st, KID_VEC);
@@ -702,9 +705,9 @@ int pty_lbfgs_reset(const pty_vspace_t* vs, void* state, void* stream) {
   int rc = check_vspace(vs);
   if (rc) return rc;
   if (!state) return PTY_ERR_INVALID;
-  reset_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<OptState*>(state), vs->weight[0], vs->n_seg > 1 ? vs->weight[1] : 0.0,
-      vs->n_seg > 2 ? vs->weight[2] : 0.0);
+  SegWeights sw{};
+  for (int i = 0; i < vs->n_seg; ++i) sw.w[i] = vs->weight[i];
+  reset_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<OptState*>(state), sw);
   return cudaGetLastError() == cudaSuccess ? PTY_OK : PTY_ERR_CUDA;
 }
 
@@ -749,7 +752,8 @@ int pty_lbfgs_two_loop(const pty_vspace_t* vs, float* const* grad, float* const*
   const int ns = vs->n_seg;
   auto Sv = [&](int i) { return s_hist + (size_t)i * ns; };
   auto Yv = [&](int i) { return y_hist + (size_t)i * ns; };
-  const double copy[6] = {1, 1, 1, 0, 0, 0};
+  double copy[2 * NSEG] = {};   // a = 1, b = 0: q = g
+  for (int i = 0; i < NSEG; ++i) copy[i] = 1.0;
   // q = g; alpha_{m-1}
   if ((rc = run_vec(vs, dir, grad, nullptr, nullptr, Sv(m - 1), 1, nullptr, copy, S, st))) return rc;
   if ((rc = run_scalar(S, OP_ALPHA, vs, slots[m - 1], 0, st))) return rc;
@@ -796,7 +800,7 @@ int pty_lbfgs_axpy(const pty_vspace_t* vs, float* const* out, float* const* a, f
     if (!out[i] || !a[i] || !b[i]) return PTY_ERR_INVALID;
     A.seg[i] = VSeg{out[i], a[i], b[i], nullptr, nullptr, vs->n[i]};
     A.hc[i] = 1.0;
-    A.hc[3 + i] = step;
+    A.hc[NSEG + i] = step;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   prof_mark(st, KID_VEC);
@@ -838,11 +842,11 @@ int pty_lbfgs_read(const void* state, double* out, void* stream) {
   if (!state || !out) return PTY_ERR_INVALID;
   const OptState* S = static_cast<const OptState*>(state);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // d_value, new_d_value, gamma[3], dot[3]
+  // d_value, new_d_value, gamma[NSEG], dot[NSEG]
   if (cudaMemcpyAsync(out, &S->dval, 2 * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess) return PTY_ERR_CUDA;
-  if (cudaMemcpyAsync(out + 2, &S->gamma[0], 3 * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
+  if (cudaMemcpyAsync(out + 2, &S->gamma[0], NSEG * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
     return PTY_ERR_CUDA;
-  if (cudaMemcpyAsync(out + 5, &S->dot[0], 3 * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
+  if (cudaMemcpyAsync(out + 2 + NSEG, &S->dot[0], NSEG * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
     return PTY_ERR_CUDA;
   return cudaStreamSynchronize(st) == cudaSuccess ? PTY_OK : PTY_ERR_CUDA;
 }

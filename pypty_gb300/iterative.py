@@ -15,7 +15,8 @@ container type they came in (NumPy arrays or CUDA tensors). The loss and gradien
 from the fused ``pty_loss_and_direction`` with the arguments the reference passes
 (``pypty/iterative.py:524,773``; ``smooth_rolloff`` 0 for the loss).
 
-Supported: object, probe and position-correction refinement, ``lazy_clean``,
+Supported: object, probe and position-correction refinement and, on the variants path, tilt
+correction, aberration-array and beam-current refinement; ``lazy_clean``,
 ``keep_probe_states_orthogonal``, ``probe_reg_weight = inf`` (aperture-cleaned probe
 gradients), ``smart_memory`` (same arithmetic), ``hist_length``, Wolfe constants,
 ``max_count``, ``reduce_factor``, ``optimism``, ``stepsize_threshold_low``, and every
@@ -98,10 +99,12 @@ def _impl(ns, a):
     update_obj = a["this_step_obj"] > 0
     update_probe = a["this_step_probe"] > 0
     update_pos = a["this_step_pos_correction"] > 0
-    _unsupported(a["this_step_tilts"] > 0, "tilt refinement")
+    update_tilts = a["this_step_tilts"] > 0
+    update_ab = a["this_step_aberrations_array"] > 0
+    update_bc = a["this_beam_current_step"] > 0
     _unsupported(a["this_step_static_background"] > 0, "static-background refinement")
-    _unsupported(a["this_step_aberrations_array"] > 0, "aberration refinement")
-    _unsupported(a["this_beam_current_step"] > 0, "beam-current refinement")
+    _unsupported(update_ab and getattr(ns, "aberrations_array", None) is None, "aberration refinement without arrays")
+    _unsupported(update_bc and getattr(ns, "beam_current", None) is None, "beam-current refinement without currents")
     _unsupported(bool(a["phase_only_obj"]), "phase_only_obj")
     _unsupported(bool(a["tune_only_probe_phase"]) or bool(a["tune_only_probe_abs"]),
                  "tune_only_probe_phase / tune_only_probe_abs")
@@ -121,13 +124,13 @@ def _impl(ns, a):
     problem, geo, variant = objective.prepare(
         ns.obj, ns.probe, ns.positions, ns.positions_correction, ns.tilts, ns.tilts_correction,
         a["this_slice_distances"], a["edge_slice_thickness_multiplier"], a["measured_array"], a["algorithm_type"],
-        a["this_wavelength"], update_probe, update_obj, update_pos, a["this_step_tilts"] > 0, a["masks"],
+        a["this_wavelength"], update_probe, update_obj, update_pos, update_tilts, a["masks"],
         a["pixel_size_x_A"], a["pixel_size_y_A"], a["recon_type"], a["Cs"], a["defocus_array"],
         a["alpha_near_field"], a["damping_cutoff_multislice"], 0, a["propmethod"], a["this_chopped_sequence"],
         a["load_one_by_one"], a["data_multiplier"], a["data_pad"], a["phase_plate_in_h5"], a["this_loss_weight"],
         a["data_bin"], a["data_shift_vector"], a["upsample_pattern"], ns.static_background, False, a["tilt_mode"],
         a["aberration_marker"], a["probe_marker"], ns.aberrations_array, a["compute_batch"], a["phase_only_obj"],
-        ns.beam_current, False, False, a["default_float"], a["default_complex"], a["xp"], a["is_first_epoch"],
+        ns.beam_current, update_bc, update_ab, a["default_float"], a["default_complex"], a["xp"], a["is_first_epoch"],
         a["scan_size"], a["scan_step_A"], a["fast_axis_reg_weight_positions"], a["slow_axis_reg_weight_positions"],
         a["slow_axis_reg_weight_tilts"], a["current_deformation_reg_weight_positions"],
         a["current_deformation_reg_weight_tilts"], a["fast_axis_reg_weight_tilts"], a["aperture_mask"],
@@ -158,16 +161,31 @@ def _impl(ns, a):
         aperture=aperture, wolfe_c1=a["wolfe_c1_constant"], wolfe_c2=a["wolfe_c2_constant"],
         max_count=a["max_count"], reduce_factor=a["reduce_factor"], optimism=a["optimism"],
         stepsize_threshold_low=a["stepsize_threshold_low"], hist_length=int(a["hist_length"]),
-        verbose=int(a["print_flag"] or 0))
+        verbose=int(a["print_flag"] or 0), update_tilts=update_tilts, update_aberrations=update_ab,
+        update_beam_current=update_bc)
+    # the variants path's extra variables: the tilt rows (without their correction), the refined
+    # tilt correction, aberration arrays and beam currents (iterative.py:472-486)
+    extras = dict(tilts=None, tilts_correction=None, aberrations=None, beam_current=None)
+    if variant is not None:
+        if variant.get("tilts") is not None:
+            extras["tilts"] = _to_device(ns.tilts, torch.float32, dev)
+            extras["tilts_correction"] = _to_device(ns.tilts_correction, torch.float32, dev)
+        if variant.get("aberrations") is not None:
+            extras["aberrations"] = variant["aberrations"]
+        if variant.get("beam_current") is not None:
+            extras["beam_current"] = variant["beam_current"]
     opt = st["opt"]
     hist = getattr(ns, "history_bfgs", None)
     empty = hist is None or bool(hist.get("empty_hist", True))
     if opt is None or tuple(opt.obj.shape) != tuple(obj_d.shape) or tuple(opt.probe.shape) != tuple(probe_d.shape) \
             or tuple(opt.corr.shape) != tuple(corr_d.shape):
-        opt = st["opt"] = LBFGS(problem, geo, st["meas"], obj_d, probe_d, corr_d, cfg, eng, variant=variant)
+        opt = st["opt"] = LBFGS(problem, geo, st["meas"], obj_d, probe_d, corr_d, cfg, eng, variant=variant,
+                                **extras)
     else:
         opt.problem, opt.geo, opt.measured, opt.cfg, opt.variant = problem, geo, st["meas"], cfg, variant
         opt.obj, opt.probe, opt.corr = obj_d, probe_d, corr_d
+        opt.tilts, opt.tcorr, opt.ab, opt.bc = (extras["tilts"], extras["tilts_correction"], extras["aberrations"],
+                                                extras["beam_current"])
     if empty:
         opt.reset()
     res = opt.step(a["actual_step"])
@@ -179,6 +197,12 @@ def _impl(ns, a):
         counter_failed_epochs = 0
         if update_pos:
             ns.positions_correction = _like(opt.corr, ns.positions_correction)
+        if update_tilts and opt.tcorr is not None:
+            ns.tilts_correction = _like(opt.tcorr, ns.tilts_correction)
+        if update_ab and opt.ab is not None:
+            ns.aberrations_array = _like(opt.ab, ns.aberrations_array)
+        if update_bc and opt.bc is not None:
+            ns.beam_current = _like(opt.bc, ns.beam_current)
         h = ns.history_bfgs if isinstance(getattr(ns, "history_bfgs", None), dict) else _fresh_history()
         h["empty_hist"] = False
         h["prev_loss"], h["prev_sse"] = opt.prev[0], opt.prev[1]

@@ -111,6 +111,11 @@ class LineSearchConfig:
     update_obj: bool = True
     update_probe: bool = True
     update_pos: bool = False
+    # the variants path's extra variables (pypty/iterative.py:477-481): tilt corrections,
+    # aberration arrays, beam currents
+    update_tilts: bool = False
+    update_aberrations: bool = False
+    update_beam_current: bool = False
     clean_cutoff: float = np.float32(2 / 3) - np.float32(0.005)   # damping_cutoff - update_extra_cut
     smooth_rolloff: float = 0.0
     lazy_clean: bool = False
@@ -150,20 +155,31 @@ class LBFGS:
 
     HMAX = 64
 
+    # refined variables in the reference's order (iterative.py:597-609): name, inner-product
+    # weight (complex segments count twice), state attribute
+    SEGMENTS = (("obj", 2.0, "obj"), ("probe", 2.0, "probe"), ("pos", 1.0, "corr"), ("tilts", 1.0, "tcorr"),
+                ("aberrations", 1.0, "ab"), ("beam_current", 1.0, "bc"))
+
     def __init__(self, problem: _lib.Problem, geometry: Geometry, measured: torch.Tensor, obj: torch.Tensor,
                  probe: torch.Tensor, corr: torch.Tensor, config: LineSearchConfig, engine: Engine | None = None,
-                 variant: dict | None = None):
+                 variant: dict | None = None, tilts: torch.Tensor | None = None,
+                 tilts_correction: torch.Tensor | None = None, aberrations: torch.Tensor | None = None,
+                 beam_current: torch.Tensor | None = None):
         self.eng = engine or default_engine(obj.device)
         # keyword arguments of Engine.loss_and_direction_variants (near field, compressed
-        # detectors, beam current, aberration plates, inside tilt), or None for the fused path
+        # detectors, beam current, aberration plates, tilts), or None for the fused path
         self.variant = variant
         self.problem, self.geo, self.measured = problem, geometry, measured
         self.obj, self.probe, self.corr = obj, probe, corr
+        # extra variables of the variants path (device float32): the tilt rows and their
+        # refined correction, the aberration arrays, the beam currents
+        self.tilts, self.tcorr, self.ab, self.bc = tilts, tilts_correction, aberrations, beam_current
         self.cfg = config
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_lbfgs_state_bytes(ctypes.byref(n)), "pty_lbfgs_state_bytes")
         self.state = torch.empty(int(n.value), dtype=torch.uint8, device=self.eng.device)
-        self.read_buf = torch.empty(8, dtype=torch.float64, pin_memory=True)
+        # pty_lbfgs_read: d_value, new_d_value, gamma[MAX_SEG], dot[MAX_SEG]
+        self.read_buf = torch.empty(2 + 2 * _lib.VSPACE_MAX_SEG, dtype=torch.float64, pin_memory=True)
         self._vs_flags = None
         self.reset()
 
@@ -177,29 +193,23 @@ class LBFGS:
         self.empty = True
         self._vs_flags = None
 
-    def _segments(self, obj, probe, corr):
+    def _flags(self):
         c = self.cfg
-        segs = []
-        if c.update_obj:
-            segs.append(("obj", obj))
-        if c.update_probe:
-            segs.append(("probe", probe))
-        if c.update_pos:
-            segs.append(("pos", corr))
-        return segs
+        return (c.update_obj, c.update_probe, c.update_pos, c.update_tilts, c.update_aberrations,
+                c.update_beam_current)
 
     def _vspace(self):
-        c = self.cfg
-        flags = (c.update_obj, c.update_probe, c.update_pos)
+        flags = self._flags()
         vs = _lib.VSpace()
-        names = [nm for nm, on in zip(("obj", "probe", "pos"), flags) if on]
+        names = [nm for (nm, _, _), on in zip(self.SEGMENTS, flags) if on]
         vs.n_seg = len(names)
         vs.obj_seg = names.index("obj") if "obj" in names else -1
-        sizes = {"obj": 2 * self.obj.numel(), "probe": 2 * self.probe.numel(), "pos": self.corr.numel()}
-        weights = {"obj": 2.0, "probe": 2.0, "pos": 1.0}
-        for i, nm in enumerate(names):
-            vs.n[i] = sizes[nm]
-            vs.weight[i] = weights[nm]
+        i = 0
+        for (nm, w, attr), on in zip(self.SEGMENTS, flags):
+            if on:
+                vs.n[i] = _f32view(getattr(self, attr)).numel()
+                vs.weight[i] = w
+                i += 1
         return vs, names, flags
 
     def _st(self):
@@ -217,27 +227,35 @@ class LBFGS:
             return fourier_clean_(t, ap, 0.0, out=t, engine=self.eng)
         return fourier_clean_(t, mask=ap, out=t, engine=self.eng)
 
-    def _lad(self, obj, probe, corr):
+    def _lad(self, x):
+        """loss_and_direction at the point x = [obj, probe, corr, tcorr, ab, bc]: returns
+        (loss_sse, [object, probe, position, tilt, aberration, beam-current gradients])."""
         p = self.problem
+        obj, probe, corr, tcorr, ab, bc = x
+        if self.variant is not None:
+            c = self.cfg
+            kw = dict(self.variant)
+            if self.tilts is not None:   # the reference evaluates tilts + tilts_correction (objective.py:343)
+                kw["tilts"] = (self.tilts + tcorr).cpu().numpy() if tcorr is not None else self.tilts.cpu().numpy()
+                kw["step_tilts"] = c.update_tilts
+            if ab is not None:
+                kw["aberrations"], kw["step_aberrations"] = ab, c.update_aberrations
+            if bc is not None:
+                kw["beam_current"], kw["step_beam_current"] = bc, c.update_beam_current
+            loss_sse, og, pg, posg, bcg, abg, tg = self.eng.loss_and_direction_variants(
+                p, obj, probe, self.geo, self.measured, pos_correction=corr, **kw)
+            return loss_sse, [og, pg, posg, tg, abg, bcg]
         out = (torch.empty(2, dtype=torch.float64, device=self.eng.device), torch.empty_like(obj),
                torch.empty_like(probe), torch.empty((p.n_positions, 2), dtype=torch.float32, device=self.eng.device))
-        if self.variant is not None:
-            return self.eng.loss_and_direction_variants(p, obj, probe, self.geo, self.measured, pos_correction=corr,
-                                                        **self.variant)[:4]
         loss_sse, og, pg, posg = self.eng.loss_and_direction(p, obj, probe, self.geo, self.measured, out=out,
                                                              pos_correction=corr)
-        return loss_sse, og, pg, posg
+        return loss_sse, [og, pg, posg, None, None, None]
 
-    def _grad_vec(self, og, pg, posg):
-        c = self.cfg
-        v = []
-        if c.update_obj:
-            v.append(_f32view(og))
-        if c.update_probe:
-            v.append(_f32view(pg))
-        if c.update_pos:
-            v.append(posg.reshape(-1))
-        return v
+    def _point(self):
+        return [self.obj, self.probe, self.corr, self.tcorr, self.ab, self.bc]
+
+    def _grad_vec(self, grads):
+        return [_f32view(gr) for gr, on in zip(grads, self._flags()) if on]
 
     def _read(self):
         _lib.check(_lib.lib().pty_lbfgs_read(self.state.data_ptr(),
@@ -276,29 +294,28 @@ class LBFGS:
             self._clean(self.probe, out=self.probe)
         if c.update_obj and not c.lazy_clean:
             self._clean(self.obj, out=self.obj)
-        q_obj = torch.empty_like(self.obj) if c.update_obj else None
-        q_probe = torch.empty_like(self.probe) if c.update_probe else None
-        q_pos = torch.empty_like(self.corr) if c.update_pos else None
-        q = [t for t, on in ((q_obj, c.update_obj), (q_probe, c.update_probe), (q_pos, c.update_pos)) if on]
-        qv = [_f32view(t) for t in q]
+        flags = self._flags()
+        point = self._point()
+        qs = [torch.empty_like(t) if on else None for t, on in zip(point, flags)]
+        q_obj = qs[0]
+        qv = [_f32view(t) for t in qs if t is not None]
         if self.empty:
-            loss_sse, og, pg, posg = self._lad(self.obj, self.probe, self.corr)
-            self._post_grad(og, pg)
-            g = self._grad_vec(og, pg, posg)
+            loss_sse, grads = self._lad(point)
+            self._post_grad(grads[0], grads[1])
+            g = self._grad_vec(grads)
             _lib.check(lib.pty_lbfgs_first_direction(ctypes.byref(vs), _ptrs(g), _ptrs(qv), self.state.data_ptr(),
                                                      st), "pty_lbfgs_first_direction")
             ls = loss_sse.cpu().numpy()
             total_loss, sse = float(ls[0]), float(ls[1])
-            grads = (og, pg, posg)
             self.empty = False
         else:
             total_loss, sse, grads = self.prev
-            og, pg, posg = grads
+            pg = grads[1]
             if c.aperture is not None:
                 self._clean_aperture(pg)
             if c.update_probe:
                 self._clean(pg, out=pg)
-            g = self._grad_vec(og, pg, posg)
+            g = self._grad_vec(grads)
             m = len(self.history)
             svec = [p for sl in self.history for p in self.pairs[sl][0]]
             yvec = [p for sl in self.history for p in self.pairs[sl][1]]
@@ -321,24 +338,19 @@ class LBFGS:
             d_value = float(self._read()[0])
         # ------------------------------------------------------------ line search (iterative.py:733-837)
         count = -1
-        new_obj = torch.empty_like(self.obj) if c.update_obj else self.obj
-        new_probe = torch.empty_like(self.probe) if c.update_probe else self.probe
-        new_corr = torch.empty_like(self.corr) if c.update_pos else self.corr
-        pvs = _lib.VSpace()
+        new = [torch.empty_like(t) if on else t for t, on in zip(point, flags)]
         while True:
             count += 1
-            if c.update_obj:
-                if c.lazy_clean:
-                    self._axpy1(new_obj, self.obj, q_obj, actual_step)
+            for i, on in enumerate(flags):
+                if not on:
+                    continue
+                if i == 0 and not c.lazy_clean:   # the object trial point is band-limited (iterative.py:759-766)
+                    self._clean(self.obj, out=new[0], dx=q_obj, step=float(np.float32(actual_step)))
                 else:
-                    self._clean(self.obj, out=new_obj, dx=q_obj, step=float(np.float32(actual_step)))
-            if c.update_probe:
-                self._axpy1(new_probe, self.probe, q_probe, actual_step)
-            if c.update_pos:
-                self._axpy1(new_corr, self.corr, q_pos, actual_step)
-            loss_sse, nog, npg, nposg = self._lad(new_obj, new_probe, new_corr)
-            self._post_grad(nog, npg)
-            ng = self._grad_vec(nog, npg, nposg)
+                    self._axpy1(new[i], point[i], qs[i], actual_step)
+            loss_sse, ngrads = self._lad(new)
+            self._post_grad(ngrads[0], ngrads[1])
+            ng = self._grad_vec(ngrads)
             _lib.check(lib.pty_lbfgs_dot(ctypes.byref(vs), _ptrs(qv), _ptrs(ng), 1, self.state.data_ptr(), st),
                        "pty_lbfgs_dot")
             new_d_value = float(self._read()[1])
@@ -381,17 +393,14 @@ class LBFGS:
                                         _ptrs(s_t), _ptrs(y_t), slot, self.state.data_ptr(), st), "pty_lbfgs_accept")
         self.pairs[slot] = (s_t, y_t)
         self.history.append(slot)
-        self.prev = (new_total_loss, new_sse, (nog, npg, nposg))
+        self.prev = (new_total_loss, new_sse, ngrads)
         while len(self.history) > c.hist_length:
             old = self.history.pop(0)
             del self.pairs[old]
             self.free.append(old)
-        if c.update_probe:
-            self.probe = new_probe
-        if c.update_obj:
-            self.obj = new_obj
-        if c.update_pos:
-            self.corr = new_corr
+        for (_, _, attr), on, t in zip(self.SEGMENTS, flags, new):
+            if on:
+                setattr(self, attr, t)
         return StepResult(total_loss, sse, actual_step, count, d_value, new_d_value, True, warnings)
 
     def _axpy1(self, out, a, b, step):

@@ -8,6 +8,7 @@
   the same line-search decisions (trial count, accepted step) as the reference, loss
   relative error <= 1e-4, arrays relative L2 <= 1e-3 after every call.
 """
+import os
 import sys
 import types
 
@@ -107,14 +108,16 @@ def _two_loop_numpy(g, S, Y, w):
     return [-qi for qi in q]
 
 
-def test_two_loop_matches_fp64_numpy():
+@pytest.mark.parametrize("nseg", [3, 6])
+def test_two_loop_matches_fp64_numpy(nseg):
     import ctypes
     import torch
     from pypty_gb300 import _lib
     from pypty_gb300.optim import _ptrs
     rng = np.random.default_rng(7)
-    sizes = [2 * 64 * 64 * 3, 2 * 32 * 32 * 2, 2 * 50]      # object, probe, positions (floats)
-    w = [2.0, 2.0, 1.0]
+    # object, probe, positions (floats); then tilt rows, aberrations, beam currents
+    sizes = [2 * 64 * 64 * 3, 2 * 32 * 32 * 2, 2 * 50, 6 * 50, 2 * 7, 50][:nseg]
+    w = [2.0, 2.0, 1.0, 1.0, 1.0, 1.0][:nseg]
     m = 4
     g = [rng.normal(size=n).astype(np.float32) for n in sizes]
     # pairs with positive curvature y.s > 0, as accepted Wolfe steps give
@@ -126,8 +129,8 @@ def test_two_loop_matches_fp64_numpy():
         Y.append(y)
     lib = _lib.lib()
     vs = _lib.VSpace()
-    vs.n_seg, vs.obj_seg = 3, 0
-    for i in range(3):
+    vs.n_seg, vs.obj_seg = nseg, 0
+    for i in range(nseg):
         vs.n[i], vs.weight[i] = sizes[i], w[i]
     n = ctypes.c_size_t(0)
     lib.pty_lbfgs_state_bytes(ctypes.byref(n))
@@ -156,7 +159,7 @@ def test_two_loop_matches_fp64_numpy():
     assert rel_l2(got, np.concatenate(ref)) <= 1e-5
     # d_value = <q, g>, weighted, FP64
     _lib.check(lib.pty_lbfgs_dot(ctypes.byref(vs), _ptrs(qd), _ptrs(gd), 0, state.data_ptr(), st), "dot")
-    out = (ctypes.c_double * 8)()
+    out = (ctypes.c_double * (2 + 2 * _lib.VSPACE_MAX_SEG))()
     _lib.check(lib.pty_lbfgs_read(state.data_ptr(), out, st), "read")
     dv = sum(wi * np.dot(qi.astype(np.float64), gi) for wi, qi, gi in
              zip(w, [t.cpu().numpy() for t in qd], g))
@@ -254,3 +257,55 @@ def test_bfgs_update_module_variables_and_reset():
     assert mod.history_bfgs["empty_hist"] is True
     r1 = _call(iterative.bfgs_update, c, 1, "", 0)     # starts again from the first-step branch
     assert r1[5] < 0
+
+
+def test_bfgs_update_refines_tilts_aberrations_and_beam_current():
+    """Object, probe, per-position tilt corrections (tilt_mode 3), aberration arrays and beam
+    currents refined together on the variants path: the same trial counts and steps as the
+    reference's bfgs_update and the refined arrays after every call
+    (tests/golden/make_golden_lbfgs.py make_refine_case)."""
+    from pypty_gb300 import iterative
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lbfgs_refine_tilts_aberr_current.npz")))
+    s = d["scalars"]
+    c = dict(d, distance=float(s[0]), edge_mult=float(s[1]), wavelength=float(s[2]), px=float(s[3]),
+             cutoff=float(s[4]), rolloff=0.0, loss_weight=float(s[6]), batch=int(s[7]), algorithm=str(d["algorithm"]),
+             step_probe=1, step_obj=1, step_pos=0, orthogonal=False, lazy_clean=False, hist_length=10)
+    ns = types.SimpleNamespace(obj=c["obj"].copy(), probe=c["probe"].copy(), positions=c["positions"].copy(),
+                               positions_correction=c["pos_correction"].astype(np.float32).copy(),
+                               tilts=c["tilts"].copy(), tilts_correction=np.zeros_like(c["tilts"]),
+                               static_background=None, aberrations_array=c["aberrations"].copy(),
+                               beam_current=c["beam_current"].copy(), history_bfgs=None)
+    fn = iterative.bind(ns)
+    np.random.seed(5)
+    warnings, failed = "", 0
+    f = np.float32
+    step = 1.0     # the generator's float first step, then the accepted one
+    for e, ref in enumerate(c["ref_scalars"]):
+        kw = dict(this_step_tilts=1, tilt_mode=3, aberration_marker=c["aberration_marker"],
+                  this_step_aberrations_array=1, this_beam_current_step=1, actual_step=step)
+        res = _call_with(fn, c, e, warnings, failed, kw)
+        total_loss, sse, _cc, step, count, dv, ndv, warnings, failed = res
+        print(e, count, step, total_loss, "ref", ref[3], ref[2], ref[0])
+        assert int(count) == int(ref[3]), (e, count, ref)
+        assert float(step) == pytest.approx(float(ref[2]), rel=1e-5)
+        assert float(total_loss) == pytest.approx(float(ref[0]), rel=1e-4)
+        assert failed == 0
+        assert rel_l2(ns.obj, c["ref_obj"][e]) <= 1e-3
+        assert rel_l2(ns.probe, c["ref_probe"][e]) <= 1e-3
+        assert rel_l2(ns.tilts_correction, c["ref_tcorr"][e]) <= 2e-3, (e, rel_l2(ns.tilts_correction,
+                                                                              c["ref_tcorr"][e]))
+        assert rel_l2(ns.aberrations_array, c["ref_ab"][e]) <= 1e-3
+        assert rel_l2(ns.beam_current, c["ref_bc"][e]) <= 1e-3
+        assert isinstance(ns.tilts_correction, np.ndarray) and ns.tilts_correction.dtype == f
+
+
+def _call_with(fn, c, epoch, warnings, failed, over):
+    """_call with some arguments replaced (the refinement flags of the variants path)."""
+    captured = {}
+
+    def grab(**kw):
+        captured.update(kw)
+        return None
+    _call(grab, c, epoch, warnings, failed)
+    captured.update(over)
+    return fn(**captured)

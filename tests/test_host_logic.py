@@ -112,8 +112,9 @@ def test_bfgs_update_signature_is_mirrored():
     assert list(inspect.signature(bound).parameters) == params
 
 
-@pytest.mark.parametrize("flag", ["phase_only_obj", "tune_only_probe_phase", "this_step_tilts", "do_charge_flip",
-                                  "current_gaussian_filter", "this_beam_current_step"])
+@pytest.mark.parametrize("flag", ["phase_only_obj", "tune_only_probe_phase", "this_step_static_background",
+                                  "do_charge_flip", "current_gaussian_filter", "this_beam_current_step",
+                                  "this_step_aberrations_array"])
 def test_bfgs_update_unsupported_options_raise_before_any_gpu_work(flag):
     import inspect
     import types
