@@ -48,6 +48,11 @@ CONFIGS = {
     # name: (W, Ny, Z, Mp, n_scan, algorithm, batch)
     "multislice": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=32, algorithm="ml", batch=256,
                        desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 32x32 jittered scan, ml, batch 256"),
+    # the "multislice" workload plus the variants path (near field, tilts, beam current,
+    # aberration plates, compressed detectors) timed on it
+    "variants": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=32, algorithm="ml", batch=256, variants=True,
+                     desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 32x32 jittered scan, ml, batch 256; "
+                          "variants path timed on the same positions"),
     # same kernels and shapes per position as "multislice", 8x8 positions: for ncu captures
     "multislice-small": dict(W=128, N_obj=512, Z=20, Mp=3, n_scan=8, algorithm="ml", batch=64,
                              desc="multislice W128 Z20 Mp3 Mo1, 512x512 object, 8x8 jittered scan, ml, batch 64"),
@@ -290,6 +295,52 @@ def run_warm_start(args, cfg):
             "train": {"dataset_s": round(t_data, 2), "train_s": round(t_train, 2), "loss": [round(h, 5) for h in hist]},
             "specimens": rows}
     print(json.dumps(line))
+
+
+def variants_timing(eng, prob, geo, meas_d, obj_d, probe_d, n_pos, steps=3):
+    """Device-timed positions/s of pty_loss_and_direction_variants on the benchmark workload
+    with each family of variant branches switched on (one warm-up call, `steps` timed calls):
+    the far-field layered path itself, near-field propagation, beam tilts (mode 4, one row per
+    position, with the tilt gradient), beam current + aberration plates (with gradients), a
+    compressed-detector loss on 8 masks, and the measured-data preprocessing."""
+    import torch
+    from pypty_gb300 import _lib
+    dev = obj_d.device
+    stream = torch.cuda.current_stream(dev)
+    W = prob.window
+    N = prob.n_positions
+    rng = np.random.default_rng(3)
+    tilts = (rng.normal(size=(N, 6)) * 2e-4).astype(np.float32)
+    bc = torch.from_numpy((1 + 0.05 * rng.normal(size=N)).astype(np.float32)).to(dev)
+    ab = torch.from_numpy((rng.normal(size=(2, 7)) * 5).astype(np.float32)).to(dev)
+    marker = torch.from_numpy((np.arange(N) % 2).astype(np.int32)).to(dev)
+    masks = torch.from_numpy(rng.uniform(0, 1, (8, W, W)).astype(np.float32)).to(dev)
+    coef = torch.from_numpy(rng.uniform(1e3, 2e3, (N, 8)).astype(np.float32)).to(dev)
+    cases = {
+        "far_field_layered": (prob, meas_d, {}),
+        "near_field": (prob, meas_d, dict(recon_type="near_field", defocus=50.0, cs=1e5)),
+        "tilts_mode4_grad": (prob, meas_d, dict(tilts=tilts, tilt_mode=4, step_tilts=True)),
+        "beam_current_aberrations_grad": (prob, meas_d, dict(beam_current=bc, step_beam_current=True,
+                                                            aberrations=ab, aberration_marker=marker,
+                                                            step_aberrations=True)),
+        "data_preprocessing": (prob, meas_d, dict(data_shift_vector=(2, -1), data_multiplier=1.1)),
+    }
+    cp = _lib.Problem.from_buffer_copy(prob)
+    cp.algorithm = _lib.COMPRESSED_ALGORITHMS["lsq_compressed"]
+    cases["compressed_lsq_8_masks"] = (cp, coef, dict(masks=masks))
+    out = {"positions": n_pos}
+    for name, (pr, meas, kw) in cases.items():
+        eng.loss_and_direction_variants(pr, obj_d, probe_d, geo, meas, **kw)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            eng.loss_and_direction_variants(pr, obj_d, probe_d, geo, meas, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"positions_per_s": round(n_pos / (ms / 1000.0), 1), "ms": round(ms, 2)}
+    return out
 
 
 def precision_sweep(eng, wl, geo, meas_d, obj_d, probe_d, cfg, common, n_sub=512, batch=256):
@@ -621,6 +672,8 @@ def main():
         "clocks": {"sm_mhz": cs.get("sm_mhz"), "sm_max_mhz": cs.get("sm_max_mhz"), "reasons": cs.get("reasons")},
         "loss": loss_val,
     }
+    if cfg.get("variants"):
+        line["variants_path"] = variants_timing(eng, prob, geo, meas_d, obj_d, probe_d, n_pos)
     if cfg.get("sweep"):
         line["precision_sweep"] = precision_sweep(eng, wl, geo, meas_d, obj_d, probe_d, cfg, common,
                                                   n_sub=min(512, n_pos), batch=min(256, cfg["batch"]))
