@@ -706,6 +706,26 @@ __global__ void var_tilted_mul_kernel(float2* __restrict__ x, TiltArgs t, PropAr
   *q = conj ? cmulc(*q, P) : cmul(*q, P);
 }
 
+// per-position propagators (and their edge powers) of one batch, tabulated once and used by
+// every propagation step of the batch   grid (WW / EB, Bn)
+__global__ void var_pos_prop_table_kernel(TiltArgs t, PropArgs a, float2* __restrict__ tab,
+                                          float2* __restrict__ tab_edge) {
+  const int u = blockIdx.x * EB + threadIdx.x, b = blockIdx.y;
+  const size_t WW = (size_t)a.W * a.W;
+  const float* row = tilt_row(t, b);
+  tab[b * WW + u] = tilted_prop(a, row, u, false);
+  if (tab_edge) tab_edge[b * WW + u] = tilted_prop(a, row, u, true);
+}
+
+// x[b][k] *= tab[b] (conj: conj(tab[b]))   grid (WW / EB, nper, Bn)
+__global__ void var_pos_table_mul_kernel(float2* __restrict__ x, const float2* __restrict__ tab, int nper, int WW,
+                                         int conj) {
+  const int u = blockIdx.x * EB + threadIdx.x, k = blockIdx.y, b = blockIdx.z;
+  const float2 P = tab[(size_t)b * WW + u];
+  float2* q = x + ((size_t)b * nper + k) * WW + u;
+  *q = conj ? cmulc(*q, P) : cmul(*q, P);
+}
+
 // spec[b][p][u] *= the position's shift ramp   grid (WW / EB, Mp, Bn)
 __global__ void var_ramp_mul_kernel(float2* __restrict__ spec, const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ mask, const float* __restrict__ corr,
@@ -834,7 +854,7 @@ struct LPlan {
   size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part;
   // beam tilts
   int n_rows, single_tilt, same_prop, before, after, inside_grad, step_tilts;
-  size_t o_tilts, o_tgrid, o_spec, o_fexit, o_exitb, o_pbt, o_pft, o_tpart;
+  size_t o_tilts, o_tgrid, o_spec, o_fexit, o_exitb, o_pbt, o_pft, o_tpart, o_pprop, o_pprop_edge;
 };
 
 inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t* v = nullptr) {
@@ -924,6 +944,9 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
     // probe spectrum (objective.py:471, 651)
     q.o_pft = take(q.before && p->probe_shift && !q.n_abs ? (size_t)q.Bb * q.Mp * WWs * c8 : 0);
     q.o_tpart = take((size_t)q.nseq * 6 * sizeof(double));
+    const bool edge = p->edge_mult > 1.0f && q.Z > 1;
+    q.o_pprop = take(!q.same_prop ? (size_t)q.Bb * WWs * c8 : 0);
+    q.o_pprop_edge = take(!q.same_prop && edge ? (size_t)q.Bb * WWs * c8 : 0);
   }
   size_t db = 0;
   const size_t maxwin = nobw > nwave ? nobw : nwave;
@@ -1113,6 +1136,12 @@ struct Run {
       size_t pin_stride = 0;
       pa.seq = seq_b;
       tg.seq = seq_b;
+      float2* pprop = at<float2>(ws, q.o_pprop);
+      float2* pprop_edge = ta.use_edge ? at<float2>(ws, q.o_pprop_edge) : nullptr;
+      if (tilted_prop) {   // the positions' propagators (objective.py:482-484), once per batch
+        prof_mark(st, KID_ELEMENTWISE);
+        var_pos_prop_table_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(tg, pr, pprop, pprop_edge);
+      }
       if (var_probe && q.before) {
         // the probe before the tilt (after beam current and plates), then the tilt mask, then
         // the shift: from the pre-plate spectrum with plates, else the tilted probe's
@@ -1167,7 +1196,8 @@ struct Run {
             return PTY_ERR_CUDA;
           prof_mark(st, KID_ELEMENTWISE);
           if (tilted_prop)
-            var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, z == 0 && ta.use_edge, 0, 0, 1.0f);
+            var_pos_table_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? pprop_edge : pprop,
+                                                                  nm, WW, 0);
           else
             prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? ta.prop_edge : ta.prop, WW,
                                                          0, unfold);
@@ -1221,7 +1251,7 @@ struct Run {
           prof_mark(st, KID_ELEMENTWISE);
           const bool edge = z == 1 && ta.use_edge;
           if (tilted_prop)
-            var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, edge, 0, 1, 1.0f);
+            var_pos_table_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, edge ? pprop_edge : pprop, nm, WW, 1);
           else
             prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, edge ? ta.prop_edge : ta.prop, WW, 1, unfold);
           if (v && q.inside_grad) {
