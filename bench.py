@@ -541,7 +541,7 @@ def main():
     torch.cuda.synchronize(dev)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n_batches = -(-n_pos // cfg["batch"])
-    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler((16 + 8 * n_batches) * max(args.steps, 1)) as prof:
+    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler((16 + 12 * n_batches) * max(args.steps, 1)) as prof:
         start.record(stream)
         for _ in range(args.steps):
             eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)

@@ -62,11 +62,14 @@ int run_common(const pty_problem_t* p, const void* obj, const void* probe, const
 
 // Launch profiler: one CUDA event per marked launch, read back in pty_profile_end.
 // Single-threaded use only (profiling / benchmarking).
+// A mark's interval ends at the next mark recorded on the same stream, so launches that run
+// on two streams at once are each timed on their own stream.
 struct Profiler {
   bool on = false;
   int cap = 0, n = 0;
   cudaEvent_t* ev = nullptr;
   int* ids = nullptr;
+  cudaStream_t* sts = nullptr;
   bool overflow = false;
 };
 Profiler g_prof;
@@ -89,7 +92,42 @@ void prof_mark(cudaStream_t st, int id) {
     return;
   }
   cudaEventRecord(P.ev[P.n], st);
+  P.sts[P.n] = st;
   P.ids[P.n++] = id;
+}
+
+constexpr int kMaxSideDevices = 64;
+struct SideStreams {
+  SideStream dev[kMaxSideDevices];
+  ~SideStreams() {
+    for (SideStream& d : dev) {
+      for (cudaEvent_t e : d.ev)
+        if (e) cudaEventDestroy(e);
+      if (d.s) cudaStreamDestroy(d.s);
+    }
+  }
+};
+static thread_local SideStreams t_side;
+
+int side_stream(SideStream** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PTY_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxSideDevices) return PTY_ERR_UNSUPPORTED;
+  SideStream& d = t_side.dev[dev];
+  if (!d.s) {
+    SideStream n;
+    bool ok = cudaStreamCreateWithFlags(&n.s, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t& e : n.ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      for (cudaEvent_t e : n.ev)
+        if (e) cudaEventDestroy(e);
+      if (n.s) cudaStreamDestroy(n.s);
+      return PTY_ERR_CUDA;
+    }
+    d = n;
+  }
+  *out = &d;
+  return PTY_OK;
 }
 }  // namespace pty
 
@@ -102,9 +140,11 @@ int pty_profile_begin(int32_t max_launches) {
     for (int i = 0; i < P.cap; ++i) cudaEventDestroy(P.ev[i]);
     delete[] P.ev;
     delete[] P.ids;
+    delete[] P.sts;
     P.cap = 0;
     P.ev = new cudaEvent_t[2 * max_launches];
     P.ids = new int[2 * max_launches];
+    P.sts = new cudaStream_t[2 * max_launches];
     for (int i = 0; i < 2 * max_launches; ++i) {
       if (cudaEventCreate(&P.ev[i]) != cudaSuccess) return PTY_ERR_CUDA;
       P.cap = i + 1;
@@ -125,12 +165,16 @@ int pty_profile_end(double* ms_by_kernel, int32_t* launches_by_kernel, int32_t n
     if (launches_by_kernel) launches_by_kernel[k] = 0;
   }
   if (P.n == 0) return PTY_OK;
-  if (cudaEventSynchronize(P.ev[P.n - 1]) != cudaSuccess) return PTY_ERR_CUDA;
+  for (int i = 0; i < P.n; ++i)
+    if (cudaEventSynchronize(P.ev[i]) != cudaSuccess) return PTY_ERR_CUDA;
   for (int i = 0; i + 1 < P.n; ++i) {
     const int id = P.ids[i];
     if (id < 0 || id >= n_kinds) continue;
+    int j = i + 1;
+    while (j < P.n && P.sts[j] != P.sts[i]) ++j;
+    if (j == P.n) continue;
     float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, P.ev[i], P.ev[i + 1]) != cudaSuccess) return PTY_ERR_CUDA;
+    if (cudaEventElapsedTime(&ms, P.ev[i], P.ev[j]) != cudaSuccess) return PTY_ERR_CUDA;
     if (ms_by_kernel) ms_by_kernel[id] += ms;
     if (launches_by_kernel) launches_by_kernel[id] += 1;
   }

@@ -24,10 +24,12 @@ struct Path {
   const Plan& q;
   void* ws;
   cudaStream_t st;
+  cudaStream_t side;   // stream of windows() and gradients(): st, or the second stream when overlapping
   float2* tw;
   TableArgs ta{};
 
-  Path(const pty_problem_t* p_, const Plan& q_, void* ws_, cudaStream_t st_) : p(p_), q(q_), ws(ws_), st(st_) {
+  Path(const pty_problem_t* p_, const Plan& q_, void* ws_, cudaStream_t st_)
+      : p(p_), q(q_), ws(ws_), st(st_), side(st_) {
     tw = at<float2>(ws, q.o_tw);
     ta.pyx = at<float2>(ws, q.o_pyx);
     ta.mask = at<float>(ws, q.o_mask);
@@ -76,6 +78,9 @@ struct Path {
   }
 
   int batch_count(int ib) const { return std::min(q.Bb, q.nseq - ib * q.Bb); }
+  float2* obl(int ib) const { return at<float2>(ws, q.o_obl + (size_t)(ib % q.nbuf) * q.s_obl); }
+  float2* gsum(int ib) const { return at<float2>(ws, q.o_gsum + (size_t)(ib % q.nbuf) * q.s_gsum); }
+  float2* fprobe(int ib) const { return at<float2>(ws, q.o_fprobe + (size_t)(ib % q.nbuf) * q.s_fprobe); }
   const int* seq_of(int ib) const { return at<int>(ws, q.o_seq) + ib * q.Bb; }
 
   int windows(int ib) {
@@ -85,12 +90,12 @@ struct Path {
     wa.seq = seq_of(ib);
     wa.mask_sc = ta.mask_sc;
     wa.tw = tw;
-    wa.out = at<float2>(ws, q.o_obl);
+    wa.out = obl(ib);
     wa.Ny = q.Ny;
     wa.Nx = q.Nx;
     wa.zm = q.zm;
-    prof_mark(st, KID_OBJECT_WINDOWS);
-    object_windows_kernel<W><<<(unsigned)(batch_count(ib) * q.zm), T, Smem<W>::bytes, st>>>(wa);
+    prof_mark(side, KID_OBJECT_WINDOWS);
+    object_windows_kernel<W><<<(unsigned)(batch_count(ib) * q.zm), T, Smem<W>::bytes, side>>>(wa);
     return cuda_status();
   }
 
@@ -115,7 +120,7 @@ struct Path {
     fa.loss_weight = p->loss_weight;
     fa.probe = probe;
     fa.probe_f = at<float2>(ws, q.o_probe_f);
-    fa.obl = at<float2>(ws, q.o_obl);
+    fa.obl = obl(ib);
     fa.prop = ta.prop;
     fa.prop_edge = ta.prop_edge;
     fa.pyx = ta.pyx;
@@ -128,8 +133,8 @@ struct Path {
     fa.measured = measured;
     fa.tw = tw;
     fa.stack = at<float2>(ws, q.o_stack);
-    fa.gsum = at<float2>(ws, q.o_gsum);
-    fa.fprobe = at<float2>(ws, q.o_fprobe);
+    fa.gsum = gsum(ib);
+    fa.fprobe = fprobe(ib);
     fa.gbuf = at<float2>(ws, q.o_gbuf);
     fa.loss_part = at<double>(ws, q.o_loss_part) + 2 * (size_t)s0;
     fa.pos_part = at<double>(ws, q.o_pos_part) + 2 * (size_t)s0 * q.Mp;
@@ -160,24 +165,24 @@ struct Path {
     const int* seq_b = seq_of(ib);
     const int* d_pos = at<int>(ws, q.o_pos);
     if (p->step_obj) {
-      float2* gs = at<float2>(ws, q.o_gsum);
-      prof_mark(st, KID_GRAD_WINDOWS);
-      grad_windows_kernel<W><<<(unsigned)(Bn * q.zm), T, Smem<W>::bytes, st>>>(gs, ta.mask_sc, tw);
+      float2* gs = gsum(ib);
+      prof_mark(side, KID_GRAD_WINDOWS);
+      grad_windows_kernel<W><<<(unsigned)(Bn * q.zm), T, Smem<W>::bytes, side>>>(gs, ta.mask_sc, tw);
       int* lists = at<int>(ws, q.o_lists);
       int* counts = at<int>(ws, q.o_counts);
-      prof_mark(st, KID_TILE_LISTS);
-      tile_lists_kernel<<<q.ntiles, 256, 0, st>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
-      prof_mark(st, KID_SCATTER);
-      scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, st>>>(
+      prof_mark(side, KID_TILE_LISTS);
+      tile_lists_kernel<<<q.ntiles, 256, 0, side>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
+      prof_mark(side, KID_SCATTER);
+      scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(
           gs, d_pos, seq_b, lists, counts, at<float2>(ws, q.o_grad), Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0);
     }
     if (p->step_probe) {
       const int nch = (Bn + q.chunk - 1) / q.chunk;
       // chunks beyond this batch's count keep their previous value: the first batch has the
       // largest count, so every chunk read later was written
-      prof_mark(st, KID_PROBE_PARTIAL);
-      probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, st>>>(
-          at<float2>(ws, q.o_fprobe), at<float2>(ws, q.o_partial), Bn, q.Mp, (int)WW, q.chunk, ib > 0 ? 1 : 0);
+      prof_mark(side, KID_PROBE_PARTIAL);
+      probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, side>>>(
+          fprobe(ib), at<float2>(ws, q.o_partial), Bn, q.Mp, (int)WW, q.chunk, ib > 0 ? 1 : 0);
     }
     return cuda_status();
   }
@@ -211,6 +216,59 @@ struct Path {
   }
 };
 
+// The batch loop on two streams (double-buffered windows, nbuf = 2). The caller's stream st
+// runs the fused kernels; the second stream runs windows(ib + 1) while fused(ib) runs and
+// gradients(ib) while fused(ib + 1) runs:
+//   second: windows(0) | windows(1) gradients(0) | windows(2) gradients(1) | ...
+//   st:                  fused(0)                | fused(1)                | fused(2) ...
+// Events (each wait is issued after the record it refers to and before that event's next
+// record): ev[0] start, then fused(ib) done; ev[1] windows(ib) done; ev[2 + ib % 2]
+// gradients(ib) done, which fused(ib + 2) waits for before it rewrites buffer ib % 2.
+// windows(ib + 1) rewrites obl((ib + 1) % 2), last read by fused(ib - 1): the second stream
+// waited for that fused kernel before gradients(ib - 1). The scatter into the object gradient
+// and the probe partial sums accumulate in batch order on the second stream, so the results
+// are those of the one-stream loop bit for bit. Each stage closes its launch-profiler interval
+// on its own stream, so profiled durations exclude the waits between the streams.
+template <int W>
+int run_batches_overlapped(Path<W>& P, const float2* probe, const float* measured, float* patterns) {
+  SideStream* sd = nullptr;
+  int rc = side_stream(&sd);
+  if (rc) return rc;
+  cudaStream_t st = P.st, ss = sd->s;
+  cudaEvent_t ev_f = sd->ev[0], ev_w = sd->ev[1];
+  auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+  prof_mark(st, -1);
+  if (!ok(cudaEventRecord(ev_f, st)) || !ok(cudaStreamWaitEvent(ss, ev_f, 0))) return PTY_ERR_CUDA;
+  P.side = ss;
+  const int n = P.q.nbatch;
+  rc = P.windows(0);
+  prof_mark(ss, -1);
+  if (!rc && !ok(cudaEventRecord(ev_w, ss))) rc = PTY_ERR_CUDA;
+  for (int ib = 0; ib < n && !rc; ++ib) {
+    if (!ok(cudaStreamWaitEvent(st, ev_w, 0))) { rc = PTY_ERR_CUDA; break; }
+    if (!patterns && ib >= 2 && !ok(cudaStreamWaitEvent(st, sd->ev[2 + ib % 2], 0))) { rc = PTY_ERR_CUDA; break; }
+    if ((rc = P.fused(ib, 0, probe, measured, patterns))) break;
+    prof_mark(st, -1);
+    if (!ok(cudaEventRecord(ev_f, st))) { rc = PTY_ERR_CUDA; break; }
+    if (ib + 1 < n) {
+      if ((rc = P.windows(ib + 1))) break;
+      prof_mark(ss, -1);
+      if (!ok(cudaEventRecord(ev_w, ss))) { rc = PTY_ERR_CUDA; break; }
+    }
+    if (!ok(cudaStreamWaitEvent(ss, ev_f, 0))) { rc = PTY_ERR_CUDA; break; }
+    if (!patterns) {
+      if ((rc = P.gradients(ib))) break;
+      prof_mark(ss, -1);
+      if (!ok(cudaEventRecord(sd->ev[2 + ib % 2], ss))) { rc = PTY_ERR_CUDA; break; }
+    }
+  }
+  // join: everything queued on the second stream completes before st's next launch
+  P.side = st;
+  cudaEvent_t ev_join = sd->ev[1];
+  if (!ok(cudaEventRecord(ev_join, ss)) || !ok(cudaStreamWaitEvent(st, ev_join, 0))) return PTY_ERR_CUDA;
+  return rc;
+}
+
 template <int W>
 int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const float2* probe,
              const float* measured, double* loss_sse, float2* object_grad, float2* probe_grad,
@@ -218,9 +276,13 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   Path<W> P(p, q, ws, st);
   int rc = P.prepare(obj, probe);
   if (rc) return rc;
-  for (int ib = 0; ib < q.nbatch; ++ib) {
-    if ((rc = P.windows(ib)) || (rc = P.fused(ib, 0, probe, measured, patterns))) return rc;
-    if (!patterns && (rc = P.gradients(ib))) return rc;
+  if (q.nbuf == 2) {
+    if ((rc = run_batches_overlapped(P, probe, measured, patterns))) return rc;
+  } else {
+    for (int ib = 0; ib < q.nbatch; ++ib) {
+      if ((rc = P.windows(ib)) || (rc = P.fused(ib, 0, probe, measured, patterns))) return rc;
+      if (!patterns && (rc = P.gradients(ib))) return rc;
+    }
   }
   if (patterns) {
     prof_mark(st, -1);

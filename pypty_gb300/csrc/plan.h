@@ -24,6 +24,11 @@ struct Plan {
   size_t total;
   int ckpt;   // kept slices every ckpt (256 windows)
   bool split;   // one batch with every position: pty_forward / pty_backward
+  // W <= 128 with several batches: object windows, gradient windows and shifted probes are
+  // double-buffered (nbuf = 2) so that batch ib + 1's windows and batch ib's gradients run on
+  // a second stream while batch ib + 1's fused kernel runs; s_* are the buffer strides in bytes
+  int nbuf;
+  size_t s_obl, s_gsum, s_fprobe;
 };
 
 // twiddle tables in global memory: W = 256 windows use the 128 tables of their sub-transforms
@@ -83,12 +88,16 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_seq = take((size_t)q.nseq * sizeof(int));
   q.o_obj = take((size_t)q.zm * q.Ny * q.Nx * c8);
   q.o_grad = take((size_t)q.zm * q.Ny * q.Nx * c8);
-  q.o_obl = take((size_t)q.Bb * q.zm * WW * c8);
+  q.nbuf = (!split && q.W <= 128 && q.nbatch > 1) ? 2 : 1;
+  q.s_obl = align_up((size_t)q.Bb * q.zm * WW * c8);
+  q.s_gsum = q.s_obl;
+  q.s_fprobe = align_up((size_t)q.Bb * q.Mp * WW * c8);
+  q.o_obl = take(q.nbuf * q.s_obl);
   q.ckpt = (p->window == 256 && p->checkpoint_every > 1) ? std::min(p->checkpoint_every, q.Z) : 1;
   const int n_kept = (q.Z + q.ckpt - 1) / q.ckpt;
   q.o_stack = take((size_t)q.Bb * n_kept * q.Mp * q.Mo * WW * c8);
-  q.o_gsum = take((size_t)q.Bb * q.zm * WW * c8);
-  q.o_fprobe = take((size_t)q.Bb * q.Mp * WW * c8);
+  q.o_gsum = take(q.nbuf * q.s_gsum);
+  q.o_fprobe = take(q.nbuf * q.s_fprobe);
   q.o_partial = take((size_t)q.nchunk * q.Mp * WW * c8);
   q.o_lists = take((size_t)q.ntiles * q.Bb * sizeof(int));
   q.o_counts = take((size_t)q.ntiles * sizeof(int));
@@ -187,8 +196,15 @@ enum KernelId : int {
 };
 
 // Records an event on `st` before a launch of kernel class `id` while profiling is on
-// (id < 0 closes the last interval). No-op otherwise.
+// (id < 0 closes the last interval on that stream). No-op otherwise.
 void prof_mark(cudaStream_t st, int id);
+// A second stream and four events for the caller's device, created on first use by each
+// host thread and kept until the thread exits.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev[4] = {};
+};
+int side_stream(SideStream** out);
 
 // Launch paths, instantiated in path_w64.cu / path_w128.cu and specialised for W = 256 in
 // path_w256.cu.

@@ -153,3 +153,23 @@ def test_simulated_patterns_match_oracle(engine):
                         pixel_size_x=c["px"], pixel_size_y=c["px"], slice_distance=2.0, compute_batch=4)
     out = engine.simulate(prob, torch.from_numpy(c["obj"]).cuda(), torch.from_numpy(c["probe"]).cuda(), geo)
     assert rel_l2(out.cpu().numpy(), sim_ref) <= 2e-6
+
+
+def test_simulated_patterns_do_not_depend_on_batching(engine):
+    """Patterns are per position: one batch and eight double-buffered batches on two streams
+    give the same bits."""
+    import torch
+    from pypty_gb300.engine import Geometry, make_problem
+    c = load_case("w128_modes_c64")
+    dev = torch.device("cuda", 0)
+    obj = torch.from_numpy(np.ascontiguousarray(c["obj"]).astype(np.complex64)).to(dev)
+    probe = torch.from_numpy(np.ascontiguousarray(c["probe"]).astype(np.complex64)).to(dev)
+    geo = Geometry.make(c["positions"], c["pos_correction"], c["sequence"])
+    outs = []
+    for batch in (len(c["sequence"]), 1):
+        prob = make_problem(probe.shape[0], tuple(obj.shape), probe.shape[2], geo, algorithm=c["algorithm"],
+                            wavelength=float(np.float32(c["wavelength"])), pixel_size_x=float(np.float32(c["px"])),
+                            pixel_size_y=float(np.float32(c["px"])), slice_distance=c["distance"],
+                            edge_mult=c["edge_mult"], compute_batch=batch)
+        outs.append(engine.simulate(prob, obj, probe, geo).cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
