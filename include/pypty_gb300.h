@@ -281,6 +281,21 @@ typedef struct pty_variant {
   int32_t tilt_mode;
   int32_t step_tilts;
   float* tilts_grad;
+  /* detector upsampling (pypty/objective.py:523-524, 590-591; utils.py:376-426): the model
+     pattern, after the data_pad crop, is summed over upsample_pattern^2 blocks before the
+     loss and dL/dI is repeated back over each block; the measured patterns are then
+     (S / u - 2 po)^2 with S the cropped side and po = data_pad / u when use_padded_intensity.
+     0 or 1: none. S must be a multiple of u; not with the compressed losses. */
+  int32_t upsample_pattern;
+  /* static background (pypty/objective.py:359-361, 525-526, 588-589): W x W float32 on the
+     device or NULL; the pattern gets static_background^2 * band-limit mask (detector order)
+     before the loss. With step_static_background its gradient
+     sum_b dL/dI * 2 * static_background * loss_weight goes to static_background_grad
+     (W x W, device). Needs data_pad = 0 or use_padded_intensity, and no upsampling (the
+     reference's shapes do not broadcast otherwise). */
+  const float* static_background;
+  int32_t step_static_background;
+  float* static_background_grad;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);
@@ -341,15 +356,16 @@ int pty_fourier_clean_apply(const void* x, const void* dx, double step, void* ou
 
 /*
  * The optimizer's vector space: up to PTY_VSPACE_MAX_SEG float32 segments (the object, the
- * probe, the position corrections, the tilt corrections, the aberration arrays and the beam
- * currents of pypty/iterative.py:583-672; a complex64 element counts as two floats). Every
+ * probe, the position corrections, the tilt corrections, the static background, the
+ * aberration arrays and the beam currents of pypty/iterative.py:583-672, in that order; a
+ * complex64 element counts as two floats). Every
  * inner product is sum_seg weight[seg] * <a_seg, b_seg>; the reference's weights are 2 for
  * the complex segments and 1 for the real ones (iterative.py:597-609). Each segment has its
  * own Barzilai-Borwein gamma (iterative.py:626-647, 869-916). obj_seg names the object
  * segment for the first step's normalisation (-1: none). Vectors are passed as arrays of
  * n_seg device pointers.
  */
-#define PTY_VSPACE_MAX_SEG 6
+#define PTY_VSPACE_MAX_SEG 7
 typedef struct pty_vspace {
   int32_t n_seg;
   int32_t obj_seg;

@@ -17,7 +17,9 @@ defocus (``is_single_defocus``) and spherical aberration ``Cs`` (``objective.py:
 687-697``); ``aberrations_array`` / ``aberration_marker`` with their gradient
 (``objective.py:324-329, 459-463, 676-684``); beam tilts (``tilt_mode`` 0-4, one tilt row or
 one per position, with the tilt gradient: ``objective.py:302-345, 464-499, 605-673``,
-``multislice_core.py:76-77, 178-182``). Every step cites the reference line it restates;
+``multislice_core.py:76-77, 178-182``); the detector upsampling (``upsample_pattern``,
+``objective.py:523-524, 590-591``) and a 2D static background with its gradient
+(``objective.py:359-361, 525-526, 588-589``). Every step cites the reference line it restates;
 dtypes follow the reference in single or double precision.
 
 The near-field partial-coherence correction (``alpha_near_field > 0``) is not restated: the
@@ -134,6 +136,15 @@ def preprocess_measured(dataset, data_shift_vector, data_multiplier, data_pad):
     return np.pad(dataset, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
 
 
+def downsample_pattern(pattern, up):
+    """``utils.py:403-426`` ``downsample_something_3d``: sums over up x up blocks (both axes
+    cut to a multiple of up of axis 1's length, as the reference does)."""
+    n = pattern.shape[1]
+    k = n // up
+    p = pattern[:, :up * k, :up * k]
+    return p.reshape(pattern.shape[0], k, up, k, up).sum(axis=(2, 4))
+
+
 def tilt_grids(W, pixel_size_x, pixel_size_y, wavelength, complex_dtype):
     """Real-space tilt ramps of ``objective.py:303-307``: (y_grid, x_grid), each (W, W)
     purely imaginary, 2*pi*i*W*px/lambda times the fftshifted frequencies (complex128, then the
@@ -151,18 +162,25 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                                 tan_y=0.0, masks=None, beam_current=None, step_beam_current=0, aberrations=None,
                                 aberration_marker=None, step_aberrations=0, data_pad=0, use_padded_intensity=True,
                                 data_shift_vector=(0, 0), data_multiplier=1.0, tilts=None, tilt_mode=0,
-                                step_tilts=0, float_dtype=np.float32, complex_dtype=np.complex64, simulate=False):
+                                step_tilts=0, upsample_pattern=1, static_background=None,
+                                step_static_background=0, float_dtype=np.float32, complex_dtype=np.complex64,
+                                simulate=False):
     """Restatement of ``pypty/objective.py:47-967`` for the flag set in the module docstring.
 
     tilts: (N_tilts, 6) rows [tan_y, tan_x] before / inside / after the specimen (the
     reference's tilt array plus its correction; one row for all positions or one per position),
     used by ``tilt_mode`` 0-4 (``objective.py:302-345, 464-499``); without it one inside tilt
-    (tan_x, tan_y). Returns (loss, sse, object_grad, probe_grad, pos_grad, beam_current_grad,
-    aberrations_grad, tilts_grad); the beam-current and aberration gradients are 0 when the
-    feature is off (the reference's zero-initialised accumulators, ``objective.py:381-382``).
-    ``simulate=True`` returns the model patterns (len(sequence), W, W) or, for compressed
-    algorithms, the coefficients (len(sequence), n_masks); with ``data_pad`` the patterns are
-    cropped to the measured (W - 2 data_pad)² detector.
+    (tan_x, tan_y). ``upsample_pattern`` sums the model pattern over blocks before the loss
+    (``objective.py:523-524, 590-591``); ``static_background`` (W, W) adds its square, band
+    limited, to every pattern (``objective.py:359-361, 525-526``) and
+    ``step_static_background`` accumulates its gradient (``objective.py:588-589``). Returns
+    (loss, sse, object_grad, probe_grad, pos_grad, beam_current_grad, aberrations_grad,
+    tilts_grad, static_background_grad); the beam-current, aberration and static-background
+    gradients are 0 (zeros for a given background) when the feature is off (the reference's
+    zero-initialised accumulators, ``objective.py:377, 381-382``).
+    ``simulate=True`` returns the model patterns at the measured detector's shape (cropped by
+    ``data_pad``, block-summed by ``upsample_pattern``) or, for compressed algorithms, the
+    coefficients (len(sequence), n_masks).
     """
     f = float_dtype
     obj = np.asarray(obj, dtype=complex_dtype)
@@ -213,6 +231,13 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     probe_grad = np.zeros((W, W, Mp), dtype=complex_dtype)
     pos_grad = np.zeros_like(pos_correction)
     tilts_grad = np.zeros_like(tilts)
+    up = int(upsample_pattern)
+    if static_background is not None:                                   # objective.py:359-361, 377
+        static_background = np.asarray(static_background, dtype=f)
+        static_square = (static_background[None, :, :] ** 2) * mask_s[None]
+        sb_grad = np.zeros_like(static_background)
+    else:
+        sb_grad = 0
     bc_grad = np.zeros_like(beam_current) if fluct else 0
     ab_grad = np.zeros_like(aberrations) if morph else 0
     helper2 = step_probe or step_beam_current or step_aberrations
@@ -279,9 +304,14 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         pattern = pattern[:, :, :, 0, 0] if coherent else np.mean(pattern, (-1, -2))
         if data_pad != 0 and not use_padded_intensity:                 # objective.py:516-517
             pattern = pattern[:, data_pad:-data_pad, data_pad:-data_pad]
+        if up != 1:                                                     # objective.py:523-524
+            pattern = downsample_pattern(pattern, up)
+        if static_background is not None:                               # objective.py:525-526
+            pattern = pattern + static_square
         if simulate:
             if data_pad != 0 and use_padded_intensity:
-                pattern = pattern[:, data_pad:-data_pad, data_pad:-data_pad]
+                po = data_pad // up
+                pattern = pattern[:, po:pattern.shape[1] - po, po:pattern.shape[2] - po]
             if compressed:
                 sim.append(np.sum(pattern[:, None] * masks[None], axis=(2, 3)))
             else:
@@ -289,7 +319,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
             continue
         meas = 1 * np.asarray(measured)[tcs]
         if not compressed:                                              # objective.py:411-412
-            meas = preprocess_measured(meas, data_shift_vector, data_multiplier, data_pad * use_padded_intensity)
+            meas = preprocess_measured(meas, data_shift_vector, data_multiplier,
+                                       (data_pad * use_padded_intensity) // up)   # utils.py:649-651
         if compressed:
             l_b, s_b, dldi = compressed_terms(pattern, meas, masks, algorithm)
         else:
@@ -298,6 +329,10 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         sse = sse + s_b
         if not coherent:
             dldi = dldi / (Mp * Mo)                                     # objective.py:586-587
+        if step_static_background and static_background is not None:    # objective.py:588-589
+            sb_grad = sb_grad + np.sum(dldi, 0) * 2 * static_background * loss_weight
+        if up != 1:                                                     # objective.py:590-591
+            dldi = np.repeat(np.repeat(dldi, up, axis=1), up, axis=2)
         if not use_padded_intensity and data_pad != 0:                  # objective.py:592-593
             dldi = np.pad(dldi, [[0, 0], [data_pad, data_pad], [data_pad, data_pad]])
         if near:                                                        # objective.py:598-619
@@ -396,7 +431,7 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     if step_probe:                                                      # objective.py:927-933
         probe_grad = ifft2(fft2(probe_grad) * mask[:, :, None])
     return (loss, sse, object_grad, np.asarray(probe_grad).astype(complex_dtype), pos_grad, bc_grad, ab_grad,
-            tilts_grad)
+            tilts_grad, sb_grad)
 
 
 def multislice_tilted(probe_b, obj_b, prop_b, edge_mult, keep_spectra):

@@ -41,19 +41,20 @@ class Problem(ctypes.Structure):
     ]
 
 
-VSPACE_MAX_SEG = 6
+VSPACE_MAX_SEG = 7
 
 
 class VSpace(ctypes.Structure):
     """Mirror of ``pty_vspace_t``: the optimizer's segments (object, probe, positions, tilts,
-    aberrations, beam current)."""
+    static background, aberrations, beam current)."""
     _fields_ = [("n_seg", ctypes.c_int32), ("obj_seg", ctypes.c_int32),
                 ("n", ctypes.c_int64 * VSPACE_MAX_SEG), ("weight", ctypes.c_double * VSPACE_MAX_SEG)]
 
 
 class Variant(ctypes.Structure):
     """Mirror of ``pty_variant_t``: near field, compressed detectors, beam current, aberration
-    plates and the inside tilt of ``pty_loss_and_direction_variants``."""
+    plates, tilts, measured-data preprocessing, detector upsampling and the static background
+    of ``pty_loss_and_direction_variants``."""
     _fields_ = [("recon_type", ctypes.c_int32), ("defocus", ctypes.c_float), ("cs", ctypes.c_float),
                 ("tan_x", ctypes.c_float), ("tan_y", ctypes.c_float), ("n_masks", ctypes.c_int32),
                 ("masks", ctypes.c_void_p), ("beam_current", ctypes.c_void_p),
@@ -64,7 +65,9 @@ class Variant(ctypes.Structure):
                 ("data_pad", ctypes.c_int32), ("use_padded_intensity", ctypes.c_int32),
                 ("shift_y", ctypes.c_int32), ("shift_x", ctypes.c_int32), ("data_multiplier", ctypes.c_float),
                 ("n_tilts", ctypes.c_int32), ("tilts_host", ctypes.c_void_p), ("tilt_mode", ctypes.c_int32),
-                ("step_tilts", ctypes.c_int32), ("tilts_grad", ctypes.c_void_p)]
+                ("step_tilts", ctypes.c_int32), ("tilts_grad", ctypes.c_void_p),
+                ("upsample_pattern", ctypes.c_int32), ("static_background", ctypes.c_void_p),
+                ("step_static_background", ctypes.c_int32), ("static_background_grad", ctypes.c_void_p)]
 
 
 class PtyError(RuntimeError):

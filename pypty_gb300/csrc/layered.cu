@@ -366,14 +366,22 @@ __global__ void var_intensity_kernel(const float2* __restrict__ field, const flo
   ibuf[(size_t)b * WW + pix] = I;
 }
 
-// measured-data preprocessing applied on the fly (pypty/utils.py:626-652): the measured
-// patterns are Wm x Wm (Wm = W - 2 pad), rolled by (sy, sx) with the rows / columns the
-// reference zeroes, scaled by mult, then either zero-padded to W (padded) or compared with
-// the model pattern cropped by pad
+// measured-data preprocessing applied on the fly (pypty/utils.py:626-652) and the detector
+// upsampling of objective.py:523-524, 590-591. The model pattern is W x W; without padded it
+// is cropped by pad (objective.py:516-517) to S = W - 2 pad, else S = W. It is summed over
+// up x up blocks (utils.py:403-426) to Sd = S / up. The measured patterns are Wm x Wm
+// (Wm = Sd - 2 po, po = pad / up when padded, else 0), rolled by (sy, sx) with the rows /
+// columns the reference zeroes, scaled by mult and zero-padded by po.
 struct MeasPrep {
   int W, pad, padded, sy, sx;
   float mult;
+  int up;
 };
+
+__host__ __device__ __forceinline__ int meas_side(const MeasPrep& mp) {
+  const int S = mp.padded ? mp.W : mp.W - 2 * mp.pad;
+  return S / mp.up - 2 * (mp.padded ? mp.pad / mp.up : 0);
+}
 
 // source index along one axis of the rolled Wm-long measured axis, or -1 for a zeroed entry
 // (np.roll then a[-s:] = 0 for s > 0, a[:-s] = 0 for s < 0)
@@ -383,39 +391,76 @@ __device__ __forceinline__ int rolled(int i, int s, int n) {
   return j < 0 ? j + n : j;
 }
 
-// per-pixel losses (objective.py:527-559) on the pattern: ibuf <- dL/dI / nm (zero outside a
-// cropped pattern), FP64 partial sums per position   grid Bn, block 1024
+// per-pixel losses (objective.py:527-559) on the (cropped, block-summed) pattern: every
+// model pixel of a block gets that block's dL/dI / nm (utils.py:376-399 without scaling),
+// pixels cropped away get zero; FP64 partial sums per position   grid Bn, block 1024
 __global__ void __launch_bounds__(1024) var_pixel_loss_kernel(float* __restrict__ ibuf, const float* __restrict__ measured,
                                                               const int* __restrict__ seq, MeasPrep mp, int nm, int alg,
                                                               double* __restrict__ loss_part) {
   __shared__ double red[64];
   const int b = blockIdx.x;
-  const int W = mp.W, WW = W * W, Wm = W - 2 * mp.pad;
+  const int W = mp.W, WW = W * W, up = mp.up;
+  const int S = mp.padded ? W : W - 2 * mp.pad, c0 = mp.padded ? 0 : mp.pad;
+  const int Sd = S / up, po = mp.padded ? mp.pad / up : 0, Wm = meas_side(mp);
   const float* meas = measured + (size_t)seq[b] * Wm * Wm;
   float* I = ibuf + (size_t)b * WW;
-  double lsum = 0.0, ssum = 0.0;
-  for (int u = threadIdx.x; u < WW; u += blockDim.x) {
-    const int y = u / W - mp.pad, x = u % W - mp.pad;
-    const bool inside = y >= 0 && y < Wm && x >= 0 && x < Wm;
-    if (!inside && !mp.padded) {   // cropped model pattern: no loss, dL/dI padded with zeros
-      I[u] = 0.0f;
-      continue;
+  if (S < W) {   // cropped model pattern: no loss, dL/dI padded with zeros
+    for (int u = threadIdx.x; u < WW; u += blockDim.x) {
+      const int y = u / W - c0, x = u % W - c0;
+      if (y < 0 || y >= S || x < 0 || x >= S) I[u] = 0.0f;
     }
+  }
+  double lsum = 0.0, ssum = 0.0;
+  for (int d = threadIdx.x; d < Sd * Sd; d += blockDim.x) {
+    const int yd = d / Sd, xd = d % Sd;
+    float* blk = I + (size_t)(c0 + yd * up) * W + c0 + xd * up;
+    float P = 0.0f;
+    for (int i = 0; i < up; ++i)
+      for (int j = 0; j < up; ++j) P += blk[i * W + j];
+    const int ym = yd - po, xm = xd - po;
     float Mv = 0.0f;
-    if (inside) {
-      const int ry = rolled(y, mp.sy, Wm), rx = rolled(x, mp.sx, Wm);
+    if (ym >= 0 && ym < Wm && xm >= 0 && xm < Wm) {
+      const int ry = rolled(ym, mp.sy, Wm), rx = rolled(xm, mp.sx, Wm);
       if (ry >= 0 && rx >= 0) Mv = meas[ry * Wm + rx];
       if (mp.mult != 1.0f) Mv = Mv * mp.mult;
     }
-    float d = loss_pixel(alg, I[u], Mv, lsum, ssum);
-    if (nm > 1) d = d / (float)nm;
-    I[u] = d;
+    float g = loss_pixel(alg, P, Mv, lsum, ssum);
+    if (nm > 1) g = g / (float)nm;
+    for (int i = 0; i < up; ++i)
+      for (int j = 0; j < up; ++j) blk[i * W + j] = g;
   }
   block_sum2(lsum, ssum, red);
   if (threadIdx.x == 0) {
     loss_part[2 * b] = lsum;
     loss_part[2 * b + 1] = ssum;
   }
+}
+
+// static background (objective.py:359-361, 525-526): pattern += bg^2 * exclude_mask, the
+// band-limit mask in detector (fftshifted) order; mask is in FFT order   grid (WW / EB, Bn)
+__global__ void var_add_static_kernel(float* __restrict__ ibuf, const float* __restrict__ bg,
+                                      const float* __restrict__ mask, int W) {
+  const int u = blockIdx.x * EB + threadIdx.x, b = blockIdx.y;
+  const int ky = u / W, kx = u % W;
+  const float mk = mask[((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1))];
+  const float s = bg[u];
+  ibuf[(size_t)b * W * W + u] += (s * s) * mk;
+}
+
+// static-background gradient (objective.py:588-589): acc[u] += sum_b dL/dI[b][u] * 2 bg[u] lw,
+// positions summed in order in FP64   grid WW / 256, block 256
+__global__ void var_static_grad_kernel(const float* __restrict__ ibuf, const float* __restrict__ bg, int Bn, int WW,
+                                       float lw, double* __restrict__ acc) {
+  const int u = blockIdx.x * 256 + threadIdx.x;
+  if (u >= WW) return;
+  double sum = 0.0;
+  for (int b = 0; b < Bn; ++b) sum += (double)ibuf[(size_t)b * WW + u];
+  acc[u] += sum * (2.0 * (double)bg[u] * (double)lw);
+}
+
+__global__ void var_static_final_kernel(const double* __restrict__ acc, int WW, float* __restrict__ grad) {
+  const int u = blockIdx.x * 256 + threadIdx.x;
+  if (u < WW) grad[u] = (float)acc[u];
 }
 
 // detector coefficients coef[b][j] = sum_u I[b][u] masks[j][u] (objective.py:561)
@@ -850,8 +895,8 @@ struct LPlan {
   size_t o_obj, o_grad, o_ob, o_tmp, o_dob, o_stack, o_psi, o_psi2, o_pb, o_pbs, o_partial, o_lists, o_counts;
   size_t o_loss_part, o_pos_part, o_dft, dft_bytes, total;
   // variants (pty_loss_and_direction_variants)
-  int near, compressed, nmask, n_abs, n_sets, has_bc;
-  size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part;
+  int near, compressed, nmask, n_abs, n_sets, has_bc, step_static;
+  size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part, o_sbg;
   // beam tilts
   int n_rows, single_tilt, same_prop, before, after, inside_grad, step_tilts;
   size_t o_tilts, o_tgrid, o_spec, o_fexit, o_exitb, o_pbt, o_pft, o_tpart, o_pprop, o_pprop_edge;
@@ -926,6 +971,8 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
     q.o_dco = take((size_t)q.Bb * q.nmask * sizeof(float));
     q.o_bc_part = take(q.has_bc ? (size_t)q.nseq * q.Mp * sizeof(double) : 0);
     q.o_ab_part = take((size_t)q.nseq * q.Mp * q.n_abs * sizeof(double));
+    q.step_static = v->static_background && v->step_static_background;
+    q.o_sbg = take(q.step_static ? WWs * sizeof(double) : 0);
     const int tm = v->n_tilts > 0 ? v->tilt_mode : 0;
     q.n_rows = v->n_tilts > 0 ? v->n_tilts : 1;
     q.single_tilt = q.n_rows == 1;
@@ -1067,6 +1114,8 @@ struct Run {
           return PTY_ERR_CUDA;
       }
       if (cudaMemsetAsync(at<double>(ws, q.o_tpart), 0, (size_t)q.nseq * 6 * sizeof(double), st) != cudaSuccess)
+        return PTY_ERR_CUDA;
+      if (q.step_static && cudaMemsetAsync(at<double>(ws, q.o_sbg), 0, (size_t)WW * sizeof(double), st) != cudaSuccess)
         return PTY_ERR_CUDA;
       va.defocus = v->defocus;
       va.cs = v->cs;
@@ -1339,6 +1388,9 @@ struct Run {
     if (v && q.step_tilts)
       var_tilt_finalize_kernel<<<1, 32, 0, st>>>(at<double>(ws, q.o_tpart), at<int>(ws, q.o_seq), q.nseq, q.n_rows,
                                                  q.single_tilt, q.before, q.inside_grad, q.after, v->tilts_grad);
+    if (v && q.step_static)
+      var_static_final_kernel<<<(WW + 255) / 256, 256, 0, st>>>(at<double>(ws, q.o_sbg), WW,
+                                                               v->static_background_grad);
     if (v && ((v->beam_current && v->step_beam_current) || (v->aberrations && v->step_aberrations))) {
       const bool gb = v->beam_current && v->step_beam_current, ga = v->aberrations && v->step_aberrations;
       var_finalize_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_bc_part), at<double>(ws, q.o_ab_part),
@@ -1371,6 +1423,9 @@ struct Run {
     }
     prof_mark(st, KID_FINALIZE);
     var_intensity_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(field, ta.mask, ibuf, W, nm, q.near);
+    if (v->static_background)
+      var_add_static_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(ibuf, v->static_background, ta.mask,
+                                                                                    W);
     if (q.compressed) {
       float* coef = at<float>(ws, q.o_coef);
       float* dco = at<float>(ws, q.o_dco);
@@ -1379,9 +1434,13 @@ struct Run {
       var_cdldi_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(ibuf, v->masks, dco, WW, q.nmask, nm);
     } else {
       MeasPrep mp{W, v->data_pad, v->use_padded_intensity != 0, v->shift_y, v->shift_x,
-                  v->data_multiplier == 0.0f ? 1.0f : v->data_multiplier};
+                  v->data_multiplier == 0.0f ? 1.0f : v->data_multiplier,
+                  v->upsample_pattern > 1 ? v->upsample_pattern : 1};
       var_pixel_loss_kernel<<<Bn, 1024, 0, st>>>(ibuf, measured, seq_b, mp, nm, p->algorithm, lpart);
     }
+    if (q.step_static)
+      var_static_grad_kernel<<<(WW + 255) / 256, 256, 0, st>>>(ibuf, v->static_background, Bn, WW, p->loss_weight,
+                                                              at<double>(ws, q.o_sbg));
     var_apply_kernel<<<grid(nm, Bn), EB, 0, st>>>(field, ibuf, ta.mask, W, nm, q.near, p->loss_weight * (float)WW);
     if (q.near) {   // dL/d(exit) = IFFT(loss_weight FFT(wave dL/dI) conj(CTF)) (objective.py:602-604)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
@@ -1474,6 +1533,18 @@ int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
       return PTY_ERR_INVALID;
     if (v->step_aberrations && !v->aberrations_grad) return PTY_ERR_INVALID;
   }
+  // detector upsampling: the cropped pattern side must be a multiple of the factor (the
+  // reference's repeat / pad back to W fails otherwise); the compressed losses take masks at
+  // the model pattern's size
+  const int up = v->upsample_pattern > 1 ? v->upsample_pattern : 1;
+  if (v->upsample_pattern < 0) return PTY_ERR_INVALID;
+  const int S = v->use_padded_intensity ? p->window : p->window - 2 * v->data_pad;
+  if (up > 1 && (compressed || S % up != 0)) return PTY_ERR_UNSUPPORTED;
+  if (up > 1 && S / up - 2 * (v->use_padded_intensity ? v->data_pad / up : 0) <= 0) return PTY_ERR_INVALID;
+  // static background: W x W, added to the full pattern (the reference's shapes only
+  // broadcast without a crop and without upsampling)
+  if (v->static_background && (S != p->window || up > 1)) return PTY_ERR_UNSUPPORTED;
+  if (v->static_background && v->step_static_background && !v->static_background_grad) return PTY_ERR_INVALID;
   return PTY_OK;
 }
 

@@ -272,7 +272,8 @@ CleanWs clean_ws(int ny, int nx) {
 constexpr int VB = 608;    // fixed reduction grid: 4 blocks per SM of a 152-SM GB300
 constexpr int VT = 256;
 constexpr int HMAX = 64;   // history slots
-constexpr int NSEG = PTY_VSPACE_MAX_SEG;   // object, probe, positions, tilts, aberrations, beam current
+constexpr int NSEG = PTY_VSPACE_MAX_SEG;   // object, probe, positions, tilts, static background,
+                                           // aberrations, beam current
 
 struct OptState {
   double w[NSEG];              // inner-product weight of each segment

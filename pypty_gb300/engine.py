@@ -184,24 +184,33 @@ class Engine:
                                     data_pad: int = 0, use_padded_intensity: bool = True,
                                     data_shift_vector=(0, 0), data_multiplier: float = 1.0,
                                     tilts=None, tilt_mode: int = 0, step_tilts: bool = False,
+                                    upsample_pattern: int = 1, static_background: torch.Tensor | None = None,
+                                    step_static_background: bool = False,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
 
-        measured is (n_positions, W - 2 data_pad, W - 2 data_pad) float32 (device memory, or
-        pinned host memory read in place), or (n_positions, n_masks) for the compressed
-        algorithms; data_pad / use_padded_intensity / data_shift_vector / data_multiplier are
-        the reference's per-batch measured-data preprocessing, applied on the fly; tilts
+        measured is (n_positions, m, m) float32 (device memory, or pinned host memory read in
+        place) with m = S / u - 2 (data_pad // u if use_padded_intensity else 0), S the pattern
+        side after the data_pad crop (W with use_padded_intensity, else W - 2 data_pad) and
+        u = upsample_pattern; or (n_positions, n_masks) for the compressed algorithms;
+        data_pad / use_padded_intensity / data_shift_vector / data_multiplier are the
+        reference's per-batch measured-data preprocessing, applied on the fly; upsample_pattern
+        sums the model pattern over u x u blocks before the loss; static_background (W, W)
+        float32 adds its square (band-limited) to every pattern, with step_static_background
+        its gradient is returned; tilts
         (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
         one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
         (n_positions,) int32; pos_correction as in ``loss_and_direction``. Returns (loss_sse,
         object_grad, probe_grad, pos_grad, beam_current_grad or None, aberrations_grad or
-        None, tilts_grad or None)."""
+        None, tilts_grad or None, static_background_grad or None)."""
         stream = stream or torch.cuda.current_stream(self.device)
         compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
         self._check_inputs(problem, obj, probe, None)
-        wm = problem.window - 2 * int(data_pad)
+        up = max(int(upsample_pattern), 1)
+        side = problem.window if use_padded_intensity else problem.window - 2 * int(data_pad)
+        wm = side // up - 2 * (int(data_pad) // up if use_padded_intensity else 0)
         want = (problem.n_positions, masks.shape[0]) if compressed else (problem.n_positions, wm, wm)
         if tuple(measured.shape) != want or measured.dtype != torch.float32 or not _readable(measured) \
                 or not measured.is_contiguous():
@@ -231,6 +240,11 @@ class Engine:
             if bc_d is not None and step_beam_current else None
         ab_grad = torch.zeros(tuple(ab_d.shape), dtype=torch.float32, device=self.device) \
             if ab_d is not None and step_aberrations else None
+        sb_d = dev(static_background, torch.float32)
+        if sb_d is not None and tuple(sb_d.shape) != (problem.window, problem.window):
+            raise ValueError("static_background must be (W, W)")
+        sb_grad = torch.zeros(tuple(sb_d.shape), dtype=torch.float32, device=self.device) \
+            if sb_d is not None and step_static_background else None
         tilts_h = None
         tilts_grad = None
         if tilts is not None:
@@ -259,7 +273,11 @@ class Engine:
                          n_tilts=0 if tilts_h is None else int(tilts_h.shape[0]),
                          tilts_host=None if tilts_h is None else tilts_h.ctypes.data,
                          tilt_mode=int(tilt_mode), step_tilts=int(tilts_grad is not None),
-                         tilts_grad=None if tilts_grad is None else tilts_grad.data_ptr())
+                         tilts_grad=None if tilts_grad is None else tilts_grad.data_ptr(),
+                         upsample_pattern=up,
+                         static_background=None if sb_d is None else sb_d.data_ptr(),
+                         step_static_background=int(sb_grad is not None),
+                         static_background_grad=None if sb_grad is None else sb_grad.data_ptr())
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")
@@ -281,7 +299,7 @@ class Engine:
         for t in keep:
             t.record_stream(stream)
         _lib.check(st, "pty_loss_and_direction_variants")
-        return loss_sse, og, pg, posg, bc_grad, ab_grad, tilts_grad
+        return loss_sse, og, pg, posg, bc_grad, ab_grad, tilts_grad, sb_grad
 
     def forward(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor, geo: Geometry,
                 measured: torch.Tensor, stream=None):

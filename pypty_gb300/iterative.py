@@ -16,7 +16,7 @@ from the fused ``pty_loss_and_direction`` with the arguments the reference passe
 (``pypty/iterative.py:524,773``; ``smooth_rolloff`` 0 for the loss).
 
 Supported: object, probe and position-correction refinement and, on the variants path, tilt
-correction, aberration-array and beam-current refinement; ``lazy_clean``,
+correction, static-background, aberration-array and beam-current refinement; ``lazy_clean``,
 ``keep_probe_states_orthogonal``, ``probe_reg_weight = inf`` (aperture-cleaned probe
 gradients), ``smart_memory`` (same arithmetic), ``hist_length``, Wolfe constants,
 ``max_count``, ``reduce_factor``, ``optimism``, ``stepsize_threshold_low``, and every
@@ -102,7 +102,9 @@ def _impl(ns, a):
     update_tilts = a["this_step_tilts"] > 0
     update_ab = a["this_step_aberrations_array"] > 0
     update_bc = a["this_beam_current_step"] > 0
-    _unsupported(a["this_step_static_background"] > 0, "static-background refinement")
+    update_sb = a["this_step_static_background"] > 0
+    _unsupported(update_sb and getattr(ns, "static_background", None) is None,
+                 "static-background refinement without a background")
     _unsupported(update_ab and getattr(ns, "aberrations_array", None) is None, "aberration refinement without arrays")
     _unsupported(update_bc and getattr(ns, "beam_current", None) is None, "beam-current refinement without currents")
     _unsupported(bool(a["phase_only_obj"]), "phase_only_obj")
@@ -128,7 +130,7 @@ def _impl(ns, a):
         a["pixel_size_x_A"], a["pixel_size_y_A"], a["recon_type"], a["Cs"], a["defocus_array"],
         a["alpha_near_field"], a["damping_cutoff_multislice"], 0, a["propmethod"], a["this_chopped_sequence"],
         a["load_one_by_one"], a["data_multiplier"], a["data_pad"], a["phase_plate_in_h5"], a["this_loss_weight"],
-        a["data_bin"], a["data_shift_vector"], a["upsample_pattern"], ns.static_background, False, a["tilt_mode"],
+        a["data_bin"], a["data_shift_vector"], a["upsample_pattern"], ns.static_background, update_sb, a["tilt_mode"],
         a["aberration_marker"], a["probe_marker"], ns.aberrations_array, a["compute_batch"], a["phase_only_obj"],
         ns.beam_current, update_bc, update_ab, a["default_float"], a["default_complex"], a["xp"], a["is_first_epoch"],
         a["scan_size"], a["scan_step_A"], a["fast_axis_reg_weight_positions"], a["slow_axis_reg_weight_positions"],
@@ -143,7 +145,7 @@ def _impl(ns, a):
     dev = eng.device
     if variant is not None:
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
-                      ("aberration_marker", torch.int32)):
+                      ("aberration_marker", torch.int32), ("static_background", torch.float32)):
             if variant[k] is not None:
                 variant[k] = _to_device(variant[k], dt, dev)
     st = _STATES.setdefault(id(ns), {"opt": None, "meas_src": None, "meas": None})
@@ -162,10 +164,11 @@ def _impl(ns, a):
         max_count=a["max_count"], reduce_factor=a["reduce_factor"], optimism=a["optimism"],
         stepsize_threshold_low=a["stepsize_threshold_low"], hist_length=int(a["hist_length"]),
         verbose=int(a["print_flag"] or 0), update_tilts=update_tilts, update_aberrations=update_ab,
-        update_beam_current=update_bc)
+        update_beam_current=update_bc, update_static_background=update_sb)
     # the variants path's extra variables: the tilt rows (without their correction), the refined
-    # tilt correction, aberration arrays and beam currents (iterative.py:472-486)
-    extras = dict(tilts=None, tilts_correction=None, aberrations=None, beam_current=None)
+    # tilt correction, static background, aberration arrays and beam currents
+    # (iterative.py:472-486)
+    extras = dict(tilts=None, tilts_correction=None, aberrations=None, beam_current=None, static_background=None)
     if variant is not None:
         if variant.get("tilts") is not None:
             extras["tilts"] = _to_device(ns.tilts, torch.float32, dev)
@@ -174,6 +177,8 @@ def _impl(ns, a):
             extras["aberrations"] = variant["aberrations"]
         if variant.get("beam_current") is not None:
             extras["beam_current"] = variant["beam_current"]
+        if variant.get("static_background") is not None:
+            extras["static_background"] = variant["static_background"]
     opt = st["opt"]
     hist = getattr(ns, "history_bfgs", None)
     empty = hist is None or bool(hist.get("empty_hist", True))
@@ -186,6 +191,7 @@ def _impl(ns, a):
         opt.obj, opt.probe, opt.corr = obj_d, probe_d, corr_d
         opt.tilts, opt.tcorr, opt.ab, opt.bc = (extras["tilts"], extras["tilts_correction"], extras["aberrations"],
                                                 extras["beam_current"])
+        opt.sb = extras["static_background"]
     if empty:
         opt.reset()
     res = opt.step(a["actual_step"])
@@ -203,12 +209,14 @@ def _impl(ns, a):
             ns.aberrations_array = _like(opt.ab, ns.aberrations_array)
         if update_bc and opt.bc is not None:
             ns.beam_current = _like(opt.bc, ns.beam_current)
+        if update_sb and opt.sb is not None:
+            ns.static_background = _like(opt.sb, ns.static_background)
         h = ns.history_bfgs if isinstance(getattr(ns, "history_bfgs", None), dict) else _fresh_history()
         h["empty_hist"] = False
         h["prev_loss"], h["prev_sse"] = opt.prev[0], opt.prev[1]
         h["rho_hist"] = list(opt.history)        # device slots of the stored pairs, oldest first
         for k, v in opt.gammas().items():
-            h["gamma_" + k] = v
+            h["gamma_" + {"static_background": "static"}.get(k, k)] = v   # the reference's key names
         ns.history_bfgs = h
     else:
         counter_failed_epochs += 1

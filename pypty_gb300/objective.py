@@ -11,9 +11,11 @@ propagation (one defocus, ``Cs``; ``pypty/objective.py:504-508``), the compresse
 algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations and their
 gradient, aberration arrays with markers and their gradient, or beam tilts (``tilt_mode``
 0-4, one tilt row or one per position, with the tilt gradient) on the variants path
-(``pty_loss_and_direction_variants``). No phase plates, probe markers, static background,
-data binning (the reference raises on it) or upsampling, near-field ``alpha_near_field``
-(the reference raises on it) or regularisers. The per-batch measured-data preprocessing
+(``pty_loss_and_direction_variants``), which also takes the detector upsampling
+(``upsample_pattern``, ``objective.py:523-524, 590-591``) and a 2D static background with
+its gradient (``objective.py:359-361, 525-526, 588-589``). No phase plates, probe markers,
+data binning (the reference raises on it), near-field ``alpha_near_field`` (the reference
+raises on it) or regularisers. The per-batch measured-data preprocessing
 (``data_pad`` with or without ``use_padded_intensity``, ``data_shift_vector``,
 ``data_multiplier``) runs on the fly on the variants path; with ``load_one_by_one`` the
 patterns stay in pinned host memory and the kernels read them in place. Any other combination raises
@@ -127,11 +129,19 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     _unsupported(aberrations_array is not None and aberration_marker is None, "aberrations without markers")
     _unsupported(bool(this_step_aberrations_array) and aberrations_array is None, "aberration steps without arrays")
     _unsupported(bool(this_beam_current_step) and beam_current is None, "beam-current steps without currents")
-    _unsupported(static_background is not None and not _is_zero(static_background), "static background")
-    _unsupported(bool(this_step_static_background), "static-background refinement")
+    # a scalar static background cannot be indexed by the reference (objective.py:361); zero
+    # is read here as no background
+    has_bg = static_background is not None and not (np.ndim(_to_numpy(static_background)) == 0
+                                                    and _is_zero(static_background))
+    _unsupported(has_bg and np.ndim(_to_numpy(static_background)) != 2, "a static background that is not 2D")
+    _unsupported(bool(this_step_static_background) and not has_bg, "static-background steps without a background")
     # the reference's binning loop indexes an undefined name (utils.py:643: i2), so it raises
     _unsupported(int(data_bin) != 1, "data binning (the reference raises NameError on it)")
-    _unsupported(int(upsample_pattern) != 1, "upsample_pattern")
+    up = max(int(upsample_pattern), 1)
+    padded = True if use_padded_intensity is None else bool(use_padded_intensity)
+    _unsupported(compressed and up != 1, "upsample_pattern with compressed detectors")
+    _unsupported(has_bg and (up != 1 or (int(data_pad) != 0 and not padded)),
+                 "a static background with upsampling or a cropped pattern (the reference's shapes do not broadcast)")
     _unsupported(compressed and int(data_pad) != 0, "data_pad with compressed detectors")
     prep = not compressed and (int(data_pad) != 0 or not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0)
     _unsupported(bool(data_simulation_flag), "data simulation output files")
@@ -163,7 +173,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         compute_batch=int(compute_batch), step_obj=bool(this_step_obj), step_probe=bool(this_step_probe),
         step_pos=bool(this_step_pos_correction))
     variant = None
-    if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted:
+    if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted \
+            or up != 1 or has_bg:
         variant = dict(recon_type=recon_type,
                        defocus=float(np.asarray(_to_numpy(defocus_array)).reshape(-1)[0]) if near else 0.0,
                        cs=float(Cs) if near else 0.0, tilts=tilts, tilt_mode=tmode,
@@ -175,9 +186,12 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                        aberration_marker=None if aberration_marker is None else _to_numpy(aberration_marker),
                        step_aberrations=bool(this_step_aberrations_array),
                        data_pad=0 if compressed else int(data_pad),
-                       use_padded_intensity=True if use_padded_intensity is None else bool(use_padded_intensity),
+                       use_padded_intensity=padded,
                        data_shift_vector=(0, 0) if compressed else tuple(int(x) for x in data_shift_vector),
-                       data_multiplier=1.0 if compressed else float(data_multiplier))
+                       data_multiplier=1.0 if compressed else float(data_multiplier),
+                       upsample_pattern=up,
+                       static_background=_to_numpy(static_background) if has_bg else None,
+                       step_static_background=bool(this_step_static_background) and has_bg)
     return problem, geo, variant
 
 
@@ -214,18 +228,22 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     obj_d = _device_tensor(this_obj, torch.complex64, dev)
     probe_d = _device_tensor(full_probe, torch.complex64, dev)
     meas_d = measured_tensor(measured_array, dev, bool(load_one_by_one))
-    bc_grad, ab_grad = 0, 0
+    bc_grad, ab_grad, sb_grad = 0, 0, 0
     tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))    # objective.py:380
     if variant is None:
         loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
     else:
         kw = dict(variant)
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
-                      ("aberration_marker", torch.int32)):
+                      ("aberration_marker", torch.int32), ("static_background", torch.float32)):
             if kw[k] is not None:
                 kw[k] = _device_tensor(kw[k], dt, dev)
-        loss_sse, og, pg, posg, bcg, abg, tg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo,
-                                                                               meas_d, **kw)
+        loss_sse, og, pg, posg, bcg, abg, tg, sbg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo,
+                                                                                    meas_d, **kw)
+        # objective.py:377: zeros shaped like the background, 0 without one
+        if kw["static_background"] is not None:
+            sb_grad = np.zeros_like(_to_numpy(static_background)) if sbg is None else \
+                sbg.cpu().numpy().astype(_to_numpy(static_background).dtype, copy=False)
         if tg is not None:
             tilts_grad = tg.cpu().numpy().astype(_to_numpy(this_tilts_correction).dtype, copy=False)
         # zero-initialised accumulators of the reference (objective.py:381-382)
@@ -248,4 +266,4 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         posg_out = posg.cpu().numpy().astype(np.asarray(_to_numpy(this_pos_correction)).dtype, copy=False)
     else:
         og_out, pg_out, posg_out = og, pg, posg
-    return loss, sse, og_out, pg_out, posg_out, tilts_grad, 0, ab_grad, bc_grad, constraints
+    return loss, sse, og_out, pg_out, posg_out, tilts_grad, sb_grad, ab_grad, bc_grad, constraints

@@ -114,6 +114,7 @@ class LineSearchConfig:
     # the variants path's extra variables (pypty/iterative.py:477-481): tilt corrections,
     # aberration arrays, beam currents
     update_tilts: bool = False
+    update_static_background: bool = False
     update_aberrations: bool = False
     update_beam_current: bool = False
     clean_cutoff: float = np.float32(2 / 3) - np.float32(0.005)   # damping_cutoff - update_extra_cut
@@ -158,13 +159,13 @@ class LBFGS:
     # refined variables in the reference's order (iterative.py:597-609): name, inner-product
     # weight (complex segments count twice), state attribute
     SEGMENTS = (("obj", 2.0, "obj"), ("probe", 2.0, "probe"), ("pos", 1.0, "corr"), ("tilts", 1.0, "tcorr"),
-                ("aberrations", 1.0, "ab"), ("beam_current", 1.0, "bc"))
+                ("static_background", 1.0, "sb"), ("aberrations", 1.0, "ab"), ("beam_current", 1.0, "bc"))
 
     def __init__(self, problem: _lib.Problem, geometry: Geometry, measured: torch.Tensor, obj: torch.Tensor,
                  probe: torch.Tensor, corr: torch.Tensor, config: LineSearchConfig, engine: Engine | None = None,
                  variant: dict | None = None, tilts: torch.Tensor | None = None,
                  tilts_correction: torch.Tensor | None = None, aberrations: torch.Tensor | None = None,
-                 beam_current: torch.Tensor | None = None):
+                 beam_current: torch.Tensor | None = None, static_background: torch.Tensor | None = None):
         self.eng = engine or default_engine(obj.device)
         # keyword arguments of Engine.loss_and_direction_variants (near field, compressed
         # detectors, beam current, aberration plates, tilts), or None for the fused path
@@ -172,8 +173,9 @@ class LBFGS:
         self.problem, self.geo, self.measured = problem, geometry, measured
         self.obj, self.probe, self.corr = obj, probe, corr
         # extra variables of the variants path (device float32): the tilt rows and their
-        # refined correction, the aberration arrays, the beam currents
+        # refined correction, the static background, the aberration arrays, the beam currents
         self.tilts, self.tcorr, self.ab, self.bc = tilts, tilts_correction, aberrations, beam_current
+        self.sb = static_background
         self.cfg = config
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_lbfgs_state_bytes(ctypes.byref(n)), "pty_lbfgs_state_bytes")
@@ -195,8 +197,8 @@ class LBFGS:
 
     def _flags(self):
         c = self.cfg
-        return (c.update_obj, c.update_probe, c.update_pos, c.update_tilts, c.update_aberrations,
-                c.update_beam_current)
+        return (c.update_obj, c.update_probe, c.update_pos, c.update_tilts, c.update_static_background,
+                c.update_aberrations, c.update_beam_current)
 
     def _vspace(self):
         flags = self._flags()
@@ -228,10 +230,11 @@ class LBFGS:
         return fourier_clean_(t, mask=ap, out=t, engine=self.eng)
 
     def _lad(self, x):
-        """loss_and_direction at the point x = [obj, probe, corr, tcorr, ab, bc]: returns
-        (loss_sse, [object, probe, position, tilt, aberration, beam-current gradients])."""
+        """loss_and_direction at the point x = [obj, probe, corr, tcorr, sb, ab, bc]: returns
+        (loss_sse, [object, probe, position, tilt, static-background, aberration, beam-current
+        gradients])."""
         p = self.problem
-        obj, probe, corr, tcorr, ab, bc = x
+        obj, probe, corr, tcorr, sb, ab, bc = x
         if self.variant is not None:
             c = self.cfg
             kw = dict(self.variant)
@@ -242,17 +245,19 @@ class LBFGS:
                 kw["aberrations"], kw["step_aberrations"] = ab, c.update_aberrations
             if bc is not None:
                 kw["beam_current"], kw["step_beam_current"] = bc, c.update_beam_current
-            loss_sse, og, pg, posg, bcg, abg, tg = self.eng.loss_and_direction_variants(
+            if sb is not None:
+                kw["static_background"], kw["step_static_background"] = sb, c.update_static_background
+            loss_sse, og, pg, posg, bcg, abg, tg, sbg = self.eng.loss_and_direction_variants(
                 p, obj, probe, self.geo, self.measured, pos_correction=corr, **kw)
-            return loss_sse, [og, pg, posg, tg, abg, bcg]
+            return loss_sse, [og, pg, posg, tg, sbg, abg, bcg]
         out = (torch.empty(2, dtype=torch.float64, device=self.eng.device), torch.empty_like(obj),
                torch.empty_like(probe), torch.empty((p.n_positions, 2), dtype=torch.float32, device=self.eng.device))
         loss_sse, og, pg, posg = self.eng.loss_and_direction(p, obj, probe, self.geo, self.measured, out=out,
                                                              pos_correction=corr)
-        return loss_sse, [og, pg, posg, None, None, None]
+        return loss_sse, [og, pg, posg, None, None, None, None]
 
     def _point(self):
-        return [self.obj, self.probe, self.corr, self.tcorr, self.ab, self.bc]
+        return [self.obj, self.probe, self.corr, self.tcorr, self.sb, self.ab, self.bc]
 
     def _grad_vec(self, grads):
         return [_f32view(gr) for gr, on in zip(grads, self._flags()) if on]

@@ -1,10 +1,11 @@
-"""Golden vectors for the near-field, compressed-detector, beam-current, aberration and
-inside-tilt branches, produced by running the reference's own NumPy path.
+"""Golden vectors for the near-field, compressed-detector, beam-current, aberration, tilt,
+measured-data preprocessing, detector-upsampling and static-background branches, produced by
+running the reference's own NumPy path.
 
 Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
 /root/reference)::
 
-    python tests/golden/make_golden_variants.py
+    python tests/golden/make_golden_variants.py [case names]   # every case without names
 
 Every case builds seeded inputs (``pypty_gb300.synth``), simulates measurements with the
 variants oracle at the true specimen (patterns plus Poisson noise, or detector coefficients
@@ -50,8 +51,9 @@ def ref_call(pypty, c):
         alpha_near_field=f(c["alpha"]), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
         propmethod="multislice", this_chopped_sequence=c["sequence"], load_one_by_one=False,
         data_multiplier=f(c["mult"]), data_pad=c["data_pad"], phase_plate_in_h5=None, this_loss_weight=c["loss_weight"],
-        data_bin=1, data_shift_vector=[c["shift0"], c["shift1"]], upsample_pattern=1, static_background=None,
-        this_step_static_background=0,
+        data_bin=1, data_shift_vector=[c["shift0"], c["shift1"]], upsample_pattern=c["upsample"],
+        static_background=None if c["static_background"] is None else c["static_background"].astype(f),
+        this_step_static_background=c["step_sb"],
         tilt_mode=c["tilt_mode"], aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
         compute_batch=c["batch"], phase_only_obj=False, beam_current=bc,
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], default_float=f,
@@ -64,7 +66,7 @@ def ref_call(pypty, c):
         probe_mod_tol=0.05, smart_memory=False, print_flag=0, data_simulation_flag=False,
         data_simulation_exitwave=False, use_padded_intensity=bool(c["use_padded"]))
     # outer return order (objective.py:967): aberrations gradient before beam-current gradient
-    return res[0], res[1], res[2], res[3], res[4], res[8], res[7], res[5]
+    return res[0], res[1], res[2], res[3], res[4], res[8], res[7], res[5], res[6]
 
 
 def detector_masks(W, n, rng):
@@ -85,7 +87,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                loss_weight=1.0, step_probe=1, step_obj=1, step_pos=0, dose=1e4, double=False, recon_type="far_field",
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
                n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
-               mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0):
+               mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0, upsample=1, static=0.0,
+               step_sb=0):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
@@ -104,9 +107,16 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
     # tilt rows [tan_y, tan_x] before / inside / after: one row, or one per position
     tilts = (rng.normal(size=(N if tilt_rows == "per_position" else 1, 6)) * tilt_scale).astype(f) \
         if tilt_rows else None
+    # a smooth static background, a fraction `static` of the mean pattern's amplitude
+    sb = None
+    if static:
+        yy, xx = np.mgrid[:W, :W] - W / 2
+        sb = (static * np.sqrt(dose / (W * W)) * (0.5 + np.exp(-(yy ** 2 + xx ** 2) / (0.1 * W * W)))
+              * rng.uniform(0.8, 1.2, size=(W, W))).astype(f)
     kw = dict(recon_type=recon_type, defocus=defocus, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
               masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
-              use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode)
+              use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode, upsample_pattern=upsample,
+              static_background=sb)
     sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, distance, edge_mult, None, algorithm, lam,
                                           1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
     if n_masks:
@@ -128,7 +138,9 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 recon_type=recon_type, defocus=defocus, cs=cs, alpha=alpha_nf, tan_x=tan_x, tan_y=tan_y, masks=masks,
                 beam_current=bc, step_bc=step_bc, aberrations=ab, aberration_marker=marker, step_ab=step_ab,
                 data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult,
-                tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts)
+                tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts, upsample=upsample,
+                static_background=None if sb is None else (sb.astype(np.float64) if double else sb),
+                step_sb=step_sb)
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -183,16 +195,32 @@ CASES = [
     # the same with sub-pixel shifts: the shift spectrum excludes the plates (objective.py:461, 471)
     dict(BASE, name="current_aberr_shift_c64", seed=37, algorithm="lsq_sqrt", beam_current=True, step_bc=1,
          n_ab_sets=2, n_abs=4, step_ab=1, step_pos=1),
+    # detector upsampling (objective.py:523-524, 590-591): 2 x 2 block sums of the model
+    # pattern; alone, with the cropped pattern, and with zero-padded measurements
+    dict(BASE, name="upsample2_c64", seed=47, algorithm="ml", upsample=2, step_pos=1),
+    dict(BASE, name="upsample2_crop_c64", seed=48, algorithm="lsq_sqrt", upsample=2, data_pad=6, use_padded=0),
+    dict(BASE, name="upsample2_pad_c64", seed=49, algorithm="ml", upsample=2, data_pad=6, use_padded=1,
+         shift=(1, -2)),
+    # static background with its gradient (objective.py:359-361, 525-526, 588-589): far field,
+    # near field, a compressed loss, and an FP64 twin
+    dict(BASE, name="static_c64", seed=50, algorithm="lsq_sqrt", static=0.3, step_sb=1, step_pos=1),
+    dict(BASE, name="static_c128", seed=50, algorithm="lsq_sqrt", static=0.3, step_sb=1, step_pos=1, double=True),
+    dict(BASE, name="static_near_c64", seed=51, algorithm="ml", static=0.2, step_sb=1, recon_type="near_field",
+         defocus=60.0, cs=2e5),
+    dict(BASE, name="static_compressed_c64", seed=52, algorithm="lsq_compressed", n_masks=6, static=0.2,
+         step_sb=1),
 ]
 
 
-def main():
+def main(names=None):
     pypty = import_reference()
     for spec in CASES:
         spec = dict(spec)
         name = spec.pop("name")
+        if names and name not in names:
+            continue
         c = build_case(name, **spec)
-        loss, sse, og, pg, posg, bcg, abg, tg = ref_call(pypty, c)
+        loss, sse, og, pg, posg, bcg, abg, tg, sbg = ref_call(pypty, c)
         out = os.path.join(HERE, "variant_" + name + ".npz")
         none = np.zeros(0, np.float32)
         np.savez_compressed(
@@ -202,7 +230,7 @@ def main():
                               c["loss_weight"], c["batch"], c["step_probe"], c["step_obj"], c["step_pos"],
                               c["defocus"], c["cs"], c["alpha"], c["tan_x"], c["tan_y"], c["step_bc"], c["step_ab"],
                               c["data_pad"], c["use_padded"], c["shift0"], c["shift1"], c["mult"], c["tilt_mode"],
-                              c["step_tilts"]],
+                              c["step_tilts"], c["upsample"], c["step_sb"]],
                              dtype=np.float64),
             algorithm=np.array(c["algorithm"]), recon_type=np.array(c["recon_type"]), double=np.array(c["double"]),
             masks=none if c["masks"] is None else c["masks"],
@@ -212,11 +240,13 @@ def main():
             ref_loss=np.array(loss, dtype=np.float64), ref_sse=np.array(sse, dtype=np.float64),
             ref_object_grad=og, ref_probe_grad=np.asarray(pg), ref_pos_grad=posg,
             ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg),
-            tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg))
+            tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg),
+            static_background=none if c["static_background"] is None else c["static_background"],
+            ref_static_grad=np.asarray(sbg))
         print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
             np.linalg.norm(np.asarray(abg)), os.path.basename(out)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -45,16 +45,19 @@ def load_variant_case(name):
     s = d["scalars"]
     keys = ["distance", "edge_mult", "wavelength", "px", "cutoff", "rolloff", "loss_weight", "batch", "step_probe",
             "step_obj", "step_pos", "defocus", "cs", "alpha", "tan_x", "tan_y", "step_bc", "step_ab", "data_pad",
-            "use_padded", "shift0", "shift1", "mult", "tilt_mode", "step_tilts"]
+            "use_padded", "shift0", "shift1", "mult", "tilt_mode", "step_tilts", "upsample", "step_sb"]
+    defaults = dict(upsample=1.0, step_sb=0.0)   # fixtures written before these scalars existed
     for i, k in enumerate(keys):
-        d[k] = float(s[i])
+        d[k] = float(s[i]) if i < len(s) else defaults[k]
     for k in ("batch", "step_probe", "step_obj", "step_pos", "step_bc", "step_ab", "data_pad", "use_padded", "shift0",
-              "shift1", "tilt_mode", "step_tilts"):
+              "shift1", "tilt_mode", "step_tilts", "upsample", "step_sb"):
         d[k] = int(d[k])
     d["algorithm"] = str(d["algorithm"])
     d["recon_type"] = str(d["recon_type"])
     d["double"] = bool(d["double"])
-    for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts"):
+    for k in ("static_background", "ref_static_grad"):
+        d.setdefault(k, np.zeros(0, np.float32))
+    for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts", "static_background"):
         if d[k].size == 0:
             d[k] = None
     return d

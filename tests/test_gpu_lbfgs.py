@@ -108,16 +108,17 @@ def _two_loop_numpy(g, S, Y, w):
     return [-qi for qi in q]
 
 
-@pytest.mark.parametrize("nseg", [3, 6])
+@pytest.mark.parametrize("nseg", [3, 7])
 def test_two_loop_matches_fp64_numpy(nseg):
     import ctypes
     import torch
     from pypty_gb300 import _lib
     from pypty_gb300.optim import _ptrs
     rng = np.random.default_rng(7)
-    # object, probe, positions (floats); then tilt rows, aberrations, beam currents
-    sizes = [2 * 64 * 64 * 3, 2 * 32 * 32 * 2, 2 * 50, 6 * 50, 2 * 7, 50][:nseg]
-    w = [2.0, 2.0, 1.0, 1.0, 1.0, 1.0][:nseg]
+    # object, probe, positions (floats); then tilt rows, static background, aberrations, beam
+    # currents
+    sizes = [2 * 64 * 64 * 3, 2 * 32 * 32 * 2, 2 * 50, 6 * 50, 32 * 32, 2 * 7, 50][:nseg]
+    w = [2.0, 2.0, 1.0, 1.0, 1.0, 1.0, 1.0][:nseg]
     m = 4
     g = [rng.normal(size=n).astype(np.float32) for n in sizes]
     # pairs with positive curvature y.s > 0, as accepted Wolfe steps give
@@ -297,6 +298,39 @@ def test_bfgs_update_refines_tilts_aberrations_and_beam_current():
         assert rel_l2(ns.aberrations_array, c["ref_ab"][e]) <= 1e-3
         assert rel_l2(ns.beam_current, c["ref_bc"][e]) <= 1e-3
         assert isinstance(ns.tilts_correction, np.ndarray) and ns.tilts_correction.dtype == f
+
+
+def test_bfgs_update_refines_the_static_background():
+    """Object, probe and static background refined together (the reference's
+    update_static_background): the same trial counts and steps as the reference's bfgs_update
+    and the background after every call (tests/golden/make_golden_lbfgs.py make_static_case)."""
+    from pypty_gb300 import iterative
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lbfgs_refine_static_background.npz")))
+    s = d["scalars"]
+    c = dict(d, distance=float(s[0]), edge_mult=float(s[1]), wavelength=float(s[2]), px=float(s[3]),
+             cutoff=float(s[4]), rolloff=0.0, loss_weight=float(s[6]), batch=int(s[7]), algorithm=str(d["algorithm"]),
+             step_probe=1, step_obj=1, step_pos=0, orthogonal=False, lazy_clean=False, hist_length=10)
+    ns = types.SimpleNamespace(obj=c["obj"].copy(), probe=c["probe"].copy(), positions=c["positions"].copy(),
+                               positions_correction=c["pos_correction"].astype(np.float32).copy(),
+                               tilts=np.zeros((1, 6), np.float32), tilts_correction=np.zeros((1, 6), np.float32),
+                               static_background=c["static_background"].copy(), aberrations_array=None,
+                               beam_current=None, history_bfgs=None)
+    fn = iterative.bind(ns)
+    np.random.seed(6)
+    warnings, failed = "", 0
+    step = 1.0
+    for e, ref in enumerate(c["ref_scalars"]):
+        res = _call_with(fn, c, e, warnings, failed, dict(this_step_static_background=1, actual_step=step))
+        total_loss, sse, _cc, step, count, dv, ndv, warnings, failed = res
+        print(e, count, step, total_loss, "ref", ref[3], ref[2], ref[0])
+        assert int(count) == int(ref[3]), (e, count, ref)
+        assert float(step) == pytest.approx(float(ref[2]), rel=1e-5)
+        assert float(total_loss) == pytest.approx(float(ref[0]), rel=1e-4)
+        assert failed == 0
+        assert rel_l2(ns.obj, c["ref_obj"][e]) <= 1e-3
+        assert rel_l2(ns.probe, c["ref_probe"][e]) <= 1e-3
+        assert rel_l2(ns.static_background, c["ref_sb"][e]) <= 1e-3
+        assert isinstance(ns.static_background, np.ndarray) and ns.static_background.dtype == np.float32
 
 
 def _call_with(fn, c, epoch, warnings, failed, over):

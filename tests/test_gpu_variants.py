@@ -27,7 +27,7 @@ def run_gpu_variant(c, engine=None):
                         compute_batch=c["batch"], step_obj=c["step_obj"], step_probe=c["step_probe"],
                         step_pos=c["step_pos"])
     t = lambda a, dt=None: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
-    ls, og, pg, posg, bcg, abg, tg = eng.loss_and_direction_variants(
+    ls, og, pg, posg, bcg, abg, tg, sbg = eng.loss_and_direction_variants(
         prob, t(obj), t(probe), geo, t(c["measured"], np.float32), recon_type=c["recon_type"],
         defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"], masks=t(c["masks"], np.float32),
         beam_current=t(c["beam_current"], np.float32), step_beam_current=bool(c["step_bc"]),
@@ -35,12 +35,14 @@ def run_gpu_variant(c, engine=None):
         aberration_marker=t(c["aberration_marker"], np.int32), step_aberrations=bool(c["step_ab"]),
         data_pad=c.get("data_pad", 0), use_padded_intensity=bool(c.get("use_padded", 1)),
         data_shift_vector=(c.get("shift0", 0), c.get("shift1", 0)), data_multiplier=c.get("mult", 1.0),
-        tilts=c.get("tilts"), tilt_mode=c.get("tilt_mode", 0), step_tilts=bool(c.get("step_tilts", 0)))
+        tilts=c.get("tilts"), tilt_mode=c.get("tilt_mode", 0), step_tilts=bool(c.get("step_tilts", 0)),
+        upsample_pattern=c.get("upsample", 1), static_background=t(c.get("static_background"), np.float32),
+        step_static_background=bool(c.get("step_sb", 0)))
     torch.cuda.synchronize()
     ls = ls.cpu().numpy()
     cpu = lambda a: None if a is None else a.cpu().numpy()
     return (float(ls[0]), float(ls[1]), og.cpu().numpy(), pg.cpu().numpy(), posg.cpu().numpy(), cpu(bcg), cpu(abg),
-            cpu(tg))
+            cpu(tg), cpu(sbg))
 
 
 def fp64_variant_oracle(c):
@@ -54,13 +56,14 @@ def fp64_variant_oracle(c):
         beam_current=c["beam_current"], step_beam_current=c["step_bc"], aberrations=c["aberrations"],
         aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], data_pad=c["data_pad"],
         use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]), data_multiplier=c["mult"],
-        tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"], float_dtype=np.float64,
+        tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"], upsample_pattern=c["upsample"],
+        static_background=c["static_background"], step_static_background=c["step_sb"], float_dtype=np.float64,
         complex_dtype=np.complex128)
 
 
 def errors(res, ref):
-    loss, _, og, pg, posg, bcg, abg, tg = res
-    rl, _, rog, rpg, rposg, rbcg, rabg, rtg = ref
+    loss, _, og, pg, posg, bcg, abg, tg, sbg = res
+    rl, _, rog, rpg, rposg, rbcg, rabg, rtg, rsbg = ref
     e = dict(loss=abs(loss - float(rl)) / abs(float(rl)), obj=rel_l2(og, rog),
              probe=rel_l2(pg, np.asarray(rpg).reshape(pg.shape)))
     if posg is not None and np.linalg.norm(np.asarray(rposg)) > 0:
@@ -71,6 +74,8 @@ def errors(res, ref):
         e["ab"] = rel_l2(abg, rabg)
     if tg is not None:
         e["tilt"] = rel_l2(tg, rtg)
+    if sbg is not None:
+        e["static"] = rel_l2(sbg, rsbg)
     return e
 
 
@@ -92,7 +97,7 @@ def test_variants_against_fp64_oracle_and_reference(name):
         assert v <= (lt if k == "loss" else gt), (k, v)
     # the reference's own complex64 result carries its FP32 error too: twice the bound
     ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
-           c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"])
+           c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"], c["ref_static_grad"])
     eref = errors(res, ref)
     print(name, "vs reference c64", {k: "%.1e" % v for k, v in eref.items()})
     for k, v in eref.items():
@@ -105,7 +110,7 @@ def test_variants_against_reference_fp64(name):
     c = load_variant_case(name)
     res = run_gpu_variant(c)
     ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
-           c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"])
+           c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"], c["ref_static_grad"])
     e = errors(res, ref)
     print(name, {k: "%.1e" % v for k, v in e.items()})
     for k, v in e.items():
@@ -155,7 +160,8 @@ def test_variants_reject_bad_arguments():
 
 
 @pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64", "crop_c64",
-                                  "shift_mult_c64", "tilt4_rows_c64", "tilt2_single_c64"])
+                                  "shift_mult_c64", "tilt4_rows_c64", "tilt2_single_c64", "upsample2_pad_c64",
+                                  "static_compressed_c64"])
 def test_reference_signature_call_routes_variants(name):
     """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
     variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
@@ -182,7 +188,8 @@ def test_reference_signature_call_routes_variants(name):
         data_shift_vector=[c["shift0"], c["shift1"]], data_multiplier=np.float32(c["mult"]), load_one_by_one=True,
         aberration_marker=c["aberration_marker"], aberrations_array=c["aberrations"], beam_current=c["beam_current"],
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], tilt_mode=c["tilt_mode"],
-        this_step_tilts=c["step_tilts"])
+        this_step_tilts=c["step_tilts"], upsample_pattern=c["upsample"], static_background=c["static_background"],
+        this_step_static_background=c["step_sb"])
     out = objective.loss_and_direction(**kw)
     assert len(out) == 10
     lt, gt = TOL.get(c["algorithm"], (1e-5, 1e-4))
@@ -197,6 +204,8 @@ def test_reference_signature_call_routes_variants(name):
         assert rel_l2(out[8], c["ref_beam_current_grad"]) <= 2 * gt
     if c["step_tilts"]:
         assert rel_l2(out[5], c["ref_tilts_grad"]) <= 2 * gt
+    if c["step_sb"]:
+        assert rel_l2(out[6], c["ref_static_grad"]) <= 2 * gt
 
 
 def test_lbfgs_runs_on_the_variants_path():

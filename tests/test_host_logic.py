@@ -46,7 +46,10 @@ def base_kwargs(**over):
     dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
     dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_bin=2),
     dict(algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32), data_pad=4),
-    dict(upsample_pattern=2), dict(atv_weight=0.1), dict(static_background=np.ones((64, 64))),
+    dict(upsample_pattern=2, algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32)),
+    dict(atv_weight=0.1), dict(static_background=np.ones((64, 64)), upsample_pattern=2),
+    dict(static_background=np.ones((64, 64)), data_pad=4, use_padded_intensity=False),
+    dict(static_background=np.ones(64)), dict(this_step_static_background=1),
     dict(data_simulation_flag="sim.npy"),
 ])
 def test_unsupported_flags_raise_before_any_gpu_work(over):
@@ -162,3 +165,15 @@ def test_measured_preprocessing_routes_to_the_variants_path():
     assert v["data_pad"] == 4 and v["use_padded_intensity"] is False
     _, _, v = objective.prepare(**base_kwargs(data_shift_vector=[1, -2], data_multiplier=2.0))
     assert v["data_shift_vector"] == (1, -2) and v["data_multiplier"] == 2.0
+
+
+def test_upsampling_and_static_background_route_to_the_variants_path():
+    """upsample_pattern and a 2D static background (with its step) select the variants path;
+    a scalar zero background is no background."""
+    _, _, v = objective.prepare(**base_kwargs(upsample_pattern=2, measured_array=np.zeros((2, 32, 32), np.float32)))
+    assert v["upsample_pattern"] == 2 and v["static_background"] is None
+    bg = np.full((64, 64), 0.5, np.float32)
+    _, _, v = objective.prepare(**base_kwargs(static_background=bg, this_step_static_background=1))
+    assert v["static_background"].shape == (64, 64) and v["step_static_background"]
+    _, _, v = objective.prepare(**base_kwargs(static_background=0))
+    assert v is None

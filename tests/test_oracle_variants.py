@@ -1,5 +1,6 @@
 """Pin the variants oracle (near field, compressed detectors, beam current, aberration plates,
-inside tilt) to golden vectors produced by the reference's own NumPy path."""
+tilts, measured-data preprocessing, detector upsampling, static background) to golden vectors
+produced by the reference's own NumPy path."""
 import numpy as np
 import pytest
 
@@ -18,13 +19,14 @@ def run_variant_oracle(c):
         aberrations=c["aberrations"], aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"],
         data_pad=c["data_pad"], use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]),
         data_multiplier=f(c["mult"]), tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"],
-        float_dtype=f, complex_dtype=cx)
+        upsample_pattern=c["upsample"], static_background=c["static_background"],
+        step_static_background=c["step_sb"], float_dtype=f, complex_dtype=cx)
 
 
 @pytest.mark.parametrize("name", variant_case_names())
 def test_variants_oracle_matches_reference(name):
     c = load_variant_case(name)
-    loss, sse, og, pg, posg, bcg, abg, tg = run_variant_oracle(c)
+    loss, sse, og, pg, posg, bcg, abg, tg, sbg = run_variant_oracle(c)
     tol = 1e-12 if c["double"] else 5e-6
     assert abs(float(loss) - float(c["ref_loss"])) <= tol * abs(float(c["ref_loss"]))
     assert abs(float(sse) - float(c["ref_sse"])) <= tol * abs(float(c["ref_sse"]))
@@ -39,6 +41,8 @@ def test_variants_oracle_matches_reference(name):
         assert rel_l2(abg, c["ref_aberrations_grad"]) <= (1e-12 if c["double"] else 1e-5)
     if c["step_tilts"]:
         assert rel_l2(tg, c["ref_tilts_grad"]) <= (1e-12 if c["double"] else 1e-5)
+    if c["step_sb"]:
+        assert rel_l2(sbg, c["ref_static_grad"]) <= (1e-12 if c["double"] else 1e-5)
 
 
 def test_near_field_alpha_is_rejected():
