@@ -541,7 +541,7 @@ def main():
     torch.cuda.synchronize(dev)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n_batches = -(-n_pos // cfg["batch"])
-    with ClockSampler(local_rank) as clocks, _lib.LaunchProfiler((16 + 12 * n_batches) * max(args.steps, 1)) as prof:
+    with ClockSampler(local_rank) as clocks:
         start.record(stream)
         for _ in range(args.steps):
             eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)
@@ -549,6 +549,17 @@ def main():
         torch.cuda.synchronize(dev)
     barrier()
     ms = start.elapsed_time(stop) / args.steps
+    # the same steps again under the launch profiler: the library then issues every launch on
+    # one stream, one after another, so each kernel's CUDA-event interval is that kernel alone
+    # (the roofline's launch duration and the kernel shares)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with _lib.LaunchProfiler((16 + 12 * n_batches) * max(args.steps, 1)) as prof:
+        p0.record(stream)
+        for _ in range(args.steps):
+            eng.loss_and_direction(prob, obj_d, probe_d, geo, meas_d, out=out)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+    profiled_ms = p0.elapsed_time(p1) / args.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -662,7 +673,12 @@ def main():
                                  if (W, Z, Mp) in TRAFFIC_PER_POSITION else None),
                      "traffic_source": "ncu dram bytes of a 64-position capture of the same shape, scaled by "
                                        "positions per launch (profiles/)",
-                     "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3},
+                     "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3,
+                     "timing": "CUDA events around each launch in a second pass of the same steps with the "
+                               "launch profiler on (launches serialised on one stream: kernels %.2f ms per step "
+                               "there; %.2f ms per step in the timed region, where batches overlap on three "
+                               "streams)" % (total_prof_ms / max(args.steps, 1), ms),
+                     "profiled_pass_ms_per_step": profiled_ms},
         "path_roofline": {"alg_bytes_per_position": alg_bytes_per_position(W, Z, Mp),
                           "achieved_gbs": path_bytes / (ms / 1000.0) / 1e9,
                           "frac": path_bytes / (ms / 1000.0) / 1e9 / hbm_peak,

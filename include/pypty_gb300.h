@@ -465,8 +465,11 @@ int pty_atom_slices(const float* atoms, int32_t n_atoms, int32_t ny, int32_t nx,
  * pypty/utils.py:1894). While enabled, every kernel launch of the library records a CUDA
  * event on its stream just before the launch, and every call records one when its last
  * launch is queued. pty_profile_end synchronises, disables profiling and returns, per
- * kernel class, the summed device time between each launch's event and the next event
- * (ms) and the launch count. Class names: pty_kernel_name(0 .. pty_kernel_count()-1).
+ * kernel class, the summed device time between each launch's event and the next event on
+ * the same stream (ms) and the launch count. Class names: pty_kernel_name(0 ..
+ * pty_kernel_count()-1). While enabled, pty_loss_and_direction issues its batches on the
+ * caller's stream one launch after another (without profiling, consecutive batches overlap
+ * on three streams), so each timed interval is one kernel running alone.
  * Single-threaded use only. Returns PTY_ERR_WORKSPACE if more than max_launches launches
  * were made (the extra ones are not timed).
  */

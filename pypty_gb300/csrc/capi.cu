@@ -96,6 +96,8 @@ void prof_mark(cudaStream_t st, int id) {
   P.ids[P.n++] = id;
 }
 
+bool prof_active() { return g_prof.on; }
+
 constexpr int kMaxSideDevices = 64;
 struct SideStreams {
   SideStream dev[kMaxSideDevices];
@@ -104,6 +106,7 @@ struct SideStreams {
       for (cudaEvent_t e : d.ev)
         if (e) cudaEventDestroy(e);
       if (d.s) cudaStreamDestroy(d.s);
+      if (d.s2) cudaStreamDestroy(d.s2);
     }
   }
 };
@@ -117,11 +120,13 @@ int side_stream(SideStream** out) {
   if (!d.s) {
     SideStream n;
     bool ok = cudaStreamCreateWithFlags(&n.s, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&n.s2, cudaStreamNonBlocking) == cudaSuccess;
     for (cudaEvent_t& e : n.ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
       for (cudaEvent_t e : n.ev)
         if (e) cudaEventDestroy(e);
       if (n.s) cudaStreamDestroy(n.s);
+      if (n.s2) cudaStreamDestroy(n.s2);
       return PTY_ERR_CUDA;
     }
     d = n;

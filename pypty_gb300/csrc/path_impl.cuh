@@ -24,12 +24,13 @@ struct Path {
   const Plan& q;
   void* ws;
   cudaStream_t st;
-  cudaStream_t side;   // stream of windows() and gradients(): st, or the second stream when overlapping
+  cudaStream_t side;   // stream of windows() and gradients(): st, or a second stream when overlapping
+  cudaStream_t fst;    // stream of fused(): st, or alternately st and a third stream when overlapping
   float2* tw;
   TableArgs ta{};
 
   Path(const pty_problem_t* p_, const Plan& q_, void* ws_, cudaStream_t st_)
-      : p(p_), q(q_), ws(ws_), st(st_), side(st_) {
+      : p(p_), q(q_), ws(ws_), st(st_), side(st_), fst(st_) {
     tw = at<float2>(ws, q.o_tw);
     ta.pyx = at<float2>(ws, q.o_pyx);
     ta.mask = at<float>(ws, q.o_mask);
@@ -81,6 +82,7 @@ struct Path {
   float2* obl(int ib) const { return at<float2>(ws, q.o_obl + (size_t)(ib % q.nbuf) * q.s_obl); }
   float2* gsum(int ib) const { return at<float2>(ws, q.o_gsum + (size_t)(ib % q.nbuf) * q.s_gsum); }
   float2* fprobe(int ib) const { return at<float2>(ws, q.o_fprobe + (size_t)(ib % q.nbuf) * q.s_fprobe); }
+  float2* stack(int ib) const { return at<float2>(ws, q.o_stack + (size_t)(ib % q.nbuf) * q.s_stack); }
   const int* seq_of(int ib) const { return at<int>(ws, q.o_seq) + ib * q.Bb; }
 
   int windows(int ib) {
@@ -132,7 +134,7 @@ struct Path {
     fa.seq = seq_of(ib);
     fa.measured = measured;
     fa.tw = tw;
-    fa.stack = at<float2>(ws, q.o_stack);
+    fa.stack = stack(ib);
     fa.gsum = gsum(ib);
     fa.fprobe = fprobe(ib);
     fa.gbuf = at<float2>(ws, q.o_gbuf);
@@ -145,7 +147,7 @@ struct Path {
     cfg.gridDim = dim3((unsigned)(Bn * nmodes));
     cfg.blockDim = dim3(T);
     cfg.dynamicSmemBytes = FusedSmem<W>::bytes;
-    cfg.stream = st;
+    cfg.stream = fst;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)nmodes;
@@ -153,7 +155,7 @@ struct Path {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    prof_mark(st, KID_FUSED);
+    prof_mark(fst, KID_FUSED);
     const cudaError_t e = fa.phase == 0 ? cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W, 0>, fa)
                                         : cudaLaunchKernelEx(&cfg, fused_multislice_kernel<W, 1>, fa);
     if (e != cudaSuccess) return PTY_ERR_CUDA;
@@ -216,40 +218,49 @@ struct Path {
   }
 };
 
-// The batch loop on two streams (double-buffered windows, nbuf = 2). The caller's stream st
-// runs the fused kernels; the second stream runs windows(ib + 1) while fused(ib) runs and
-// gradients(ib) while fused(ib + 1) runs:
-//   second: windows(0) | windows(1) gradients(0) | windows(2) gradients(1) | ...
-//   st:                  fused(0)                | fused(1)                | fused(2) ...
+// The batch loop on three streams (double-buffered windows, wave stacks, gradient windows
+// and shifted probes, nbuf = 2). Batch ib's fused kernel runs on F(ib % 2) -- the caller's
+// stream st for even batches, a second stream for odd ones -- so that one launch's last,
+// partly filled wave overlaps the next launch's first; a third stream S extracts windows and
+// scatters gradients:
+//   S:    windows(0) | windows(1) gradients(0) | windows(2) gradients(1) | ...
+//   F(0): fused(0)                             | fused(2)                | ...
+//   F(1):              fused(1)                           | fused(3)     | ...
 // Events (each wait is issued after the record it refers to and before that event's next
 // record): ev[0] start, then fused(ib) done; ev[1] windows(ib) done; ev[2 + ib % 2]
-// gradients(ib) done, which fused(ib + 2) waits for before it rewrites buffer ib % 2.
-// windows(ib + 1) rewrites obl((ib + 1) % 2), last read by fused(ib - 1): the second stream
-// waited for that fused kernel before gradients(ib - 1). The scatter into the object gradient
-// and the probe partial sums accumulate in batch order on the second stream, so the results
-// are those of the one-stream loop bit for bit. Each stage closes its launch-profiler interval
-// on its own stream, so profiled durations exclude the waits between the streams.
+// gradients(ib) done, which fused(ib + 2) waits for before it rewrites gradient buffer ib % 2.
+// fused(ib + 2) follows fused(ib) on its stream, so its wave stack is free. windows(ib + 1)
+// rewrites obl((ib + 1) % 2), last read by fused(ib - 1): S waited for that fused kernel before
+// gradients(ib - 1). The scatter into the object gradient and the probe partial sums accumulate
+// in batch order on S, so the results are those of the one-stream loop bit for bit. Each
+// stage closes its launch-profiler interval on its own stream, so profiled durations exclude
+// the waits between the streams.
 template <int W>
 int run_batches_overlapped(Path<W>& P, const float2* probe, const float* measured, float* patterns) {
   SideStream* sd = nullptr;
   int rc = side_stream(&sd);
   if (rc) return rc;
   cudaStream_t st = P.st, ss = sd->s;
+  const cudaStream_t fs[2] = {st, sd->s2};
   cudaEvent_t ev_f = sd->ev[0], ev_w = sd->ev[1];
   auto ok = [](cudaError_t e) { return e == cudaSuccess; };
   prof_mark(st, -1);
-  if (!ok(cudaEventRecord(ev_f, st)) || !ok(cudaStreamWaitEvent(ss, ev_f, 0))) return PTY_ERR_CUDA;
+  if (!ok(cudaEventRecord(ev_f, st)) || !ok(cudaStreamWaitEvent(ss, ev_f, 0)) ||
+      !ok(cudaStreamWaitEvent(fs[1], ev_f, 0)))
+    return PTY_ERR_CUDA;
   P.side = ss;
   const int n = P.q.nbatch;
   rc = P.windows(0);
   prof_mark(ss, -1);
   if (!rc && !ok(cudaEventRecord(ev_w, ss))) rc = PTY_ERR_CUDA;
   for (int ib = 0; ib < n && !rc; ++ib) {
-    if (!ok(cudaStreamWaitEvent(st, ev_w, 0))) { rc = PTY_ERR_CUDA; break; }
-    if (!patterns && ib >= 2 && !ok(cudaStreamWaitEvent(st, sd->ev[2 + ib % 2], 0))) { rc = PTY_ERR_CUDA; break; }
+    cudaStream_t f = fs[ib % 2];
+    P.fst = f;
+    if (!ok(cudaStreamWaitEvent(f, ev_w, 0))) { rc = PTY_ERR_CUDA; break; }
+    if (!patterns && ib >= 2 && !ok(cudaStreamWaitEvent(f, sd->ev[2 + ib % 2], 0))) { rc = PTY_ERR_CUDA; break; }
     if ((rc = P.fused(ib, 0, probe, measured, patterns))) break;
-    prof_mark(st, -1);
-    if (!ok(cudaEventRecord(ev_f, st))) { rc = PTY_ERR_CUDA; break; }
+    prof_mark(f, -1);
+    if (!ok(cudaEventRecord(ev_f, f))) { rc = PTY_ERR_CUDA; break; }
     if (ib + 1 < n) {
       if ((rc = P.windows(ib + 1))) break;
       prof_mark(ss, -1);
@@ -262,9 +273,12 @@ int run_batches_overlapped(Path<W>& P, const float2* probe, const float* measure
       if (!ok(cudaEventRecord(sd->ev[2 + ib % 2], ss))) { rc = PTY_ERR_CUDA; break; }
     }
   }
-  // join: everything queued on the second stream completes before st's next launch
+  // join: S waited for every fused kernel it followed; everything queued on S and on the
+  // second fused stream completes before st's next launch
   P.side = st;
+  P.fst = st;
   cudaEvent_t ev_join = sd->ev[1];
+  if (!ok(cudaEventRecord(ev_join, fs[1])) || !ok(cudaStreamWaitEvent(st, ev_join, 0))) return PTY_ERR_CUDA;
   if (!ok(cudaEventRecord(ev_join, ss)) || !ok(cudaStreamWaitEvent(st, ev_join, 0))) return PTY_ERR_CUDA;
   return rc;
 }
@@ -276,7 +290,7 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   Path<W> P(p, q, ws, st);
   int rc = P.prepare(obj, probe);
   if (rc) return rc;
-  if (q.nbuf == 2) {
+  if (q.nbuf == 2 && !prof_active()) {
     if ((rc = run_batches_overlapped(P, probe, measured, patterns))) return rc;
   } else {
     for (int ib = 0; ib < q.nbatch; ++ib) {

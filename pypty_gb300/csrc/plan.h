@@ -24,11 +24,13 @@ struct Plan {
   size_t total;
   int ckpt;   // kept slices every ckpt (256 windows)
   bool split;   // one batch with every position: pty_forward / pty_backward
-  // W <= 128 with several batches: object windows, gradient windows and shifted probes are
-  // double-buffered (nbuf = 2) so that batch ib + 1's windows and batch ib's gradients run on
-  // a second stream while batch ib + 1's fused kernel runs; s_* are the buffer strides in bytes
+  // W <= 128 with several batches: object windows, wave stacks, gradient windows and shifted
+  // probes are double-buffered (nbuf = 2): consecutive batches' fused kernels run on two
+  // streams (one's tail overlaps the next one's start) and a third stream extracts batch
+  // ib + 1's windows and scatters batch ib's gradients meanwhile; s_* are the buffer strides
+  // in bytes
   int nbuf;
-  size_t s_obl, s_gsum, s_fprobe;
+  size_t s_obl, s_gsum, s_fprobe, s_stack;
 };
 
 // twiddle tables in global memory: W = 256 windows use the 128 tables of their sub-transforms
@@ -95,7 +97,8 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_obl = take(q.nbuf * q.s_obl);
   q.ckpt = (p->window == 256 && p->checkpoint_every > 1) ? std::min(p->checkpoint_every, q.Z) : 1;
   const int n_kept = (q.Z + q.ckpt - 1) / q.ckpt;
-  q.o_stack = take((size_t)q.Bb * n_kept * q.Mp * q.Mo * WW * c8);
+  q.s_stack = align_up((size_t)q.Bb * n_kept * q.Mp * q.Mo * WW * c8);
+  q.o_stack = take(q.nbuf * q.s_stack);
   q.o_gsum = take(q.nbuf * q.s_gsum);
   q.o_fprobe = take(q.nbuf * q.s_fprobe);
   q.o_partial = take((size_t)q.nchunk * q.Mp * WW * c8);
@@ -198,10 +201,14 @@ enum KernelId : int {
 // Records an event on `st` before a launch of kernel class `id` while profiling is on
 // (id < 0 closes the last interval on that stream). No-op otherwise.
 void prof_mark(cudaStream_t st, int id);
-// A second stream and four events for the caller's device, created on first use by each
+// True while the launch profiler records. The batch loops then issue every launch on the
+// caller's stream, one after another, so that each profiled interval is one kernel running
+// alone (the durations the roofline is computed from).
+bool prof_active();
+// Two more streams and four events for the caller's device, created on first use by each
 // host thread and kept until the thread exits.
 struct SideStream {
-  cudaStream_t s = nullptr;
+  cudaStream_t s = nullptr, s2 = nullptr;
   cudaEvent_t ev[4] = {};
 };
 int side_stream(SideStream** out);
