@@ -72,6 +72,10 @@ typedef struct pty_problem {
   int32_t checkpoint_every; /* 256-px windows: keep every k-th slice's wave and recompute the
                                others in the adjoint (k <= 1: keep all). No counterpart in the
                                reference, which keeps every slice (multislice_core.py:66). */
+  const float* slice_distances; /* NULL: slice_distance for every step. Else n_slices - 1
+                               distances in HOST memory, step z (slice z to z + 1) using entry z:
+                               the reference's this_distances with more than one entry
+                               (is_single_dist false, multislice_core.py:69-74, 164-174) */
 } pty_problem_t;
 
 /* Library version (major * 10000 + minor * 100 + patch). */

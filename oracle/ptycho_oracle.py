@@ -6,7 +6,8 @@ is never part of it.
 Supported flag set (the one the GPU path implements): far-field propagation,
 ``propmethod="multislice"``, no beam tilts (tilt_mode 0, tilts zero), no phase plates,
 aberration arrays, beam-current fluctuations, static background, data padding, binning or
-compressed detectors, a single slice distance, algorithms ``lsq_sqrt``, ``ml``, ``lsq``
+compressed detectors, one slice distance or one per slice step (``distance`` an array with
+more than one entry, ``multislice_core.py:69-74, 164-174``), algorithms ``lsq_sqrt``, ``ml``, ``lsq``
 and ``lsq_sqrt_2``, sub-pixel probe shifts and the position gradient. Regularisers are off.
 
 Every step cites the reference line it restates. The arithmetic is done in the array dtype
@@ -88,7 +89,8 @@ def shift_ramp_tables(W, mask, complex_dtype):
 def multislice(probe_b, obj_b, prop, edge_mult):
     """Forward split-step multislice, ``pypty/multislice_core.py:61-82``.
 
-    probe_b: (B, W, W, Mp); obj_b: (B, W, W, Z, Mo); prop: (W, W) propagator (mask applied).
+    probe_b: (B, W, W, Mp); obj_b: (B, W, W, Z, Mo); prop: (W, W) propagator (mask applied),
+    or a list of one per slice step (per-slice distances, ``multislice_core.py:69-71``).
     Returns the conjugated input-wave stack (B, W, W, Z, Mp, Mo) and the exit wave
     (B, W, W, Mp, Mo).
     """
@@ -100,7 +102,7 @@ def multislice(probe_b, obj_b, prop, edge_mult):
         stack[:, :, :, z] = wave
         wave = wave * obj_b[:, :, :, z:z + 1, :]
         if z < Z - 1:
-            p = prop
+            p = prop[z] if isinstance(prop, list) else prop
             if edge_mult > 1 and z == 0:
                 p = p ** edge_mult
             wave = fft2(wave, axes=(1, 2))
@@ -122,7 +124,8 @@ def multislice_grads(g, stack_conj, obj_b, prop, edge_mult, mask):
         contrib[:, :, :, z] = stack_conj[:, :, :, z] * g
         g = g * obj_c[:, :, :, z:z + 1, :]
         if z > 0:
-            p = np.conjugate(prop)
+            # the step from slice z - 1 (multislice_core.py:164-172: P(-d) = conj P(d))
+            p = np.conjugate(prop[z - 1] if isinstance(prop, list) else prop)
             if edge_mult > 1 and z == 1:
                 p = p ** edge_mult
             g = fft2(g, axes=(1, 2))
@@ -204,8 +207,12 @@ def loss_and_direction(obj, probe, positions, pos_correction, distance, edge_mul
     q2, qx, qy, mask_s, mask = spatial_frequencies(pixel_size_x, pixel_size_y, W,
                                                    damping_cutoff, smooth_rolloff, float_dtype)
     smy, smx = shift_ramp_tables(W, mask, complex_dtype)
-    prop = propagator(float_dtype(distance), float_dtype(wavelength), q2, qx, qy, mask,
-                      complex_dtype)
+    dists = np.asarray(distance, dtype=float_dtype).reshape(-1)
+    if dists.shape[0] > 1:   # one propagator per slice step (is_single_dist false)
+        prop = [propagator(dists[z], float_dtype(wavelength), q2, qx, qy, mask, complex_dtype)
+                for z in range(Z - 1)]
+    else:
+        prop = propagator(dists[0], float_dtype(wavelength), q2, qx, qy, mask, complex_dtype)
     probe_shift = bool(np.sum(pos_correction.astype(np.float64) ** 2) != 0.0) or bool(step_pos)
     runx, runy = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
     object_grad = np.zeros_like(obj)

@@ -207,10 +207,18 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         yx = np.stack((yg[None, :, :, None], xg[None, :, :, None]), axis=1)   # (1, 2, W, W, 1), objective.py:307
     # one propagator for all positions unless per-position inside tilts (objective.py:330-345)
     same_prop = single_tilt or tilt_mode in (1, 2)
-    d = f(distance)
-    if same_prop:
+    # per-slice distances (is_single_dist false): multislice builds each step's propagator from
+    # the batch's own inside tilts, for every tilt mode (multislice_core.py:69-71, 164-170)
+    dists = np.asarray(distance, dtype=f).reshape(-1)
+    per_step = dists.shape[0] > 1 and Z > 1
+    d = dists[0]
+    pos_prop = not same_prop or (per_step and not single_tilt)
+    if not pos_prop:
         t0 = tilts[0]
-        prop = propagator(d, lam, q2, qx, qy, mask, complex_dtype, t0[3], t0[2])
+        if per_step:
+            prop = [propagator(dists[z], lam, q2, qx, qy, mask, complex_dtype, t0[3], t0[2]) for z in range(Z - 1)]
+        else:
+            prop = propagator(d, lam, q2, qx, qy, mask, complex_dtype, t0[3], t0[2])
     probe_shift = bool(np.sum(np.asarray(pos_correction, np.float64) ** 2) != 0.0) or bool(step_pos)
     fluct = beam_current is not None
     morph = aberrations is not None
@@ -281,11 +289,13 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         if this_probe.shape[0] == 1 and B > 1:
             this_probe = np.repeat(this_probe, B, axis=0)
         this_probe = this_probe.astype(complex_dtype)
-        if same_prop:
-            prop_b = prop[None]
+        if not pos_prop:
+            prop_b = [p[None] for p in prop] if per_step else prop[None]
         else:                                                           # objective.py:482-484
-            prop_b = (np.exp(-3.141592654j * d * (lam * q2 + 2 * (qx * tx_i + qy * ty_i))) * mask)
-            prop_b = prop_b.astype(complex_dtype)
+            def pos_propagator(dz):
+                return (np.exp(-3.141592654j * dz * (lam * q2 + 2 * (qx * tx_i + qy * ty_i))) * mask).astype(
+                    complex_dtype)
+            prop_b = [pos_propagator(dists[z]) for z in range(Z - 1)] if per_step else pos_propagator(d)
         stack, exit_wave, spec_stack = multislice_tilted(this_probe, ob, prop_b, edge_mult, inside_grad)
         if after:                                                       # objective.py:490-499
             tmask_a = np.exp(xg[None, :, :, None] * tx_a + yg[None, :, :, None] * ty_a)[:, :, :, :, None]
@@ -373,7 +383,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         # a single tilt row with more than one position per batch makes the reference add a
         # (B,) vector into one row of tilts_grad (multislice_core.py:180-182): NumPy raises
         # ValueError there, as the reference does
-        grad_w, pgrad = multislice_grads_tilted(g, stack, spec_stack, ob, prop_b, edge_mult, mask, d, qx, qy,
+        grad_w, pgrad = multislice_grads_tilted(g, stack, spec_stack, ob, prop_b, edge_mult, mask,
+                                                list(dists[:Z - 1]) if per_step else d, qx, qy,
                                                 tilts_grad if inside_grad else None, tind)
         if step_obj:
             scatteradd(object_grad, my, mx, grad_w.astype(complex_dtype))
@@ -435,8 +446,9 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
 
 
 def multislice_tilted(probe_b, obj_b, prop_b, edge_mult, keep_spectra):
-    """Forward multislice with one propagator per position (prop_b (n, W, W), n = 1 or B),
-    ``multislice_core.py:61-82``; with ``keep_spectra`` also the conjugated spectra
+    """Forward multislice with one propagator per position (prop_b (n, W, W), n = 1 or B, or
+    a list of those per slice step), ``multislice_core.py:61-82``; with ``keep_spectra`` also
+    the conjugated spectra
     FFT(psi_z O_z) of every propagated slice (the second stack channel, ``:76-77``)."""
     B, W, _, Z, Mo = obj_b.shape
     Mp = probe_b.shape[-1]
@@ -447,7 +459,7 @@ def multislice_tilted(probe_b, obj_b, prop_b, edge_mult, keep_spectra):
         stack[:, :, :, z] = wave
         wave = wave * obj_b[:, :, :, z:z + 1, :]
         if z < Z - 1:
-            p = prop_b
+            p = prop_b[z] if isinstance(prop_b, list) else prop_b
             if edge_mult > 1 and z == 0:
                 p = p ** edge_mult
             wave = fft2(wave, axes=(1, 2))
@@ -471,8 +483,9 @@ def multislice_grads_tilted(g, stack_conj, spec_conj, obj_b, prop_b, edge_mult, 
         contrib[:, :, :, z] = stack_conj[:, :, :, z] * g
         g = g * obj_c[:, :, :, z:z + 1, :]
         if z > 0:
-            p = np.conjugate(prop_b)
-            dist = 1 * distance
+            # the step from slice z - 1 and its distance (multislice_core.py:164-172)
+            p = np.conjugate(prop_b[z - 1] if isinstance(prop_b, list) else prop_b)
+            dist = 1 * (distance[z - 1] if isinstance(distance, list) else distance)
             if edge_mult > 1 and z == 1:
                 p = p ** edge_mult
                 dist *= edge_mult

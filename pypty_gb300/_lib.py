@@ -38,6 +38,7 @@ class Problem(ctypes.Structure):
         ("slice_distance", ctypes.c_float), ("edge_mult", ctypes.c_float),
         ("damping_cutoff", ctypes.c_float), ("smooth_rolloff", ctypes.c_float),
         ("loss_weight", ctypes.c_float), ("checkpoint_every", ctypes.c_int32),
+        ("slice_distances", ctypes.c_void_p),
     ]
 
 

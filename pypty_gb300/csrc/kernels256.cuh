@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(512, 1) fused256_kernel(FusedArgs a) {
       const int zstep = adjoint ? z - 1 : z;
       const bool edge = a.use_edge && zstep == 0;
       const bool tab = !a.use_sep || edge;
-      const float2* pr = edge ? a.prop_edge : a.prop;
+      const float2* pr = a.prop_steps ? a.prop_steps + (size_t)zstep * (256 * 256) : (edge ? a.prop_edge : a.prop);
       WinFFT256::cross_propagate(v, s.xbuf, cl, c, adjoint, [&](int i, int q) {
         const int ky = G::fky(q, t, i), kx = G::fkx(q, t, i);
         if (tab) return pr[ky * 256 + kx];

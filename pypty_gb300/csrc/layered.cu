@@ -894,11 +894,14 @@ struct LPlan {
   size_t o_pos, o_corr, o_seq, o_tab_pyx, o_mask, o_mask_sc, o_prop, o_prop_edge, o_sx, o_sy, o_planes, o_pf;
   size_t o_obj, o_grad, o_ob, o_tmp, o_dob, o_stack, o_psi, o_psi2, o_pb, o_pbs, o_partial, o_lists, o_counts;
   size_t o_loss_part, o_pos_part, o_dft, dft_bytes, total;
+  int per_step;     // per-slice distances: one propagator table per step
+  size_t o_steps;
   // variants (pty_loss_and_direction_variants)
   int near, compressed, nmask, n_abs, n_sets, has_bc, step_static;
   size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part, o_sbg;
   // beam tilts
   int n_rows, single_tilt, same_prop, before, after, inside_grad, step_tilts;
+  int pos_prop;   // per-position propagator tables (per-position inside tilts that apply)
   size_t o_tilts, o_tgrid, o_spec, o_fexit, o_exitb, o_pbt, o_pft, o_tpart, o_pprop, o_pprop_edge;
 };
 
@@ -956,6 +959,8 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
   q.o_counts = take((size_t)q.ntiles * sizeof(int));
   q.o_loss_part = take((size_t)q.nseq * 2 * sizeof(double));
   q.o_pos_part = take((size_t)q.nseq * q.Mp * 2 * sizeof(double));
+  q.per_step = p->slice_distances && q.Z > 1;
+  q.o_steps = take(q.per_step ? (size_t)(q.Z - 1) * WWs * c8 : 0);
   if (v) {
     q.near = v->recon_type == 1;
     q.compressed = p->algorithm >= PTY_LSQ_COMPRESSED;
@@ -992,8 +997,11 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
     q.o_pft = take(q.before && p->probe_shift && !q.n_abs ? (size_t)q.Bb * q.Mp * WWs * c8 : 0);
     q.o_tpart = take((size_t)q.nseq * 6 * sizeof(double));
     const bool edge = p->edge_mult > 1.0f && q.Z > 1;
-    q.o_pprop = take(!q.same_prop ? (size_t)q.Bb * WWs * c8 : 0);
-    q.o_pprop_edge = take(!q.same_prop && edge ? (size_t)q.Bb * WWs * c8 : 0);
+    // with per-slice distances the reference builds every step's propagator from the batch's
+    // own inside tilts, in every tilt mode (multislice_core.py:69-71)
+    q.pos_prop = !q.same_prop || (q.per_step && !q.single_tilt);
+    q.o_pprop = take(q.pos_prop ? (size_t)q.Bb * WWs * c8 : 0);
+    q.o_pprop_edge = take(q.pos_prop && edge ? (size_t)q.Bb * WWs * c8 : 0);
   }
   size_t db = 0;
   const size_t maxwin = nobw > nwave ? nobw : nwave;
@@ -1121,6 +1129,23 @@ struct Run {
       va.cs = v->cs;
       var_tables_kernel<<<(WW + 255) / 256, 256, 0, st>>>(va);
     }
+    // per-slice distances: one table per step with the shared inside tilt (multislice_core.py:69-74)
+    float2* steps = at<float2>(ws, q.o_steps);
+    if (q.per_step) {
+      const float tx = v ? (v->n_tilts > 0 ? v->tilts_host[3] : v->tan_x) : 0.0f;
+      const float ty = v ? (v->n_tilts > 0 ? v->tilts_host[2] : v->tan_y) : 0.0f;
+      if (W == 64)
+        launch_step_props<64>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                              ta.use_edge, tx, ty, steps, st);
+      else if (W == 128)
+        launch_step_props<128>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                               ta.use_edge, tx, ty, steps, st);
+      else
+        launch_step_props<256>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                               ta.use_edge, tx, ty, steps, st);
+    }
+    // distance of slice step z (the step from slice z to z + 1)
+    auto step_distance = [&](int z) { return q.per_step ? p->slice_distances[z] : p->slice_distance; };
     float2* planes = at<float2>(ws, q.o_planes);
     float2* pf = at<float2>(ws, q.o_pf);
     prof_mark(st, KID_LAYOUT);
@@ -1167,7 +1192,7 @@ struct Run {
     pr.defocus = v ? v->defocus : 0.0f;
     pr.cs = v ? v->cs : 0.0f;
     pr.W = W;
-    const bool tilted_prop = v && !q.same_prop;
+    const bool tilted_prop = v && q.pos_prop;
     float2* spec = at<float2>(ws, q.o_spec);
     const size_t spec_stride = (size_t)q.Bb * nm * WWs;   // one forward step of the batch
     for (int i0 = 0, ib = 0; i0 < q.nseq; i0 += q.Bb, ++ib) {
@@ -1187,10 +1212,16 @@ struct Run {
       tg.seq = seq_b;
       float2* pprop = at<float2>(ws, q.o_pprop);
       float2* pprop_edge = ta.use_edge ? at<float2>(ws, q.o_pprop_edge) : nullptr;
-      if (tilted_prop) {   // the positions' propagators (objective.py:482-484), once per batch
+      // the positions' propagators (objective.py:482-484): once per batch, or per step with
+      // per-slice distances (multislice_core.py:69-74)
+      auto pos_props = [&](int zstep) {
+        PropArgs pz = pr;
+        pz.distance = step_distance(zstep);
         prof_mark(st, KID_ELEMENTWISE);
-        var_pos_prop_table_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(tg, pr, pprop, pprop_edge);
-      }
+        var_pos_prop_table_kernel<<<dim3((unsigned)(WW / EB), (unsigned)Bn), EB, 0, st>>>(
+            tg, pz, pprop, (zstep == 0 && ta.use_edge) ? pprop_edge : nullptr);
+      };
+      if (tilted_prop && !q.per_step) pos_props(0);
       if (var_probe && q.before) {
         // the probe before the tilt (after beam current and plates), then the tilt mask, then
         // the shift: from the pre-plate spectrum with plates, else the tilted probe's
@@ -1243,13 +1274,15 @@ struct Run {
               cudaMemcpyAsync(spec + z * spec_stride, psi2, (size_t)Bn * nm * WWs * sizeof(float2),
                               cudaMemcpyDeviceToDevice, st) != cudaSuccess)
             return PTY_ERR_CUDA;
+          if (tilted_prop && q.per_step) pos_props(z);
           prof_mark(st, KID_ELEMENTWISE);
           if (tilted_prop)
             var_pos_table_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? pprop_edge : pprop,
                                                                   nm, WW, 0);
           else
-            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, (z == 0 && ta.use_edge) ? ta.prop_edge : ta.prop, WW,
-                                                         0, unfold);
+            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(
+                psi2, q.per_step ? steps + (size_t)z * WWs : ((z == 0 && ta.use_edge) ? ta.prop_edge : ta.prop), WW,
+                0, unfold);
           if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
         }
       }
@@ -1297,16 +1330,18 @@ struct Run {
         adj_slice_kernel<<<grid(q.Mo, Bn), EB, 0, st>>>(psi, stack, ob, dob, z, q.Z, q.Mp, q.Mo, WW);
         if (z > 0) {
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
-          prof_mark(st, KID_ELEMENTWISE);
           const bool edge = z == 1 && ta.use_edge;
+          if (tilted_prop && q.per_step) pos_props(z - 1);
+          prof_mark(st, KID_ELEMENTWISE);
           if (tilted_prop)
             var_pos_table_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, edge ? pprop_edge : pprop, nm, WW, 1);
           else
-            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, edge ? ta.prop_edge : ta.prop, WW, 1, unfold);
+            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(
+                psi2, q.per_step ? steps + (size_t)(z - 1) * WWs : (edge ? ta.prop_edge : ta.prop), WW, 1, unfold);
           if (v && q.inside_grad) {
-            // sh = -4 pi d / W^2 in float32, d times the edge multiplier on the thick step
-            // (multislice_core.py:171-180)
-            const float dist = edge ? p->slice_distance * p->edge_mult : p->slice_distance;
+            // sh = -4 pi d / W^2 in float32, d (the step's distance) times the edge multiplier on
+            // the thick step (multislice_core.py:164-180)
+            const float dist = edge ? step_distance(z - 1) * p->edge_mult : step_distance(z - 1);
             const float shf = fdiv_host((float)-12.566370614359172 * dist, (float)WW);
             var_inside_tilt_kernel<<<Bn, 1024, 0, st>>>(psi2, spec + (size_t)(z - 1) * spec_stride, nm, W,
                                                         p->pixel_size_x, p->pixel_size_y, (double)shf, tpart);

@@ -67,6 +67,9 @@ struct Path {
     build_twiddles_kernel<W><<<1, 256, 0, st>>>(tw);
     prof_mark(st, KID_TABLES);
     tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);
+    if (q.per_step)
+      launch_step_props<W>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                           ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
     if (p->probe_shift) {
       prof_mark(st, KID_PROBE_FFT);
       probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, st>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
@@ -126,7 +129,8 @@ struct Path {
     fa.prop = ta.prop;
     fa.prop_edge = ta.prop_edge;
     fa.pyx = ta.pyx;
-    fa.use_sep = p->smooth_rolloff == 0.0f ? 1 : 0;
+    fa.use_sep = (p->smooth_rolloff == 0.0f && !q.per_step) ? 1 : 0;
+    fa.prop_steps = q.per_step ? at<float2>(ws, q.o_steps) : nullptr;
     fa.mask = ta.mask;
     fa.sx = ta.sx;
     fa.sy = ta.sy;

@@ -70,6 +70,9 @@ struct Path256 {
     build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
     prof_mark(st, KID_TABLES);
     tables_kernel<256><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);
+    if (q.per_step)
+      launch_step_props<256>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                             ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
     if (p->probe_shift) {
       prof_mark(st, KID_PROBE_FFT);
       if ((rc = launch4(probe_fft256_kernel, q.Mp, Smem256::small, st, probe, q.Mp, (const float2*)tw,
@@ -125,7 +128,8 @@ struct Path256 {
     fa.prop = ta.prop;
     fa.prop_edge = ta.prop_edge;
     fa.pyx = ta.pyx;
-    fa.use_sep = p->smooth_rolloff == 0.0f ? 1 : 0;
+    fa.use_sep = (p->smooth_rolloff == 0.0f && !q.per_step) ? 1 : 0;
+    fa.prop_steps = q.per_step ? at<float2>(ws, q.o_steps) : nullptr;
     fa.mask = ta.mask;
     fa.sx = ta.sx;
     fa.sy = ta.sy;

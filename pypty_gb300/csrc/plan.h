@@ -31,6 +31,8 @@ struct Plan {
   // in bytes
   int nbuf;
   size_t s_obl, s_gsum, s_fprobe, s_stack;
+  int per_step;   // one propagator table per slice step (slice_distances given, Z > 1)
+  size_t o_steps;
 };
 
 // twiddle tables in global memory: W = 256 windows use the 128 tables of their sub-transforms
@@ -49,6 +51,9 @@ inline int validate(const pty_problem_t* p) {
   if (p->step_pos && !p->probe_shift) return PTY_ERR_INVALID;
   if ((int64_t)p->obj_ny * p->obj_nx >= (int64_t)1 << 31) return PTY_ERR_UNSUPPORTED;
   if (p->checkpoint_every > 1 && p->window != 256) return PTY_ERR_UNSUPPORTED;
+  if (p->slice_distances)
+    for (int z = 0; z + 1 < p->n_slices; ++z)
+      if (!(p->slice_distances[z] == p->slice_distances[z])) return PTY_ERR_INVALID;   // NaN
   return PTY_OK;
 }
 
@@ -115,6 +120,8 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_pgr = take(w256 && q.Mo > 1 ? (size_t)q.Bb * q.Mp * WW * c8 : 0);
   q.o_seg = take(q.ckpt > 1 ? (size_t)q.Bb * q.ckpt * WW * c8 : 0);
   q.o_gpark = take(q.ckpt > 1 ? (size_t)q.Bb * WW * c8 : 0);
+  q.per_step = p->slice_distances && q.Z > 1;
+  q.o_steps = take(q.per_step ? (size_t)(q.Z - 1) * WW * c8 : 0);
   q.total = o;
   return q;
 }

@@ -49,6 +49,60 @@ __device__ __forceinline__ float fftfreq_f32(int k, int n, float d) {
   return (float)((double)kk * (double)val);
 }
 
+// One slice step's propagator for per-slice distances (multislice_core.py:69-74 with
+// is_single_dist false): exp(-i pi d (lambda q^2 + 2 (qx tan_x + qy tan_y))) * mask, the phase
+// rounded as tables_kernel rounds it, raised to edge_mult (principal branch, numpy's complex
+// ** float) when edge, scaled by 1/W^2 like prop   grid (W^2 / 256), block 256
+struct StepPropArgs {
+  const float* mask;
+  float px, py, wavelength, distance, tan_x, tan_y, edge_mult;
+  int edge;
+  float2* out;
+};
+
+template <int W>
+__global__ void step_prop_kernel(StepPropArgs a) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= W * W) return;
+  const int ky = idx / W, kx = idx % W;
+  const float qx = fftfreq_f32(kx, W, a.px);
+  const float qy = fftfreq_f32(ky, W, a.py);
+  const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, a.tan_x), __fmul_rn(qy, a.tan_y)));
+  const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
+  const float phase = __fmul_rn(__fmul_rn(-3.141592654f, a.distance), x);
+  const float mk = a.mask[idx];
+  float s, c;
+  sincosf(phase, &s, &c);
+  float2 p = make_float2(c * mk, s * mk);
+  if (a.edge) {
+    const float r = sqrtf(p.x * p.x + p.y * p.y);
+    float2 pe = make_float2(0.f, 0.f);
+    if (r > 0.f) {
+      const float ang = atan2f(p.y, p.x) * a.edge_mult;
+      const float re = powf(r, a.edge_mult);
+      float se, ce;
+      sincosf(ang, &se, &ce);
+      pe = make_float2(re * ce, re * se);
+    }
+    p = pe;
+  }
+  const float inv = 1.0f / (float)(W * W);
+  a.out[idx] = make_float2(p.x * inv, p.y * inv);
+}
+
+// the Z - 1 per-step tables of a problem with slice_distances (host), one launch per step
+template <int W>
+inline void launch_step_props(const float* mask, const float* distances_host, int nsteps, float px, float py,
+                              float wavelength, float edge_mult, int use_edge, float tan_x, float tan_y,
+                              float2* out, cudaStream_t st) {
+  for (int z = 0; z < nsteps; ++z) {
+    StepPropArgs sa{mask, px, py, wavelength, distances_host[z], tan_x, tan_y, edge_mult, (z == 0 && use_edge) ? 1 : 0,
+                    out + (size_t)z * W * W};
+    step_prop_kernel<W><<<(W * W + 255) / 256, 256, 0, st>>>(sa);
+  }
+}
+
 template <int W>
 __global__ void tables_kernel(TableArgs a) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -241,6 +295,8 @@ struct FusedArgs {
   const float2* prop_edge;
   const float2* pyx;        // separable propagator factors (used when the mask is binary)
   int use_sep;
+  const float2* prop_steps; // per-step tables [Z-1] (slice distances), step 0 with the edge
+                            // power; nullptr: prop / prop_edge for every step
   const float* mask;        // natural, unscaled
   const float* sx;
   const float* sy;
@@ -585,7 +641,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           v[i] = ((mbits >> i) & 1u) ? cmul(v[i], P) : make_float2(0.f, 0.f);
         }
       } else {
-        const float2* pr = (z == 0 && a.use_edge) ? a.prop_edge : a.prop;
+        const float2* pr = a.prop_steps ? a.prop_steps + (size_t)z * WW
+                                        : ((z == 0 && a.use_edge) ? a.prop_edge : a.prop);
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = cmul(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
       }
@@ -650,7 +707,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           v[i] = ((mbits >> i) & 1u) ? cmulc(v[i], P) : make_float2(0.f, 0.f);
         }
       } else {
-        const float2* pr = (z == 1 && a.use_edge) ? a.prop_edge : a.prop;
+        const float2* pr = a.prop_steps ? a.prop_steps + (size_t)(z - 1) * WW
+                                        : ((z == 1 && a.use_edge) ? a.prop_edge : a.prop);
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = cmulc(v[i], pr[G::fky(t, i) * W + G::fkx(t, i)]);
       }

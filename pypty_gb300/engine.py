@@ -40,7 +40,10 @@ def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, 
                  pixel_size_x, pixel_size_y, slice_distance, edge_mult=1.0,
                  damping_cutoff=2 / 3, smooth_rolloff=0.0, loss_weight=1.0, compute_batch=None,
                  step_obj=True, step_probe=True, step_pos=False, probe_shift=None,
-                 checkpoint_every=1) -> _lib.Problem:
+                 checkpoint_every=1, slice_distances=None) -> _lib.Problem:
+    """The C-ABI problem description. ``slice_distances``: the reference's ``this_distances``
+    when it has more than one entry (step z from slice z to z + 1 uses entry z,
+    ``multislice_core.py:69-74``); None or one entry: ``slice_distance`` for every step."""
     ny, nx, nz, mo = obj_shape
     if isinstance(algorithm, str):
         codes = dict(_lib.ALGORITHMS, **_lib.COMPRESSED_ALGORITHMS)
@@ -66,6 +69,15 @@ def make_problem(W, obj_shape, n_probe_modes, geometry: Geometry, *, algorithm, 
     p.slice_distance, p.edge_mult = slice_distance, edge_mult
     p.damping_cutoff, p.smooth_rolloff, p.loss_weight = damping_cutoff, smooth_rolloff, loss_weight
     p.checkpoint_every = int(checkpoint_every)
+    p.slice_distances = None
+    if slice_distances is not None:
+        d = np.asarray(slice_distances, dtype=np.float32).reshape(-1)
+        if d.shape[0] > 1 and nz > 1:
+            if d.shape[0] < nz - 1:   # the reference indexes this_distances[z] for z < Z - 1
+                raise ValueError("slice_distances needs n_slices - 1 = %d entries, got %d" % (nz - 1, d.shape[0]))
+            d = np.ascontiguousarray(d[:nz - 1])
+            p._slice_distances = d    # keeps the host array the struct points to alive
+            p.slice_distances = d.ctypes.data
     return p
 
 

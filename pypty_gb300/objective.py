@@ -5,7 +5,8 @@
 (``pypty/objective.py:967``). Installing it in place of the reference function
 (``pypty_gb300.shim.install``) lets ``pypty.iterative.run`` drive the GB300 kernels.
 
-Supported flag set: ``propmethod="multislice"``, one slice distance, algorithms ``lsq_sqrt``,
+Supported flag set: ``propmethod="multislice"``, one slice distance or one per slice step
+(``this_distances`` with more than one entry, ``multislice_core.py:69-74``), algorithms ``lsq_sqrt``,
 ``ml``, ``lsq``, ``lsq_sqrt_2`` on the fused path; with any of far-field or near-field
 propagation (one defocus, ``Cs``; ``pypty/objective.py:504-508``), the compressed-detector
 algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations and their
@@ -119,7 +120,12 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     _unsupported(tilts.ndim != 2 or tilts.shape[1] != 6 or tilts.shape[0] not in (1, n_pos),
                  "tilt arrays that are not one row or one row per position")
     tilted = tmode != 0 or bool(this_step_tilts) or not _is_zero(tilts)
-    _unsupported(np.asarray(_to_numpy(this_distances)).reshape(-1).shape[0] != 1, "per-slice distances")
+    dists = np.asarray(_to_numpy(this_distances), dtype=np.float32).reshape(-1)
+    n_slices = int(tuple(this_obj.shape)[2]) if len(tuple(this_obj.shape)) == 4 else 1
+    # more than one entry: step z uses entry z (multislice_core.py:69-74); the reference indexes
+    # past a shorter array
+    _unsupported(dists.shape[0] > 1 and dists.shape[0] < n_slices - 1,
+                 "this_distances with fewer than n_slices - 1 entries (the reference raises IndexError)")
     _unsupported(phase_plate_in_h5 is not None, "phase plates")
     _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
     near = recon_type == "near_field"
@@ -166,7 +172,7 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     problem = make_problem(
         W, obj_shape, Mp, geo, algorithm=algorithm_type, wavelength=float(this_wavelength),
         pixel_size_x=float(pixel_size_x_A), pixel_size_y=float(pixel_size_y_A),
-        slice_distance=float(np.asarray(_to_numpy(this_distances)).reshape(-1)[0]),
+        slice_distance=float(dists[0]), slice_distances=dists if dists.shape[0] > 1 else None,
         edge_mult=float(edge_slice_thickness_multiplier),
         damping_cutoff=None if damping_cutoff_multislice is None else float(damping_cutoff_multislice),
         smooth_rolloff=float(smooth_rolloff), loss_weight=float(this_loss_weight),

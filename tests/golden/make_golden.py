@@ -3,7 +3,7 @@
 Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
 /root/reference)::
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]   # every case and the core case without names
 
 For every case it builds seeded inputs (``pypty_gb300.synth``), simulates measured
 patterns with the oracle's forward model plus Poisson noise, evaluates the reference's
@@ -36,7 +36,8 @@ def ref_loss_and_direction(pypty, c, obj, probe):
         this_obj=obj.astype(cx), full_probe=probe.astype(cx),
         this_pos_array=c["positions"].copy(), this_pos_correction=c["pos_correction"].astype(f),
         this_tilt_array=tilts, this_tilts_correction=np.zeros_like(tilts),
-        this_distances=np.array([c["distance"]], dtype=f),
+        this_distances=(np.array([c["distance"]], dtype=f) if c.get("distances") is None
+                        else np.asarray(c["distances"], dtype=f)),
         edge_slice_thickness_multiplier=c["edge_mult"], measured_array=c["measured"],
         algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"],
@@ -68,7 +69,7 @@ def build_case(name, seed, W, ny, nx, Z, Mo, Mp, n_scan, step_px, jitter_px, alg
                batch, px=0.2, kV=200.0, alpha=25.0, defocus=80.0, distance=2.0,
                edge_mult=1.0, cutoff=2 / 3, rolloff=0.0, loss_weight=1, step_probe=1,
                step_obj=1, step_pos=0, dose=1e4, double=False, sequence=None,
-               integer_positions=False):
+               integer_positions=False, distances=None):
     rng = np.random.default_rng(seed)
     # inputs are always built in single precision; the double-precision cases upcast the
     # very same inputs so that complex64 and complex128 results are comparable
@@ -87,7 +88,8 @@ def build_case(name, seed, W, ny, nx, Z, Mo, Mp, n_scan, step_px, jitter_px, alg
     N = ipos.shape[0]
     seq = np.arange(N) if sequence is None else np.asarray(sequence)
     # measured: oracle forward at the truth, plus Poisson noise
-    sim = orc.loss_and_direction(truth, probe_true, ipos, corr, distance, edge_mult, None,
+    sim = orc.loss_and_direction(truth, probe_true, ipos, corr,
+                                 distance if distances is None else np.asarray(distances, f), edge_mult, None,
                                  algorithm, lam, 1, 1, 0, px, px, cutoff, rolloff,
                                  np.arange(N), 1, 64, float_dtype=f, complex_dtype=cx,
                                  simulate=True)
@@ -106,7 +108,7 @@ def build_case(name, seed, W, ny, nx, Z, Mo, Mp, n_scan, step_px, jitter_px, alg
                 algorithm=algorithm, wavelength=lam, step_probe=step_probe,
                 step_obj=step_obj, step_pos=step_pos, px=px, cutoff=cutoff,
                 rolloff=rolloff, sequence=seq, loss_weight=loss_weight, batch=batch,
-                obj=obj0, probe=probe0)
+                obj=obj0, probe=probe0, distances=None if distances is None else np.asarray(distances, f))
 
 
 CASES = [
@@ -136,13 +138,27 @@ CASES = [
     dict(name="w128_modes_c64", seed=5, W=128, ny=176, nx=176, Z=3, Mo=1, Mp=3, n_scan=3,
          step_px=12.0, jitter_px=2.0, algorithm="lsq_sqrt", batch=4, px=0.1, kV=300.0,
          alpha=30.0, defocus=50.0, dose=1e5),
+    # one distance per slice step (this_distances with Z - 1 entries, multislice_core.py:69-74,
+    # 164-174), with a thick first slice; 64 and 128 px windows, and an FP64 twin
+    dict(name="distances_ml_c64", seed=6, W=64, ny=112, nx=112, Z=4, Mo=1, Mp=2, n_scan=6,
+         step_px=6.0, jitter_px=1.5, algorithm="ml", batch=16, px=0.1, kV=300.0,
+         alpha=30.0, defocus=40.0, step_pos=1, dose=1e5, edge_mult=1.3, distances=[1.5, 2.5, 4.0]),
+    dict(name="distances_ml_c128", seed=6, W=64, ny=112, nx=112, Z=4, Mo=1, Mp=2, n_scan=6,
+         step_px=6.0, jitter_px=1.5, algorithm="ml", batch=16, px=0.1, kV=300.0,
+         alpha=30.0, defocus=40.0, step_pos=1, dose=1e5, edge_mult=1.3, distances=[1.5, 2.5, 4.0],
+         double=True),
+    dict(name="w128_distances_c64", seed=7, W=128, ny=176, nx=176, Z=3, Mo=1, Mp=3, n_scan=3,
+         step_px=12.0, jitter_px=2.0, algorithm="lsq_sqrt", batch=4, px=0.1, kV=300.0,
+         alpha=30.0, defocus=50.0, dose=1e5, distances=[1.0, 3.0]),
 ]
 
 
-def make_loss_cases(pypty):
+def make_loss_cases(pypty, names=None):
     for spec in CASES:
         spec = dict(spec)
         name = spec.pop("name")
+        if names and name not in names:
+            continue
         c = build_case(name, **spec)
         loss, sse, og, pg, posg = ref_loss_and_direction(pypty, c, c["obj"], c["probe"])
         out = os.path.join(HERE, name + ".npz")
@@ -156,7 +172,8 @@ def make_loss_cases(pypty):
                              dtype=np.float64),
             algorithm=np.array(c["algorithm"]), double=np.array(c["double"]),
             ref_loss=np.array(loss, dtype=np.float64), ref_sse=np.array(sse, dtype=np.float64),
-            ref_object_grad=og, ref_probe_grad=np.asarray(pg), ref_pos_grad=posg)
+            ref_object_grad=og, ref_probe_grad=np.asarray(pg), ref_pos_grad=posg,
+            **({} if c["distances"] is None else {"distances": c["distances"]}))
         print("%-20s loss=%.8e sse=%.6e |og|=%.4e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), out))
 
@@ -201,5 +218,7 @@ def make_core_case(pypty):
 
 if __name__ == "__main__":
     pypty = import_reference()
-    make_loss_cases(pypty)
-    make_core_case(pypty)
+    names = sys.argv[1:]
+    make_loss_cases(pypty, names)
+    if not names:
+        make_core_case(pypty)

@@ -43,7 +43,9 @@ def ref_call(pypty, c):
         this_obj=c["obj"].astype(cx), full_probe=c["probe"].astype(cx),
         this_pos_array=c["positions"].copy(), this_pos_correction=c["pos_correction"].astype(f),
         this_tilt_array=tilts, this_tilts_correction=np.zeros_like(tilts),
-        this_distances=np.array([c["distance"]], dtype=f), edge_slice_thickness_multiplier=c["edge_mult"],
+        this_distances=(np.array([c["distance"]], dtype=f) if c["distances"] is None
+                        else np.asarray(c["distances"], dtype=f)),
+        edge_slice_thickness_multiplier=c["edge_mult"],
         measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
         this_step_tilts=c["step_tilts"], masks=masks, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
@@ -88,7 +90,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
                n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
                mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0, upsample=1, static=0.0,
-               step_sb=0):
+               step_sb=0, distances=None):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
@@ -117,7 +119,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
               masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
               use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode, upsample_pattern=upsample,
               static_background=sb)
-    sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, distance, edge_mult, None, algorithm, lam,
+    dist = distance if distances is None else np.asarray(distances, f)
+    sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, dist, edge_mult, None, algorithm, lam,
                                           1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
     if n_masks:
         measured = (sim * (1.0 + 0.02 * rng.normal(size=sim.shape))).astype(f)
@@ -140,7 +143,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult,
                 tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts, upsample=upsample,
                 static_background=None if sb is None else (sb.astype(np.float64) if double else sb),
-                step_sb=step_sb)
+                step_sb=step_sb, distances=None if distances is None else np.asarray(distances, f))
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -209,6 +212,15 @@ CASES = [
          defocus=60.0, cs=2e5),
     dict(BASE, name="static_compressed_c64", seed=52, algorithm="lsq_compressed", n_masks=6, static=0.2,
          step_sb=1),
+    # one distance per slice step (multislice_core.py:69-74, 164-182): per-position inside tilts
+    # with their gradient and a thick first slice; tilts after the specimen, per position (each
+    # step's propagator then takes the position's own inside tilt); near field
+    dict(BASE, name="distances_tilt0_rows_c64", seed=53, algorithm="ml", Z=3, tilt_mode=0,
+         tilt_rows="per_position", step_tilts=1, edge_mult=1.2, distances=[1.5, 2.5], step_pos=1),
+    dict(BASE, name="distances_tilt1_rows_c64", seed=54, algorithm="lsq_sqrt", Z=3, tilt_mode=1,
+         tilt_rows="per_position", step_tilts=1, distances=[1.0, 3.0]),
+    dict(BASE, name="distances_near_c64", seed=55, algorithm="lsq_sqrt", Z=3, recon_type="near_field",
+         defocus=60.0, cs=2e5, tan_x=2e-3, distances=[1.2, 2.2], step_pos=1),
 ]
 
 
@@ -242,7 +254,7 @@ def main(names=None):
             ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg),
             tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg),
             static_background=none if c["static_background"] is None else c["static_background"],
-            ref_static_grad=np.asarray(sbg))
+            ref_static_grad=np.asarray(sbg), distances=none if c["distances"] is None else c["distances"])
         print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
             np.linalg.norm(np.asarray(abg)), os.path.basename(out)))

@@ -24,6 +24,7 @@ def load_case(name):
              loss_weight=float(s[6]), batch=int(s[7]), step_probe=int(s[8]),
              step_obj=int(s[9]), step_pos=int(s[10]), algorithm=str(d["algorithm"]),
              double=bool(d["double"]))
+    d.setdefault("distances", None)   # one distance per slice step, when the case has them
     return d
 
 
@@ -55,9 +56,9 @@ def load_variant_case(name):
     d["algorithm"] = str(d["algorithm"])
     d["recon_type"] = str(d["recon_type"])
     d["double"] = bool(d["double"])
-    for k in ("static_background", "ref_static_grad"):
+    for k in ("static_background", "ref_static_grad", "distances"):
         d.setdefault(k, np.zeros(0, np.float32))
-    for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts", "static_background"):
+    for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts", "static_background", "distances"):
         if d[k].size == 0:
             d[k] = None
     return d

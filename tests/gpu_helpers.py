@@ -17,7 +17,7 @@ def run_gpu(c, compute_batch=None, engine=None):
                         edge_mult=c["edge_mult"], damping_cutoff=float(np.float32(c["cutoff"])),
                         smooth_rolloff=float(np.float32(c["rolloff"])), loss_weight=c["loss_weight"],
                         compute_batch=compute_batch or c["batch"], step_obj=c["step_obj"],
-                        step_probe=c["step_probe"], step_pos=c["step_pos"])
+                        step_probe=c["step_probe"], step_pos=c["step_pos"], slice_distances=c.get("distances"))
     ls, og, pg, posg = eng.loss_and_direction(
         prob, torch.from_numpy(obj).to(dev), torch.from_numpy(probe).to(dev), geo,
         torch.from_numpy(np.ascontiguousarray(c["measured"]).astype(np.float32)).to(dev))

@@ -44,7 +44,7 @@ def run_layered(eng, c, dft, compute_batch=None):
                         edge_mult=c["edge_mult"], damping_cutoff=float(np.float32(c["cutoff"])),
                         smooth_rolloff=float(np.float32(c["rolloff"])), loss_weight=c["loss_weight"],
                         compute_batch=compute_batch or c["batch"], step_obj=c["step_obj"],
-                        step_probe=c["step_probe"], step_pos=c["step_pos"])
+                        step_probe=c["step_probe"], step_pos=c["step_pos"], slice_distances=c.get("distances"))
     ls, og, pg, posg = eng.loss_and_direction_layered(
         prob, torch.from_numpy(obj).cuda(), torch.from_numpy(probe).cuda(), geo,
         torch.from_numpy(np.ascontiguousarray(c["measured"]).astype(np.float32)).cuda(), engine=dft)

@@ -173,3 +173,25 @@ def test_simulated_patterns_do_not_depend_on_batching(engine):
                             edge_mult=c["edge_mult"], compute_batch=batch)
         outs.append(engine.simulate(prob, obj, probe, geo).cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_drop_in_objective_with_per_slice_distances():
+    """this_distances with one entry per slice step through the reference-signature mirror."""
+    from pypty_gb300 import objective
+    from test_host_logic import base_kwargs
+    c = load_case("distances_ml_c64")
+    f = np.float32
+    kw = base_kwargs(this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
+                     this_pos_correction=c["pos_correction"], this_distances=np.asarray(c["distances"], f),
+                     edge_slice_thickness_multiplier=c["edge_mult"], measured_array=c["measured"],
+                     algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
+                     this_step_probe=c["step_probe"], this_step_obj=c["step_obj"],
+                     this_step_pos_correction=c["step_pos"], pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+                     damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
+                     this_chopped_sequence=c["sequence"], this_loss_weight=c["loss_weight"],
+                     compute_batch=c["batch"])
+    res = objective.loss_and_direction(**kw)
+    assert abs(res[0] - float(c["ref_loss"])) <= LOSS_TOL * abs(float(c["ref_loss"]))
+    assert rel_l2(res[2], c["ref_object_grad"]) <= GRAD_TOL
+    assert rel_l2(res[3], c["ref_probe_grad"]) <= GRAD_TOL
+    assert rel_l2(res[4], c["ref_pos_grad"]) <= GRAD_TOL

@@ -25,7 +25,7 @@ def run_gpu_variant(c, engine=None):
                         edge_mult=c["edge_mult"], damping_cutoff=float(np.float32(c["cutoff"])),
                         smooth_rolloff=float(np.float32(c["rolloff"])), loss_weight=c["loss_weight"],
                         compute_batch=c["batch"], step_obj=c["step_obj"], step_probe=c["step_probe"],
-                        step_pos=c["step_pos"])
+                        step_pos=c["step_pos"], slice_distances=c.get("distances"))
     t = lambda a, dt=None: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
     ls, og, pg, posg, bcg, abg, tg, sbg = eng.loss_and_direction_variants(
         prob, t(obj), t(probe), geo, t(c["measured"], np.float32), recon_type=c["recon_type"],
@@ -48,7 +48,8 @@ def run_gpu_variant(c, engine=None):
 def fp64_variant_oracle(c):
     return vor.loss_and_direction_variants(
         np.asarray(c["obj"], np.complex128), np.asarray(c["probe"], np.complex128), c["positions"],
-        np.asarray(c["pos_correction"], np.float64), c["distance"], c["edge_mult"],
+        np.asarray(c["pos_correction"], np.float64),
+        c["distance"] if c["distances"] is None else np.asarray(c["distances"], np.float64), c["edge_mult"],
         np.asarray(c["measured"], np.float64), c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"],
         c["step_pos"], c["px"], c["px"], c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"],
         recon_type=c["recon_type"], defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
@@ -161,7 +162,7 @@ def test_variants_reject_bad_arguments():
 
 @pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64", "crop_c64",
                                   "shift_mult_c64", "tilt4_rows_c64", "tilt2_single_c64", "upsample2_pad_c64",
-                                  "static_compressed_c64"])
+                                  "static_compressed_c64", "distances_tilt0_rows_c64"])
 def test_reference_signature_call_routes_variants(name):
     """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
     variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
@@ -177,7 +178,9 @@ def test_reference_signature_call_routes_variants(name):
     kw = base_kwargs(
         this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
         this_pos_correction=c["pos_correction"], this_tilt_array=tilts, this_tilts_correction=np.zeros_like(tilts),
-        this_distances=np.array([c["distance"]], np.float32), edge_slice_thickness_multiplier=c["edge_mult"],
+        this_distances=(np.array([c["distance"]], np.float32) if c["distances"] is None
+                        else np.asarray(c["distances"], np.float32)),
+        edge_slice_thickness_multiplier=c["edge_mult"],
         measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=np.float32(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
         masks=c["masks"], pixel_size_x_A=np.float32(c["px"]), pixel_size_y_A=np.float32(c["px"]),

@@ -25,7 +25,7 @@ def test_window_fft_256_matches_numpy(inverse, shift):
     assert rel_l2(out, ref) <= 2e-6
 
 
-def _case(Z, Mp, Mo, alg, seed, n_scan=2, rolloff=0.0, edge=1.0):
+def _case(Z, Mp, Mo, alg, seed, n_scan=2, rolloff=0.0, edge=1.0, distances=None):
     from oracle import ptycho_oracle as orc
     from pypty_gb300 import synth
     rng = np.random.default_rng(seed)
@@ -36,15 +36,16 @@ def _case(Z, Mp, Mo, alg, seed, n_scan=2, rolloff=0.0, edge=1.0):
     ipos, corr = synth.split_positions(synth.raster_positions(n_scan, n_scan, 9.0, 2.0, rng))
     lam = synth.wavelength_A(kV)
     seq = np.arange(ipos.shape[0])
-    sim = orc.loss_and_direction(truth, probe, ipos, corr, 1.0, edge, None, alg, lam, 1, 1, 1, px, px, 2 / 3,
+    dist = 1.0 if distances is None else np.asarray(distances, np.float32)
+    sim = orc.loss_and_direction(truth, probe, ipos, corr, dist, edge, None, alg, lam, 1, 1, 1, px, px, 2 / 3,
                                  rolloff, seq, 1, 4, simulate=True)
     meas = synth.poisson_patterns(sim, 1.0, rng)
     obj0 = np.exp(0.6j * np.angle(truth)).astype(np.complex64)
     c = dict(obj=obj0, probe=probe, positions=ipos, pos_correction=corr, sequence=seq, measured=meas,
              algorithm=alg, wavelength=lam, px=px, cutoff=2 / 3, rolloff=rolloff, distance=1.0, edge_mult=edge,
-             loss_weight=1, batch=3, step_obj=1, step_probe=1, step_pos=1)
+             loss_weight=1, batch=3, step_obj=1, step_probe=1, step_pos=1, distances=distances)
     ref = orc.loss_and_direction(obj0.astype(np.complex128), probe.astype(np.complex128), ipos,
-                                 corr.astype(np.float64), 1.0, edge, meas.astype(np.float64), alg, lam, 1, 1, 1, px,
+                                 corr.astype(np.float64), dist, edge, meas.astype(np.float64), alg, lam, 1, 1, 1, px,
                                  px, 2 / 3, rolloff, seq, 1, 3, float_dtype=np.float64, complex_dtype=np.complex128)
     return c, ref
 
@@ -55,6 +56,19 @@ def test_w256_against_fp64_oracle(Z, Mp, Mo, alg, rolloff, edge):
     from gpu_helpers import run_gpu
     c, ref = _case(Z, Mp, Mo, alg, seed=Z * 10 + Mp, rolloff=rolloff, edge=edge)
     loss, sse, og, pg, posg = run_gpu(c)
+    assert abs(loss - ref[0]) <= 1e-5 * abs(ref[0])
+    assert rel_l2(og, ref[2]) <= 1e-4
+    assert rel_l2(pg, ref[3]) <= 1e-4
+    assert rel_l2(posg, ref[4]) <= 1e-4
+
+
+@pytest.mark.parametrize("ckpt", [1, 2])
+def test_w256_per_slice_distances_against_fp64_oracle(ckpt):
+    """One distance per slice step (the reference's this_distances with Z - 1 entries), with a
+    thick first slice, kept or recomputed in the adjoint."""
+    c, ref = _case(4, 2, 1, "lsq_sqrt", seed=77, edge=1.4, distances=[0.8, 1.6, 2.4])
+    ls, og, pg, posg = _run_with(c, checkpoint_every=ckpt, slice_distances=c["distances"])
+    loss = float(ls[0])
     assert abs(loss - ref[0]) <= 1e-5 * abs(ref[0])
     assert rel_l2(og, ref[2]) <= 1e-4
     assert rel_l2(pg, ref[3]) <= 1e-4

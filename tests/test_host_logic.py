@@ -42,7 +42,7 @@ def base_kwargs(**over):
     dict(recon_type="near_field", defocus_array=np.array([1.0, 2.0])), dict(propmethod="yoshida"),
     dict(algorithm_type="lsq_compressed"), dict(algorithm_type="huber"),
     dict(tilt_mode=7), dict(this_tilt_array=np.ones((3, 6), np.float32)),
-    dict(this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
+    dict(this_obj=np.ones((96, 96, 4, 1), np.complex64), this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
     dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
     dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_bin=2),
     dict(algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32), data_pad=4),
@@ -177,3 +177,14 @@ def test_upsampling_and_static_background_route_to_the_variants_path():
     assert v["static_background"].shape == (64, 64) and v["step_static_background"]
     _, _, v = objective.prepare(**base_kwargs(static_background=0))
     assert v is None
+
+
+def test_per_slice_distances_reach_the_problem():
+    """this_distances with one entry per slice step is passed to the C ABI (slice_distances);
+    one entry keeps the single-distance tables."""
+    obj = np.ones((96, 96, 4, 1), np.complex64)
+    p, _, v = objective.prepare(**base_kwargs(this_obj=obj, this_distances=np.array([1.0, 2.0, 3.0], np.float32)))
+    assert v is None and p.slice_distances
+    assert list(p._slice_distances) == [1.0, 2.0, 3.0] and p.slice_distance == 1.0
+    p, _, _ = objective.prepare(**base_kwargs(this_obj=obj, this_distances=np.array([2.0], np.float32)))
+    assert not p.slice_distances and p.slice_distance == 2.0

@@ -9,7 +9,8 @@ from oracle import ptycho_oracle as orc
 def run_oracle(c):
     f, cx = (np.float64, np.complex128) if c["double"] else (np.float32, np.complex64)
     return orc.loss_and_direction(
-        c["obj"], c["probe"], c["positions"], c["pos_correction"], c["distance"],
+        c["obj"], c["probe"], c["positions"], c["pos_correction"],
+        c["distance"] if c["distances"] is None else c["distances"],
         c["edge_mult"], c["measured"], c["algorithm"], c["wavelength"], c["step_probe"],
         c["step_obj"], c["step_pos"], c["px"], c["px"], c["cutoff"], c["rolloff"],
         c["sequence"], c["loss_weight"], c["batch"], float_dtype=f, complex_dtype=cx)

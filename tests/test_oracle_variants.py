@@ -11,7 +11,8 @@ from oracle import variants_oracle as vor
 def run_variant_oracle(c):
     f, cx = (np.float64, np.complex128) if c["double"] else (np.float32, np.complex64)
     return vor.loss_and_direction_variants(
-        c["obj"], c["probe"], c["positions"], c["pos_correction"], c["distance"], c["edge_mult"], c["measured"],
+        c["obj"], c["probe"], c["positions"], c["pos_correction"],
+        c["distance"] if c["distances"] is None else c["distances"], c["edge_mult"], c["measured"],
         c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"], c["step_pos"], c["px"], c["px"],
         c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"], recon_type=c["recon_type"],
         defocus=c["defocus"], cs=c["cs"], alpha_near_field=c["alpha"], tan_x=c["tan_x"], tan_y=c["tan_y"],
