@@ -300,6 +300,12 @@ typedef struct pty_variant {
   const float* static_background;
   int32_t step_static_background;
   float* static_background_grad;
+  /* near field: one defocus per position (device, n_positions entries; the reference's
+     defocus_array with more than one entry, is_single_defocus false, objective.py:413-418),
+     or NULL: `defocus` for every position. The reference's (B,) array broadcasts against its
+     (1, W, W) grids only for batches of one position; here every batch size applies each
+     position's own defocus. */
+  const float* defocus_per_position;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

@@ -10,7 +10,8 @@ Flag set (beyond ``ptycho_oracle``'s): the per-batch measured-data preprocessing
 ``objective.py:411-412`` (shift vector, multiplier, zero padding by ``data_pad`` with
 ``use_padded_intensity``, or the cropped model pattern without it, ``objective.py:516-517,
 592-593``); ``recon_type`` "far_field" or "near_field" with one
-defocus (``is_single_defocus``) and spherical aberration ``Cs`` (``objective.py:504-508,
+defocus or one per position (``is_single_defocus`` false, ``objective.py:413-418``) and
+spherical aberration ``Cs`` (``objective.py:504-508,
 598-604``); algorithms
 ``lsq_compressed``, ``gauss_compressed`` and ``poisson_compressed`` with detector masks
 (``objective.py:560-585``); ``beam_current`` with its gradient (``objective.py:448-452,
@@ -231,7 +232,12 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     if compressed and data_pad != 0:
         raise ValueError("data_pad with compressed detectors: the masks would need the cropped shape")
     if near:
-        dfc = f(defocus)
+        # defocus_array with one entry per position (is_single_defocus false): each batch takes
+        # its positions' entries (objective.py:413-418); the reference's (B,) array broadcasts
+        # against the (1, W, W) grids only for batches of one position
+        dfa = np.asarray(defocus, dtype=f).reshape(-1)
+        per_pos_defocus = dfa.shape[0] > 1
+        dfc = dfa[0]
         if alpha_near_field > 0:
             raise ValueError("near-field alpha_near_field > 0: the reference raises (objective.py:600)")
     runx, runy = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
@@ -303,6 +309,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                 exit_wave = ifft2(fft2(exit_wave, axes=(1, 2)) * mask[None, :, :, None, None], axes=(1, 2))
             exit_before_tilt = exit_wave
             exit_wave = exit_before_tilt * tmask_a
+        if near and per_pos_defocus:
+            dfc = dfa[tcs][:, None, None]                               # (B, 1, 1)
         if near:                                                        # objective.py:504-508
             ctf = (np.exp(-3.141592654j * (((lam * q2 + 2 * (qx * tx_i + qy * ty_i)) * dfc)
                                           + (0.5 * f(cs) * lam ** 3 * q2 ** 2))) * mask)[:, :, :, None, None]
@@ -356,8 +364,9 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                     gx = np.sum(np.imag(fwg[:, :, :, 0, 0] * qx * dfc), (1, 2))
                     gy = np.sum(np.imag(fwg[:, :, :, 0, 0] * qy * dfc), (1, 2))
                 else:
-                    gx = np.sum(np.imag(fwg * qx[None, :, :, None, None] * dfc), (1, 2, 3, 4))
-                    gy = np.sum(np.imag(fwg * qy[None, :, :, None, None] * dfc), (1, 2, 3, 4))
+                    d5 = dfc[:, :, :, None, None] if per_pos_defocus else dfc
+                    gx = np.sum(np.imag(fwg * qx[None, :, :, None, None] * d5), (1, 2, 3, 4))
+                    gy = np.sum(np.imag(fwg * qy[None, :, :, None, None] * d5), (1, 2, 3, 4))
                 if single_tilt:
                     gx, gy = np.sum(gx), np.sum(gy)
                 tilts_grad[tind, 2] += gy * rsc

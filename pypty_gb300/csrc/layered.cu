@@ -693,6 +693,7 @@ struct PropArgs {
   const float* mask;
   float distance, wavelength, px, py, edge_mult, defocus, cs;
   int W;
+  const float* defoci;   // per-position near-field defocus [N] (device), or nullptr: defocus
 };
 
 // propagator of the position's inside tilt (objective.py:482-484), or its edge power
@@ -724,7 +725,7 @@ __device__ __forceinline__ float2 tilted_prop(const PropArgs& a, const float* ro
 }
 
 // near-field CTF of the position's inside tilt (objective.py:505)
-__device__ __forceinline__ float2 tilted_ctf(const PropArgs& a, const float* row, int u) {
+__device__ __forceinline__ float2 tilted_ctf(const PropArgs& a, const float* row, int u, float defocus) {
   const int W = a.W, ky = u / W, kx = u % W;
   const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
   const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
@@ -732,7 +733,7 @@ __device__ __forceinline__ float2 tilted_ctf(const PropArgs& a, const float* row
   const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
   const float l3 = __fmul_rn(__fmul_rn(a.wavelength, a.wavelength), a.wavelength);
   const float sph = __fmul_rn(__fmul_rn(__fmul_rn(0.5f, a.cs), l3), __fmul_rn(q2, q2));
-  const float phase = __fmul_rn(-3.141592654f, __fadd_rn(__fmul_rn(x, a.defocus), sph));
+  const float phase = __fmul_rn(-3.141592654f, __fadd_rn(__fmul_rn(x, defocus), sph));
   const float mk = a.mask[u];
   float s, c;
   sincosf(phase, &s, &c);
@@ -746,7 +747,8 @@ __global__ void var_tilted_mul_kernel(float2* __restrict__ x, TiltArgs t, PropAr
   const int u = blockIdx.x * EB + threadIdx.x, k = blockIdx.y, b = blockIdx.z;
   const int WW = a.W * a.W;
   const float* row = tilt_row(t, b);
-  const float2 P = cscale(ctf ? tilted_ctf(a, row, u) : tilted_prop(a, row, u, edge != 0), scale);
+  const float df = a.defoci ? a.defoci[t.seq[b]] : a.defocus;
+  const float2 P = cscale(ctf ? tilted_ctf(a, row, u, df) : tilted_prop(a, row, u, edge != 0), scale);
   float2* q = x + ((size_t)b * nper + k) * WW + u;
   *q = conj ? cmulc(*q, P) : cmul(*q, P);
 }
@@ -811,9 +813,12 @@ __global__ void __launch_bounds__(1024) var_inside_tilt_kernel(const float2* __r
 // Im(FWG conj(FFT(exit)))   grid Bn, block 1024
 __global__ void __launch_bounds__(1024) var_near_tilt_kernel(const float2* __restrict__ FWG, const float2* __restrict__ FE,
                                                              int nm, int W, float px, float py, float defocus,
-                                                             double rsc, double* __restrict__ part) {
+                                                             const float* __restrict__ defoci,
+                                                             const int* __restrict__ seq, double rsc,
+                                                             double* __restrict__ part) {
   __shared__ double red[64];
   const int b = blockIdx.x, WW = W * W;
+  if (defoci) defocus = defoci[seq[b]];
   double gy = 0.0, gx = 0.0;
   for (int u = threadIdx.x; u < WW; u += blockDim.x) {
     float im = 0.0f;
@@ -1120,6 +1125,10 @@ struct Run {
         if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), v->tilts_host, (size_t)q.n_rows * 6 * sizeof(float),
                             cudaMemcpyHostToDevice, st) != cudaSuccess)
           return PTY_ERR_CUDA;
+      } else {   // one row holding the inside tilt, for the per-position CTF kernels
+        const float row[6] = {0.0f, 0.0f, v->tan_y, v->tan_x, 0.0f, 0.0f};
+        if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), row, sizeof(row), cudaMemcpyHostToDevice, st) != cudaSuccess)
+          return PTY_ERR_CUDA;
       }
       if (cudaMemsetAsync(at<double>(ws, q.o_tpart), 0, (size_t)q.nseq * 6 * sizeof(double), st) != cudaSuccess)
         return PTY_ERR_CUDA;
@@ -1191,6 +1200,7 @@ struct Run {
     pr.edge_mult = p->edge_mult;
     pr.defocus = v ? v->defocus : 0.0f;
     pr.cs = v ? v->cs : 0.0f;
+    pr.defoci = v ? v->defocus_per_position : nullptr;
     pr.W = W;
     const bool tilted_prop = v && q.pos_prop;
     float2* spec = at<float2>(ws, q.o_spec);
@@ -1449,7 +1459,7 @@ struct Run {
     float2* field = psi2;
     prof_mark(st, KID_FINALIZE);
     if (q.near) {   // wave = IFFT(FFT(exit) * CTF) (objective.py:506-508)
-      if (q.single_tilt)
+      if (q.single_tilt && !v->defocus_per_position)
         prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 0, 1.0f);
       else   // the position's inside tilt
         var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, 0, 1, 0, 1.0f);
@@ -1480,13 +1490,14 @@ struct Run {
     if (q.near) {   // dL/d(exit) = IFFT(loss_weight FFT(wave dL/dI) conj(CTF)) (objective.py:602-604)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
       prof_mark(st, KID_ELEMENTWISE);
-      if (q.single_tilt)
+      if (q.single_tilt && !v->defocus_per_position)
         prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(psi2, ctf, WW, 1, p->loss_weight);
       else
         var_tilted_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, tg, pr, nm, 0, 1, 1, p->loss_weight);
       if (q.inside_grad)   // near-field inside-tilt gradient (objective.py:605-619)
         var_near_tilt_kernel<<<Bn, 1024, 0, st>>>(psi2, at<float2>(ws, q.o_fexit), nm, W, p->pixel_size_x,
-                                                  p->pixel_size_y, v->defocus, -12.566370614359172 / (double)WW,
+                                                  p->pixel_size_y, v->defocus, v->defocus_per_position, seq_b,
+                                                  -12.566370614359172 / (double)WW,
                                                   at<double>(ws, q.o_tpart) + (size_t)i0 * 6);
     }
     return dft(psi2, psi, (long long)Bn * nm, 1);

@@ -198,6 +198,7 @@ class Engine:
                                     tilts=None, tilt_mode: int = 0, step_tilts: bool = False,
                                     upsample_pattern: int = 1, static_background: torch.Tensor | None = None,
                                     step_static_background: bool = False,
+                                    defocus_per_position: torch.Tensor | None = None,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
@@ -210,7 +211,8 @@ class Engine:
         reference's per-batch measured-data preprocessing, applied on the fly; upsample_pattern
         sums the model pattern over u x u blocks before the loss; static_background (W, W)
         float32 adds its square (band-limited) to every pattern, with step_static_background
-        its gradient is returned; tilts
+        its gradient is returned; defocus_per_position (n_positions,) float32: near-field
+        defocus of every position instead of ``defocus``; tilts
         (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
         one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
@@ -252,6 +254,9 @@ class Engine:
             if bc_d is not None and step_beam_current else None
         ab_grad = torch.zeros(tuple(ab_d.shape), dtype=torch.float32, device=self.device) \
             if ab_d is not None and step_aberrations else None
+        dfp_d = dev(defocus_per_position, torch.float32)
+        if dfp_d is not None and tuple(dfp_d.shape) != (problem.n_positions,):
+            raise ValueError("defocus_per_position must hold one defocus per position")
         sb_d = dev(static_background, torch.float32)
         if sb_d is not None and tuple(sb_d.shape) != (problem.window, problem.window):
             raise ValueError("static_background must be (W, W)")
@@ -289,7 +294,8 @@ class Engine:
                          upsample_pattern=up,
                          static_background=None if sb_d is None else sb_d.data_ptr(),
                          step_static_background=int(sb_grad is not None),
-                         static_background_grad=None if sb_grad is None else sb_grad.data_ptr())
+                         static_background_grad=None if sb_grad is None else sb_grad.data_ptr(),
+                         defocus_per_position=None if dfp_d is None else dfp_d.data_ptr())
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")

@@ -145,7 +145,8 @@ def _impl(ns, a):
     dev = eng.device
     if variant is not None:
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
-                      ("aberration_marker", torch.int32), ("static_background", torch.float32)):
+                      ("aberration_marker", torch.int32), ("static_background", torch.float32),
+                      ("defocus_per_position", torch.float32)):
             if variant[k] is not None:
                 variant[k] = _to_device(variant[k], dt, dev)
     st = _STATES.setdefault(id(ns), {"opt": None, "meas_src": None, "meas": None})

@@ -8,7 +8,7 @@
 Supported flag set: ``propmethod="multislice"``, one slice distance or one per slice step
 (``this_distances`` with more than one entry, ``multislice_core.py:69-74``), algorithms ``lsq_sqrt``,
 ``ml``, ``lsq``, ``lsq_sqrt_2`` on the fused path; with any of far-field or near-field
-propagation (one defocus, ``Cs``; ``pypty/objective.py:504-508``), the compressed-detector
+propagation (one defocus or one per position, ``Cs``; ``pypty/objective.py:413-418, 504-508``), the compressed-detector
 algorithms with ``masks`` (``objective.py:560-585``), beam-current fluctuations and their
 gradient, aberration arrays with markers and their gradient, or beam tilts (``tilt_mode``
 0-4, one tilt row or one per position, with the tilt gradient) on the variants path
@@ -129,8 +129,11 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     _unsupported(phase_plate_in_h5 is not None, "phase plates")
     _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
     near = recon_type == "near_field"
+    dfa = np.asarray(_to_numpy(defocus_array), dtype=np.float32).reshape(-1)
     if near:
-        _unsupported(np.asarray(_to_numpy(defocus_array)).reshape(-1).shape[0] != 1, "per-position defocus")
+        # one defocus per position (objective.py:413-418): indexed by position
+        _unsupported(dfa.shape[0] != 1 and dfa.shape[0] != n_pos,
+                     "defocus_array that is neither one value nor one per position")
         _unsupported(float(alpha_near_field) > 0, "alpha_near_field > 0 (the reference raises on it)")
     _unsupported(aberrations_array is not None and aberration_marker is None, "aberrations without markers")
     _unsupported(bool(this_step_aberrations_array) and aberrations_array is None, "aberration steps without arrays")
@@ -182,7 +185,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted \
             or up != 1 or has_bg:
         variant = dict(recon_type=recon_type,
-                       defocus=float(np.asarray(_to_numpy(defocus_array)).reshape(-1)[0]) if near else 0.0,
+                       defocus=float(dfa[0]) if near else 0.0,
+                       defocus_per_position=dfa if near and dfa.shape[0] > 1 else None,
                        cs=float(Cs) if near else 0.0, tilts=tilts, tilt_mode=tmode,
                        step_tilts=bool(this_step_tilts),
                        masks=None if not compressed else _to_numpy(masks),
@@ -241,7 +245,8 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     else:
         kw = dict(variant)
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
-                      ("aberration_marker", torch.int32), ("static_background", torch.float32)):
+                      ("aberration_marker", torch.int32), ("static_background", torch.float32),
+                      ("defocus_per_position", torch.float32)):
             if kw[k] is not None:
                 kw[k] = _device_tensor(kw[k], dt, dev)
         loss_sse, og, pg, posg, bcg, abg, tg, sbg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo,

@@ -49,7 +49,9 @@ def ref_call(pypty, c):
         measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
         this_step_tilts=c["step_tilts"], masks=masks, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
-        recon_type=c["recon_type"], Cs=f(c["cs"]), defocus_array=np.array([c["defocus"]], dtype=f),
+        recon_type=c["recon_type"], Cs=f(c["cs"]),
+        defocus_array=(np.array([c["defocus"]], dtype=f) if c["defocus_array"] is None
+                       else np.asarray(c["defocus_array"], dtype=f)),
         alpha_near_field=f(c["alpha"]), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
         propmethod="multislice", this_chopped_sequence=c["sequence"], load_one_by_one=False,
         data_multiplier=f(c["mult"]), data_pad=c["data_pad"], phase_plate_in_h5=None, this_loss_weight=c["loss_weight"],
@@ -90,7 +92,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
                n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
                mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0, upsample=1, static=0.0,
-               step_sb=0, distances=None):
+               step_sb=0, distances=None, defocus_rows=False):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
@@ -115,7 +117,9 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
         yy, xx = np.mgrid[:W, :W] - W / 2
         sb = (static * np.sqrt(dose / (W * W)) * (0.5 + np.exp(-(yy ** 2 + xx ** 2) / (0.1 * W * W)))
               * rng.uniform(0.8, 1.2, size=(W, W))).astype(f)
-    kw = dict(recon_type=recon_type, defocus=defocus, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
+    # one near-field defocus per position around the nominal one
+    dfa = (defocus + 15.0 * rng.normal(size=N)).astype(f) if defocus_rows else None
+    kw = dict(recon_type=recon_type, defocus=defocus if dfa is None else dfa, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
               masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
               use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode, upsample_pattern=upsample,
               static_background=sb)
@@ -143,7 +147,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 data_pad=data_pad, use_padded=use_padded, shift0=shift[0], shift1=shift[1], mult=mult,
                 tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts, upsample=upsample,
                 static_background=None if sb is None else (sb.astype(np.float64) if double else sb),
-                step_sb=step_sb, distances=None if distances is None else np.asarray(distances, f))
+                step_sb=step_sb, distances=None if distances is None else np.asarray(distances, f),
+                defocus_array=dfa)
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -221,6 +226,13 @@ CASES = [
          tilt_rows="per_position", step_tilts=1, distances=[1.0, 3.0]),
     dict(BASE, name="distances_near_c64", seed=55, algorithm="lsq_sqrt", Z=3, recon_type="near_field",
          defocus=60.0, cs=2e5, tan_x=2e-3, distances=[1.2, 2.2], step_pos=1),
+    # near field with one defocus per position (objective.py:413-418): batches of one position,
+    # the only size for which the reference's (B,) defocus broadcasts; with an inside tilt, and
+    # with per-position inside tilts and their gradient
+    dict(BASE, name="near_defocus_rows_c64", seed=56, algorithm="lsq_sqrt", recon_type="near_field", defocus=60.0,
+         cs=2e5, tan_x=2e-3, defocus_rows=True, batch=1, n_scan=4, step_pos=1),
+    dict(BASE, name="near_defocus_tilt0_c64", seed=57, algorithm="ml", recon_type="near_field", defocus=50.0,
+         cs=1e5, defocus_rows=True, batch=1, n_scan=4, tilt_mode=0, tilt_rows="per_position", step_tilts=1),
 ]
 
 
@@ -254,7 +266,8 @@ def main(names=None):
             ref_beam_current_grad=np.asarray(bcg), ref_aberrations_grad=np.asarray(abg),
             tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg),
             static_background=none if c["static_background"] is None else c["static_background"],
-            ref_static_grad=np.asarray(sbg), distances=none if c["distances"] is None else c["distances"])
+            ref_static_grad=np.asarray(sbg), distances=none if c["distances"] is None else c["distances"],
+            defocus_array=none if c["defocus_array"] is None else c["defocus_array"])
         print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
             np.linalg.norm(np.asarray(abg)), os.path.basename(out)))

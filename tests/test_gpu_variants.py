@@ -37,7 +37,8 @@ def run_gpu_variant(c, engine=None):
         data_shift_vector=(c.get("shift0", 0), c.get("shift1", 0)), data_multiplier=c.get("mult", 1.0),
         tilts=c.get("tilts"), tilt_mode=c.get("tilt_mode", 0), step_tilts=bool(c.get("step_tilts", 0)),
         upsample_pattern=c.get("upsample", 1), static_background=t(c.get("static_background"), np.float32),
-        step_static_background=bool(c.get("step_sb", 0)))
+        step_static_background=bool(c.get("step_sb", 0)),
+        defocus_per_position=t(c.get("defocus_array"), np.float32))
     torch.cuda.synchronize()
     ls = ls.cpu().numpy()
     cpu = lambda a: None if a is None else a.cpu().numpy()
@@ -52,7 +53,8 @@ def fp64_variant_oracle(c):
         c["distance"] if c["distances"] is None else np.asarray(c["distances"], np.float64), c["edge_mult"],
         np.asarray(c["measured"], np.float64), c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"],
         c["step_pos"], c["px"], c["px"], c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"],
-        recon_type=c["recon_type"], defocus=c["defocus"], cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
+        recon_type=c["recon_type"], defocus=c["defocus"] if c["defocus_array"] is None else c["defocus_array"],
+        cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
         masks=None if c["masks"] is None else np.asarray(c["masks"], np.float64),
         beam_current=c["beam_current"], step_beam_current=c["step_bc"], aberrations=c["aberrations"],
         aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], data_pad=c["data_pad"],
@@ -162,7 +164,7 @@ def test_variants_reject_bad_arguments():
 
 @pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64", "crop_c64",
                                   "shift_mult_c64", "tilt4_rows_c64", "tilt2_single_c64", "upsample2_pad_c64",
-                                  "static_compressed_c64", "distances_tilt0_rows_c64"])
+                                  "static_compressed_c64", "distances_tilt0_rows_c64", "near_defocus_tilt0_c64"])
 def test_reference_signature_call_routes_variants(name):
     """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
     variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
@@ -184,7 +186,9 @@ def test_reference_signature_call_routes_variants(name):
         measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=np.float32(c["wavelength"]),
         this_step_probe=c["step_probe"], this_step_obj=c["step_obj"], this_step_pos_correction=c["step_pos"],
         masks=c["masks"], pixel_size_x_A=np.float32(c["px"]), pixel_size_y_A=np.float32(c["px"]),
-        recon_type=c["recon_type"], Cs=np.float32(c["cs"]), defocus_array=np.array([c["defocus"]], np.float32),
+        recon_type=c["recon_type"], Cs=np.float32(c["cs"]),
+        defocus_array=(np.array([c["defocus"]], np.float32) if c["defocus_array"] is None
+                       else np.asarray(c["defocus_array"], np.float32)),
         damping_cutoff_multislice=np.float32(c["cutoff"]), smooth_rolloff=np.float32(c["rolloff"]),
         this_chopped_sequence=c["sequence"], this_loss_weight=c["loss_weight"], compute_batch=c["batch"],
         data_pad=c["data_pad"], use_padded_intensity=bool(c["use_padded"]),
@@ -277,3 +281,14 @@ def test_pinned_host_measured_is_read_in_place():
             assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
     with pytest.raises(ValueError):   # pageable host memory is not readable by the kernels
         eng.loss_and_direction(prob, obj, probe, geo, host.clone())
+
+
+def test_per_position_defocus_with_larger_batches():
+    """One near-field defocus per position: batches of eight positions (the reference's (B,)
+    defocus only broadcasts for one) against the FP64 oracle, which takes each position's own."""
+    c = dict(load_variant_case("near_defocus_rows_c64"), batch=8)
+    res = run_gpu_variant(c)
+    e = errors(res, fp64_variant_oracle(c))
+    print({k: "%.1e" % v for k, v in e.items()})
+    for k, v in e.items():
+        assert v <= (1e-5 if k == "loss" else 1e-4), (k, v)

@@ -39,7 +39,7 @@ def base_kwargs(**over):
 
 @pytest.mark.parametrize("over", [
     dict(recon_type="fresnel"), dict(recon_type="near_field", alpha_near_field=0.1),
-    dict(recon_type="near_field", defocus_array=np.array([1.0, 2.0])), dict(propmethod="yoshida"),
+    dict(recon_type="near_field", defocus_array=np.array([1.0, 2.0, 3.0])), dict(propmethod="yoshida"),
     dict(algorithm_type="lsq_compressed"), dict(algorithm_type="huber"),
     dict(tilt_mode=7), dict(this_tilt_array=np.ones((3, 6), np.float32)),
     dict(this_obj=np.ones((96, 96, 4, 1), np.complex64), this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
@@ -188,3 +188,10 @@ def test_per_slice_distances_reach_the_problem():
     assert list(p._slice_distances) == [1.0, 2.0, 3.0] and p.slice_distance == 1.0
     p, _, _ = objective.prepare(**base_kwargs(this_obj=obj, this_distances=np.array([2.0], np.float32)))
     assert not p.slice_distances and p.slice_distance == 2.0
+
+
+def test_per_position_defocus_routes_to_the_variants_path():
+    _, _, v = objective.prepare(**base_kwargs(recon_type="near_field", defocus_array=np.array([10.0, 20.0])))
+    assert v["defocus"] == 10.0 and list(v["defocus_per_position"]) == [10.0, 20.0]
+    _, _, v = objective.prepare(**base_kwargs(recon_type="near_field", defocus_array=np.array([10.0])))
+    assert v["defocus_per_position"] is None

@@ -15,7 +15,8 @@ def run_variant_oracle(c):
         c["distance"] if c["distances"] is None else c["distances"], c["edge_mult"], c["measured"],
         c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"], c["step_pos"], c["px"], c["px"],
         c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"], recon_type=c["recon_type"],
-        defocus=c["defocus"], cs=c["cs"], alpha_near_field=c["alpha"], tan_x=c["tan_x"], tan_y=c["tan_y"],
+        defocus=c["defocus"] if c["defocus_array"] is None else c["defocus_array"], cs=c["cs"],
+        alpha_near_field=c["alpha"], tan_x=c["tan_x"], tan_y=c["tan_y"],
         masks=c["masks"], beam_current=c["beam_current"], step_beam_current=c["step_bc"],
         aberrations=c["aberrations"], aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"],
         data_pad=c["data_pad"], use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]),
