@@ -306,6 +306,12 @@ typedef struct pty_variant {
      (1, W, W) grids only for batches of one position; here every batch size applies each
      position's own defocus. */
   const float* defocus_per_position;
+  /* several probe scenarios (pypty/objective.py:285, 355-356, 443-444, 700-701, 754-755):
+     n_probe_scenarios = S > 1 makes probe and probe_grad (W, W, Mp, S) arrays and gives every
+     position the scenario probe_marker[position] (device int32, n_positions entries in
+     [0, S); an entry outside that range reads scenario 0). 0 or 1: one probe. */
+  int32_t n_probe_scenarios;
+  const int32_t* probe_marker;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

@@ -164,8 +164,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                                 aberration_marker=None, step_aberrations=0, data_pad=0, use_padded_intensity=True,
                                 data_shift_vector=(0, 0), data_multiplier=1.0, tilts=None, tilt_mode=0,
                                 step_tilts=0, upsample_pattern=1, static_background=None,
-                                step_static_background=0, float_dtype=np.float32, complex_dtype=np.complex64,
-                                simulate=False):
+                                step_static_background=0, probe_marker=None, float_dtype=np.float32,
+                                complex_dtype=np.complex64, simulate=False):
     """Restatement of ``pypty/objective.py:47-967`` for the flag set in the module docstring.
 
     tilts: (N_tilts, 6) rows [tan_y, tan_x] before / inside / after the specimen (the
@@ -174,7 +174,10 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     (tan_x, tan_y). ``upsample_pattern`` sums the model pattern over blocks before the loss
     (``objective.py:523-524, 590-591``); ``static_background`` (W, W) adds its square, band
     limited, to every pattern (``objective.py:359-361, 525-526``) and
-    ``step_static_background`` accumulates its gradient (``objective.py:588-589``). Returns
+    ``step_static_background`` accumulates its gradient (``objective.py:588-589``). A 4D probe
+    (W, W, Mp, S) with ``probe_marker`` (one scenario index per position) gives every position
+    its scenario's probe and returns the (W, W, Mp, S) probe gradient (``objective.py:355-356,
+    443-444, 700-701, 754-755, 929-931``). Returns
     (loss, sse, object_grad, probe_grad, pos_grad, beam_current_grad, aberrations_grad,
     tilts_grad, static_background_grad); the beam-current, aberration and static-background
     gradients are 0 (zeros for a given background) when the feature is off (the reference's
@@ -242,7 +245,13 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
             raise ValueError("near-field alpha_near_field > 0: the reference raises (objective.py:600)")
     runx, runy = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
     object_grad = np.zeros_like(obj)
-    probe_grad = np.zeros((W, W, Mp), dtype=complex_dtype)
+    scen = probe_marker is not None and probe.ndim == 4                 # multiple_scenarios, objective.py:285
+    if scen:
+        probe_s = np.moveaxis(probe, 3, 0)                              # (S, W, W, Mp), objective.py:355-356
+        probe_marker = np.asarray(probe_marker)
+        probe_grad = np.zeros(probe_s.shape, dtype=complex_dtype)
+    else:
+        probe_grad = np.zeros((W, W, Mp), dtype=complex_dtype)
     pos_grad = np.zeros_like(pos_correction)
     tilts_grad = np.zeros_like(tilts)
     up = int(upsample_pattern)
@@ -271,7 +280,7 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
         mx = positions[tcs, 1][:, None, None] + runx[None]
         ob = obj[my, mx, :, :]                                          # objective.py:436-441
         ob = ifft2(fft2(ob, axes=(1, 2)) * mask[None, :, :, None, None], axes=(1, 2)).astype(complex_dtype)
-        this_probe = probe[None]                                        # objective.py:443-447
+        this_probe = probe_s[probe_marker[tcs]] if scen else probe[None]   # objective.py:443-447
         probe_f = None
         if fluct:                                                       # objective.py:448-452
             bc = np.abs(beam_current[tcs])
@@ -442,13 +451,19 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                         if step_probe:
                             pgrad = pgrad * bc[:, None, None, None]
                     if step_probe:
-                        probe_grad = probe_grad + np.sum(pgrad, 0)      # objective.py:703
+                        if scen:                                        # objective.py:700-701, 972-989
+                            np.add.at(probe_grad, probe_marker[tcs], pgrad)
+                        else:
+                            probe_grad = probe_grad + np.sum(pgrad, 0)  # objective.py:703
     if simulate:
         return np.concatenate(sim, 0)
     loss = loss * loss_weight                                           # objective.py:742
     if loss != loss:
         raise ValueError('A very specific bad thing. Loss is Nan.')
-    if step_probe:                                                      # objective.py:927-933
+    if step_probe and scen:                                             # objective.py:754-755, 927-933
+        probe_grad = np.moveaxis(probe_grad, 0, 3)
+        probe_grad = ifft2(fft2(probe_grad) * mask[:, :, None, None])
+    elif step_probe:                                                    # objective.py:927-933
         probe_grad = ifft2(fft2(probe_grad) * mask[:, :, None])
     return (loss, sse, object_grad, np.asarray(probe_grad).astype(complex_dtype), pos_grad, bc_grad, ab_grad,
             tilts_grad, sb_grad)

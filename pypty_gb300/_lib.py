@@ -69,7 +69,8 @@ class Variant(ctypes.Structure):
                 ("step_tilts", ctypes.c_int32), ("tilts_grad", ctypes.c_void_p),
                 ("upsample_pattern", ctypes.c_int32), ("static_background", ctypes.c_void_p),
                 ("step_static_background", ctypes.c_int32), ("static_background_grad", ctypes.c_void_p),
-                ("defocus_per_position", ctypes.c_void_p)]
+                ("defocus_per_position", ctypes.c_void_p), ("n_probe_scenarios", ctypes.c_int32),
+                ("probe_marker", ctypes.c_void_p)]
 
 
 class PtyError(RuntimeError):

@@ -199,6 +199,38 @@ __global__ void probe_total_kernel(const float2* __restrict__ partial, int nchun
   out[(size_t)p * WW + u] = cscale(s, mask[u]);
 }
 
+// (W, W, Mp, S) reference layout <-> S x Mp natural planes   grid (WW / EB, Mp, S)
+__global__ void probe_to_planes_s_kernel(const float2* __restrict__ ref, float2* __restrict__ planes, int Mp, int S,
+                                         int WW) {
+  const int u = blockIdx.x * EB + threadIdx.x, p = blockIdx.y, s = blockIdx.z;
+  planes[((size_t)s * Mp + p) * WW + u] = ref[((size_t)u * Mp + p) * S + s];
+}
+__global__ void planes_to_probe_s_kernel(const float2* __restrict__ planes, float2* __restrict__ ref, int Mp, int S,
+                                         int WW) {
+  const int u = blockIdx.x * EB + threadIdx.x, p = blockIdx.y, s = blockIdx.z;
+  ref[((size_t)u * Mp + p) * S + s] = planes[((size_t)s * Mp + p) * WW + u];
+}
+
+// per-scenario chunk sums of the batch's probe-gradient spectra: partial[c][s][p] (+)= the sum
+// over positions b of chunk c whose scenario is s (objective.py:700-701), in position order
+// grid (WW / 256, Mp * S, nchunk), block 256
+__global__ void probe_partial_s_kernel(const float2* __restrict__ fprobe, float2* __restrict__ partial, int Bn, int Mp,
+                                       int S, int WW, int chunk, int accumulate, const int* __restrict__ pmarker,
+                                       const int* __restrict__ seq) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int sp = blockIdx.y, c = blockIdx.z, s = sp / Mp, p = sp % Mp;
+  if (e >= WW) return;
+  float2 acc = make_float2(0.f, 0.f);
+  const int b1 = min(Bn, (c + 1) * chunk);
+  for (int b = c * chunk; b < b1; ++b) {
+    int m = pmarker[seq[b]];
+    if (m < 0 || m >= S) m = 0;
+    if (m == s) acc = cadd(acc, fprobe[((size_t)b * Mp + p) * WW + e]);
+  }
+  float2* dst = partial + ((size_t)c * S * Mp + sp) * WW + e;
+  *dst = accumulate ? cadd(*dst, acc) : acc;
+}
+
 // (W, W, Mp) reference layout <-> Mp natural planes   grid (WW / EB, Mp)
 __global__ void probe_to_planes_kernel(const float2* __restrict__ ref, float2* __restrict__ planes, int Mp, int WW) {
   const int u = blockIdx.x * EB + threadIdx.x, p = blockIdx.y;
@@ -314,7 +346,17 @@ struct VarProbeArgs {
   const int* marker;         // [N]
   const float2* pspec;       // [Bn][Mp][WW] per-position probe spectra the shift was applied to, or null (bc FFT(P))
   int W, Mp, shift, n_abs, n_sets;
+  const int* pmarker;        // probe scenario per position [N] (pf / planes hold S scenarios), or null
+  int S;
 };
+
+// offset of position gi's probe scenario in [S][Mp][WW] planes / spectra (objective.py:443-444);
+// a marker outside [0, S) reads scenario 0
+__device__ __forceinline__ size_t scenario_off(const VarProbeArgs& a, int gi) {
+  if (!a.pmarker) return 0;
+  const int m = a.pmarker[gi];
+  return (m >= 0 && m < a.S) ? (size_t)m * a.Mp * a.W * a.W : 0;
+}
 
 // aberration coefficients of position gi, or null (no plates, or a marker out of range)
 __device__ __forceinline__ const float* coefs_of(const VarProbeArgs& a, int gi) {
@@ -338,9 +380,10 @@ __global__ void var_probe_in_kernel(VarProbeArgs a, float2* __restrict__ out) {
     const float2 w = a.shift ? ramp(a.sx, a.sy, u / W, u % W, mk, a.corr[2 * gi], a.corr[2 * gi + 1])
                      : coef  ? plate_at(a.abasis, coef, a.n_abs, WW, u, mk)
                              : make_float2(mk, 0.0f);
-    v = cmul(a.bc ? cscale(a.pf[(size_t)p * WW + u], bc) : a.pf[(size_t)p * WW + u], w);
+    const float2* pf = a.pf + scenario_off(a, gi);
+    v = cmul(a.bc ? cscale(pf[(size_t)p * WW + u], bc) : pf[(size_t)p * WW + u], w);
   } else {
-    v = cscale(a.planes[(size_t)p * WW + u], bc);
+    v = cscale(a.planes[scenario_off(a, gi) + (size_t)p * WW + u], bc);
   }
   out[((size_t)b * a.Mp + p) * WW + u] = v;
 }
@@ -568,7 +611,7 @@ __global__ void __launch_bounds__(1024) var_probe_adj_kernel(float2* __restrict_
   const bool sh = a.shift && do_shift, bcr = a.bc && do_rest;
   const float dy = a.corr[2 * gi], dx = a.corr[2 * gi + 1];
   float2* f = F + ((size_t)b * a.Mp + p) * WW;
-  const float2* pf = a.pf + (size_t)p * WW;
+  const float2* pf = a.pf + scenario_off(a, gi) + (size_t)p * WW;
   double gy = 0.0, gx = 0.0, gb = 0.0;
   for (int u = threadIdx.x; u < WW; u += blockDim.x) {
     const int ky = u / W, kx = u % W;
@@ -901,6 +944,7 @@ struct LPlan {
   size_t o_loss_part, o_pos_part, o_dft, dft_bytes, total;
   int per_step;     // per-slice distances: one propagator table per step
   size_t o_steps;
+  int S;            // probe scenarios (1: one probe)
   // variants (pty_loss_and_direction_variants)
   int near, compressed, nmask, n_abs, n_sets, has_bc, step_static;
   size_t o_ctf, o_abasis, o_abidx, o_ibuf, o_coef, o_dco, o_bc_part, o_ab_part, o_sbg;
@@ -946,8 +990,9 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
   q.o_prop_edge = take(WWs * c8);
   q.o_sx = take((size_t)q.W * sizeof(float));
   q.o_sy = take((size_t)q.W * sizeof(float));
-  q.o_planes = take((size_t)q.Mp * WWs * c8);
-  q.o_pf = take((size_t)q.Mp * WWs * c8);
+  q.S = (v && v->n_probe_scenarios > 1) ? v->n_probe_scenarios : 1;
+  q.o_planes = take((size_t)q.S * q.Mp * WWs * c8);
+  q.o_pf = take((size_t)q.S * q.Mp * WWs * c8);
   q.o_obj = take((size_t)q.zm * q.Ny * q.Nx * c8);
   q.o_grad = take((size_t)q.zm * q.Ny * q.Nx * c8);
   const size_t nobw = (size_t)q.Bb * q.zm, nwave = (size_t)q.Bb * q.Mp * q.Mo;
@@ -957,9 +1002,11 @@ inline LPlan make_lplan(const pty_problem_t* p, int engine, const pty_variant_t*
   q.o_stack = take((size_t)q.Z * nwave * WWs * c8);
   q.o_psi = take(nwave * WWs * c8);
   q.o_psi2 = take(nwave * WWs * c8);
-  q.o_pb = take((size_t)q.Bb * q.Mp * WWs * c8);
-  q.o_pbs = take((size_t)q.Bb * q.Mp * WWs * c8);
-  q.o_partial = take((size_t)q.nchunk * q.Mp * WWs * c8);
+  // pb / pbs also carry the S x Mp probe-gradient planes at the end
+  const size_t npb = (size_t)(q.Bb > q.S ? q.Bb : q.S) * q.Mp;
+  q.o_pb = take(npb * WWs * c8);
+  q.o_pbs = take(npb * WWs * c8);
+  q.o_partial = take((size_t)q.nchunk * q.S * q.Mp * WWs * c8);
   q.o_lists = take((size_t)q.ntiles * q.Bb * sizeof(int));
   q.o_counts = take((size_t)q.ntiles * sizeof(int));
   q.o_loss_part = take((size_t)q.nseq * 2 * sizeof(double));
@@ -1158,8 +1205,9 @@ struct Run {
     float2* planes = at<float2>(ws, q.o_planes);
     float2* pf = at<float2>(ws, q.o_pf);
     prof_mark(st, KID_LAYOUT);
-    probe_to_planes_kernel<<<grid(q.Mp, 1), EB, 0, st>>>(probe, planes, q.Mp, WW);
-    if ((rc = dft(planes, pf, q.Mp, 0))) return rc;
+    probe_to_planes_s_kernel<<<dim3((unsigned)(WW / EB), (unsigned)q.Mp, (unsigned)q.S), EB, 0, st>>>(
+        probe, planes, q.Mp, q.S, WW);
+    if ((rc = dft(planes, pf, (long long)q.S * q.Mp, 0))) return rc;
     const int nyx = q.Ny * q.Nx;
     prof_mark(st, KID_OBJ_TO_SLICES);
     obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(obj, at<float2>(ws, q.o_obj), nyx, q.zm);
@@ -1185,7 +1233,9 @@ struct Run {
     pa.shift = shift ? 1 : 0;
     pa.n_abs = q.n_abs;
     pa.n_sets = q.n_sets;
-    const bool var_probe = v && (shift || pa.bc || pa.coefs || q.before);
+    pa.pmarker = q.S > 1 ? v->probe_marker : nullptr;
+    pa.S = q.S;
+    const bool var_probe = v && (shift || pa.bc || pa.coefs || q.before || q.S > 1);
     TiltArgs tg{};
     tg.rows = at<float>(ws, q.o_tilts);
     tg.grid = at<float>(ws, q.o_tgrid);
@@ -1407,18 +1457,24 @@ struct Run {
         if (p->step_probe) {
           const int nch = (Bn + q.chunk - 1) / q.chunk;
           prof_mark(st, KID_PROBE_PARTIAL);
-          probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, st>>>(
-              pb, at<float2>(ws, q.o_partial), Bn, q.Mp, WW, q.chunk, ib > 0 ? 1 : 0);
+          if (q.S > 1)
+            probe_partial_s_kernel<<<dim3((unsigned)((WW + 255) / 256), (unsigned)(q.Mp * q.S), nch), 256, 0, st>>>(
+                pb, at<float2>(ws, q.o_partial), Bn, q.Mp, q.S, WW, q.chunk, ib > 0 ? 1 : 0, pa.pmarker, seq_b);
+          else
+            probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, st>>>(
+                pb, at<float2>(ws, q.o_partial), Bn, q.Mp, WW, q.chunk, ib > 0 ? 1 : 0);
         }
       }
     }
     // probe gradient: IFFT(mask * sum_b spectra) (objective.py:703, 927-933)
     if (p->step_probe) {
       prof_mark(st, KID_PROBE_FINAL);
-      probe_total_kernel<<<grid(q.Mp, 1), EB, 0, st>>>(at<float2>(ws, q.o_partial), q.nchunk, q.Mp, ta.mask, pbs, WW);
-      if ((rc = dft(pbs, pb, q.Mp, 1))) return rc;
+      probe_total_kernel<<<grid(q.Mp * q.S, 1), EB, 0, st>>>(at<float2>(ws, q.o_partial), q.nchunk, q.Mp * q.S,
+                                                             ta.mask, pbs, WW);
+      if ((rc = dft(pbs, pb, (long long)q.Mp * q.S, 1))) return rc;
       prof_mark(st, KID_LAYOUT);
-      planes_to_probe_kernel<<<grid(q.Mp, 1), EB, 0, st>>>(pb, probe_grad, q.Mp, WW);
+      planes_to_probe_s_kernel<<<dim3((unsigned)(WW / EB), (unsigned)q.Mp, (unsigned)q.S), EB, 0, st>>>(
+          pb, probe_grad, q.Mp, q.S, WW);
     }
     if (p->step_obj) {
       prof_mark(st, KID_SLICES_TO_OBJ);
@@ -1591,6 +1647,7 @@ int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
   // broadcast without a crop and without upsampling)
   if (v->static_background && (S != p->window || up > 1)) return PTY_ERR_UNSUPPORTED;
   if (v->static_background && v->step_static_background && !v->static_background_grad) return PTY_ERR_INVALID;
+  if (v->n_probe_scenarios < 0 || (v->n_probe_scenarios > 1 && !v->probe_marker)) return PTY_ERR_INVALID;
   return PTY_OK;
 }
 

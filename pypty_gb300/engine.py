@@ -199,6 +199,7 @@ class Engine:
                                     upsample_pattern: int = 1, static_background: torch.Tensor | None = None,
                                     step_static_background: bool = False,
                                     defocus_per_position: torch.Tensor | None = None,
+                                    probe_marker: torch.Tensor | None = None,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
@@ -212,7 +213,9 @@ class Engine:
         sums the model pattern over u x u blocks before the loss; static_background (W, W)
         float32 adds its square (band-limited) to every pattern, with step_static_background
         its gradient is returned; defocus_per_position (n_positions,) float32: near-field
-        defocus of every position instead of ``defocus``; tilts
+        defocus of every position instead of ``defocus``; probe_marker (n_positions,) int with a
+        4D probe (W, W, Mp, S): every position's probe scenario (the probe gradient is then
+        (W, W, Mp, S) too); tilts
         (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
         one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
@@ -221,7 +224,8 @@ class Engine:
         None, tilts_grad or None, static_background_grad or None)."""
         stream = stream or torch.cuda.current_stream(self.device)
         compressed = problem.algorithm in _lib.COMPRESSED_ALGORITHMS.values()
-        self._check_inputs(problem, obj, probe, None)
+        n_scen = int(probe.shape[3]) if probe_marker is not None and probe.dim() == 4 else 1
+        self._check_inputs(problem, obj, probe, None, n_scen)
         up = max(int(upsample_pattern), 1)
         side = problem.window if use_padded_intensity else problem.window - 2 * int(data_pad)
         wm = side // up - 2 * (int(data_pad) // up if use_padded_intensity else 0)
@@ -254,6 +258,12 @@ class Engine:
             if bc_d is not None and step_beam_current else None
         ab_grad = torch.zeros(tuple(ab_d.shape), dtype=torch.float32, device=self.device) \
             if ab_d is not None and step_aberrations else None
+        pm_d = None
+        if n_scen > 1:
+            pm = np.asarray(probe_marker.cpu() if torch.is_tensor(probe_marker) else probe_marker)
+            if pm.shape != (problem.n_positions,) or pm.min() < 0 or pm.max() >= n_scen:
+                raise ValueError("probe_marker must hold one scenario index in [0, %d) per position" % n_scen)
+            pm_d = dev(probe_marker, torch.int32)
         dfp_d = dev(defocus_per_position, torch.float32)
         if dfp_d is not None and tuple(dfp_d.shape) != (problem.n_positions,):
             raise ValueError("defocus_per_position must hold one defocus per position")
@@ -295,7 +305,8 @@ class Engine:
                          static_background=None if sb_d is None else sb_d.data_ptr(),
                          step_static_background=int(sb_grad is not None),
                          static_background_grad=None if sb_grad is None else sb_grad.data_ptr(),
-                         defocus_per_position=None if dfp_d is None else dfp_d.data_ptr())
+                         defocus_per_position=None if dfp_d is None else dfp_d.data_ptr(),
+                         n_probe_scenarios=n_scen, probe_marker=None if pm_d is None else pm_d.data_ptr())
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")
@@ -406,12 +417,16 @@ class Engine:
         return out
 
     @staticmethod
-    def _check_inputs(problem, obj, probe, measured):
+    def _check_inputs(problem, obj, probe, measured, scenarios=1):
         W = problem.window
         want_obj = (problem.obj_ny, problem.obj_nx, problem.n_slices, problem.n_obj_modes)
         if tuple(obj.shape) != want_obj or obj.dtype != torch.complex64 or not obj.is_contiguous():
             raise ValueError("object must be a contiguous complex64 tensor of shape %s" % (want_obj,))
-        if tuple(probe.shape) != (W, W, problem.n_probe_modes) or probe.dtype != torch.complex64 \
+        if scenarios > 1:
+            want = (W, W, problem.n_probe_modes, scenarios)
+            if tuple(probe.shape) != want or probe.dtype != torch.complex64 or not probe.is_contiguous():
+                raise ValueError("probe must be a contiguous complex64 tensor of shape %s" % (want,))
+        elif tuple(probe.shape) != (W, W, problem.n_probe_modes) or probe.dtype != torch.complex64 \
                 or not probe.is_contiguous():
             raise ValueError("probe must be a contiguous complex64 tensor of shape %s" %
                              ((W, W, problem.n_probe_modes),))

@@ -115,7 +115,8 @@ def _impl(ns, a):
                  "Gaussian object filters")
     _unsupported(update_pos and bool(a["dynamically_resize_yx_object"]), "dynamically_resize_yx_object")
     _unsupported(update_pos and bool(a["pos_puzzling"]), "pos_puzzling")
-    _unsupported(len(tuple(ns.probe.shape)) != 3, "multiple probe scenarios")
+    _unsupported(len(tuple(ns.probe.shape)) == 4 and a["probe_marker"] is None,
+                 "a 4D probe without probe_marker")
     probe_reg_weight = a["probe_reg_weight"]
     aperture = None
     if probe_reg_weight == np.inf:             # iterative.py:483-490
@@ -146,7 +147,7 @@ def _impl(ns, a):
     if variant is not None:
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
                       ("aberration_marker", torch.int32), ("static_background", torch.float32),
-                      ("defocus_per_position", torch.float32)):
+                      ("defocus_per_position", torch.float32), ("probe_marker", torch.int32)):
             if variant[k] is not None:
                 variant[k] = _to_device(variant[k], dt, dev)
     st = _STATES.setdefault(id(ns), {"opt": None, "meas_src": None, "meas": None})

@@ -14,7 +14,8 @@ gradient, aberration arrays with markers and their gradient, or beam tilts (``ti
 0-4, one tilt row or one per position, with the tilt gradient) on the variants path
 (``pty_loss_and_direction_variants``), which also takes the detector upsampling
 (``upsample_pattern``, ``objective.py:523-524, 590-591``) and a 2D static background with
-its gradient (``objective.py:359-361, 525-526, 588-589``). No phase plates, probe markers,
+its gradient (``objective.py:359-361, 525-526, 588-589``), and several probe scenarios (a 4D
+probe with ``probe_marker``, ``objective.py:355-356, 443-444, 700-701``). No phase plates,
 data binning (the reference raises on it), near-field ``alpha_near_field`` (the reference
 raises on it) or regularisers. The per-batch measured-data preprocessing
 (``data_pad`` with or without ``use_padded_intensity``, ``data_shift_vector``,
@@ -127,7 +128,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     _unsupported(dists.shape[0] > 1 and dists.shape[0] < n_slices - 1,
                  "this_distances with fewer than n_slices - 1 entries (the reference raises IndexError)")
     _unsupported(phase_plate_in_h5 is not None, "phase plates")
-    _unsupported(probe_marker is not None, "multiple probe scenarios (probe_marker)")
+    # a 4D probe with probe_marker: one probe per scenario (multiple_scenarios, objective.py:285)
+    scen = probe_marker is not None and len(tuple(full_probe.shape)) == 4
     near = recon_type == "near_field"
     dfa = np.asarray(_to_numpy(defocus_array), dtype=np.float32).reshape(-1)
     if near:
@@ -166,7 +168,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         _unsupported(bool(this_step_probe) and w != 0, name)
     obj_shape = tuple(this_obj.shape)
     _unsupported(len(obj_shape) != 4, "objects that are not 4D (y, x, slice, mode)")
-    _unsupported(len(tuple(full_probe.shape)) != 3, "probes that are not 3D (y, x, mode)")
+    _unsupported(len(tuple(full_probe.shape)) != (4 if scen else 3),
+                 "probes that are not 3D (y, x, mode), or 4D (y, x, mode, scenario) with probe_marker")
     _unsupported(mixed_variance_weight != 0 and obj_shape[3] > 1, "mixed_variance_weight")
     W = int(full_probe.shape[0])
     Mp = int(full_probe.shape[2])
@@ -183,7 +186,7 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         step_pos=bool(this_step_pos_correction))
     variant = None
     if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted \
-            or up != 1 or has_bg:
+            or up != 1 or has_bg or scen:
         variant = dict(recon_type=recon_type,
                        defocus=float(dfa[0]) if near else 0.0,
                        defocus_per_position=dfa if near and dfa.shape[0] > 1 else None,
@@ -201,7 +204,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                        data_multiplier=1.0 if compressed else float(data_multiplier),
                        upsample_pattern=up,
                        static_background=_to_numpy(static_background) if has_bg else None,
-                       step_static_background=bool(this_step_static_background) and has_bg)
+                       step_static_background=bool(this_step_static_background) and has_bg,
+                       probe_marker=_to_numpy(probe_marker) if scen else None)
     return problem, geo, variant
 
 
@@ -246,7 +250,7 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         kw = dict(variant)
         for k, dt in (("masks", torch.float32), ("beam_current", torch.float32), ("aberrations", torch.float32),
                       ("aberration_marker", torch.int32), ("static_background", torch.float32),
-                      ("defocus_per_position", torch.float32)):
+                      ("defocus_per_position", torch.float32), ("probe_marker", torch.int32)):
             if kw[k] is not None:
                 kw[k] = _device_tensor(kw[k], dt, dev)
         loss_sse, og, pg, posg, bcg, abg, tg, sbg = eng.loss_and_direction_variants(problem, obj_d, probe_d, geo,

@@ -97,8 +97,21 @@ def _clean_tables(eng: Engine, ny, nx, cutoff, rolloff, mask):
 
 def orthogonalize_modes_(probe: torch.Tensor, engine: Engine | None = None) -> torch.Tensor:
     """Gram-Schmidt over the last axis of a (W, W, Mp) complex64 CUDA probe, in place
-    (``pypty/objective.py:1119-1141``)."""
+    (``pypty/objective.py:1119-1141``). A (W, W, Mp, S) probe of S scenarios is treated as the
+    reference treats it: its first S modes, each spanning every pixel of every scenario, are
+    orthogonalised (``n_states`` is the last axis, the modes are indexed on the third)."""
     eng = engine or default_engine(probe.device)
+    if probe.dim() == 4:
+        mp, ns = int(probe.shape[2]), int(probe.shape[3])
+        if ns > mp:   # the reference indexes mode ns - 1 of mp modes
+            raise IndexError("index %d is out of bounds for axis 2 with size %d" % (mp, mp))
+        x = probe.permute(0, 1, 3, 2).contiguous()          # (W, W, S, Mp): modes innermost
+        sub = x[..., :ns].contiguous()
+        _lib.check(_lib.lib().pty_orthogonalize_modes(sub.data_ptr(), sub.numel() // ns, ns, _stream(eng)),
+                   "pty_orthogonalize_modes")
+        x[..., :ns] = sub
+        probe.copy_(x.permute(0, 1, 3, 2))
+        return probe
     mp = int(probe.shape[-1])
     _lib.check(_lib.lib().pty_orthogonalize_modes(probe.data_ptr(), probe.numel() // mp, mp, _stream(eng)),
                "pty_orthogonalize_modes")

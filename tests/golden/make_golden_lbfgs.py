@@ -3,7 +3,7 @@
 Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
 /root/reference)::
 
-    python tests/golden/make_golden_lbfgs.py [clean lbfgs refine static]   # all without names
+    python tests/golden/make_golden_lbfgs.py [clean lbfgs refine static scenarios]   # all without names
 
 * ``fourier_clean_c64.npz``: ``pypty.utils.fourier_clean`` (``pypty/utils.py:102``) on 2D,
   3D and 4D complex64 arrays with and without a cosine roll-off and with a given mask.
@@ -14,6 +14,8 @@ Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
 * ``lbfgs_refine_tilts_aberr_current.npz`` / ``lbfgs_refine_static_background.npz``: the same
   with tilt corrections, aberration arrays and beam currents, or the static background,
   refined together with the object and probe.
+* ``lbfgs_refine_probe_scenarios.npz``: two probe scenarios (a 4D probe with probe_marker),
+  modes kept orthogonal.
 """
 import os
 import sys
@@ -26,6 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 from refimport import import_reference  # noqa: E402
+from pypty_gb300 import synth  # noqa: E402
 from make_golden import build_case  # noqa: E402
 
 
@@ -293,9 +296,81 @@ def make_static_case(pypty):
     print("static %s -> %s" % (" ".join("%.5g/%d" % (s[0], s[3]) for s in rec["scalars"]), path))
 
 
+def make_scenario_case(pypty):
+    """Two probe scenarios (a 4D probe with probe_marker) with two modes each, kept orthogonal
+    (keep_probe_states_orthogonal, objective.py:1119-1141 as bfgs_update calls it): three
+    bfgs_update calls of the reference, object and probe after every call."""
+    it = pypty.iterative
+    f, cx = np.float32, np.complex64
+    c = build_case("scenarios", seed=38, W=64, ny=128, nx=128, Z=2, Mo=1, Mp=2, n_scan=5, step_px=8.0,
+                   jitter_px=1.0, algorithm="ml", batch=10, px=0.15, kV=300.0, alpha=30.0, defocus=40.0,
+                   distance=2.0, dose=1e5)
+    W = c["probe"].shape[0]
+    probe2 = synth.make_probe(W, 0.15, 300.0, 30.0, 70.0, 2, [0.5, 0.3], 1e5, dtype=cx)
+    probe4 = np.stack([c["probe"], probe2], -1)                     # (W, W, Mp, S)
+    N = c["positions"].shape[0]
+    marker = (np.arange(N) % 2).astype(np.int64)
+    it.obj, it.probe = c["obj"].copy(), probe4.copy()
+    it.positions = c["positions"].copy()
+    it.positions_correction = c["pos_correction"].astype(f).copy()
+    it.tilts = np.zeros((1, 6), f)
+    it.tilts_correction = np.zeros((1, 6), f)
+    it.static_background = None
+    it.aberrations_array, it.beam_current = None, None
+    it.reset_bfgs_history()
+    np.random.seed(7)
+    rec = dict(scalars=[], obj=[], probe=[])
+    warnings, failed = "", 0
+    step = 1.0
+    for epoch in range(3):
+        res = it.bfgs_update(
+            algorithm_type=c["algorithm"], this_slice_distances=np.array([c["distance"]], dtype=f),
+            edge_slice_thickness_multiplier=c["edge_mult"], this_step_probe=1, this_step_obj=1,
+            this_step_pos_correction=0, this_step_tilts=0, measured_array=c["measured"],
+            this_wavelength=f(c["wavelength"]), masks=None, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+            phase_norm_weight=0, abs_norm_weight=0, stepsize_threshold_low=1e-20, probe_reg_weight=0,
+            aperture_mask=None, recon_type="far_field", defocus_array=np.array([0.0], dtype=f), Cs=f(0),
+            alpha_near_field=f(0), damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(0),
+            update_extra_cut=f(0.005), keep_probe_states_orthogonal=True, do_charge_flip=False, cf_delta_phase=0,
+            cf_delta_abs=0, cf_beta_phase=0, cf_beta_abs=0, phase_only_obj=False, wedge_mu=0, beta_wedge=0,
+            wolfe_c1_constant=0.1, wolfe_c2_constant=0.9, atv_weight=0, atv_q=1, atv_p=2,
+            tune_only_probe_phase=False, propmethod="multislice", this_chopped_sequence=c["sequence"],
+            load_one_by_one=False, data_multiplier=f(1), data_pad=0, phase_plate_in_h5=None, print_flag=0,
+            this_loss_weight=c["loss_weight"], max_count=20, reduce_factor=f(0.1), optimism=3,
+            mixed_variance_weight=0, mixed_variance_sigma=0.5, data_bin=1, data_shift_vector=[0, 0],
+            smart_memory=False, default_float=f, default_complex=cx, default_int=np.int32, upsample_pattern=1,
+            this_step_static_background=0, tilt_mode=0, fancy_sigma=None, tune_only_probe_abs=False,
+            aberration_marker=None, this_step_aberrations_array=0, probe_marker=marker,
+            compute_batch=c["batch"], current_window=None, current_window_weight=0,
+            dynamically_resize_yx_object=False, lazy_clean=False, current_gaussian_filter=False,
+            current_apply_gaussian_filter_amplitude=False, this_beam_current_step=0, xp=np,
+            remove_fft_cache=False, is_first_epoch=epoch == 0, hist_length=10, actual_step=step,
+            fast_axis_reg_weight_positions=0, fast_axis_reg_weight_tilts=0, slow_axis_reg_weight_positions=0,
+            slow_axis_reg_weight_tilts=0, scan_size=None, scan_step_A=1,
+            current_deformation_reg_weight_positions=0, current_deformation_reg_weight_tilts=0,
+            warnings=warnings, data_simulation_flag=False, data_simulation_exitwave=False, pos_puzzling=False,
+            probe_mod_reg_weight=0, probe_mod_tol=0.05, use_padded_intensity=True, counter_failed_epochs=failed)
+        total_loss, sse, _cc, actual_step, count, d_value, new_d_value, warnings, failed = res
+        step = actual_step
+        rec["scalars"].append([float(total_loss), float(sse), float(actual_step), float(count), float(d_value),
+                               float(new_d_value), float(failed)])
+        rec["obj"].append(np.asarray(it.obj).copy())
+        rec["probe"].append(np.asarray(it.probe).copy())
+    path = os.path.join(HERE, "lbfgs_refine_probe_scenarios.npz")
+    np.savez_compressed(
+        path, obj=c["obj"], probe=probe4, positions=c["positions"], pos_correction=c["pos_correction"],
+        measured=c["measured"], sequence=c["sequence"], probe_marker=marker,
+        scalars=np.array([c["distance"], c["edge_mult"], c["wavelength"], c["px"], c["cutoff"], c["rolloff"],
+                          c["loss_weight"], c["batch"]], dtype=np.float64),
+        algorithm=np.array(c["algorithm"]), ref_scalars=np.array(rec["scalars"]), ref_obj=np.stack(rec["obj"]),
+        ref_probe=np.stack(rec["probe"]))
+    print("scenarios %s -> %s" % (" ".join("%.5g/%d" % (s[0], s[3]) for s in rec["scalars"]), path))
+
+
 if __name__ == "__main__":
     pypty = import_reference()
     from pypty import iterative  # noqa: F401
-    makers = dict(clean=make_clean_case, lbfgs=make_lbfgs_cases, refine=make_refine_case, static=make_static_case)
+    makers = dict(clean=make_clean_case, lbfgs=make_lbfgs_cases, refine=make_refine_case, static=make_static_case,
+                  scenarios=make_scenario_case)
     for name in sys.argv[1:] or list(makers):
         makers[name](pypty)

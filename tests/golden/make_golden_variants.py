@@ -58,7 +58,8 @@ def ref_call(pypty, c):
         data_bin=1, data_shift_vector=[c["shift0"], c["shift1"]], upsample_pattern=c["upsample"],
         static_background=None if c["static_background"] is None else c["static_background"].astype(f),
         this_step_static_background=c["step_sb"],
-        tilt_mode=c["tilt_mode"], aberration_marker=c["aberration_marker"], probe_marker=None, aberrations_array=ab,
+        tilt_mode=c["tilt_mode"], aberration_marker=c["aberration_marker"], probe_marker=c["probe_marker"],
+        aberrations_array=ab,
         compute_batch=c["batch"], phase_only_obj=False, beam_current=bc,
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], default_float=f,
         default_complex=cx, xp=np, is_first_epoch=True, scan_size=None, scan_step_A=1,
@@ -92,11 +93,15 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                defocus=0.0, cs=0.0, alpha_nf=0.0, tan_x=0.0, tan_y=0.0, n_masks=0, beam_current=False, step_bc=0,
                n_ab_sets=0, n_abs=0, step_ab=0, integer_positions=False, data_pad=0, use_padded=1, shift=(0, 0),
                mult=1.0, tilt_mode=0, tilt_rows=0, tilt_scale=5e-4, step_tilts=0, upsample=1, static=0.0,
-               step_sb=0, distances=None, defocus_rows=False):
+               step_sb=0, distances=None, defocus_rows=False, scenarios=0):
     rng = np.random.default_rng(seed)
     cx, f = np.complex64, np.float32
     truth = synth.gaussian_phase_object(ny, nx, Z, 12 * Z + 20, 0.35, px, 0.2, 0.9, rng, dtype=cx)
     probe_true = synth.make_probe(W, px, kV, alpha, probe_defocus, Mp, [0.6, 0.3, 0.1][:Mp], dose, dtype=cx)
+    pmarker = None
+    if scenarios:   # one probe per scenario (defocus steps of 20 A), positions assigned round robin
+        probe_true = np.stack([synth.make_probe(W, px, kV, alpha, probe_defocus + 20.0 * k, Mp,
+                                                [0.6, 0.3, 0.1][:Mp], dose, dtype=cx) for k in range(scenarios)], -1)
     pos = synth.raster_positions(n_scan, n_scan, step_px, jitter_px, rng)
     if integer_positions:
         pos = np.round(pos)
@@ -104,6 +109,8 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
     assert ipos.max() + W <= min(ny, nx), "object too small for the scan"
     lam = synth.wavelength_A(kV)
     N = ipos.shape[0]
+    if scenarios:
+        pmarker = (np.arange(N) % scenarios).astype(np.int64)
     masks = detector_masks(W, n_masks, rng) if n_masks else None
     bc = (1.0 + 0.1 * rng.normal(size=N)).astype(f) if beam_current else None
     ab = (rng.normal(size=(n_ab_sets, n_abs)) * 20.0).astype(f) if n_ab_sets else None
@@ -122,7 +129,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
     kw = dict(recon_type=recon_type, defocus=defocus if dfa is None else dfa, cs=cs, alpha_near_field=alpha_nf, tan_x=tan_x, tan_y=tan_y,
               masks=masks, beam_current=bc, aberrations=ab, aberration_marker=marker, data_pad=data_pad,
               use_padded_intensity=use_padded, tilts=tilts, tilt_mode=tilt_mode, upsample_pattern=upsample,
-              static_background=sb)
+              static_background=sb, probe_marker=pmarker)
     dist = distance if distances is None else np.asarray(distances, f)
     sim = vor.loss_and_direction_variants(truth, probe_true, ipos, corr, dist, edge_mult, None, algorithm, lam,
                                           1, 1, 0, px, px, cutoff, rolloff, np.arange(N), 1, 64, simulate=True, **kw)
@@ -135,6 +142,9 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
         measured = (np.roll(measured, (-shift[0], -shift[1]), axis=(1, 2)) / mult).astype(f)
     obj0 = np.exp(0.5j * np.angle(truth)).astype(cx)
     probe0 = synth.make_probe(W, px, kV, alpha, probe_defocus + 15.0, Mp, [0.5, 0.3, 0.2][:Mp], dose, dtype=cx)
+    if scenarios:
+        probe0 = np.stack([synth.make_probe(W, px, kV, alpha, probe_defocus + 15.0 + 20.0 * k, Mp,
+                                            [0.5, 0.3, 0.2][:Mp], dose, dtype=cx) for k in range(scenarios)], -1)
     if double:
         measured, corr = measured.astype(np.float64), corr.astype(np.float64)
         obj0, probe0 = obj0.astype(np.complex128), probe0.astype(np.complex128)
@@ -148,7 +158,7 @@ def build_case(name, seed, W, ny, nx, Z, Mp, n_scan, step_px, jitter_px, algorit
                 tilts=tilts, tilt_mode=tilt_mode, step_tilts=step_tilts, upsample=upsample,
                 static_background=None if sb is None else (sb.astype(np.float64) if double else sb),
                 step_sb=step_sb, distances=None if distances is None else np.asarray(distances, f),
-                defocus_array=dfa)
+                defocus_array=dfa, probe_marker=pmarker)
 
 
 BASE = dict(W=64, ny=112, nx=112, Z=2, Mp=2, n_scan=5, step_px=8.0, jitter_px=1.2, batch=10, px=0.15, kV=300.0,
@@ -233,6 +243,15 @@ CASES = [
          cs=2e5, tan_x=2e-3, defocus_rows=True, batch=1, n_scan=4, step_pos=1),
     dict(BASE, name="near_defocus_tilt0_c64", seed=57, algorithm="ml", recon_type="near_field", defocus=50.0,
          cs=1e5, defocus_rows=True, batch=1, n_scan=4, tilt_mode=0, tilt_rows="per_position", step_tilts=1),
+    # several probe scenarios (a 4D probe with probe_marker, objective.py:355-356, 443-444,
+    # 700-701): sub-pixel shifts with the position gradient, and its FP64 twin; with beam
+    # current and aberration plates; with a tilt before the specimen
+    dict(BASE, name="scenarios_c64", seed=58, algorithm="ml", scenarios=3, step_pos=1),
+    dict(BASE, name="scenarios_c128", seed=58, algorithm="ml", scenarios=3, step_pos=1, double=True),
+    dict(BASE, name="scenarios_current_aberr_c64", seed=59, algorithm="lsq_sqrt", scenarios=2, beam_current=True,
+         step_bc=1, n_ab_sets=2, n_abs=4, step_ab=1, step_pos=1),
+    dict(BASE, name="scenarios_tilt4_c64", seed=60, algorithm="lsq_sqrt", scenarios=2, tilt_mode=4,
+         tilt_rows="per_position", step_tilts=1, step_pos=1),
 ]
 
 
@@ -267,7 +286,8 @@ def main(names=None):
             tilts=none if c["tilts"] is None else c["tilts"], ref_tilts_grad=np.asarray(tg),
             static_background=none if c["static_background"] is None else c["static_background"],
             ref_static_grad=np.asarray(sbg), distances=none if c["distances"] is None else c["distances"],
-            defocus_array=none if c["defocus_array"] is None else c["defocus_array"])
+            defocus_array=none if c["defocus_array"] is None else c["defocus_array"],
+            probe_marker=np.zeros(0, np.int64) if c["probe_marker"] is None else c["probe_marker"])
         print("%-26s loss=%.8e sse=%.6e |og|=%.4e |bcg|=%.3e |abg|=%.3e -> %s" % (
             name, float(loss), float(sse), np.linalg.norm(og), np.linalg.norm(np.asarray(bcg)),
             np.linalg.norm(np.asarray(abg)), os.path.basename(out)))

@@ -56,10 +56,10 @@ def load_variant_case(name):
     d["algorithm"] = str(d["algorithm"])
     d["recon_type"] = str(d["recon_type"])
     d["double"] = bool(d["double"])
-    for k in ("static_background", "ref_static_grad", "distances", "defocus_array"):
+    for k in ("static_background", "ref_static_grad", "distances", "defocus_array", "probe_marker"):
         d.setdefault(k, np.zeros(0, np.float32))
     for k in ("masks", "beam_current", "aberrations", "aberration_marker", "tilts", "static_background", "distances",
-              "defocus_array"):
+              "defocus_array", "probe_marker"):
         if d[k].size == 0:
             d[k] = None
     return d

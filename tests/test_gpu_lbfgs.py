@@ -333,6 +333,36 @@ def test_bfgs_update_refines_the_static_background():
         assert isinstance(ns.static_background, np.ndarray) and ns.static_background.dtype == np.float32
 
 
+def test_bfgs_update_with_probe_scenarios():
+    """Two probe scenarios (a 4D probe with probe_marker) whose modes are kept orthogonal:
+    the same trial counts and steps as the reference's bfgs_update, object and 4D probe after
+    every call (tests/golden/make_golden_lbfgs.py make_scenario_case)."""
+    from pypty_gb300 import iterative
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lbfgs_refine_probe_scenarios.npz")))
+    s = d["scalars"]
+    c = dict(d, distance=float(s[0]), edge_mult=float(s[1]), wavelength=float(s[2]), px=float(s[3]),
+             cutoff=float(s[4]), rolloff=0.0, loss_weight=float(s[6]), batch=int(s[7]), algorithm=str(d["algorithm"]),
+             step_probe=1, step_obj=1, step_pos=0, orthogonal=True, lazy_clean=False, hist_length=10)
+    ns = types.SimpleNamespace(obj=c["obj"].copy(), probe=c["probe"].copy(), positions=c["positions"].copy(),
+                               positions_correction=c["pos_correction"].astype(np.float32).copy(),
+                               tilts=np.zeros((1, 6), np.float32), tilts_correction=np.zeros((1, 6), np.float32),
+                               static_background=None, aberrations_array=None, beam_current=None, history_bfgs=None)
+    fn = iterative.bind(ns)
+    np.random.seed(7)
+    warnings, failed = "", 0
+    step = 1.0
+    for e, ref in enumerate(c["ref_scalars"]):
+        res = _call_with(fn, c, e, warnings, failed, dict(probe_marker=c["probe_marker"], actual_step=step))
+        total_loss, sse, _cc, step, count, dv, ndv, warnings, failed = res
+        print(e, count, step, total_loss, "ref", ref[3], ref[2], ref[0])
+        assert int(count) == int(ref[3]), (e, count, ref)
+        assert float(step) == pytest.approx(float(ref[2]), rel=1e-5)
+        assert float(total_loss) == pytest.approx(float(ref[0]), rel=1e-4)
+        assert rel_l2(ns.obj, c["ref_obj"][e]) <= 1e-3
+        assert ns.probe.shape == c["probe"].shape
+        assert rel_l2(ns.probe, c["ref_probe"][e]) <= 1e-3
+
+
 def _call_with(fn, c, epoch, warnings, failed, over):
     """_call with some arguments replaced (the refinement flags of the variants path)."""
     captured = {}

@@ -38,7 +38,8 @@ def run_gpu_variant(c, engine=None):
         tilts=c.get("tilts"), tilt_mode=c.get("tilt_mode", 0), step_tilts=bool(c.get("step_tilts", 0)),
         upsample_pattern=c.get("upsample", 1), static_background=t(c.get("static_background"), np.float32),
         step_static_background=bool(c.get("step_sb", 0)),
-        defocus_per_position=t(c.get("defocus_array"), np.float32))
+        defocus_per_position=t(c.get("defocus_array"), np.float32),
+        probe_marker=t(c.get("probe_marker"), np.int32))
     torch.cuda.synchronize()
     ls = ls.cpu().numpy()
     cpu = lambda a: None if a is None else a.cpu().numpy()
@@ -60,8 +61,8 @@ def fp64_variant_oracle(c):
         aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], data_pad=c["data_pad"],
         use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]), data_multiplier=c["mult"],
         tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"], upsample_pattern=c["upsample"],
-        static_background=c["static_background"], step_static_background=c["step_sb"], float_dtype=np.float64,
-        complex_dtype=np.complex128)
+        static_background=c["static_background"], step_static_background=c["step_sb"],
+        probe_marker=c["probe_marker"], float_dtype=np.float64, complex_dtype=np.complex128)
 
 
 def errors(res, ref):
@@ -164,7 +165,8 @@ def test_variants_reject_bad_arguments():
 
 @pytest.mark.parametrize("name", ["near_c64", "lsq_compressed_c64", "current_aberr_shift_c64", "crop_c64",
                                   "shift_mult_c64", "tilt4_rows_c64", "tilt2_single_c64", "upsample2_pad_c64",
-                                  "static_compressed_c64", "distances_tilt0_rows_c64", "near_defocus_tilt0_c64"])
+                                  "static_compressed_c64", "distances_tilt0_rows_c64", "near_defocus_tilt0_c64",
+                                  "scenarios_current_aberr_c64"])
 def test_reference_signature_call_routes_variants(name):
     """The drop-in ``loss_and_direction`` (reference signature, objective.py:47) with the
     variant arguments set returns the reference's 10-tuple: gradients of the aberrations at
@@ -196,7 +198,7 @@ def test_reference_signature_call_routes_variants(name):
         aberration_marker=c["aberration_marker"], aberrations_array=c["aberrations"], beam_current=c["beam_current"],
         this_beam_current_step=c["step_bc"], this_step_aberrations_array=c["step_ab"], tilt_mode=c["tilt_mode"],
         this_step_tilts=c["step_tilts"], upsample_pattern=c["upsample"], static_background=c["static_background"],
-        this_step_static_background=c["step_sb"])
+        this_step_static_background=c["step_sb"], probe_marker=c["probe_marker"])
     out = objective.loss_and_direction(**kw)
     assert len(out) == 10
     lt, gt = TOL.get(c["algorithm"], (1e-5, 1e-4))

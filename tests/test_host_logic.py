@@ -43,7 +43,7 @@ def base_kwargs(**over):
     dict(algorithm_type="lsq_compressed"), dict(algorithm_type="huber"),
     dict(tilt_mode=7), dict(this_tilt_array=np.ones((3, 6), np.float32)),
     dict(this_obj=np.ones((96, 96, 4, 1), np.complex64), this_distances=np.array([1.0, 2.0])), dict(phase_plate_in_h5="x.h5"),
-    dict(probe_marker=np.zeros(2, int)), dict(this_beam_current_step=1),
+    dict(full_probe=np.ones((64, 64, 1, 2), np.complex64)), dict(this_beam_current_step=1),
     dict(aberrations_array=np.zeros((1, 3), np.float32)), dict(data_bin=2),
     dict(algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32), data_pad=4),
     dict(upsample_pattern=2, algorithm_type="lsq_compressed", masks=np.ones((2, 64, 64), np.float32)),
@@ -195,3 +195,13 @@ def test_per_position_defocus_routes_to_the_variants_path():
     assert v["defocus"] == 10.0 and list(v["defocus_per_position"]) == [10.0, 20.0]
     _, _, v = objective.prepare(**base_kwargs(recon_type="near_field", defocus_array=np.array([10.0])))
     assert v["defocus_per_position"] is None
+
+
+def test_probe_scenarios_route_to_the_variants_path():
+    """A 4D probe with probe_marker selects the variants path; a marker with a 3D probe is
+    ignored, as the reference ignores it (multiple_scenarios needs both, objective.py:285)."""
+    probe = np.ones((64, 64, 1, 3), np.complex64)
+    _, _, v = objective.prepare(**base_kwargs(full_probe=probe, probe_marker=np.array([0, 2])))
+    assert list(v["probe_marker"]) == [0, 2]
+    _, _, v = objective.prepare(**base_kwargs(probe_marker=np.array([0, 1])))
+    assert v is None

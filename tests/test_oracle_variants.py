@@ -22,7 +22,7 @@ def run_variant_oracle(c):
         data_pad=c["data_pad"], use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]),
         data_multiplier=f(c["mult"]), tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"],
         upsample_pattern=c["upsample"], static_background=c["static_background"],
-        step_static_background=c["step_sb"], float_dtype=f, complex_dtype=cx)
+        step_static_background=c["step_sb"], probe_marker=c["probe_marker"], float_dtype=f, complex_dtype=cx)
 
 
 @pytest.mark.parametrize("name", variant_case_names())
