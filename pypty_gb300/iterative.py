@@ -108,6 +108,7 @@ def _impl(ns, a):
     _unsupported(update_ab and getattr(ns, "aberrations_array", None) is None, "aberration refinement without arrays")
     _unsupported(update_bc and getattr(ns, "beam_current", None) is None, "beam-current refinement without currents")
     _unsupported(bool(a["phase_only_obj"]), "phase_only_obj")
+    _unsupported(bool(a["data_simulation_flag"]), "data_simulation_flag inside bfgs_update")
     _unsupported(bool(a["tune_only_probe_phase"]) or bool(a["tune_only_probe_abs"]),
                  "tune_only_probe_phase / tune_only_probe_abs")
     _unsupported(update_obj and bool(a["do_charge_flip"]), "do_charge_flip")

@@ -155,7 +155,9 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                  "a static background with upsampling or a cropped pattern (the reference's shapes do not broadcast)")
     _unsupported(compressed and int(data_pad) != 0, "data_pad with compressed detectors")
     prep = not compressed and (int(data_pad) != 0 or not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0)
-    _unsupported(bool(data_simulation_flag), "data simulation output files")
+    # data_simulation_flag: the model patterns are also saved to that file (objective.py:286-293,
+    # 518-522, 744-749); the exit-wave variant and the variants path are not built
+    _unsupported(bool(data_simulation_flag) and bool(data_simulation_exitwave), "data_simulation_exitwave")
     for name, w in [("fast_axis_reg_weight_positions", fast_axis_reg_weight_positions),
                     ("slow_axis_reg_weight_positions", slow_axis_reg_weight_positions),
                     ("current_deformation_reg_weight_positions", current_deformation_reg_weight_positions)]:
@@ -268,6 +270,15 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         if aberrations_array is not None:
             ab_grad = np.zeros_like(_to_numpy(aberrations_array)) if abg is None else \
                 abg.cpu().numpy().astype(_to_numpy(aberrations_array).dtype, copy=False)
+    if data_simulation_flag:
+        _unsupported(variant is not None, "data_simulation_flag with the variants path's flags")
+        # sim_patterns[tcs] = this_pattern over every batch, then np.save (objective.py:518-522,
+        # 744-749): float64, indexed by the sequence's position entries
+        pat = eng.simulate(problem, obj_d, probe_d, geo).cpu().numpy()
+        seq = np.asarray(_to_numpy(this_chopped_sequence))
+        sim = np.zeros((seq.shape[0],) + pat.shape[1:], dtype=np.float64)
+        sim[seq] = pat
+        np.save(data_simulation_flag, sim)
     ls = loss_sse.cpu().numpy()
     loss, sse = float(ls[0]), float(ls[1])
     if loss != loss:

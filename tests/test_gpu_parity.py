@@ -195,3 +195,33 @@ def test_drop_in_objective_with_per_slice_distances():
     assert rel_l2(res[2], c["ref_object_grad"]) <= GRAD_TOL
     assert rel_l2(res[3], c["ref_probe_grad"]) <= GRAD_TOL
     assert rel_l2(res[4], c["ref_pos_grad"]) <= GRAD_TOL
+
+
+def test_drop_in_saves_simulated_patterns(tmp_path):
+    """data_simulation_flag: the mean-over-modes model patterns of every position are saved
+    (float64, detector order) while the loss and gradients are returned as usual."""
+    from oracle import ptycho_oracle as orc
+    from pypty_gb300 import objective
+    from test_host_logic import base_kwargs
+    c = load_case("multislice_ml_c64")
+    f = np.float32
+    path = str(tmp_path / "sim.npy")
+    kw = base_kwargs(this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
+                     this_pos_correction=c["pos_correction"], this_distances=np.array([c["distance"]], f),
+                     edge_slice_thickness_multiplier=c["edge_mult"], measured_array=c["measured"],
+                     algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
+                     this_step_probe=c["step_probe"], this_step_obj=c["step_obj"],
+                     this_step_pos_correction=c["step_pos"], pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+                     damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]),
+                     this_chopped_sequence=c["sequence"], this_loss_weight=c["loss_weight"],
+                     compute_batch=c["batch"], data_simulation_flag=path)
+    res = objective.loss_and_direction(**kw)
+    assert abs(res[0] - float(c["ref_loss"])) <= LOSS_TOL * abs(float(c["ref_loss"]))
+    sim = np.load(path)
+    ref = orc.loss_and_direction(c["obj"].astype(np.complex128), c["probe"].astype(np.complex128), c["positions"],
+                                 c["pos_correction"].astype(np.float64), c["distance"], c["edge_mult"], None,
+                                 c["algorithm"], c["wavelength"], 1, 1, 0, c["px"], c["px"], c["cutoff"],
+                                 c["rolloff"], c["sequence"], 1, c["batch"], float_dtype=np.float64,
+                                 complex_dtype=np.complex128, simulate=True)
+    assert sim.dtype == np.float64 and sim.shape == ref.shape
+    assert rel_l2(sim, ref) <= 1e-5
