@@ -1105,7 +1105,74 @@ struct Run {
       return pty_fft2_bf16x3(in, out, (int32_t)nwin, q.W, inverse, at<void>(ws, q.o_dft), q.dft_bytes, st);
     if (q.engine == PTY_DFT_BF16X6)
       return pty_fft2_bf16x6(in, out, (int32_t)nwin, q.W, inverse, at<void>(ws, q.o_dft), q.dft_bytes, st);
-    return pty_fft2(in, out, (int32_t)nwin, q.W, inverse, 0, at<void>(ws, q.o_dft), q.dft_bytes, st);
+    // the FP32 engine's twiddle tables are built by the first transform of the call and reused
+    float2* tw = at<float2>(ws, q.o_dft);
+    const int build = tw_built ? 0 : 1;
+    tw_built = true;
+    if (q.W == 64) return run_fft2<64>(in, out, (int)nwin, inverse, 0, tw, st, build);
+    if (q.W == 128) return run_fft2<128>(in, out, (int)nwin, inverse, 0, tw, st, build);
+    return run_fft2<256>(in, out, (int)nwin, inverse, 0, tw, st, build);
+  }
+  bool tw_built = false;
+
+  // one forward step of the batch in one pass (FP32 engine, 64 / 128 px windows)
+  int fwd_prop(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Bn,
+               const float2* tab, size_t tab_stride, float scale) {
+    float2* tw = at<float2>(ws, q.o_dft);
+    if (!tw_built) {
+      prof_mark(st, KID_TWIDDLES);
+      if (q.W == 64) build_twiddles_kernel<64><<<1, 256, 0, st>>>(tw);
+      else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
+      tw_built = true;
+    }
+    prof_mark(st, KID_FUSED);
+    const unsigned nwin = (unsigned)(Bn * q.Mp * q.Mo);
+    if (q.W == 64) {
+      if (set_smem(fwd_prop_kernel<64>, Smem<64>::bytes)) return PTY_ERR_CUDA;
+      fwd_prop_kernel<64><<<nwin, Geo<64>::T, Smem<64>::bytes, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp,
+                                                                     q.Mo, tab, tab_stride, scale, tw);
+    } else {
+      if (set_smem(fwd_prop_kernel<128>, Smem<128>::bytes)) return PTY_ERR_CUDA;
+      fwd_prop_kernel<128><<<nwin, Geo<128>::T, Smem<128>::bytes, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z,
+                                                                       q.Mp, q.Mo, tab, tab_stride, scale, tw);
+    }
+    return cuda_status();
+  }
+
+  // psi <- IFFT(FFT(psi) * P) through psi2 (or in one pass on the FP32 engine for 64 / 128 px
+  // windows): the table per group of nper windows, tab_stride apart, 1/W^2 folded in or not
+  int prop_step(float2* psi, float2* psi2, long long nwin, const float2* tab, size_t tab_stride, int nper,
+                int conj, bool folded) {
+    const float WWf = (float)q.WW;
+    if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
+      float2* tw = at<float2>(ws, q.o_dft);
+      if (!tw_built) {
+        prof_mark(st, KID_TWIDDLES);
+        if (q.W == 64) build_twiddles_kernel<64><<<1, 256, 0, st>>>(tw);
+        else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
+        tw_built = true;
+      }
+      prof_mark(st, KID_FFT2);
+      const float scale = folded ? 1.0f : 1.0f / WWf;
+      if (q.W == 64) {
+        if (set_smem(prop_step_kernel<64>, Smem<64>::bytes)) return PTY_ERR_CUDA;
+        prop_step_kernel<64><<<(unsigned)nwin, Geo<64>::T, Smem<64>::bytes, st>>>(psi, psi, tab, tab_stride, nper,
+                                                                                 conj, scale, tw);
+      } else {
+        if (set_smem(prop_step_kernel<128>, Smem<128>::bytes)) return PTY_ERR_CUDA;
+        prop_step_kernel<128><<<(unsigned)nwin, Geo<128>::T, Smem<128>::bytes, st>>>(psi, psi, tab, tab_stride,
+                                                                                    nper, conj, scale, tw);
+      }
+      return cuda_status();
+    }
+    int rc;
+    if ((rc = dft(psi, psi2, nwin, 0))) return rc;
+    prof_mark(st, KID_ELEMENTWISE);
+    if (tab_stride == 0)
+      prop_kernel<<<grid((int)nwin, 1), EB, 0, st>>>(psi2, tab, q.WW, conj, folded ? WWf : 1.0f);
+    else
+      var_pos_table_mul_kernel<<<grid(nper, (int)(nwin / nper)), EB, 0, st>>>(psi2, tab, nper, q.WW, conj);
+    return dft(psi2, psi, nwin, 1);
   }
 
   dim3 grid(int y, int z) const { return dim3((unsigned)(q.WW / EB), (unsigned)y, (unsigned)z); }
@@ -1326,9 +1393,30 @@ struct Run {
       }
       // forward multislice (multislice_core.py:61-82)
       for (int z = 0; z < q.Z; ++z) {
+        if (z < q.Z - 1 && !(v && q.inside_grad) && q.engine == PTY_DFT_FP32_FFT && W <= 128) {
+          // slice, stack and propagation in one pass (multislice_core.py:61-80)
+          if (tilted_prop && q.per_step) pos_props(z);
+          const bool edge = z == 0 && ta.use_edge;
+          const float2* tab = tilted_prop ? (edge ? pprop_edge : pprop)
+                                          : (q.per_step ? steps + (size_t)z * WWs : (edge ? ta.prop_edge : ta.prop));
+          const size_t tstride = tilted_prop ? WWs : 0;
+          const float scale = tilted_prop ? 1.0f / (float)WW : 1.0f;
+          if ((rc = fwd_prop(pin, pin_stride, psi, stack, ob, z, Bn, tab, tstride, scale))) return rc;
+          continue;
+        }
         prof_mark(st, KID_FUSED);
         fwd_slice_kernel<<<grid(nm, Bn), EB, 0, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp, q.Mo, WW);
-        if (z < q.Z - 1) {
+        if (z < q.Z - 1 && !(v && q.inside_grad)) {
+          // propagation (multislice_core.py:69-80), one pass on the FP32 engine
+          if (tilted_prop && q.per_step) pos_props(z);
+          const bool edge = z == 0 && ta.use_edge;
+          if (tilted_prop)
+            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 0, false);
+          else
+            rc = prop_step(psi, psi2, (long long)Bn * nm,
+                           q.per_step ? steps + (size_t)z * WWs : (edge ? ta.prop_edge : ta.prop), 0, 1, 0, true);
+          if (rc) return rc;
+        } else if (z < q.Z - 1) {
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
           if (v && q.inside_grad &&   // FFT(psi O) of the step, for the inside-tilt gradient
               cudaMemcpyAsync(spec + z * spec_stride, psi2, (size_t)Bn * nm * WWs * sizeof(float2),
@@ -1388,7 +1476,18 @@ struct Run {
       for (int z = q.Z - 1; z >= 0; --z) {
         prof_mark(st, KID_FUSED);
         adj_slice_kernel<<<grid(q.Mo, Bn), EB, 0, st>>>(psi, stack, ob, dob, z, q.Z, q.Mp, q.Mo, WW);
-        if (z > 0) {
+        if (z > 0 && !(v && q.inside_grad)) {
+          // adjoint propagation (multislice_core.py:164-183), one pass on the FP32 engine
+          const bool edge = z == 1 && ta.use_edge;
+          if (tilted_prop && q.per_step) pos_props(z - 1);
+          if (tilted_prop)
+            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 1, false);
+          else
+            rc = prop_step(psi, psi2, (long long)Bn * nm,
+                           q.per_step ? steps + (size_t)(z - 1) * WWs : (edge ? ta.prop_edge : ta.prop), 0, 1, 1,
+                           true);
+          if (rc) return rc;
+        } else if (z > 0) {
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
           const bool edge = z == 1 && ta.use_edge;
           if (tilted_prop && q.per_step) pos_props(z - 1);

@@ -490,10 +490,13 @@ int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, 
 }
 
 template <int W>
-int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st) {
+int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
+             int build_tw) {
   if (set_smem(fft2_batch_kernel<W>, Smem<W>::bytes)) return PTY_ERR_CUDA;
-  prof_mark(st, KID_TWIDDLES);
-  build_twiddles_kernel<W><<<1, 256, 0, st>>>(tw);
+  if (build_tw) {
+    prof_mark(st, KID_TWIDDLES);
+    build_twiddles_kernel<W><<<1, 256, 0, st>>>(tw);
+  }
   prof_mark(st, KID_FFT2);
   fft2_batch_kernel<W><<<batch, Geo<W>::T, Smem<W>::bytes, st>>>(in, out, inverse, shift, tw);
   prof_mark(st, -1);

@@ -269,11 +269,14 @@ int run_backward<256>(const pty_problem_t* p, const Plan& q, double* loss_sse, f
 }
 
 template <>
-int run_fft2<256>(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st) {
+int run_fft2<256>(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
+                  int build_tw) {
   int rc = set_attrs256();
   if (rc) return rc;
-  prof_mark(st, KID_TWIDDLES);
-  build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
+  if (build_tw) {
+    prof_mark(st, KID_TWIDDLES);
+    build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
+  }
   prof_mark(st, KID_FFT2);
   if ((rc = launch4(fft2_batch256_kernel, (unsigned)batch, Smem256::small, st, in, out, inverse, shift,
                     (const float2*)tw)))

@@ -13,5 +13,5 @@ template int run_ms_forward<64>(const MsPlan&, const float2*, const float2*, con
 template int run_ms_grads<64>(const MsPlan&, const float2*, const float2*, const float2*, const float2*, float,
                               const float*, int, float2*, float2*, void*, cudaStream_t);
 template int run_scatteradd<64>(const MsPlan&, float2*, const float2*, void*, cudaStream_t);
-template int run_fft2<64>(const float2*, float2*, int, int, int, float2*, cudaStream_t);
+template int run_fft2<64>(const float2*, float2*, int, int, int, float2*, cudaStream_t, int);
 }  // namespace pty

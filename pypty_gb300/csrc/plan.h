@@ -258,8 +258,9 @@ template <int W>
 int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, cudaStream_t st);
 
 template <int W>
-int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st);
+int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
+             int build_tw = 1);   // build_tw = 0: tw already holds this window's twiddles
 template <>
-int run_fft2<256>(const float2*, float2*, int, int, int, float2*, cudaStream_t);
+int run_fft2<256>(const float2*, float2*, int, int, int, float2*, cudaStream_t, int);
 
 }  // namespace pty

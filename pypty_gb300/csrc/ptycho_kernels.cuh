@@ -1049,4 +1049,82 @@ __global__ void __launch_bounds__(Geo<W>::T) fft2_batch_kernel(const float2* __r
   }
 }
 
+// One propagation step of a batch of windows: out = IFFT(FFT(in) * P) (conj: conj(P)) with
+// P = tab[k] (natural (ky, kx)) and the inverse's 1/W^2 applied as `scale` (1 for tables that
+// fold it in already), one table per group of nper windows (tab_stride elements apart; 0: one
+// table). The same products and rounding as fft2 -> multiply -> ifft2.   grid n windows
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, float2* out,   // may alias
+                                                              const float2* __restrict__ tab, size_t tab_stride,
+                                                              int nper, int conj, float scale,
+                                                              const float2* __restrict__ g_tw) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  __syncthreads();
+  const int t = threadIdx.x;
+  const size_t WW = (size_t)W * W;
+  const float2* src = in + (size_t)blockIdx.x * WW;
+  float2* dst = out + (size_t)blockIdx.x * WW;
+  const float2* P = tab + (size_t)(blockIdx.x / nper) * tab_stride;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = src[G::ry(t) * W + G::rx(t, i)];
+  WinFFT<W>::forward(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const float2 pk = P[G::fky(t, i) * W + G::fkx(t, i)];
+    v[i] = cscale(conj ? cmulc(v[i], pk) : cmul(v[i], pk), scale);
+  }
+  __syncthreads();   // the inverse reuses the exchange buffer
+  WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[G::ry(t) * W + G::rx(t, i)] = v[i];
+}
+
+// One forward multislice step of a batch of windows (multislice_core.py:61-80) in one pass:
+// in = z == 0 ? the position's incoming probe (mode p) : psi; stack[b][z][p][m] = conj(in);
+// psi = IFFT(FFT(in * O[b][z][m]) * P), P as in prop_step_kernel.   grid Bn * Mp * Mo windows
+template <int W>
+__global__ void __launch_bounds__(Geo<W>::T) fwd_prop_kernel(const float2* __restrict__ pin, size_t pin_stride,
+                                                             float2* psi, float2* __restrict__ stack,
+                                                             const float2* __restrict__ ob, int z, int Z, int Mp,
+                                                             int Mo, const float2* __restrict__ tab,
+                                                             size_t tab_stride, float scale,
+                                                             const float2* __restrict__ g_tw) {
+  using G = Geo<W>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *xbuf, *tw1, *tw2;
+  double* red;
+  carve<W>(smem, xbuf, tw1, tw2, red);
+  load_twiddles<W>(tw1, tw2, g_tw);
+  __syncthreads();
+  const int t = threadIdx.x;
+  const size_t WW = (size_t)W * W;
+  const int nm = Mp * Mo, wi = blockIdx.x, b = wi / nm, pm = wi % nm, p = pm / Mo, m = pm % Mo;
+  const float2* src = z == 0 ? pin + (size_t)b * pin_stride + (size_t)p * WW : psi + (size_t)wi * WW;
+  float2* st = stack + (((size_t)b * Z + z) * nm + pm) * WW;
+  const float2* o = ob + (((size_t)b * Z + z) * Mo + m) * WW;
+  const float2* P = tab + (size_t)b * tab_stride;
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int u = G::ry(t) * W + G::rx(t, i);
+    const float2 in = src[u];
+    st[u] = cconj(in);
+    v[i] = cmul(in, o[u]);
+  }
+  WinFFT<W>::forward(v, xbuf, tw1, tw2);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = cscale(cmul(v[i], P[G::fky(t, i) * W + G::fkx(t, i)]), scale);
+  __syncthreads();   // the inverse reuses the exchange buffer
+  WinFFT<W>::inverse(v, xbuf, tw1, tw2);
+  float2* dst = psi + (size_t)wi * WW;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[G::ry(t) * W + G::rx(t, i)] = v[i];
+}
+
 }  // namespace pty
