@@ -1139,6 +1139,37 @@ struct Run {
     return cuda_status();
   }
 
+  // x <- IFFT(FFT(x) * mask) for nwin windows (the band limit, objective.py:436-441,
+  // multislice_core.py:189-191), in one pass on the FP32 engine for 64 / 128 px windows
+  int band_limit(float2* x, float2* tmp, long long nwin) {
+    if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
+      float2* tw = at<float2>(ws, q.o_dft);
+      if (!tw_built) {
+        prof_mark(st, KID_TWIDDLES);
+        if (q.W == 64) build_twiddles_kernel<64><<<1, 256, 0, st>>>(tw);
+        else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
+        tw_built = true;
+      }
+      prof_mark(st, KID_FFT2);
+      const float inv = 1.0f / (float)q.WW;
+      if (q.W == 64) {
+        if (set_smem(prop_step_kernel<64>, Smem<64>::bytes)) return PTY_ERR_CUDA;
+        prop_step_kernel<64><<<(unsigned)nwin, Geo<64>::T, Smem<64>::bytes, st>>>(x, x, nullptr, 0, 1, 0, inv, tw,
+                                                                                 ta.mask);
+      } else {
+        if (set_smem(prop_step_kernel<128>, Smem<128>::bytes)) return PTY_ERR_CUDA;
+        prop_step_kernel<128><<<(unsigned)nwin, Geo<128>::T, Smem<128>::bytes, st>>>(x, x, nullptr, 0, 1, 0, inv, tw,
+                                                                                    ta.mask);
+      }
+      return cuda_status();
+    }
+    int rc;
+    if ((rc = dft(x, tmp, nwin, 0))) return rc;
+    prof_mark(st, KID_ELEMENTWISE);
+    mask_kernel<<<grid((int)nwin, 1), EB, 0, st>>>(tmp, ta.mask, q.WW);
+    return dft(tmp, x, nwin, 1);
+  }
+
   // psi <- IFFT(FFT(psi) * P) through psi2 (or in one pass on the FP32 engine for 64 / 128 px
   // windows): the table per group of nper windows, tab_stride apart, 1/W^2 folded in or not
   int prop_step(float2* psi, float2* psi2, long long nwin, const float2* tab, size_t tab_stride, int nper,
@@ -1328,10 +1359,7 @@ struct Run {
       // object windows, band-limited (objective.py:436-441)
       prof_mark(st, KID_OBJECT_WINDOWS);
       gather_kernel<<<grid(q.zm, Bn), EB, 0, st>>>(at<float2>(ws, q.o_obj), ob, d_pos, seq_b, W, q.Ny, q.Nx, q.zm);
-      if ((rc = dft(ob, tmp, (long long)Bn * q.zm, 0))) return rc;
-      prof_mark(st, KID_ELEMENTWISE);
-      mask_kernel<<<grid(Bn * q.zm, 1), EB, 0, st>>>(tmp, ta.mask, WW);
-      if ((rc = dft(tmp, ob, (long long)Bn * q.zm, 1))) return rc;
+      if ((rc = band_limit(ob, tmp, (long long)Bn * q.zm))) return rc;
       // incoming probe per position (objective.py:469-476)
       const float2* pin = planes;
       size_t pin_stride = 0;
@@ -1510,10 +1538,7 @@ struct Run {
       }
       if (p->step_obj) {
         // band-limited gradient windows (multislice_core.py:189-191), deterministic scatter
-        if ((rc = dft(dob, tmp, (long long)Bn * q.zm, 0))) return rc;
-        prof_mark(st, KID_ELEMENTWISE);
-        mask_kernel<<<grid(Bn * q.zm, 1), EB, 0, st>>>(tmp, ta.mask, WW);
-        if ((rc = dft(tmp, dob, (long long)Bn * q.zm, 1))) return rc;
+        if ((rc = band_limit(dob, tmp, (long long)Bn * q.zm))) return rc;
         int* lists = at<int>(ws, q.o_lists);
         int* counts = at<int>(ws, q.o_counts);
         prof_mark(st, KID_TILE_LISTS);

@@ -1049,7 +1049,8 @@ __global__ void __launch_bounds__(Geo<W>::T) fft2_batch_kernel(const float2* __r
   }
 }
 
-// One propagation step of a batch of windows: out = IFFT(FFT(in) * P) (conj: conj(P)) with
+// One propagation step of a batch of windows (or, with rtab, one band limit by a real mask):
+// out = IFFT(FFT(in) * P) (conj: conj(P)) with
 // P = tab[k] (natural (ky, kx)) and the inverse's 1/W^2 applied as `scale` (1 for tables that
 // fold it in already), one table per group of nper windows (tab_stride elements apart; 0: one
 // table). The same products and rounding as fft2 -> multiply -> ifft2.   grid n windows
@@ -1057,7 +1058,8 @@ template <int W>
 __global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, float2* out,   // may alias
                                                               const float2* __restrict__ tab, size_t tab_stride,
                                                               int nper, int conj, float scale,
-                                                              const float2* __restrict__ g_tw) {
+                                                              const float2* __restrict__ g_tw,
+                                                              const float* __restrict__ rtab = nullptr) {
   using G = Geo<W>;
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
@@ -1076,8 +1078,13 @@ __global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, 
   WinFFT<W>::forward(v, xbuf, tw1, tw2);
 #pragma unroll
   for (int i = 0; i < 32; ++i) {
-    const float2 pk = P[G::fky(t, i) * W + G::fkx(t, i)];
-    v[i] = cscale(conj ? cmulc(v[i], pk) : cmul(v[i], pk), scale);
+    const int k = G::fky(t, i) * W + G::fkx(t, i);
+    if (rtab) {   // a real table (the band-limit mask)
+      v[i] = cscale(cscale(v[i], rtab[k]), scale);
+    } else {
+      const float2 pk = P[k];
+      v[i] = cscale(conj ? cmulc(v[i], pk) : cmul(v[i], pk), scale);
+    }
   }
   __syncthreads();   // the inverse reuses the exchange buffer
   WinFFT<W>::inverse(v, xbuf, tw1, tw2);
