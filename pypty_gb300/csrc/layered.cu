@@ -1115,9 +1115,8 @@ struct Run {
   }
   bool tw_built = false;
 
-  // one forward step of the batch in one pass (FP32 engine, 64 / 128 px windows)
-  int fwd_prop(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Bn,
-               const float2* tab, size_t tab_stride, float scale) {
+  // the FP32 engine's twiddle tables for 64 / 128 px windows, built once per call
+  float2* fp32_twiddles() {
     float2* tw = at<float2>(ws, q.o_dft);
     if (!tw_built) {
       prof_mark(st, KID_TWIDDLES);
@@ -1125,6 +1124,13 @@ struct Run {
       else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
       tw_built = true;
     }
+    return tw;
+  }
+
+  // one forward step of the batch in one pass (FP32 engine, 64 / 128 px windows)
+  int fwd_prop(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Bn,
+               const float2* tab, size_t tab_stride, float scale) {
+    float2* tw = fp32_twiddles();
     prof_mark(st, KID_FUSED);
     const unsigned nwin = (unsigned)(Bn * q.Mp * q.Mo);
     if (q.W == 64) {
@@ -1143,13 +1149,7 @@ struct Run {
   // multislice_core.py:189-191), in one pass on the FP32 engine for 64 / 128 px windows
   int band_limit(float2* x, float2* tmp, long long nwin) {
     if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
-      float2* tw = at<float2>(ws, q.o_dft);
-      if (!tw_built) {
-        prof_mark(st, KID_TWIDDLES);
-        if (q.W == 64) build_twiddles_kernel<64><<<1, 256, 0, st>>>(tw);
-        else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
-        tw_built = true;
-      }
+      float2* tw = fp32_twiddles();
       prof_mark(st, KID_FFT2);
       const float inv = 1.0f / (float)q.WW;
       if (q.W == 64) {
@@ -1176,13 +1176,7 @@ struct Run {
                 int conj, bool folded) {
     const float WWf = (float)q.WW;
     if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
-      float2* tw = at<float2>(ws, q.o_dft);
-      if (!tw_built) {
-        prof_mark(st, KID_TWIDDLES);
-        if (q.W == 64) build_twiddles_kernel<64><<<1, 256, 0, st>>>(tw);
-        else build_twiddles_kernel<128><<<1, 256, 0, st>>>(tw);
-        tw_built = true;
-      }
+      float2* tw = fp32_twiddles();
       prof_mark(st, KID_FFT2);
       const float scale = folded ? 1.0f : 1.0f / WWf;
       if (q.W == 64) {
