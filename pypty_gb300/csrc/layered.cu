@@ -1129,18 +1129,19 @@ struct Run {
 
   // one forward step of the batch in one pass (FP32 engine, 64 / 128 px windows)
   int fwd_prop(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Bn,
-               const float2* tab, size_t tab_stride, float scale) {
+               const float2* tab, size_t tab_stride, float scale, float2* spec_out) {
     float2* tw = fp32_twiddles();
     prof_mark(st, KID_FUSED);
     const unsigned nwin = (unsigned)(Bn * q.Mp * q.Mo);
     if (q.W == 64) {
       if (set_smem(fwd_prop_kernel<64>, Smem<64>::bytes)) return PTY_ERR_CUDA;
       fwd_prop_kernel<64><<<nwin, Geo<64>::T, Smem<64>::bytes, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp,
-                                                                     q.Mo, tab, tab_stride, scale, tw);
+                                                                     q.Mo, tab, tab_stride, scale, tw, spec_out);
     } else {
       if (set_smem(fwd_prop_kernel<128>, Smem<128>::bytes)) return PTY_ERR_CUDA;
       fwd_prop_kernel<128><<<nwin, Geo<128>::T, Smem<128>::bytes, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z,
-                                                                       q.Mp, q.Mo, tab, tab_stride, scale, tw);
+                                                                       q.Mp, q.Mo, tab, tab_stride, scale, tw,
+                                                                       spec_out);
     }
     return cuda_status();
   }
@@ -1171,22 +1172,28 @@ struct Run {
   }
 
   // psi <- IFFT(FFT(psi) * P) through psi2 (or in one pass on the FP32 engine for 64 / 128 px
-  // windows): the table per group of nper windows, tab_stride apart, 1/W^2 folded in or not
+  // windows): the table per group of nper windows, tab_stride apart, 1/W^2 folded in or not.
+  // keep_g: psi2 holds FFT(psi) * P afterwards (with the unfolded P), as the separate passes
+  // leave it
   int prop_step(float2* psi, float2* psi2, long long nwin, const float2* tab, size_t tab_stride, int nper,
-                int conj, bool folded) {
+                int conj, bool folded, bool keep_g = false) {
     const float WWf = (float)q.WW;
     if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
       float2* tw = fp32_twiddles();
       prof_mark(st, KID_FFT2);
       const float scale = folded ? 1.0f : 1.0f / WWf;
+      float2* gout = keep_g ? psi2 : nullptr;
+      const float gscale = folded ? WWf : 1.0f;
       if (q.W == 64) {
         if (set_smem(prop_step_kernel<64>, Smem<64>::bytes)) return PTY_ERR_CUDA;
         prop_step_kernel<64><<<(unsigned)nwin, Geo<64>::T, Smem<64>::bytes, st>>>(psi, psi, tab, tab_stride, nper,
-                                                                                 conj, scale, tw);
+                                                                                 conj, scale, tw, nullptr, gout,
+                                                                                 gscale);
       } else {
         if (set_smem(prop_step_kernel<128>, Smem<128>::bytes)) return PTY_ERR_CUDA;
         prop_step_kernel<128><<<(unsigned)nwin, Geo<128>::T, Smem<128>::bytes, st>>>(psi, psi, tab, tab_stride,
-                                                                                    nper, conj, scale, tw);
+                                                                                    nper, conj, scale, tw, nullptr,
+                                                                                    gout, gscale);
       }
       return cuda_status();
     }
@@ -1414,31 +1421,24 @@ struct Run {
         pin_stride = (size_t)q.Mp * WWs;
       }
       // forward multislice (multislice_core.py:61-82)
+      const bool one_pass = q.engine == PTY_DFT_FP32_FFT && W <= 128;
       for (int z = 0; z < q.Z; ++z) {
-        if (z < q.Z - 1 && !(v && q.inside_grad) && q.engine == PTY_DFT_FP32_FFT && W <= 128) {
-          // slice, stack and propagation in one pass (multislice_core.py:61-80)
+        if (z < q.Z - 1 && one_pass) {
+          // slice, stack and propagation in one pass (multislice_core.py:61-80); FFT(psi O) kept
+          // for the inside-tilt gradient
           if (tilted_prop && q.per_step) pos_props(z);
           const bool edge = z == 0 && ta.use_edge;
           const float2* tab = tilted_prop ? (edge ? pprop_edge : pprop)
                                           : (q.per_step ? steps + (size_t)z * WWs : (edge ? ta.prop_edge : ta.prop));
           const size_t tstride = tilted_prop ? WWs : 0;
           const float scale = tilted_prop ? 1.0f / (float)WW : 1.0f;
-          if ((rc = fwd_prop(pin, pin_stride, psi, stack, ob, z, Bn, tab, tstride, scale))) return rc;
+          float2* spec_out = (v && q.inside_grad) ? spec + z * spec_stride : nullptr;
+          if ((rc = fwd_prop(pin, pin_stride, psi, stack, ob, z, Bn, tab, tstride, scale, spec_out))) return rc;
           continue;
         }
         prof_mark(st, KID_FUSED);
         fwd_slice_kernel<<<grid(nm, Bn), EB, 0, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp, q.Mo, WW);
-        if (z < q.Z - 1 && !(v && q.inside_grad)) {
-          // propagation (multislice_core.py:69-80), one pass on the FP32 engine
-          if (tilted_prop && q.per_step) pos_props(z);
-          const bool edge = z == 0 && ta.use_edge;
-          if (tilted_prop)
-            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 0, false);
-          else
-            rc = prop_step(psi, psi2, (long long)Bn * nm,
-                           q.per_step ? steps + (size_t)z * WWs : (edge ? ta.prop_edge : ta.prop), 0, 1, 0, true);
-          if (rc) return rc;
-        } else if (z < q.Z - 1) {
+        if (z < q.Z - 1) {   // the other engines: separate transforms
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
           if (v && q.inside_grad &&   // FFT(psi O) of the step, for the inside-tilt gradient
               cudaMemcpyAsync(spec + z * spec_stride, psi2, (size_t)Bn * nm * WWs * sizeof(float2),
@@ -1498,36 +1498,28 @@ struct Run {
       for (int z = q.Z - 1; z >= 0; --z) {
         prof_mark(st, KID_FUSED);
         adj_slice_kernel<<<grid(q.Mo, Bn), EB, 0, st>>>(psi, stack, ob, dob, z, q.Z, q.Mp, q.Mo, WW);
-        if (z > 0 && !(v && q.inside_grad)) {
-          // adjoint propagation (multislice_core.py:164-183), one pass on the FP32 engine
+        if (z > 0) {
+          // adjoint propagation (multislice_core.py:164-183); psi2 keeps FFT(g) conj(P) for the
+          // inside-tilt gradient
           const bool edge = z == 1 && ta.use_edge;
+          const bool keep = v && q.inside_grad;
           if (tilted_prop && q.per_step) pos_props(z - 1);
           if (tilted_prop)
-            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 1, false);
+            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 1, false, keep);
           else
             rc = prop_step(psi, psi2, (long long)Bn * nm,
                            q.per_step ? steps + (size_t)(z - 1) * WWs : (edge ? ta.prop_edge : ta.prop), 0, 1, 1,
-                           true);
+                           true, keep);
           if (rc) return rc;
-        } else if (z > 0) {
-          if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
-          const bool edge = z == 1 && ta.use_edge;
-          if (tilted_prop && q.per_step) pos_props(z - 1);
-          prof_mark(st, KID_ELEMENTWISE);
-          if (tilted_prop)
-            var_pos_table_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi2, edge ? pprop_edge : pprop, nm, WW, 1);
-          else
-            prop_kernel<<<grid(Bn * nm, 1), EB, 0, st>>>(
-                psi2, q.per_step ? steps + (size_t)(z - 1) * WWs : (edge ? ta.prop_edge : ta.prop), WW, 1, unfold);
-          if (v && q.inside_grad) {
+          if (keep) {
             // sh = -4 pi d / W^2 in float32, d (the step's distance) times the edge multiplier on
             // the thick step (multislice_core.py:164-180)
             const float dist = edge ? step_distance(z - 1) * p->edge_mult : step_distance(z - 1);
             const float shf = fdiv_host((float)-12.566370614359172 * dist, (float)WW);
+            prof_mark(st, KID_ELEMENTWISE);
             var_inside_tilt_kernel<<<Bn, 1024, 0, st>>>(psi2, spec + (size_t)(z - 1) * spec_stride, nm, W,
                                                         p->pixel_size_x, p->pixel_size_y, (double)shf, tpart);
           }
-          if ((rc = dft(psi2, psi, (long long)Bn * nm, 1))) return rc;
         }
       }
       if (p->step_obj) {

@@ -1050,7 +1050,7 @@ __global__ void __launch_bounds__(Geo<W>::T) fft2_batch_kernel(const float2* __r
 }
 
 // One propagation step of a batch of windows (or, with rtab, one band limit by a real mask):
-// out = IFFT(FFT(in) * P) (conj: conj(P)) with
+// out = IFFT(FFT(in) * P) (conj: conj(P)); gout, when given, receives FFT(in) * P * gscale with
 // P = tab[k] (natural (ky, kx)) and the inverse's 1/W^2 applied as `scale` (1 for tables that
 // fold it in already), one table per group of nper windows (tab_stride elements apart; 0: one
 // table). The same products and rounding as fft2 -> multiply -> ifft2.   grid n windows
@@ -1059,7 +1059,9 @@ __global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, 
                                                               const float2* __restrict__ tab, size_t tab_stride,
                                                               int nper, int conj, float scale,
                                                               const float2* __restrict__ g_tw,
-                                                              const float* __restrict__ rtab = nullptr) {
+                                                              const float* __restrict__ rtab = nullptr,
+                                                              float2* __restrict__ gout = nullptr,
+                                                              float gscale = 1.0f) {
   using G = Geo<W>;
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
@@ -1083,7 +1085,9 @@ __global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, 
       v[i] = cscale(cscale(v[i], rtab[k]), scale);
     } else {
       const float2 pk = P[k];
-      v[i] = cscale(conj ? cmulc(v[i], pk) : cmul(v[i], pk), scale);
+      const float2 prod = conj ? cmulc(v[i], pk) : cmul(v[i], pk);
+      if (gout) gout[(size_t)blockIdx.x * WW + k] = cscale(prod, gscale);   // the product spectrum
+      v[i] = cscale(prod, scale);
     }
   }
   __syncthreads();   // the inverse reuses the exchange buffer
@@ -1094,14 +1098,16 @@ __global__ void __launch_bounds__(Geo<W>::T) prop_step_kernel(const float2* in, 
 
 // One forward multislice step of a batch of windows (multislice_core.py:61-80) in one pass:
 // in = z == 0 ? the position's incoming probe (mode p) : psi; stack[b][z][p][m] = conj(in);
-// psi = IFFT(FFT(in * O[b][z][m]) * P), P as in prop_step_kernel.   grid Bn * Mp * Mo windows
+// psi = IFFT(FFT(in * O[b][z][m]) * P), P as in prop_step_kernel; spec_out, when given,
+// receives FFT(in * O).   grid Bn * Mp * Mo windows
 template <int W>
 __global__ void __launch_bounds__(Geo<W>::T) fwd_prop_kernel(const float2* __restrict__ pin, size_t pin_stride,
                                                              float2* psi, float2* __restrict__ stack,
                                                              const float2* __restrict__ ob, int z, int Z, int Mp,
                                                              int Mo, const float2* __restrict__ tab,
                                                              size_t tab_stride, float scale,
-                                                             const float2* __restrict__ g_tw) {
+                                                             const float2* __restrict__ g_tw,
+                                                             float2* __restrict__ spec_out) {
   using G = Geo<W>;
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
@@ -1126,7 +1132,11 @@ __global__ void __launch_bounds__(Geo<W>::T) fwd_prop_kernel(const float2* __res
   }
   WinFFT<W>::forward(v, xbuf, tw1, tw2);
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = cscale(cmul(v[i], P[G::fky(t, i) * W + G::fkx(t, i)]), scale);
+  for (int i = 0; i < 32; ++i) {
+    const int k = G::fky(t, i) * W + G::fkx(t, i);
+    if (spec_out) spec_out[(size_t)wi * WW + k] = v[i];   // FFT(in O), kept for the inside-tilt gradient
+    v[i] = cscale(cmul(v[i], P[k]), scale);
+  }
   __syncthreads();   // the inverse reuses the exchange buffer
   WinFFT<W>::inverse(v, xbuf, tw1, tw2);
   float2* dst = psi + (size_t)wi * WW;

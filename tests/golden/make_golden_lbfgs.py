@@ -174,8 +174,10 @@ def make_refine_case(pypty):
     np.random.seed(5)
     rec = dict(scalars=[], obj=[], probe=[], tcorr=[], ab=[], bc=[])
     warnings, failed = "", 0
-    # a float first step: with the integer 1 a random-step trial truncates to 0 (iterative.py:831)
-    step = 1.0
+    # a float first step (with the integer 1 a random-step trial truncates to 0, iterative.py:831),
+    # small enough that the Wolfe search settles without random trial steps: a sequence that
+    # draws random steps flips with any rounding difference
+    step = 1e-3
     for epoch in range(3):
         res = it.bfgs_update(
             algorithm_type=c["algorithm"], this_slice_distances=np.array([c["distance"]], dtype=f),

@@ -280,7 +280,7 @@ def test_bfgs_update_refines_tilts_aberrations_and_beam_current():
     np.random.seed(5)
     warnings, failed = "", 0
     f = np.float32
-    step = 1.0     # the generator's float first step, then the accepted one
+    step = 1e-3    # the generator's float first step, then the accepted one
     for e, ref in enumerate(c["ref_scalars"]):
         kw = dict(this_step_tilts=1, tilt_mode=3, aberration_marker=c["aberration_marker"],
                   this_step_aberrations_array=1, this_beam_current_step=1, actual_step=step)
