@@ -84,7 +84,8 @@ int pty_version(void);
 /* Human-readable text of a PTY_* status code (static storage). */
 const char* pty_status_string(int status);
 
-/* Device workspace (bytes) that pty_loss_and_direction / pty_simulate_patterns need. */
+/* Device workspace (bytes) that pty_loss_and_direction / pty_simulate_patterns need (0 for an
+ * empty sequence). */
 int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes);
 
 /*
@@ -101,6 +102,8 @@ int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes);
  *   probe_grad                  device, complex64 (W, W, Mp), overwritten (band-limited)
  *   pos_grad                    device, float32 (n_positions, 2), overwritten; rows not
  *                               in the sequence are zero
+ * An empty sequence (n_sequence = 0) gives a zero loss, sse and gradients, as the reference's
+ * loop over no batches does; the workspace is not used then.
  */
 int pty_loss_and_direction(const pty_problem_t* problem, const void* obj, const void* probe,
                            const int32_t* positions_host, const float* pos_correction_host,

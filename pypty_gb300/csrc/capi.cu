@@ -207,6 +207,15 @@ const char* pty_status_string(int status) {
 }
 
 int pty_workspace_bytes(const pty_problem_t* problem, size_t* bytes) {
+  if (problem && problem->n_sequence == 0) {   // an empty sequence needs no workspace
+    pty_problem_t one = *problem;
+    one.n_sequence = 1;
+    const int rc = validate(&one);
+    if (rc) return rc;
+    if (!bytes) return PTY_ERR_INVALID;
+    *bytes = 0;
+    return PTY_OK;
+  }
   int rc = validate(problem);
   if (rc) return rc;
   if (!bytes) return PTY_ERR_INVALID;
@@ -219,6 +228,30 @@ int pty_loss_and_direction(const pty_problem_t* problem, const void* obj, const 
                            const int32_t* sequence_host, const float* measured, double* loss_sse,
                            void* object_grad, void* probe_grad, float* pos_grad, void* workspace,
                            size_t workspace_bytes, void* stream) {
+  if (problem && problem->n_sequence == 0) {
+    // no positions: the reference's batch loop does not run, so the loss, sse and every
+    // gradient are zero (pypty/objective.py:372-382, 741-742)
+    pty_problem_t one = *problem;
+    one.n_sequence = 1;
+    const int rc = validate(&one);
+    if (rc) return rc;
+    if (!loss_sse || (problem->step_obj && !object_grad) || (problem->step_probe && !probe_grad) ||
+        (problem->step_pos && !pos_grad))
+      return PTY_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t W = (size_t)problem->window;
+    bool ok = cudaMemsetAsync(loss_sse, 0, 2 * sizeof(double), st) == cudaSuccess;
+    if (object_grad)
+      ok = ok && cudaMemsetAsync(object_grad, 0,
+                                 (size_t)problem->obj_ny * problem->obj_nx * problem->n_slices *
+                                     problem->n_obj_modes * sizeof(float2),
+                                 st) == cudaSuccess;
+    if (probe_grad)
+      ok = ok && cudaMemsetAsync(probe_grad, 0, W * W * problem->n_probe_modes * sizeof(float2), st) == cudaSuccess;
+    if (pos_grad)
+      ok = ok && cudaMemsetAsync(pos_grad, 0, (size_t)problem->n_positions * 2 * sizeof(float), st) == cudaSuccess;
+    return ok ? PTY_OK : PTY_ERR_CUDA;
+  }
   return run_common(problem, obj, probe, positions_host, pos_correction_host, sequence_host, measured, loss_sse,
                     object_grad, probe_grad, pos_grad, nullptr, workspace, workspace_bytes, stream);
 }

@@ -246,6 +246,19 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
     meas_d = measured_tensor(measured_array, dev, bool(load_one_by_one))
     bc_grad, ab_grad, sb_grad = 0, 0, 0
     tilts_grad = np.zeros_like(_to_numpy(this_tilts_correction))    # objective.py:380
+    if problem.n_sequence == 0:
+        # no positions: the batch loop does not run and every accumulator stays zero
+        # (objective.py:372-382); the variant accumulators are zeros shaped like their inputs
+        variant = None
+        if beam_current is not None:
+            bc_grad = np.zeros_like(_to_numpy(beam_current))
+        if aberrations_array is not None:
+            ab_grad = np.zeros_like(_to_numpy(aberrations_array))
+        if static_background is not None and np.ndim(_to_numpy(static_background)) == 2:
+            sb_grad = np.zeros_like(_to_numpy(static_background))
+        problem.algorithm = min(int(problem.algorithm), 3)   # the loss is not evaluated
+        W = problem.window   # no pattern is read: any measured array of the checked shape
+        meas_d = torch.empty((problem.n_positions, W, W), dtype=torch.float32, device=dev)
     if variant is None:
         loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
     else:

@@ -74,6 +74,16 @@ def test_invalid_problems_rejected(lib, kw, status):
     assert lib.pty_workspace_bytes(ctypes.byref(problem(**kw)), ctypes.byref(n)) == status
 
 
+def test_empty_sequence_needs_no_workspace(lib):
+    n = ctypes.c_size_t(123)
+    assert lib.pty_workspace_bytes(ctypes.byref(problem(n_sequence=0)), ctypes.byref(n)) == _lib.PTY_OK
+    assert n.value == 0
+    # the other fields are still checked
+    assert lib.pty_workspace_bytes(ctypes.byref(problem(n_sequence=0, window=96)),
+                                   ctypes.byref(n)) == _lib.PTY_ERR_UNSUPPORTED
+    assert lib.pty_workspace_bytes(ctypes.byref(problem(n_sequence=-1)), ctypes.byref(n)) == _lib.PTY_ERR_INVALID
+
+
 def _call_with_positions(lib, pos, seq):
     p = problem(n_positions=pos.shape[0], n_sequence=seq.shape[0])
     corr = np.zeros(pos.shape, np.float32)

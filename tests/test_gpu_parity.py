@@ -225,3 +225,21 @@ def test_drop_in_saves_simulated_patterns(tmp_path):
                                  complex_dtype=np.complex128, simulate=True)
     assert sim.dtype == np.float64 and sim.shape == ref.shape
     assert rel_l2(sim, ref) <= 1e-5
+
+
+def test_empty_sequence_gives_zero_loss_and_gradients():
+    """No positions in the sequence: the reference's batch loop does not run, so the loss, sse
+    and every gradient are zero (pypty/objective.py:372-382)."""
+    from pypty_gb300 import objective
+    from test_host_logic import base_kwargs
+    c = load_case("multislice_ml_c64")
+    f = np.float32
+    kw = base_kwargs(this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
+                     this_pos_correction=c["pos_correction"], this_distances=np.array([c["distance"]], f),
+                     measured_array=c["measured"], algorithm_type=c["algorithm"], this_wavelength=f(c["wavelength"]),
+                     this_step_pos_correction=1, pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+                     this_chopped_sequence=np.zeros(0, np.int64), compute_batch=c["batch"])
+    res = objective.loss_and_direction(**kw)
+    assert res[0] == 0.0 and res[1] == 0.0
+    assert not np.any(res[2]) and not np.any(res[3]) and not np.any(res[4])
+    assert res[2].shape == c["obj"].shape and res[4].shape == c["pos_correction"].shape
