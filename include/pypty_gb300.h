@@ -315,6 +315,10 @@ typedef struct pty_variant {
      [0, S); an entry outside that range reads scenario 0). 0 or 1: one probe. */
   int32_t n_probe_scenarios;
   const int32_t* probe_marker;
+  /* NULL, or device complex64 [n_sequence][Mp][Mo][W][W]: the exit wave of every position of
+     the sequence (after a tilt after the specimen), as data_simulation_exitwave saves it
+     (pypty/objective.py:289-291, 518-520) */
+  void* exit_waves;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

@@ -184,7 +184,8 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
     zero-initialised accumulators, ``objective.py:377, 381-382``).
     ``simulate=True`` returns the model patterns at the measured detector's shape (cropped by
     ``data_pad``, block-summed by ``upsample_pattern``) or, for compressed algorithms, the
-    coefficients (len(sequence), n_masks).
+    coefficients (len(sequence), n_masks); ``simulate="exit"`` the exit waves (len(sequence),
+    W, W, Mp, Mo) after a tilt after the specimen (``data_simulation_exitwave``).
     """
     f = float_dtype
     obj = np.asarray(obj, dtype=complex_dtype)
@@ -318,6 +319,9 @@ def loss_and_direction_variants(obj, probe, positions, pos_correction, distance,
                 exit_wave = ifft2(fft2(exit_wave, axes=(1, 2)) * mask[None, :, :, None, None], axes=(1, 2))
             exit_before_tilt = exit_wave
             exit_wave = exit_before_tilt * tmask_a
+        if simulate == "exit":                                          # objective.py:518-520
+            sim.append(exit_wave)
+            continue
         if near and per_pos_defocus:
             dfc = dfa[tcs][:, None, None]                               # (B, 1, 1)
         if near:                                                        # objective.py:504-508

@@ -1469,6 +1469,10 @@ struct Run {
           return PTY_ERR_CUDA;
         var_tilt_mul_kernel<<<grid(nm, Bn), EB, 0, st>>>(psi, tg, nm, 4, 0);
       }
+      if (v && v->exit_waves &&   // the exit waves (objective.py:518-520, data_simulation_exitwave)
+          cudaMemcpyAsync(static_cast<float2*>(v->exit_waves) + (size_t)i0 * nm * WWs, psi,
+                          (size_t)Bn * nm * WWs * sizeof(float2), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return PTY_ERR_CUDA;
       // far field, loss, dL/dPsi (objective.py:501-597)
       if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
       if (v && q.inside_grad && q.near &&   // FFT(exit) for the near-field inside-tilt gradient

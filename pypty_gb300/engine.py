@@ -200,6 +200,7 @@ class Engine:
                                     step_static_background: bool = False,
                                     defocus_per_position: torch.Tensor | None = None,
                                     probe_marker: torch.Tensor | None = None,
+                                    exit_waves: torch.Tensor | None = None,
                                     stream=None, pos_correction: torch.Tensor | None = None):
         """loss_and_direction with the near-field, compressed-detector, beam-current,
         aberration-plate and inside-tilt branches (``pty_loss_and_direction_variants``).
@@ -215,7 +216,8 @@ class Engine:
         its gradient is returned; defocus_per_position (n_positions,) float32: near-field
         defocus of every position instead of ``defocus``; probe_marker (n_positions,) int with a
         4D probe (W, W, Mp, S): every position's probe scenario (the probe gradient is then
-        (W, W, Mp, S) too); tilts
+        (W, W, Mp, S) too); exit_waves (n_sequence, Mp, Mo, W, W) complex64 CUDA tensor: filled
+        with every position's exit wave; tilts
         (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
         one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
@@ -264,6 +266,11 @@ class Engine:
             if pm.shape != (problem.n_positions,) or pm.min() < 0 or pm.max() >= n_scen:
                 raise ValueError("probe_marker must hold one scenario index in [0, %d) per position" % n_scen)
             pm_d = dev(probe_marker, torch.int32)
+        if exit_waves is not None:
+            want_e = (problem.n_sequence, problem.n_probe_modes, problem.n_obj_modes, problem.window, problem.window)
+            if (tuple(exit_waves.shape) != want_e or exit_waves.dtype != torch.complex64 or not exit_waves.is_cuda
+                    or not exit_waves.is_contiguous()):
+                raise ValueError("exit_waves must be a contiguous complex64 CUDA tensor of shape %s" % (want_e,))
         dfp_d = dev(defocus_per_position, torch.float32)
         if dfp_d is not None and tuple(dfp_d.shape) != (problem.n_positions,):
             raise ValueError("defocus_per_position must hold one defocus per position")
@@ -306,7 +313,8 @@ class Engine:
                          step_static_background=int(sb_grad is not None),
                          static_background_grad=None if sb_grad is None else sb_grad.data_ptr(),
                          defocus_per_position=None if dfp_d is None else dfp_d.data_ptr(),
-                         n_probe_scenarios=n_scen, probe_marker=None if pm_d is None else pm_d.data_ptr())
+                         n_probe_scenarios=n_scen, probe_marker=None if pm_d is None else pm_d.data_ptr(),
+                         exit_waves=None if exit_waves is None else exit_waves.data_ptr())
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_variants_workspace_bytes(ctypes.byref(problem), ctypes.byref(v), ctypes.byref(n)),
                    "pty_variants_workspace_bytes")

@@ -155,9 +155,10 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
                  "a static background with upsampling or a cropped pattern (the reference's shapes do not broadcast)")
     _unsupported(compressed and int(data_pad) != 0, "data_pad with compressed detectors")
     prep = not compressed and (int(data_pad) != 0 or not _is_zero(data_shift_vector) or float(data_multiplier) != 1.0)
-    # data_simulation_flag: the model patterns are also saved to that file (objective.py:286-293,
-    # 518-522, 744-749); the exit-wave variant and the variants path are not built
-    _unsupported(bool(data_simulation_flag) and bool(data_simulation_exitwave), "data_simulation_exitwave")
+    # data_simulation_flag: the model patterns (fused path) or the exit waves
+    # (data_simulation_exitwave, variants path) are also saved to that file
+    # (objective.py:286-293, 518-522, 744-749)
+    exitwave = bool(data_simulation_flag) and bool(data_simulation_exitwave)
     for name, w in [("fast_axis_reg_weight_positions", fast_axis_reg_weight_positions),
                     ("slow_axis_reg_weight_positions", slow_axis_reg_weight_positions),
                     ("current_deformation_reg_weight_positions", current_deformation_reg_weight_positions)]:
@@ -188,7 +189,7 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
         step_pos=bool(this_step_pos_correction))
     variant = None
     if near or compressed or prep or beam_current is not None or aberrations_array is not None or tilted \
-            or up != 1 or has_bg or scen:
+            or up != 1 or has_bg or scen or exitwave:
         variant = dict(recon_type=recon_type,
                        defocus=float(dfa[0]) if near else 0.0,
                        defocus_per_position=dfa if near and dfa.shape[0] > 1 else None,
@@ -259,6 +260,11 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         problem.algorithm = min(int(problem.algorithm), 3)   # the loss is not evaluated
         W = problem.window   # no pattern is read: any measured array of the checked shape
         meas_d = torch.empty((problem.n_positions, W, W), dtype=torch.float32, device=dev)
+    sim_exit = None
+    if data_simulation_flag and data_simulation_exitwave and variant is not None:
+        sim_exit = torch.empty((problem.n_sequence, problem.n_probe_modes, problem.n_obj_modes, problem.window,
+                                problem.window), dtype=torch.complex64, device=dev)
+        variant = dict(variant, exit_waves=sim_exit)
     if variant is None:
         loss_sse, og, pg, posg = eng.loss_and_direction(problem, obj_d, probe_d, geo, meas_d)
     else:
@@ -283,7 +289,15 @@ def loss_and_direction(this_obj, full_probe, this_pos_array, this_pos_correction
         if aberrations_array is not None:
             ab_grad = np.zeros_like(_to_numpy(aberrations_array)) if abg is None else \
                 abg.cpu().numpy().astype(_to_numpy(aberrations_array).dtype, copy=False)
-    if data_simulation_flag:
+    if sim_exit is not None:
+        # sim_patterns[tcs] = this_exit_wave, complex128 (N, W, W, Mp, Mo), then np.save
+        # (objective.py:289-291, 518-520, 744-749)
+        ew = sim_exit.permute(0, 3, 4, 1, 2).cpu().numpy().astype(np.complex128)
+        seq = np.asarray(_to_numpy(this_chopped_sequence))
+        sim = np.zeros((seq.shape[0],) + ew.shape[1:], dtype=np.complex128)
+        sim[seq] = ew
+        np.save(data_simulation_flag, sim)
+    elif data_simulation_flag:
         _unsupported(variant is not None, "data_simulation_flag with the variants path's flags")
         # sim_patterns[tcs] = this_pattern over every batch, then np.save (objective.py:518-522,
         # 744-749): float64, indexed by the sequence's position entries

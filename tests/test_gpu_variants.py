@@ -294,3 +294,35 @@ def test_per_position_defocus_with_larger_batches():
     print({k: "%.1e" % v for k, v in e.items()})
     for k, v in e.items():
         assert v <= (1e-5 if k == "loss" else 1e-4), (k, v)
+
+
+def test_drop_in_saves_exit_waves(tmp_path):
+    """data_simulation_exitwave: the exit wave of every position (after a tilt after the
+    specimen) is saved as complex128 (N, W, W, Mp, Mo), against the FP64 oracle's exit waves."""
+    from pypty_gb300 import objective
+    from test_host_logic import base_kwargs
+    c = load_variant_case("tilt1_rows_z1_c64")
+    f = np.float32
+    path = str(tmp_path / "exit.npy")
+    kw = base_kwargs(
+        this_obj=c["obj"], full_probe=c["probe"], this_pos_array=c["positions"],
+        this_pos_correction=c["pos_correction"], this_tilt_array=c["tilts"].astype(f),
+        this_tilts_correction=np.zeros_like(c["tilts"], dtype=f), this_distances=np.array([c["distance"]], f),
+        edge_slice_thickness_multiplier=c["edge_mult"], measured_array=c["measured"], algorithm_type=c["algorithm"],
+        this_wavelength=f(c["wavelength"]), this_step_probe=c["step_probe"], this_step_obj=c["step_obj"],
+        this_step_pos_correction=c["step_pos"], pixel_size_x_A=f(c["px"]), pixel_size_y_A=f(c["px"]),
+        damping_cutoff_multislice=f(c["cutoff"]), smooth_rolloff=f(c["rolloff"]), this_chopped_sequence=c["sequence"],
+        this_loss_weight=c["loss_weight"], compute_batch=c["batch"], tilt_mode=c["tilt_mode"],
+        data_simulation_flag=path, data_simulation_exitwave=True)
+    res = objective.loss_and_direction(**kw)
+    assert abs(res[0] - float(c["ref_loss"])) <= 2e-5 * abs(float(c["ref_loss"]))
+    ew = np.load(path)
+    W, Mp, Mo = c["probe"].shape[0], c["probe"].shape[2], c["obj"].shape[3]
+    assert ew.dtype == np.complex128 and ew.shape == (len(c["sequence"]), W, W, Mp, Mo)
+    ref = vor.loss_and_direction_variants(
+        np.asarray(c["obj"], np.complex128), np.asarray(c["probe"], np.complex128), c["positions"],
+        np.asarray(c["pos_correction"], np.float64), c["distance"], c["edge_mult"], None, c["algorithm"],
+        c["wavelength"], 1, 1, 0, c["px"], c["px"], c["cutoff"], c["rolloff"], c["sequence"], 1, c["batch"],
+        tilts=c["tilts"], tilt_mode=c["tilt_mode"], float_dtype=np.float64, complex_dtype=np.complex128,
+        simulate="exit")
+    assert rel_l2(ew, ref) <= 1e-5

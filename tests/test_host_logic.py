@@ -50,7 +50,7 @@ def base_kwargs(**over):
     dict(atv_weight=0.1), dict(static_background=np.ones((64, 64)), upsample_pattern=2),
     dict(static_background=np.ones((64, 64)), data_pad=4, use_padded_intensity=False),
     dict(static_background=np.ones(64)), dict(this_step_static_background=1),
-    dict(data_simulation_flag="sim.npy", data_simulation_exitwave=True),
+    dict(data_simulation_flag="sim.npy", data_bin=2),
 ])
 def test_unsupported_flags_raise_before_any_gpu_work(over):
     with pytest.raises(NotImplementedError):
