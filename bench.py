@@ -445,6 +445,22 @@ def optimizer_step(eng, prob, geo, meas_d, obj_d, probe_d, wl, lad_ms, hbm_peak,
             "lad_ms": round(lad_ms, 3)}
 
 
+def max_over_ranks(ms, world, device=None):
+    """The job's step time: the slowest rank's (all_reduce MAX; one rank: unchanged)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_pos_per_rank, world, ms):
+    """Positions/s of the whole job: every rank processes its own replica of the workload
+    (independent positions, no data-path collective) in the job's step time."""
+    return world * n_pos_per_rank / (ms / 1000.0)
+
+
 def run_reference(args, cfg):
     """--impl reference: the reference algorithm on the host cores, same metric and config."""
     rank = int(os.environ.get("RANK", "0"))
@@ -453,6 +469,8 @@ def run_reference(args, cfg):
     wl = build_workload(cfg)
     # each step times a bounded sample; the whole run stays within a few minutes
     budget = max(2.0, min(15.0, 150.0 / max(args.steps, 1)))
+    for _ in range(args.warmup):   # untimed warm-up steps on a short sample
+        cpu_baseline(cfg, wl, cfg["algorithm"], budget_s=0.5)
     vals = []
     last = None
     for _ in range(max(args.steps, 1)):
@@ -560,14 +578,11 @@ def main():
         p1.record(stream)
         torch.cuda.synchronize(dev)
     profiled_ms = p0.elapsed_time(p1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     loss_val = float(out[0][0].item())
     if not np.isfinite(loss_val):
         raise RuntimeError("non-finite loss in the benchmark")
-    value = world * n_pos / (ms / 1000.0)
+    value = replica_throughput(n_pos, world, ms)
 
     # ---------------- end-to-end through the public call with host buffers
     obj_h = torch.from_numpy(wl["obj0"]).pin_memory()
@@ -602,10 +617,7 @@ def main():
     torch.cuda.synchronize(dev)
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, world, dev)
     h2d = obj_h.numel() * 8 + probe_h.numel() * 8 + meas_h.numel() * 4 + geo.positions.nbytes + \
         geo.pos_correction.nbytes + geo.sequence.nbytes
 
@@ -624,10 +636,7 @@ def main():
     torch.cuda.synchronize(dev)
     barrier()
     streamed_ms = s0.elapsed_time(s1) / args.steps
-    if world > 1:
-        t = torch.tensor([streamed_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        streamed_ms = float(t.item())
+    streamed_ms = max_over_ranks(streamed_ms, world, dev)
     d2h = og_h.numel() * 8 + pg_h.numel() * 8 + posg_h.numel() * 4 + 16
 
     if rank != 0:
@@ -662,9 +671,9 @@ def main():
                    "workspace_gb": round(_lib.workspace_bytes(prob) / 1e9, 2),
                    "parallelism": "replicas x%d" % world if world > 1 else "single GPU",
                    "l2": "working set per step >> 129 MB L2 (inputs 110 MB + 2 GB wave stack per batch); no flush"},
-        "e2e": {"value": world * n_pos / (e2e_ms / 1000.0), "unit": "positions/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": replica_throughput(n_pos, world, e2e_ms), "unit": "positions/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "streamed_patterns": {"value": world * n_pos / (streamed_ms / 1000.0), "unit": "positions/s",
+        "streamed_patterns": {"value": replica_throughput(n_pos, world, streamed_ms), "unit": "positions/s",
                               "ms_per_step": streamed_ms, "host_read_bytes_per_step": int(meas_h.numel() * 4),
                               "note": "measured patterns read in place from pinned host memory"},
         "roofline": {"bound": "hbm", "kernel": "fused_multislice", "achieved": achieved, "peak": hbm_peak,
