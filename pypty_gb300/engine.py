@@ -93,8 +93,11 @@ class Engine:
         self.device = torch.device(device if device is not None else "cuda")
         self._ws = None
         self._aux = {}
-        self._stage = None
-        self._stage_event = None
+        # two page-locked geometry buffers used in turn, each with the event of the call that
+        # last read it: the host fills one while the GPU may still run the previous call
+        self._stages = [None, None]
+        self._stage_events = [None, None]
+        self._stage_i = 0
 
     # ---------------------------------------------------------------- buffers
     def workspace(self, nbytes: int) -> torch.Tensor:
@@ -111,27 +114,35 @@ class Engine:
             buf = self._aux[key] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
         return buf
 
-    def _staging(self, geo: Geometry):
-        """Page-locked copies of the geometry (the C ABI uploads them asynchronously)."""
+    def _staging(self, geo: Geometry, stream):
+        """Page-locked copies of the geometry (the C ABI uploads them asynchronously). The call
+        is also ordered on `stream` after the previous call (which may have run on another stream):
+        the workspace is shared."""
         need = geo.positions.nbytes + geo.pos_correction.nbytes + geo.sequence.nbytes + 64
-        if self._stage_event is not None:
-            self._stage_event.synchronize()     # the previous upload has left the buffer
-        if self._stage is None or self._stage.numel() < need:
-            self._stage = torch.empty(need, dtype=torch.uint8, pin_memory=True)
-        buf = self._stage.numpy()
+        self._stage_i ^= 1
+        i = self._stage_i
+        if self._stage_events[i ^ 1] is not None:
+            stream.wait_event(self._stage_events[i ^ 1])
+        if self._stage_events[i] is not None:
+            self._stage_events[i].synchronize()     # the call before last has read this buffer
+        if self._stages[i] is None or self._stages[i].numel() < need:
+            self._stages[i] = torch.empty(need, dtype=torch.uint8, pin_memory=True)
+        stage = self._stages[i]
+        buf = stage.numpy()
         o = 0
         ptrs = []
         for arr in (geo.positions, geo.pos_correction, geo.sequence):
             n = arr.nbytes
             buf[o:o + n] = arr.view(np.uint8).reshape(-1)
-            ptrs.append(self._stage.data_ptr() + o)
+            ptrs.append(stage.data_ptr() + o)
             o += (n + 15) // 16 * 16
         return ptrs
 
     def _mark_staging(self, stream):
-        if self._stage_event is None:
-            self._stage_event = torch.cuda.Event()
-        self._stage_event.record(stream)
+        i = self._stage_i
+        if self._stage_events[i] is None:
+            self._stage_events[i] = torch.cuda.Event()
+        self._stage_events[i].record(stream)
 
     # ---------------------------------------------------------------- calls
     def loss_and_direction(self, problem: _lib.Problem, obj: torch.Tensor, probe: torch.Tensor,
@@ -150,7 +161,7 @@ class Engine:
                    torch.empty((problem.n_positions, 2), dtype=torch.float32, device=self.device))
         loss_sse, og, pg, posg = out
         ws = self.workspace(_lib.workspace_bytes(problem))
-        pp, pc, ps = self._staging(geo)
+        pp, pc, ps = self._staging(geo, stream)
         if pos_correction is not None:
             if (not pos_correction.is_cuda or pos_correction.dtype != torch.float32
                     or tuple(pos_correction.shape) != (problem.n_positions, 2)
@@ -179,7 +190,7 @@ class Engine:
         out = (torch.empty(2, dtype=torch.float64, device=self.device), torch.empty_like(obj),
                torch.empty_like(probe), torch.zeros((problem.n_positions, 2), dtype=torch.float32, device=self.device))
         loss_sse, og, pg, posg = out
-        pp, pc, ps = self._staging(geo)
+        pp, pc, ps = self._staging(geo, stream)
         st = _lib.lib().pty_loss_and_direction_layered(
             ctypes.byref(problem), eid, _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured), _ptr(loss_sse),
             _ptr(og), _ptr(pg), _ptr(posg), _ptr(ws), ws.numel(), stream.cuda_stream)
@@ -322,7 +333,7 @@ class Engine:
         loss_sse = torch.empty(2, dtype=torch.float64, device=self.device)
         og, pg = torch.empty_like(obj), torch.empty_like(probe)
         posg = torch.zeros((problem.n_positions, 2), dtype=torch.float32, device=self.device)
-        pp, pc, ps = self._staging(geo)
+        pp, pc, ps = self._staging(geo, stream)
         if pos_correction is not None:
             if (not pos_correction.is_cuda or pos_correction.dtype != torch.float32
                     or tuple(pos_correction.shape) != (problem.n_positions, 2)
@@ -346,7 +357,7 @@ class Engine:
         self._check_inputs(problem, obj, probe, measured)
         ws = torch.empty(max(_lib.split_workspace_bytes(problem), 256), dtype=torch.uint8, device=self.device)
         loss_sse = torch.empty(2, dtype=torch.float64, device=self.device)
-        pp, pc, ps = self._staging(geo)
+        pp, pc, ps = self._staging(geo, stream)
         st = _lib.lib().pty_forward(ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps, _ptr(measured),
                                     _ptr(loss_sse), _ptr(ws), ws.numel(), stream.cuda_stream)
         self._mark_staging(stream)
@@ -377,7 +388,7 @@ class Engine:
         if out is None:
             out = torch.empty((problem.n_sequence, W, W), dtype=torch.float32, device=self.device)
         ws = self.workspace(_lib.workspace_bytes(problem))
-        pp, pc, ps = self._staging(geo)
+        pp, pc, ps = self._staging(geo, stream)
         st = _lib.lib().pty_simulate_patterns(ctypes.byref(problem), _ptr(obj), _ptr(probe), pp, pc, ps,
                                               _ptr(out), _ptr(ws), ws.numel(), stream.cuda_stream)
         self._mark_staging(stream)
