@@ -213,6 +213,36 @@ __global__ void __launch_bounds__(512, 1) fft2_batch256_kernel(const float2* __r
   }
 }
 
+// ------------------------------------------------------------------ layered steps, 256
+// One propagation step (P given, one table per group of nper windows, tab_stride apart) or,
+// with rtab, one band limit by a real mask, of a batch of natural-layout 256-px windows in
+// place: the folded butterfly-table-butterfly exchange of the fused kernel.   4 blocks / window
+__global__ void __launch_bounds__(512, 1) layered_step256_kernel(float2* x, const float2* __restrict__ tab,
+                                                                size_t tab_stride, int nper, int conj, float scale,
+                                                                const float* __restrict__ rtab,
+                                                                const float2* __restrict__ g_tw) {
+  using G = Geo256;
+  extern __shared__ __align__(16) unsigned char smem[];
+  Carve256 s(smem);
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank(), t = threadIdx.x;
+  const size_t w = blockIdx.x / 4;
+  float2* win = x + w * 65536;
+  load_twiddles<128>(s.tw1, s.tw2, g_tw);
+  load_tw256(s.tw256);
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = win[G::ry(c, t) * 256 + G::rx(c, t, i)];
+  __syncthreads();
+  // the cluster barriers inside the transforms order every block's reads before any write
+  if (rtab)
+    WinFFT256::band_limit(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl, rtab);
+  else
+    WinFFT256::propagate(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl, tab + (w / nper) * tab_stride, conj != 0, scale);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) win[G::ry(c, t) * 256 + G::rx(c, t, i)] = v[i];
+}
+
 // ------------------------------------------------------------------ fused multislice, 256
 // One cluster of 4 blocks per position; modes one after another (forward: k = m*Mp + p
 // ascending; adjoint: probe mode outer, object mode inner). Extra buffers (FusedArgs): psi

@@ -1115,7 +1115,7 @@ struct Run {
   }
   bool tw_built = false;
 
-  // the FP32 engine's twiddle tables for 64 / 128 px windows, built once per call
+  // the FP32 engine's twiddle tables (the 128-point ones for 256 px windows), built once per call
   float2* fp32_twiddles() {
     float2* tw = at<float2>(ws, q.o_dft);
     if (!tw_built) {
@@ -1149,6 +1149,8 @@ struct Run {
   // x <- IFFT(FFT(x) * mask) for nwin windows (the band limit, objective.py:436-441,
   // multislice_core.py:189-191), in one pass on the FP32 engine for 64 / 128 px windows
   int band_limit(float2* x, float2* tmp, long long nwin) {
+    if (q.engine == PTY_DFT_FP32_FFT && q.W == 256) return layered_step256(x, nwin, nullptr, 0, 1, 0, 1.0f, ta.mask_sc,
+                                                                             fp32_twiddles(), st);
     if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
       float2* tw = fp32_twiddles();
       prof_mark(st, KID_FFT2);
@@ -1178,6 +1180,9 @@ struct Run {
   int prop_step(float2* psi, float2* psi2, long long nwin, const float2* tab, size_t tab_stride, int nper,
                 int conj, bool folded, bool keep_g = false) {
     const float WWf = (float)q.WW;
+    if (q.engine == PTY_DFT_FP32_FFT && q.W == 256 && !keep_g)   // the folded cluster exchange
+      return layered_step256(psi, nwin, tab, tab_stride, nper, conj, folded ? 1.0f : 1.0f / WWf, nullptr,
+                             fp32_twiddles(), st);
     if (q.engine == PTY_DFT_FP32_FFT && q.W <= 128) {
       float2* tw = fp32_twiddles();
       prof_mark(st, KID_FFT2);
@@ -1438,7 +1443,16 @@ struct Run {
         }
         prof_mark(st, KID_FUSED);
         fwd_slice_kernel<<<grid(nm, Bn), EB, 0, st>>>(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp, q.Mo, WW);
-        if (z < q.Z - 1) {   // the other engines: separate transforms
+        if (z < q.Z - 1 && !(v && q.inside_grad)) {   // 256 px or the tensor-core engines
+          if (tilted_prop && q.per_step) pos_props(z);
+          const bool edge = z == 0 && ta.use_edge;
+          if (tilted_prop)
+            rc = prop_step(psi, psi2, (long long)Bn * nm, edge ? pprop_edge : pprop, WWs, nm, 0, false);
+          else
+            rc = prop_step(psi, psi2, (long long)Bn * nm,
+                           q.per_step ? steps + (size_t)z * WWs : (edge ? ta.prop_edge : ta.prop), 0, 1, 0, true);
+          if (rc) return rc;
+        } else if (z < q.Z - 1) {   // separate transforms that keep the step's spectrum
           if ((rc = dft(psi, psi2, (long long)Bn * nm, 0))) return rc;
           if (v && q.inside_grad &&   // FFT(psi O) of the step, for the inside-tilt gradient
               cudaMemcpyAsync(spec + z * spec_stride, psi2, (size_t)Bn * nm * WWs * sizeof(float2),

@@ -268,6 +268,16 @@ int run_backward<256>(const pty_problem_t* p, const Plan& q, double* loss_sse, f
   return P.finalize(loss_sse, object_grad, probe_grad, pos_grad, true);
 }
 
+// one-pass propagation step / band limit of the layered path's 256-px windows (in place)
+int layered_step256(float2* x, long long nwin, const float2* tab, size_t tab_stride, int nper, int conj, float scale,
+                    const float* rtab, const float2* tw, cudaStream_t st) {
+  if (set_smem(layered_step256_kernel, Smem256::small)) return PTY_ERR_CUDA;
+  prof_mark(st, KID_FFT2);
+  const int rc = launch4(layered_step256_kernel, (unsigned)nwin, Smem256::small, st, x, tab, tab_stride, nper, conj,
+                         scale, rtab, tw);
+  return rc ? rc : cuda_status();
+}
+
 template <>
 int run_fft2<256>(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
                   int build_tw) {

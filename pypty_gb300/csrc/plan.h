@@ -257,6 +257,12 @@ int run_ms_grads(const MsPlan& q, const float2* d_exit, const float2* waves, con
 template <int W>
 int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, cudaStream_t st);
 
+// one-pass propagation step (tab, tab_stride apart per group of nper windows, conj, scale) or
+// band limit (rtab: real mask, unscaled; scale folds the inverse's 1/W^2) of nwin natural 256-px
+// windows in place; tw holds the 128-point twiddle tables
+int layered_step256(float2* x, long long nwin, const float2* tab, size_t tab_stride, int nper, int conj, float scale,
+                    const float* rtab, const float2* tw, cudaStream_t st);
+
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
              int build_tw = 1);   // build_tw = 0: tw already holds this window's twiddles

@@ -181,6 +181,22 @@ struct WinFFT256 {
     twiddle(v, tw256, c, true);
     WinFFT<128>::inverse(v, xbuf, tw1, tw2);
   }
+
+  // x <- IFFT(FFT(x) * P * scale) (conj: conj(P)) for a (256, 256) table P in natural (ky, kx)
+  // order, in the same single folded exchange
+  static __device__ __forceinline__ void propagate(float2 (&v)[32], float2* xbuf, const float2* tw1,
+                                                   const float2* tw2, const float2* tw256, cg256::cluster_group& cl,
+                                                   const float2* __restrict__ P, bool conj, float scale) {
+    const int c = (int)cl.block_rank();
+    const int t = threadIdx.x;
+    WinFFT<128>::forward(v, xbuf, tw1, tw2);
+    twiddle(v, tw256, c, false);
+    cross_propagate(v, xbuf, cl, c, conj, [&](int i, int q) {
+      return cscale(P[(G::fky(t, i) + 128 * (q >> 1)) * 256 + G::fkx(t, i) + 128 * (q & 1)], scale);
+    });
+    twiddle(v, tw256, c, true);
+    WinFFT<128>::inverse(v, xbuf, tw1, tw2);
+  }
 };
 
 }  // namespace pty
