@@ -243,6 +243,42 @@ __global__ void __launch_bounds__(512, 1) layered_step256_kernel(float2* x, cons
   for (int i = 0; i < 32; ++i) win[G::ry(c, t) * 256 + G::rx(c, t, i)] = v[i];
 }
 
+// One forward multislice step of the layered path for 256-px windows (multislice_core.py:61-80)
+// in one pass: in = z == 0 ? the incoming probe (mode p) : psi; stack = conj(in);
+// psi = IFFT(FFT(in * O[b][z][m]) * P) with the folded exchange.   4 blocks / window
+__global__ void __launch_bounds__(512, 1) layered_fwd256_kernel(const float2* __restrict__ pin, size_t pin_stride,
+                                                               float2* psi, float2* __restrict__ stack,
+                                                               const float2* __restrict__ ob, int z, int Z, int Mp,
+                                                               int Mo, const float2* __restrict__ tab,
+                                                               size_t tab_stride, float scale,
+                                                               const float2* __restrict__ g_tw) {
+  using G = Geo256;
+  extern __shared__ __align__(16) unsigned char smem[];
+  Carve256 s(smem);
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank(), t = threadIdx.x;
+  const size_t WW = 65536;
+  const int nm = Mp * Mo, wi = blockIdx.x / 4, b = wi / nm, pm = wi % nm, p = pm / Mo, m = pm % Mo;
+  const float2* src = z == 0 ? pin + (size_t)b * pin_stride + (size_t)p * WW : psi + (size_t)wi * WW;
+  float2* stw = stack + (((size_t)b * Z + z) * nm + pm) * WW;
+  const float2* o = ob + (((size_t)b * Z + z) * Mo + m) * WW;
+  load_twiddles<128>(s.tw1, s.tw2, g_tw);
+  load_tw256(s.tw256);
+  float2 v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int u = G::ry(c, t) * 256 + G::rx(c, t, i);
+    const float2 in = src[u];
+    stw[u] = cconj(in);
+    v[i] = cmul(in, o[u]);
+  }
+  __syncthreads();
+  WinFFT256::propagate(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl, tab + (size_t)b * tab_stride, false, scale);
+  float2* dst = psi + (size_t)wi * WW;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[G::ry(c, t) * 256 + G::rx(c, t, i)] = v[i];
+}
+
 // ------------------------------------------------------------------ fused multislice, 256
 // One cluster of 4 blocks per position; modes one after another (forward: k = m*Mp + p
 // ascending; adjoint: probe mode outer, object mode inner). Extra buffers (FusedArgs): psi

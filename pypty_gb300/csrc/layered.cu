@@ -1131,6 +1131,8 @@ struct Run {
   int fwd_prop(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Bn,
                const float2* tab, size_t tab_stride, float scale, float2* spec_out) {
     float2* tw = fp32_twiddles();
+    if (q.W == 256)
+      return layered_fwd256(pin, pin_stride, psi, stack, ob, z, q.Z, q.Mp, q.Mo, Bn, tab, tab_stride, scale, tw, st);
     prof_mark(st, KID_FUSED);
     const unsigned nwin = (unsigned)(Bn * q.Mp * q.Mo);
     if (q.W == 64) {
@@ -1426,7 +1428,8 @@ struct Run {
         pin_stride = (size_t)q.Mp * WWs;
       }
       // forward multislice (multislice_core.py:61-82)
-      const bool one_pass = q.engine == PTY_DFT_FP32_FFT && W <= 128;
+      // one-pass forward steps: the FP32 engine (at 256 px only where no step spectrum is kept)
+      const bool one_pass = q.engine == PTY_DFT_FP32_FFT && !(W == 256 && v && q.inside_grad);
       for (int z = 0; z < q.Z; ++z) {
         if (z < q.Z - 1 && one_pass) {
           // slice, stack and propagation in one pass (multislice_core.py:61-80); FFT(psi O) kept

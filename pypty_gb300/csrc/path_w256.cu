@@ -278,6 +278,17 @@ int layered_step256(float2* x, long long nwin, const float2* tab, size_t tab_str
   return rc ? rc : cuda_status();
 }
 
+// one-pass forward step of the layered path's 256-px windows
+int layered_fwd256(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Z,
+                   int Mp, int Mo, int Bn, const float2* tab, size_t tab_stride, float scale, const float2* tw,
+                   cudaStream_t st) {
+  if (set_smem(layered_fwd256_kernel, Smem256::small)) return PTY_ERR_CUDA;
+  prof_mark(st, KID_FUSED);
+  const int rc = launch4(layered_fwd256_kernel, (unsigned)(Bn * Mp * Mo), Smem256::small, st, pin, pin_stride, psi,
+                         stack, ob, z, Z, Mp, Mo, tab, tab_stride, scale, tw);
+  return rc ? rc : cuda_status();
+}
+
 template <>
 int run_fft2<256>(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
                   int build_tw) {

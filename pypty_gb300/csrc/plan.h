@@ -262,6 +262,10 @@ int run_scatteradd(const MsPlan& q, float2* full, const float2* chop, void* ws, 
 // windows in place; tw holds the 128-point twiddle tables
 int layered_step256(float2* x, long long nwin, const float2* tab, size_t tab_stride, int nper, int conj, float scale,
                     const float* rtab, const float2* tw, cudaStream_t st);
+// one-pass forward step (slice, stack, propagation) of Bn positions' 256-px windows
+int layered_fwd256(const float2* pin, size_t pin_stride, float2* psi, float2* stack, const float2* ob, int z, int Z,
+                   int Mp, int Mo, int Bn, const float2* tab, size_t tab_stride, float scale, const float2* tw,
+                   cudaStream_t st);
 
 template <int W>
 int run_fft2(const float2* in, float2* out, int batch, int inverse, int shift, float2* tw, cudaStream_t st,
