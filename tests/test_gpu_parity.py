@@ -243,3 +243,44 @@ def test_empty_sequence_gives_zero_loss_and_gradients():
     assert res[0] == 0.0 and res[1] == 0.0
     assert not np.any(res[2]) and not np.any(res[3]) and not np.any(res[4])
     assert res[2].shape == c["obj"].shape and res[4].shape == c["pos_correction"].shape
+
+
+@pytest.mark.parametrize("W", [64, 128, 256])
+def test_windows_at_object_edges(engine, W):
+    """Windows that touch every edge of a non-square object (first and last valid row and
+    column), in a ragged last batch, against the FP64 oracle."""
+    from gpu_helpers import run_gpu
+    from oracle import ptycho_oracle as orc
+    from pypty_gb300 import synth
+    rng = np.random.default_rng(W + 11)
+    px, kV, Z, Mp = 0.1, 300.0, 3, 2
+    ny, nx = W + 20, W + 37
+    truth = synth.gaussian_phase_object(ny, nx, Z, 40, 0.3, px, 0.2, 1.0, rng)
+    probe = synth.make_probe(W, px, kV, 30.0, 50.0, Mp, 0.5 ** np.arange(Mp), 1e5)
+    ipos = np.array([[0, 0], [0, nx - W], [ny - W, 0], [ny - W, nx - W], [7, 13]], np.int32)
+    corr = rng.uniform(-0.5, 0.5, ipos.shape).astype(np.float32)
+    seq = np.array([3, 0, 4, 1, 2])
+    lam = synth.wavelength_A(kV)
+    sim = orc.loss_and_direction(truth, probe, ipos, corr, 2.0, 1.0, None, "ml", lam, 1, 1, 1, px, px,
+                                 2 / 3, 0.0, seq, 1, 2, simulate=True)
+    meas = synth.poisson_patterns(sim, 1.0, rng)
+    obj0 = np.exp(0.6j * np.angle(truth)).astype(np.complex64)
+    c = dict(obj=obj0, probe=probe, positions=ipos, pos_correction=corr, sequence=seq, measured=meas,
+             algorithm="ml", wavelength=lam, px=px, cutoff=2 / 3, rolloff=0.0, distance=2.0,
+             edge_mult=1.0, loss_weight=1, batch=2, step_obj=1, step_probe=1, step_pos=1)
+    ref = orc.loss_and_direction(obj0.astype(np.complex128), probe.astype(np.complex128), ipos,
+                                 corr.astype(np.float64), 2.0, 1.0, meas.astype(np.float64), "ml", lam,
+                                 1, 1, 1, px, px, 2 / 3, 0.0, seq, 1, 2, float_dtype=np.float64,
+                                 complex_dtype=np.complex128)
+    # the same computation in complex64 on the CPU: its distance from FP64 is the floor that
+    # single precision sets for these inputs (at 256 px about 1e-4 for the object and probe
+    # gradients); the GPU result stays within 1e-4 or three times that floor
+    r32 = orc.loss_and_direction(obj0, probe.astype(np.complex64), ipos, corr, 2.0, 1.0, meas.astype(np.float32),
+                                 "ml", lam, 1, 1, 1, px, px, 2 / 3, 0.0, seq, 1, 2, float_dtype=np.float32,
+                                 complex_dtype=np.complex64)
+    loss, sse, og, pg, posg = run_gpu(c, engine=engine)
+    assert abs(loss - ref[0]) <= LOSS_TOL * abs(ref[0])
+    for k, g in ((2, og), (3, pg), (4, posg)):
+        assert rel_l2(g, ref[k]) <= max(GRAD_TOL, 3 * rel_l2(r32[k], ref[k])), (k, rel_l2(g, ref[k]))
+    # the object gradient reaches the last row and column
+    assert np.abs(og[-1]).max() > 0 and np.abs(og[:, -1]).max() > 0
