@@ -206,7 +206,8 @@ def test_unet_gradients_match_torch_autograd(levels, base, size, out_ch, batch):
     out = F.conv2d(h, wo[:, :, None, None], bo)
     lref = ((out - t) ** 2).mean()
     lref.backward()
-    assert abs(float(loss) - float(lref)) <= 5e-2 * float(lref)
+    lref = float(lref.detach())
+    assert abs(float(loss) - lref) <= 5e-2 * lref
     assert rel_l2(net.gwout.cpu().numpy(), wo.grad.numpy()) <= 5e-2
     errs = [rel_l2(c.gw.cpu().numpy(), w.grad.numpy()) for c, w, b in params]
     print("layer weight-gradient errors:", ["%.1e" % e for e in errs])
