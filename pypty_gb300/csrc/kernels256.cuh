@@ -167,14 +167,18 @@ __global__ void __launch_bounds__(512, 1) probe_final256_kernel(const float2* __
   load_twiddles<128>(s.tw1, s.tw2, g_tw);
   load_tw256(s.tw256);
   __syncthreads();
+  // chunks outer, elements inner: each chunk's 32 loads are in flight together (the chunk
+  // order of every element's sum is unchanged)
   float2 v[32];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    float2 acc = make_float2(0.f, 0.f);
-    for (int ch = 0; ch < nchunk; ++ch)
-      acc = cadd(acc, partial[((size_t)ch * Mp + p) * 65536 + c * G::PART + nidx<128>(i, t)]);
-    v[i] = cscale(acc, mask_sc[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
+  for (int i = 0; i < 32; ++i) v[i] = make_float2(0.f, 0.f);
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const float2* src = partial + ((size_t)ch * Mp + p) * 65536 + c * G::PART;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = cadd(v[i], src[nidx<128>(i, t)]);
   }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], mask_sc[G::fky(c, t, i) * 256 + G::fkx(c, t, i)]);
   WinFFT256::inverse(v, s.xbuf, s.tw1, s.tw2, s.tw256, cl);
 #pragma unroll
   for (int i = 0; i < 32; ++i) probe_grad[(size_t)(G::ry(c, t) * 256 + G::rx(c, t, i)) * Mp + p] = v[i];

@@ -966,13 +966,18 @@ __global__ void __launch_bounds__(Geo<W>::T) probe_final_kernel(const float2* __
   __syncthreads();
   const int t = threadIdx.x, p = blockIdx.x;
   const size_t WW = (size_t)W * W;
+  // chunks outer, elements inner: each chunk's 32 loads are independent and in flight
+  // together (the chunk order of every element's sum is unchanged)
   float2 v[32];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    float2 s = make_float2(0.f, 0.f);
-    for (int c = 0; c < nchunk; ++c) s = cadd(s, partial[((size_t)c * Mp + p) * WW + nidx<W>(i, t)]);
-    v[i] = cscale(s, mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
+  for (int i = 0; i < 32; ++i) v[i] = make_float2(0.f, 0.f);
+  for (int c = 0; c < nchunk; ++c) {
+    const float2* src = partial + ((size_t)c * Mp + p) * WW;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = cadd(v[i], src[nidx<W>(i, t)]);
   }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = cscale(v[i], mask_sc[G::fky(t, i) * W + G::fkx(t, i)]);
   WinFFT<W>::inverse(v, xbuf, tw1, tw2);
 #pragma unroll
   for (int i = 0; i < 32; ++i) probe_grad[(size_t)(G::ry(t) * W + G::rx(t, i)) * Mp + p] = v[i];
