@@ -917,7 +917,31 @@ static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const
     }
     __syncthreads();
     const int jn = min(256, n - j0);
-    for (int j = 0; j < jn; ++j) {
+    int j = 0;
+    // groups of four windows: all their loads first, then the adds in window order (the
+    // same order and the same skipped pixels as one window at a time)
+    for (; j + 4 <= jn; j += 4) {
+      float2 val[4][4];
+      bool ok[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int ox = x - s_x[j + u];
+        const bool inx = (unsigned)ox < (unsigned)W;
+        const float2* src = gw + ((size_t)s_b[j + u] * zm + k) * WW + (inx ? ox : 0);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int oy = ty0 + ly + 8 * r - s_y[j + u];
+          ok[u][r] = inx && (unsigned)oy < (unsigned)W;
+          val[u][r] = ok[u][r] ? src[(size_t)oy * W] : make_float2(0.f, 0.f);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          if (ok[u][r]) acc[r] = cadd(acc[r], val[u][r]);
+    }
+    for (; j < jn; ++j) {
       const int b = s_b[j];
       const int ox = x - s_x[j];
       if ((unsigned)ox >= (unsigned)W) continue;
