@@ -15,8 +15,10 @@ evaluated at a half-phase start, so no step is skipped or cached.
 `streamed_patterns` positions/s with the measured patterns left in pinned host memory and
           read in place by the kernels (a dataset larger than HBM), object and probe in HBM.
 `roofline` the dominant kernel (fused_multislice) timed live with CUDA events on its
-          stream; algorithmic bytes per launch: the per-position figure of the fused
-          kernel's traffic (fused_bytes_per_position below) times the positions per launch.
+          stream; algorithmic bytes per launch: the path's algorithmic bytes per position
+          W^2 (32 Z Mo + 16 Z Mp Mo + 4) (alg_bytes_per_position below: object windows read
+          forward and adjoint, gradient read-modify-write, wave stack write + read, measured
+          pattern read) times the positions per launch.
 
 The working set of a step (object 42 MB, patterns 67 MB, per-batch wave stack 2 GB) is
 far larger than the 129 MB L2, so no explicit L2 flush is needed between steps.
@@ -135,6 +137,21 @@ def build_workload(cfg, seed=0):
     obj0 = np.exp(0.5j * np.angle(truth)).astype(np.complex64)
     return dict(truth=truth, obj0=obj0, probe=probe, ipos=ipos, corr=corr, px=px, kV=kV, dz=dz, dose=dose,
                 wavelength=synth.wavelength_A(kV), rng=rng)
+
+
+def simulate_measured(eng, prob, wl, geo):
+    """Measured patterns of a workload: the library's forward model at the true specimen
+    (float32 mean-over-modes intensities, detector order) plus Poisson noise drawn on the
+    device with a generator seeded 1. Returns a (N, W, W) float32 CUDA tensor."""
+    import torch
+    dev = eng.device
+    truth_d = torch.from_numpy(wl["truth"]).to(dev)
+    probe_d = torch.from_numpy(wl["probe"]).to(dev)
+    sim = eng.simulate(prob, truth_d, probe_d, geo)
+    gen = torch.Generator(device=dev).manual_seed(1)
+    meas_d = torch.poisson(sim.clamp_min(0), generator=gen).contiguous()
+    del truth_d, sim
+    return meas_d
 
 
 class ClockSampler:
@@ -535,13 +552,8 @@ def main():
     common = dict(algorithm=cfg["algorithm"], wavelength=wl["wavelength"], pixel_size_x=wl["px"],
                   pixel_size_y=wl["px"], slice_distance=wl["dz"], compute_batch=cfg["batch"])
     prob = make_problem(W, wl["obj0"].shape, Mp, geo, step_pos=True, checkpoint_every=args.checkpoint, **common)
-    # measured data: forward model at the true specimen + Poisson noise
-    truth_d = torch.from_numpy(wl["truth"]).to(dev)
+    meas_d = simulate_measured(eng, prob, wl, geo)
     probe_d = torch.from_numpy(wl["probe"]).to(dev)
-    sim = eng.simulate(prob, truth_d, probe_d, geo)
-    gen = torch.Generator(device=dev).manual_seed(1)
-    meas_d = torch.poisson(sim.clamp_min(0), generator=gen).contiguous()
-    del truth_d, sim
     obj_d = torch.from_numpy(wl["obj0"]).to(dev)
     out = (torch.empty(2, dtype=torch.float64, device=dev), torch.empty_like(obj_d), torch.empty_like(probe_d),
            torch.empty((n_pos, 2), dtype=torch.float32, device=dev))
@@ -655,8 +667,8 @@ def main():
     fused_n = max(prof.launches.get("fused_multislice", 0), 1)
     fused_avg_s = fused_ms / fused_n / 1000.0
     per_launch_pos = n_pos / (fused_n / args.steps)
-    fused_bytes = fused_bytes_per_position(W, Z, Mp) * per_launch_pos
-    achieved = fused_bytes / fused_avg_s / 1e9
+    launch_bytes = alg_bytes_per_position(W, Z, Mp) * per_launch_pos
+    achieved = launch_bytes / fused_avg_s / 1e9
     path_bytes = alg_bytes_per_position(W, Z, Mp) * n_pos
     total_prof_ms = sum(prof.ms.values())
     kernel_share = {k: round(v / total_prof_ms, 4) for k, v in sorted(prof.ms.items(), key=lambda kv: -kv[1])
@@ -682,7 +694,10 @@ def main():
                                  if (W, Z, Mp) in TRAFFIC_PER_POSITION else None),
                      "traffic_source": "ncu dram bytes of a 64-position capture of the same shape, scaled by "
                                        "positions per launch (profiles/)",
-                     "alg_bytes_per_launch": fused_bytes, "avg_launch_ms": fused_avg_s * 1e3,
+                     "alg_bytes_per_launch": launch_bytes,
+                     "alg_bytes_per_position": alg_bytes_per_position(W, Z, Mp),
+                     "kernel_bytes_per_position": fused_bytes_per_position(W, Z, Mp),
+                     "avg_launch_ms": fused_avg_s * 1e3,
                      "timing": "CUDA events around each launch in a second pass of the same steps with the "
                                "launch profiler on (launches serialised on one stream: kernels %.2f ms per step "
                                "there; %.2f ms per step in the timed region, where batches overlap on three "

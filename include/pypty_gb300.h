@@ -319,6 +319,9 @@ typedef struct pty_variant {
      the sequence (after a tilt after the specimen), as data_simulation_exitwave saves it
      (pypty/objective.py:289-291, 518-520) */
   void* exit_waves;
+  /* the tilt rows of tilts_host in DEVICE memory instead (n_tilts rows of 6 float32), or
+     NULL: an optimizer's trial tilts stay on the device. When set, tilts_host is not read. */
+  const float* tilts_device;
 } pty_variant_t;
 
 int pty_variants_workspace_bytes(const pty_problem_t* problem, const pty_variant_t* variant, size_t* bytes);

@@ -70,7 +70,8 @@ class Variant(ctypes.Structure):
                 ("upsample_pattern", ctypes.c_int32), ("static_background", ctypes.c_void_p),
                 ("step_static_background", ctypes.c_int32), ("static_background_grad", ctypes.c_void_p),
                 ("defocus_per_position", ctypes.c_void_p), ("n_probe_scenarios", ctypes.c_int32),
-                ("probe_marker", ctypes.c_void_p), ("exit_waves", ctypes.c_void_p)]
+                ("probe_marker", ctypes.c_void_p), ("exit_waves", ctypes.c_void_p),
+                ("tilts_device", ctypes.c_void_p)]
 
 
 class PtyError(RuntimeError):

@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], drain_bar[2];
   __shared__ uint32_t tmem_base;
+  __shared__ int s_abort;   // a bounded wait ran out somewhere in the CTA: issue nothing more
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // the N tiles of one row tile are adjacent in the grid: the second read of A hits L2
   const long long row0 = (long long)blockIdx.y * BM;
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     mbar_init(&drain_bar[0], 1);
     mbar_init(&drain_bar[1], 1);
+    s_abort = 0;
     fence_async_shared();
   }
   if (warp == 0) umma::tmem_alloc(&tmem_base, C::TMEM_COLS);
@@ -129,8 +131,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   for (int j = 0; j < HALF; ++j) acc[j] = 0.0f;
   // add the partial product of K block kc (TMEM buffer kc & 1) to the registers: FP32 adds with
   // round-to-nearest, so the tensor core's accumulation runs over one K block only
+  int drained = -1;   // last K block drained
   auto drain = [&](int kc) {
     const int buf = kc & 1;
+    drained = kc;
     mbar_wait(&drain_bar[buf], drain_par[buf], &e);
     umma::fence_after_sync();
 #pragma unroll
@@ -165,17 +169,25 @@ __global__ void __launch_bounds__(THREADS, 1)
   };
   load_a(0);
 
+  // Failure handling: every wait is bounded; a thread whose wait ran out sets s_abort, which the
+  // whole CTA reads after the next barrier (uniformly) and then stops issuing copies and MMAs.
+  // Thread 0 tracks what it has in flight (bulk copies not yet waited for, MMAs of the previous
+  // K block not yet drained) and waits for those, again bounded, before TMEM is freed.
+  bool copy_pending[STAGES] = {false, false};   // thread 0 only
+  int committed = -1;                           // thread 0: last K block whose MMAs were committed
+  bool aborted = false;
   for (int kc = 0; kc < C::KC; ++kc) {
     const int s = kc % STAGES;
     uint8_t* sA = base + s * C::STAGE;            // S terms of A, then S terms of B
     uint8_t* sB = sA + S * C::A_BYTES;
     if (kc >= STAGES) mbar_wait(&empty_bar[s], empty_par[s], &e);   // the MMAs of kc - STAGES are done
-    if (tid == 0) {
+    if (tid == 0 && !e) {
       mbar_expect_tx(&full_bar[s], S * C::B_BYTES);
 #pragma unroll
       for (int term = 0; term < S; ++term)
         bulk_copy_g2s(sB + term * C::B_BYTES, img_nt + term * TERM + (size_t)kc * C::B_BYTES, C::B_BYTES,
                       &full_bar[s]);
+      copy_pending[s] = true;
     }
 #pragma unroll
     for (int i = 0; i < APT; ++i) {
@@ -199,11 +211,23 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
     }
     if (kc + 1 < C::KC) load_a(kc + 1);
+    if (e) s_abort = 1;
     fence_async_shared();
     umma::fence_before_sync();
     __syncthreads();   // A is written; every thread has drained TMEM buffer kc & 1 (block kc - 2)
+    if (s_abort) {     // uniform: every write of s_abort precedes this barrier
+      aborted = true;
+      break;
+    }
     if (tid == 0) {
       mbar_wait(&full_bar[s], full_par[s], &e);
+      if (e) {
+        s_abort = 1;   // the copy may still be in flight: waited for below; no MMA of this block
+      } else {
+        copy_pending[s] = false;
+      }
+    }
+    if (tid == 0 && !e) {
       umma::fence_after_sync();
       const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
       const uint32_t d = tmem + (uint32_t)((kc & 1) * C::ACCS * C::BN);
@@ -224,23 +248,42 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       umma::mma_commit(&empty_bar[s]);
       umma::mma_commit(&drain_bar[kc & 1]);
+      committed = kc;
     }
+    // block kc - 1's MMAs were committed: thread 0's wait of iteration kc - 1 succeeded, or the
+    // CTA would have stopped at this iteration's barrier
     if (kc > 0) drain(kc - 1);   // overlaps the MMAs of block kc
   }
-  drain(C::KC - 1);
-  // epilogue: out[window][k][row in window] = scale * acc (transposed, coalesced over rows)
+  if (!aborted) {
+    if (e) s_abort = 1;
+    __syncthreads();
+    aborted = s_abort != 0;   // thread 0 may have failed in the last iteration
+    if (!aborted) drain(C::KC - 1);
+  }
+  if (aborted && tid == 0) {
+    // let this CTA's own copies and MMAs finish (bounded) before TMEM and shared memory go
+    int e2 = 0;
+    for (int st = 0; st < STAGES; ++st)
+      if (copy_pending[st]) mbar_wait(&full_bar[st], full_par[st], &e2);
+    if (committed > drained) mbar_wait(&drain_bar[committed & 1], drain_par[committed & 1], &e2);
+  }
+  // epilogue: out[window][k][row in window] = scale * acc (transposed, coalesced over rows); NaN
+  // when the CTA stopped early, so that a failed transform cannot pass for a result
   const long long row = row0 + 32 * q + lane;
   const long long win = row / W;
   const int r = (int)(row % W);
   if (row < n_rows) {
     float2* o = out + win * (long long)W * W + r;
     const int k0 = (nt * C::BN + h * HALF) >> 1;
+    const float nan = __int_as_float(0x7fc00000);
 #pragma unroll
-    for (int j = 0; j < HALF / 2; ++j) o[(long long)(k0 + j) * W] = make_float2(acc[2 * j] * scale, acc[2 * j + 1] * scale);
+    for (int j = 0; j < HALF / 2; ++j)
+      o[(long long)(k0 + j) * W] = aborted ? make_float2(nan, nan)
+                                           : make_float2(acc[2 * j] * scale, acc[2 * j + 1] * scale);
   }
   __syncthreads();
   if (warp == 0) umma::tmem_dealloc(tmem, C::TMEM_COLS);
-  if (e && lane == 0 && err) atomicExch(err, 1);
+  if (aborted && tid == 0 && err) atomicExch(err, 1);
 }
 
 struct Ws {
@@ -258,8 +301,11 @@ Ws make_ws(long long batch) {
   return w;
 }
 
+// clear_err: reset the error word first (a top-level call); a caller running many transforms
+// in one call (the layered path) clears it once and reads it at its end.
 template <int W, int S>
-int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* ws, size_t ws_bytes, cudaStream_t st) {
+int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* ws, size_t ws_bytes, cudaStream_t st,
+             bool clear_err) {
   using C = Cfg<W, S>;
   const Ws w = make_ws<W, S>(batch);
   if (ws_bytes < w.total) return PTY_ERR_WORKSPACE;
@@ -268,7 +314,7 @@ int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* 
   float2* tmp = at<float2>(ws, w.o_tmp);
   prof_mark(st, KID_DFT_TABLES);
   dft_matrix_kernel<W, S><<<256, 256, 0, st>>>(img, inverse);
-  if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
+  if (clear_err && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
   auto k = dft_pass_kernel<W, S>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess) return PTY_ERR_CUDA;
   const float sc = inverse ? 1.0f / (float)W : 1.0f;   // 1/W per pass: exact
@@ -289,6 +335,34 @@ int run_fft2(const float2* in, float2* out, long long batch, int inverse, void* 
 }
 
 }  // namespace dg
+
+// The layered path's entry: one transform of a call that clears the error word itself once.
+int tc_fft2(const float2* in, float2* out, long long batch, int window, int inverse, int terms, void* ws,
+            size_t ws_bytes, cudaStream_t st) {
+  if (!in || !out || !ws || batch <= 0 || in == out) return PTY_ERR_INVALID;
+  switch (window * 10 + terms) {
+    case 642: return dg::run_fft2<64, 2>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    case 1282: return dg::run_fft2<128, 2>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    case 2562: return dg::run_fft2<256, 2>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    case 643: return dg::run_fft2<64, 3>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    case 1283: return dg::run_fft2<128, 3>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    case 2563: return dg::run_fft2<256, 3>(in, out, batch, inverse, ws, ws_bytes, st, false);
+    default: return PTY_ERR_UNSUPPORTED;
+  }
+}
+
+// The error word inside a tensor-core DFT workspace (its offset does not depend on the batch).
+int* tc_err_word(void* ws, int window, int terms) {
+  switch (window * 10 + terms) {
+    case 642: return at<int>(ws, dg::make_ws<64, 2>(1).o_err);
+    case 1282: return at<int>(ws, dg::make_ws<128, 2>(1).o_err);
+    case 2562: return at<int>(ws, dg::make_ws<256, 2>(1).o_err);
+    case 643: return at<int>(ws, dg::make_ws<64, 3>(1).o_err);
+    case 1283: return at<int>(ws, dg::make_ws<128, 3>(1).o_err);
+    case 2563: return at<int>(ws, dg::make_ws<256, 3>(1).o_err);
+    default: return nullptr;
+  }
+}
 }  // namespace pty
 
 using namespace pty;
@@ -317,12 +391,12 @@ static int fft2_tc(const void* in, void* out, int32_t batch, int32_t window, int
   float2* o = static_cast<float2*>(out);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   switch (window * 10 + terms) {
-    case 642: return dg::run_fft2<64, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 1282: return dg::run_fft2<128, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 2562: return dg::run_fft2<256, 2>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 643: return dg::run_fft2<64, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 1283: return dg::run_fft2<128, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
-    case 2563: return dg::run_fft2<256, 3>(i, o, batch, inverse, workspace, workspace_bytes, st);
+    case 642: return dg::run_fft2<64, 2>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
+    case 1282: return dg::run_fft2<128, 2>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
+    case 2562: return dg::run_fft2<256, 2>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
+    case 643: return dg::run_fft2<64, 3>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
+    case 1283: return dg::run_fft2<128, 3>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
+    case 2563: return dg::run_fft2<256, 3>(i, o, batch, inverse, workspace, workspace_bytes, st, true);
     default: return PTY_ERR_UNSUPPORTED;
   }
 }

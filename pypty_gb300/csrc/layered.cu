@@ -27,6 +27,14 @@
 extern "C" int pty_fft2(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse, int32_t shift,
                         void* workspace, size_t workspace_bytes, void* stream);
 extern "C" int pty_fft2_workspace_bytes(int32_t window, size_t* bytes);
+namespace pty {
+// dft_gemm.cu: one tensor-core transform inside a call that clears the error word once, and
+// the error word of a tensor-core DFT workspace
+int tc_fft2(const float2* in, float2* out, long long batch, int window, int inverse, int terms, void* ws,
+            size_t ws_bytes, cudaStream_t st);
+int* tc_err_word(void* ws, int window, int terms);
+}  // namespace pty
+
 extern "C" int pty_fft2_bf16x3(const void* in, void* out, int32_t batch, int32_t window, int32_t inverse,
                                void* workspace, size_t workspace_bytes, void* stream);
 extern "C" int pty_fft2_bf16x3_workspace_bytes(int32_t batch, int32_t window, size_t* bytes);
@@ -258,6 +266,7 @@ struct VarTableArgs {
   const int* abk;         // [n_abs] 0: m = 0, 1: cos (a), 2: sin (b)
   int W, use_edge, near, n_abs;
   float px, py, distance, wavelength, edge_mult, tan_x, tan_y, defocus, cs;
+  const float* tilt_row;  // device tilt row [6] whose inside tilt (2, 3) replaces tan_y, tan_x, or nullptr
 };
 
 __global__ void var_tables_kernel(VarTableArgs a) {
@@ -275,8 +284,9 @@ __global__ void var_tables_kernel(VarTableArgs a) {
   const float qx = fftfreq_f32(kx, W, a.px), qy = fftfreq_f32(ky, W, a.py);
   const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
   const float mk = a.mask[u];
+  const float tan_x = a.tilt_row ? a.tilt_row[3] : a.tan_x, tan_y = a.tilt_row ? a.tilt_row[2] : a.tan_y;
   // lambda q2 + 2 (qx tan_x + qy tan_y), float32 in the reference's order
-  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, a.tan_x), __fmul_rn(qy, a.tan_y)));
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, tan_x), __fmul_rn(qy, tan_y)));
   const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
   const float inv = 1.0f / (float)WW;
   {
@@ -1101,10 +1111,9 @@ struct Run {
 
   int dft(const float2* in, float2* out, long long nwin, int inverse) {
     if (nwin <= 0) return PTY_OK;
-    if (q.engine == PTY_DFT_BF16X3)
-      return pty_fft2_bf16x3(in, out, (int32_t)nwin, q.W, inverse, at<void>(ws, q.o_dft), q.dft_bytes, st);
-    if (q.engine == PTY_DFT_BF16X6)
-      return pty_fft2_bf16x6(in, out, (int32_t)nwin, q.W, inverse, at<void>(ws, q.o_dft), q.dft_bytes, st);
+    if (q.engine == PTY_DFT_BF16X3 || q.engine == PTY_DFT_BF16X6)
+      return tc_fft2(in, out, nwin, q.W, inverse, q.engine == PTY_DFT_BF16X3 ? 2 : 3, at<void>(ws, q.o_dft),
+                     q.dft_bytes, st);
     // the FP32 engine's twiddle tables are built by the first transform of the call and reused
     float2* tw = at<float2>(ws, q.o_dft);
     const int build = tw_built ? 0 : 1;
@@ -1114,6 +1123,13 @@ struct Run {
     return run_fft2<256>(in, out, (int)nwin, inverse, 0, tw, st, build);
   }
   bool tw_built = false;
+
+  // the tensor-core engines' error word (set when a bounded wait ran out in any transform of
+  // the call; the loss then comes back NaN), or nullptr for the FP32 engine
+  int* tc_err() {
+    if (q.engine != PTY_DFT_BF16X3 && q.engine != PTY_DFT_BF16X6) return nullptr;
+    return tc_err_word(at<void>(ws, q.o_dft), q.W, q.engine == PTY_DFT_BF16X3 ? 2 : 3);
+  }
 
   // the FP32 engine's twiddle tables (the 128-point ones for 256 px windows), built once per call
   float2* fp32_twiddles() {
@@ -1238,6 +1254,8 @@ struct Run {
     ta.edge_mult = p->edge_mult;
     ta.use_edge = (p->edge_mult > 1.0f && q.Z > 1) ? 1 : 0;
     const float unfold = (float)WW;   // the tables fold 1/W^2 for the unnormalised register FFT: exact
+    if (int* e = tc_err())   // cleared once per call: a failure in any transform of the call stays set
+      if (cudaMemsetAsync(e, 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
     prof_mark(st, KID_TABLES);
     if (W == 64) tables_kernel<64><<<(WW + 255) / 256, 256, 0, st>>>(ta);
     else if (W == 128) tables_kernel<128><<<(WW + 255) / 256, 256, 0, st>>>(ta);
@@ -1273,11 +1291,12 @@ struct Run {
       va.tan_y = v->tan_y;
       va.tgrid = at<float>(ws, q.o_tgrid);
       if (v->n_tilts > 0) {   // the shared propagator / CTF take row 0's inside tilt (objective.py:339-345)
-        va.tan_y = v->tilts_host[2];
-        va.tan_x = v->tilts_host[3];
-        if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), v->tilts_host, (size_t)q.n_rows * 6 * sizeof(float),
-                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+        const bool dev_rows = v->tilts_device != nullptr;
+        if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), dev_rows ? v->tilts_device : v->tilts_host,
+                            (size_t)q.n_rows * 6 * sizeof(float),
+                            dev_rows ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st) != cudaSuccess)
           return PTY_ERR_CUDA;
+        va.tilt_row = at<float>(ws, q.o_tilts);   // read on the device: no host copy of a trial point
       } else {   // one row holding the inside tilt, for the per-position CTF kernels
         const float row[6] = {0.0f, 0.0f, v->tan_y, v->tan_x, 0.0f, 0.0f};
         if (cudaMemcpyAsync(at<float>(ws, q.o_tilts), row, sizeof(row), cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -1294,17 +1313,18 @@ struct Run {
     // per-slice distances: one table per step with the shared inside tilt (multislice_core.py:69-74)
     float2* steps = at<float2>(ws, q.o_steps);
     if (q.per_step) {
-      const float tx = v ? (v->n_tilts > 0 ? v->tilts_host[3] : v->tan_x) : 0.0f;
-      const float ty = v ? (v->n_tilts > 0 ? v->tilts_host[2] : v->tan_y) : 0.0f;
+      const float tx = v ? v->tan_x : 0.0f;
+      const float ty = v ? v->tan_y : 0.0f;
+      const float* row = (v && v->n_tilts > 0) ? at<float>(ws, q.o_tilts) : nullptr;   // row 0's inside tilt
       if (W == 64)
         launch_step_props<64>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
-                              ta.use_edge, tx, ty, steps, st);
+                              ta.use_edge, tx, ty, steps, st, row);
       else if (W == 128)
         launch_step_props<128>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
-                               ta.use_edge, tx, ty, steps, st);
+                               ta.use_edge, tx, ty, steps, st, row);
       else
         launch_step_props<256>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
-                               ta.use_edge, tx, ty, steps, st);
+                               ta.use_edge, tx, ty, steps, st, row);
     }
     // distance of slice step z (the step from slice z to z + 1)
     auto step_distance = [&](int z) { return q.per_step ? p->slice_distances[z] : p->slice_distance; };
@@ -1616,7 +1636,7 @@ struct Run {
     prof_mark(st, KID_FINALIZE);
     finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
-                                               p->step_pos && shift, nullptr, loss_sse, pos_grad);
+                                               p->step_pos && shift, tc_err(), loss_sse, pos_grad);
     if (v && q.step_tilts)
       var_tilt_finalize_kernel<<<1, 32, 0, st>>>(at<double>(ws, q.o_tpart), at<int>(ws, q.o_seq), q.nseq, q.n_rows,
                                                  q.single_tilt, q.before, q.inside_grad, q.after, v->tilts_grad);
@@ -1756,7 +1776,8 @@ int validate_variant(const pty_problem_t* p, const pty_variant_t* v) {
   if (v->recon_type != 0 && v->recon_type != 1) return PTY_ERR_UNSUPPORTED;
   if (v->data_pad < 0 || 2 * v->data_pad >= p->window) return PTY_ERR_INVALID;
   if (compressed && v->data_pad != 0) return PTY_ERR_UNSUPPORTED;
-  if (v->n_tilts < 0 || (v->n_tilts > 0 && (!v->tilts_host || (v->n_tilts != 1 && v->n_tilts != p->n_positions))))
+  if (v->n_tilts < 0 ||
+      (v->n_tilts > 0 && ((!v->tilts_host && !v->tilts_device) || (v->n_tilts != 1 && v->n_tilts != p->n_positions))))
     return PTY_ERR_INVALID;
   if (v->n_tilts > 0 && (v->tilt_mode < 0 || v->tilt_mode > 4)) return PTY_ERR_UNSUPPORTED;
   if (compressed && (v->n_masks <= 0 || !v->masks)) return PTY_ERR_INVALID;

@@ -173,14 +173,20 @@ struct Path {
     if (p->step_obj) {
       float2* gs = gsum(ib);
       prof_mark(side, KID_GRAD_WINDOWS);
-      grad_windows_kernel<W><<<(unsigned)(Bn * q.zm), T, Smem<W>::bytes, side>>>(gs, ta.mask_sc, tw);
+      grad_windows_kernel<W><<<(unsigned)(Bn * q.zm), T, Smem<W>::bytes, side>>>(gs, ta.mask_sc, tw, q.Mp);
       int* lists = at<int>(ws, q.o_lists);
       int* counts = at<int>(ws, q.o_counts);
       prof_mark(side, KID_TILE_LISTS);
       tile_lists_kernel<<<q.ntiles, 256, 0, side>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
       prof_mark(side, KID_SCATTER);
-      scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(
-          gs, d_pos, seq_b, lists, counts, at<float2>(ws, q.o_grad), Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0);
+      float2* scpart = q.sgroups > 1 ? at<float2>(ws, q.o_scpart) : nullptr;
+      scatter_tiles_kernel<<<dim3(q.ntiles, q.zm, q.sgroups), dim3(32, 8), 0, side>>>(
+          gs, d_pos, seq_b, lists, counts, at<float2>(ws, q.o_grad), Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0,
+          q.sgroups, scpart, q.Mp);
+      if (q.sgroups > 1)
+        scatter_merge_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(scpart, at<float2>(ws, q.o_grad),
+                                                                            q.sgroups, q.Ny, q.Nx, q.ntx, q.zm,
+                                                                            ib > 0 ? 1 : 0);
     }
     if (p->step_probe) {
       const int nch = (Bn + q.chunk - 1) / q.chunk;
@@ -206,7 +212,10 @@ struct Path {
       }
       if (p->step_probe) {
         prof_mark(st, KID_PROBE_FINAL);
-        probe_final_kernel<W><<<q.Mp, T, Smem<W>::bytes, st>>>(at<float2>(ws, q.o_partial), q.nchunk, q.Mp,
+        // the chunk sum over the GPU first (into chunk 0), then one block per mode transforms
+        probe_chunks_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp), 256, 0, st>>>(at<float2>(ws, q.o_partial),
+                                                                                     q.nchunk, q.Mp, (int)WW);
+        probe_final_kernel<W><<<q.Mp, T, Smem<W>::bytes, st>>>(at<float2>(ws, q.o_partial), 1, q.Mp,
                                                                ta.mask_sc, tw, probe_grad);
       } else if (probe_grad) {
         cudaMemsetAsync(probe_grad, 0, WW * q.Mp * sizeof(float2), st);
@@ -444,7 +453,7 @@ int run_ms_grads(const MsPlan& q, const float2* d_exit, const float2* waves, con
     const int nyx = q.Ny * q.Nx;
     prof_mark(st, KID_GRAD_WINDOWS);
     grad_windows_kernel<W><<<(unsigned)(q.B * q.zm), T, Smem<W>::bytes, st>>>(gs, at<float>(ws, q.o_mask_sc),
-                                                                            at<float2>(ws, q.o_tw));
+                                                                            at<float2>(ws, q.o_tw), q.Mp);
     prof_mark(st, KID_OBJ_TO_SLICES);
     obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(object_grad, grad, nyx, q.zm);
     prof_mark(st, KID_TILE_LISTS);
@@ -453,7 +462,7 @@ int run_ms_grads(const MsPlan& q, const float2* d_exit, const float2* waves, con
     prof_mark(st, KID_SCATTER);
     scatter_tiles_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, st>>>(
         gs, at<int>(ws, q.o_pos), at<int>(ws, q.o_seq), at<int>(ws, q.o_lists), at<int>(ws, q.o_counts), grad, q.B,
-        W, q.Ny, q.Nx, q.ntx, q.zm, 1);
+        W, q.Ny, q.Nx, q.ntx, q.zm, 1, 1, nullptr, q.Mp);
     prof_mark(st, KID_SLICES_TO_OBJ);
     slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(grad, object_grad, nyx, q.zm);
   }

@@ -33,7 +33,14 @@ struct Plan {
   size_t s_obl, s_gsum, s_fprobe, s_stack;
   int per_step;   // one propagator table per slice step (slice_distances given, Z > 1)
   size_t o_steps;
+  // scatter runs per tile (scatter_tiles_kernel groups): > 1 when tiles x slices give too few
+  // blocks to fill the GPU; o_scpart holds their partial tiles
+  int sgroups;
+  size_t o_scpart;
 };
+
+// blocks the scatter aims for: two per SM of a 152-SM GB300
+constexpr int kScatterBlocks = 304;
 
 // twiddle tables in global memory: W = 256 windows use the 128 tables of their sub-transforms
 inline int tw_count(int W) { return W == 64 ? Geo<64>::TW1 + Geo<64>::TW2 : Geo<128>::TW1 + Geo<128>::TW2; }
@@ -97,7 +104,9 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_grad = take((size_t)q.zm * q.Ny * q.Nx * c8);
   q.nbuf = (!split && q.W <= 128 && q.nbatch > 1) ? 2 : 1;
   q.s_obl = align_up((size_t)q.Bb * q.zm * WW * c8);
-  q.s_gsum = q.s_obl;
+  // W <= 128: one contribution window per probe mode (the fused kernel's adjoint writes each
+  // mode's own; grad_windows_kernel sums them); 256 windows: one probe-mode-summed window
+  q.s_gsum = q.W <= 128 ? align_up((size_t)q.Bb * q.zm * q.Mp * WW * c8) : q.s_obl;
   q.s_fprobe = align_up((size_t)q.Bb * q.Mp * WW * c8);
   q.o_obl = take(q.nbuf * q.s_obl);
   q.ckpt = (p->window == 256 && p->checkpoint_every > 1) ? std::min(p->checkpoint_every, q.Z) : 1;
@@ -122,6 +131,13 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
   q.o_gpark = take(q.ckpt > 1 ? (size_t)q.Bb * WW * c8 : 0);
   q.per_step = p->slice_distances && q.Z > 1;
   q.o_steps = take(q.per_step ? (size_t)(q.Z - 1) * WW * c8 : 0);
+  {
+    const int cells = q.ntiles * q.zm;
+    int g = (kScatterBlocks + cells - 1) / cells;
+    g = std::min(g, std::max(1, q.Bb / 8));   // runs of at least ~8 windows
+    q.sgroups = std::max(1, std::min(g, 32));
+  }
+  q.o_scpart = take(q.sgroups > 1 ? (size_t)q.sgroups * q.ntiles * q.zm * kTileSize * kTileSize * c8 : 0);
   q.total = o;
   return q;
 }
@@ -183,7 +199,7 @@ inline MsPlan make_ms_plan(int W, int B, int Z, int Mp, int Mo, int Ny, int Nx) 
   q.o_obl = take((size_t)B * q.zm * WW * c8);
   q.o_stack = take((size_t)B * Z * Mp * Mo * WW * c8);
   q.o_gbuf = take((size_t)B * Mp * Mo * WW * c8);
-  q.o_gsum = take((size_t)B * q.zm * WW * c8);
+  q.o_gsum = take((size_t)B * q.zm * Mp * WW * c8);   // one contribution window per probe mode
   q.o_fprobe = take((size_t)B * Mp * WW * c8);
   q.o_grad = take((size_t)q.zm * Ny * Nx * c8);
   q.o_lists = take((size_t)q.ntiles * B * sizeof(int));

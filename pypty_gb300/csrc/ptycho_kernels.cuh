@@ -58,6 +58,7 @@ struct StepPropArgs {
   float px, py, wavelength, distance, tan_x, tan_y, edge_mult;
   int edge;
   float2* out;
+  const float* tilt_row;   // device tilt row [6]: its inside tilt (2, 3) replaces tan_y, tan_x; or nullptr
 };
 
 template <int W>
@@ -68,7 +69,8 @@ __global__ void step_prop_kernel(StepPropArgs a) {
   const float qx = fftfreq_f32(kx, W, a.px);
   const float qy = fftfreq_f32(ky, W, a.py);
   const float q2 = __fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy));
-  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, a.tan_x), __fmul_rn(qy, a.tan_y)));
+  const float tan_x = a.tilt_row ? a.tilt_row[3] : a.tan_x, tan_y = a.tilt_row ? a.tilt_row[2] : a.tan_y;
+  const float tilt = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(qx, tan_x), __fmul_rn(qy, tan_y)));
   const float x = __fadd_rn(__fmul_rn(a.wavelength, q2), tilt);
   const float phase = __fmul_rn(__fmul_rn(-3.141592654f, a.distance), x);
   const float mk = a.mask[idx];
@@ -95,10 +97,10 @@ __global__ void step_prop_kernel(StepPropArgs a) {
 template <int W>
 inline void launch_step_props(const float* mask, const float* distances_host, int nsteps, float px, float py,
                               float wavelength, float edge_mult, int use_edge, float tan_x, float tan_y,
-                              float2* out, cudaStream_t st) {
+                              float2* out, cudaStream_t st, const float* tilt_row = nullptr) {
   for (int z = 0; z < nsteps; ++z) {
     StepPropArgs sa{mask, px, py, wavelength, distances_host[z], tan_x, tan_y, edge_mult, (z == 0 && use_edge) ? 1 : 0,
-                    out + (size_t)z * W * W};
+                    out + (size_t)z * W * W, tilt_row};
     step_prop_kernel<W><<<(W * W + 255) / 256, 256, 0, st>>>(sa);
   }
 }
@@ -305,7 +307,7 @@ struct FusedArgs {
   const float* measured;    // (N, W, W) detector (fftshifted) order
   const float2* tw;
   float2* stack;            // conj input waves, native real [Bb*Z*Mp*Mo]
-  float2* gsum;             // probe-mode-summed object gradient, native real [Bb*Z*Mo]
+  float2* gsum;             // object-gradient contributions, native real [Bb*Z*Mo*Mp] (probe mode innermost)
   float2* fprobe;           // FFT of the per-position probe gradient, native freq [Bb*Mp]
   float2* gbuf;             // dL/d(exit wave) between the two halves, native real [Bb*Mp*Mo]
   float2* psi;              // 256 windows: far-field wave per mode [Bb*Mp*Mo]
@@ -331,10 +333,26 @@ __device__ __forceinline__ float2 shift_ramp(const FusedArgs& a, int ky, int kx,
   return make_float2(c * mk, s * mk);
 }
 
+// A thread's running sum of float32 terms, compensated: every add is Knuth's TwoSum, so hi + lo
+// holds the exact sum to ~2^-44 relative, read out in FP64 for the FP64 block and grid sums.
+// (Per-element FP64 adds would run at the GPU's much lower FP64 rate.)
+struct FSum {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ FSum& operator+=(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+    return *this;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // dL/dI of one detector pixel for the loss `alg` (pypty/objective.py:527-559), with the
-// per-pixel loss and squared error added to the FP64 accumulators. Float32 arithmetic per
-// pixel, as the reference's arrays; only the sums are FP64.
-__device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& lsum, double& ssum) {
+// per-pixel loss and squared error added to the accumulators (double, or FSum). Float32
+// arithmetic per pixel, as the reference's arrays; only the sums are wider.
+template <typename Acc>
+__device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, Acc& lsum, Acc& ssum) {
   float d, lp, sp;
   if (alg == ALG_LSQ_SQRT) {
     const float sI = sqrtf(I), sM = sqrtf(Mv);
@@ -363,8 +381,8 @@ __device__ __forceinline__ float loss_pixel(int alg, float I, float Mv, double& 
       d = 1.0f;
     }
   }
-  lsum += (double)lp;
-  ssum += (double)sp;
+  lsum += lp;
+  ssum += sp;
   return d;
 }
 
@@ -469,6 +487,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   };
 
   float2 v[32];
+  bool side_next = false;         // the side buffer is free and its next copy not yet issued
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
   const bool adjoint_only = (phase == 2 || phase == 4);
   const int s_begin = adjoint_only ? Z + 1 : 0;
@@ -499,7 +518,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 #pragma unroll
         for (int i = 0; i < 32; ++i) c[i] = cconj(v[i]);
         st_native<W>(stack_ptr(z), c);
-        fence_async_global();   // these stores are read back by TMA in the adjoint
+        // the adjoint reads the stack back by TMA: one proxy fence after the last store orders
+        // every earlier stack store of this thread as well
+        if (z == Z - 1) fence_async_global();
       }
       if (z == Z - 1 && adj_stack && phase == 0) issue_side(Z - 1);
       mbar_wait(&bars[0], ph_x, a.err);
@@ -526,63 +547,31 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 #pragma unroll
           for (int j = NST / 2; j < 16; ++j) otail[j - NST / 2] = og[j * T + t];
         }
-        // contribution conj(psi_z) * g, summed over the probe modes of object mode m
-        float2* gs = a.gsum + (((size_t)b * Z + z) * a.Mo + m) * WW;
-        float4* x4 = reinterpret_cast<float4*>(xbuf);
-        if (a.Mp == 1) {
-          float4* g4 = reinterpret_cast<float4*>(gs);
+        // contribution conj(psi_z) * g of this probe mode, to its own window of the gradient
+        // buffer ([position][slice][object mode][probe mode]); grad_windows_kernel adds the
+        // probe modes in ascending order before the band limit (multislice_core.py:184-191), so
+        // the adjoint needs no cluster barrier and no remote reads
+        float4* g4 = reinterpret_cast<float4*>(a.gsum + ((((size_t)b * Z + z) * a.Mo + m) * a.Mp + p) * WW);
+        const float4* x4 = reinterpret_cast<const float4*>(xbuf);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float4 q = x4[j * T + t];
-            const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
-            const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
-            g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float4 q = x4[j * T + t];
-            const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
-            const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
-            x4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
-          }
-          cluster.sync();
-          // this block sums elements p, p + Mp, ... (two at a time, loads independent)
-#pragma unroll 1
-          for (int i0 = p; i0 < 32; i0 += 2 * a.Mp) {
-            float2 acc[2];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) acc[k] = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int pp = 0; pp < 8; ++pp) {   // probe modes in ascending order
-              if (pp < a.Mp) {
-                const float2* rb = cluster.map_shared_rank(xbuf, pp + m * a.Mp);
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                  const int i = i0 + k * a.Mp;
-                  if (i < 32) acc[k] = cadd(acc[k], rb[nidx<W>(i, t)]);
-                }
-              }
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              const int i = i0 + k * a.Mp;
-              if (i < 32) gs[nidx<W>(i, t)] = acc[k];
-            }
-          }
-          cluster.sync();
+        for (int j = 0; j < 16; ++j) {
+          const float4 q = x4[j * T + t];
+          const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
+          const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
+          g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
         }
         // g *= conj(O_z): elements < NST from the side buffer, the rest from the registers
         mbar_wait(&bars[1], ph_side, a.err);
-        const float4* sd = reinterpret_cast<const float4*>(side);
+        {
+          const float4* sd = reinterpret_cast<const float4*>(side);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
-          v[2 * j] = cmulc(v[2 * j], make_float2(q.x, q.y));
-          v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
+          for (int j = 0; j < 16; ++j) {
+            const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
+            v[2 * j] = cmulc(v[2 * j], make_float2(q.x, q.y));
+            v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
+          }
         }
-        __syncthreads();   // the side buffer has been read by every thread
-        if (z > 0) issue_side(z - 1);
+        side_next = z > 0;   // the side buffer's next copy goes out after the next block barrier
       } else {
         const float4* ob = reinterpret_cast<const float4*>(xbuf);
 #pragma unroll
@@ -620,7 +609,15 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     }
 
     // ------------------------------------------------ forward FFT
-    if (s > 0) F::forward(v, xbuf, tw1, tw2);
+    if (s > 0) {
+      F::forward_round1(v, tw1);
+      F::forward_rest(v, xbuf, tw1, tw2, [&] {
+        if (side_next) {   // every thread has read the side buffer: refill it for slice z - 1
+          issue_side(z - 1);
+          side_next = false;
+        }
+      });
+    }
 
     // ------------------------------------------------ frequency op
     if (s == 0) {
@@ -674,22 +671,36 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       cluster.sync();   // every block is done reading this block's intensities
       const float inv_modes = 1.0f / (float)nmodes;
       const float* meas = a.measured + (size_t)gi * WW;
-      double lsum = 0.0, ssum = 0.0;
+      FSum lsum_c, ssum_c;
+      // eight pixels at a time: their measured values are loaded together, then used in order
 #pragma unroll 1
-      for (int i = 0; i < 32; ++i) {
-        const float acc = fs1[i * T + t];
-        const float I = (nmodes == 1) ? acc : acc * inv_modes;
-        const int ky = G::fky(t, i), kx = G::fkx(t, i);
-        const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
-        if (a.simulate) {
-          if (crank == 0) a.sim_out[(size_t)b * WW + didx] = I;
-          continue;
+      for (int i0 = 0; i0 < 32; i0 += 8) {
+        float mv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int i = i0 + k;
+          const int ky = G::fky(t, i), kx = G::fkx(t, i);
+          const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
+          mv[k] = a.simulate ? 0.0f : meas[didx];
         }
-        float d = loss_pixel(a.algorithm, I, meas[didx], lsum, ssum);
-        if (nmodes > 1) d = d / (float)nmodes;           // objective.py:586-587
-        fs1[i * T + t] = d;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int i = i0 + k;
+          const float acc = fs1[i * T + t];
+          const float I = (nmodes == 1) ? acc : acc * inv_modes;
+          if (a.simulate) {
+            const int ky = G::fky(t, i), kx = G::fkx(t, i);
+            const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
+            if (crank == 0) a.sim_out[(size_t)b * WW + didx] = I;
+            continue;
+          }
+          float d = loss_pixel(a.algorithm, I, mv[k], lsum_c, ssum_c);
+          if (nmodes > 1) d = d / (float)nmodes;           // objective.py:586-587
+          fs1[i * T + t] = d;
+        }
       }
       if (a.simulate) return;
+      double lsum = lsum_c.value(), ssum = ssum_c.value();
       block_sum2(lsum, ssum, red);
       if (t == 0 && crank == 0) {
         a.loss_part[2 * b] = lsum;
@@ -715,7 +726,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     } else {
       // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
       const float2* pf = a.probe_f + (size_t)p * WW;
-      double gy = 0.0, gx = 0.0;
+      FSum gy_c, gx_c;
       if (a.probe_shift) {
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
@@ -725,13 +736,14 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           if (a.step_pos) {
             // Re(smyx * conj(Pf) * F) with smyx = i*s*mask  ->  -(s*mask) * Im(conj(Pf) * F)
             const float im = cmulc(v[i], pf[nidx<W>(i, t)]).y;
-            gy += (double)(-(a.sy[ky] * mk) * im);
-            gx += (double)(-(a.sx[kx] * mk) * im);
+            gy_c += -(a.sy[ky] * mk) * im;
+            gx_c += -(a.sx[kx] * mk) * im;
           }
         }
       }
       if (a.step_probe) st_native<W>(a.fprobe + ((size_t)b * a.Mp + p) * WW, v);
       if (a.step_pos) {
+        double gy = gy_c.value(), gx = gx_c.value();
         block_sum2(gy, gx, red);
         if (t == 0) {
           a.pos_part[(b * a.Mp + p) * 2] = gy;
@@ -747,6 +759,13 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     if (s + 1 < s_end) {
       __syncthreads();   // every thread has finished reading the exchange buffer
       issue_x(s + 1);
+      // every block asks for its operands at about the same time: bring the operand two steps
+      // ahead (and, in the adjoint, the object window the side buffer takes next) into L2 now,
+      // so that the copies of the next steps read L2 instead of waiting for HBM
+      if (t == 0) {
+        if (s + 2 < s_end) prefetch_l2(xsrc(s + 2), (uint32_t)(WW * sizeof(float2)));
+        if (!fwd && adj_stack && z >= 2) prefetch_l2(obl_ptr(z - 2), (uint32_t)(WW * sizeof(float2)));
+      }
     }
     F::inverse_tail(v, tw1);
   }
@@ -819,11 +838,13 @@ __global__ void external_tables_kernel(const float2* __restrict__ P, const float
 }
 
 // ------------------------------------------------------------------ gradient windows
-// Band-limit the probe-mode-summed gradient window: IFFT(FFT(G) * mask)
-// (multislice_core.py:189-191); native real layout in, natural (y, x) layout out, in place.
+// Sum the nsum probe-mode contributions of a gradient window in ascending mode order
+// (multislice_core.py:184-188) and band-limit the sum: IFFT(FFT(G) * mask)
+// (multislice_core.py:189-191). Window w's contributions are the nsum consecutive native
+// windows at buf + w * nsum * W^2; the result, in natural (y, x) layout, overwrites the first.
 template <int W>
 __global__ void __launch_bounds__(Geo<W>::T) grad_windows_kernel(float2* buf, const float* __restrict__ mask_sc,
-                                                                 const float2* __restrict__ g_tw) {
+                                                                 const float2* __restrict__ g_tw, int nsum) {
   using G = Geo<W>;
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
@@ -831,9 +852,18 @@ __global__ void __launch_bounds__(Geo<W>::T) grad_windows_kernel(float2* buf, co
   carve<W>(smem, xbuf, tw1, tw2, red);
   load_twiddles<W>(tw1, tw2, g_tw);
   const int t = threadIdx.x;
-  float2* win = buf + (size_t)blockIdx.x * W * W;
+  float2* win = buf + (size_t)blockIdx.x * nsum * W * W;
   float2 v[32];
   ld_native<W>(win, v);
+  for (int p = 1; p < nsum; ++p) {
+    const float4* src = reinterpret_cast<const float4*>(win + (size_t)p * W * W);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const float4 q = src[j * G::T + t];
+      v[2 * j] = cadd(v[2 * j], make_float2(q.x, q.y));
+      v[2 * j + 1] = cadd(v[2 * j + 1], make_float2(q.z, q.w));
+    }
+  }
   __syncthreads();
   WinFFT<W>::forward(v, xbuf, tw1, tw2);
 #pragma unroll
@@ -886,13 +916,20 @@ static __global__ void tile_lists_kernel(const int* __restrict__ pos, const int*
   if (threadIdx.x == 0) counts[tile] = base_s;
 }
 
-// blockDim = (32, 8); grid = (ntiles, Z*Mo)
+// Window (b, k) of gw starts at ((b * zm + k) * wmul) * W^2 (wmul = probe modes when the
+// windows hold per-mode contributions whose first slot carries the sum).
+// blockDim = (32, 8); grid = (ntiles, Z*Mo, groups). With groups = 1 a block adds its tile's
+// whole list onto the gradient plane. With groups > 1 (few tiles: a small object or a single
+// slice) the list is cut into `groups` consecutive runs; block (tile, k, g) sums run g alone
+// into part[g][k][tile] and scatter_merge_kernel adds the runs in order -- still a fixed order,
+// now with groups x more blocks at work.
 static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const int* __restrict__ pos,
                                      const int* __restrict__ seq, const int* __restrict__ lists,
                                      const int* __restrict__ counts, float2* __restrict__ grad,
-                                     int Bb, int W, int Ny, int Nx, int ntx, int zm, int accumulate) {
+                                     int Bb, int W, int Ny, int Nx, int ntx, int zm, int accumulate,
+                                     int groups = 1, float2* __restrict__ part = nullptr, int wmul = 1) {
   __shared__ int s_b[256], s_y[256], s_x[256];
-  const int tile = blockIdx.x, k = blockIdx.y;
+  const int tile = blockIdx.x, k = blockIdx.y, g = blockIdx.z;
   const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
   const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
   const int x = tx0 + lx;
@@ -901,12 +938,14 @@ static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int y = ty0 + ly + 8 * r;
-    acc[r] = (accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
+    acc[r] = (groups == 1 && accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
   }
-  const int n = counts[tile];
+  const int n_all = counts[tile];
+  const int per = (n_all + groups - 1) / groups;
+  const int jb = min(n_all, g * per), n = min(n_all, jb + per);
   const int* lst = lists + (size_t)tile * Bb;
   const size_t WW = (size_t)W * W;
-  for (int j0 = 0; j0 < n; j0 += 256) {
+  for (int j0 = jb; j0 < n; j0 += 256) {
     __syncthreads();
     if (j0 + tid < n) {
       const int b = lst[j0 + tid];
@@ -927,7 +966,7 @@ static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const
       for (int u = 0; u < 4; ++u) {
         const int ox = x - s_x[j + u];
         const bool inx = (unsigned)ox < (unsigned)W;
-        const float2* src = gw + ((size_t)s_b[j + u] * zm + k) * WW + (inx ? ox : 0);
+        const float2* src = gw + ((size_t)s_b[j + u] * zm + k) * wmul * WW + (inx ? ox : 0);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int oy = ty0 + ly + 8 * r - s_y[j + u];
@@ -945,13 +984,46 @@ static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const
       const int b = s_b[j];
       const int ox = x - s_x[j];
       if ((unsigned)ox >= (unsigned)W) continue;
-      const float2* src = gw + ((size_t)b * zm + k) * WW + ox;
+      const float2* src = gw + ((size_t)b * zm + k) * wmul * WW + ox;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int oy = ty0 + ly + 8 * r - s_y[j];
         if ((unsigned)oy < (unsigned)W) acc[r] = cadd(acc[r], src[(size_t)oy * W]);
       }
     }
+  }
+  if (groups > 1) {
+    float2* pt = part + (((size_t)g * zm + k) * (gridDim.x) + tile) * (TS * TS);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) pt[(ly + 8 * r) * TS + lx] = acc[r];
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int y = ty0 + ly + 8 * r;
+    if (y < Ny && x < Nx) plane[(size_t)y * Nx + x] = acc[r];
+  }
+}
+
+// The runs of scatter_tiles_kernel with groups > 1, added onto the plane in run order.
+// blockDim = (32, 8); grid = (ntiles, Z*Mo)
+static __global__ void scatter_merge_kernel(const float2* __restrict__ part, float2* __restrict__ grad, int groups,
+                                            int Ny, int Nx, int ntx, int zm, int accumulate) {
+  const int tile = blockIdx.x, k = blockIdx.y;
+  const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
+  const int lx = threadIdx.x, ly = threadIdx.y;
+  const int x = tx0 + lx;
+  float2* plane = grad + (size_t)k * Ny * Nx;
+  float2 acc[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int y = ty0 + ly + 8 * r;
+    acc[r] = (accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
+  }
+  for (int g = 0; g < groups; ++g) {
+    const float2* pt = part + (((size_t)g * zm + k) * gridDim.x + tile) * (TS * TS);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[r] = cadd(acc[r], pt[(ly + 8 * r) * TS + lx]);
   }
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
@@ -972,6 +1044,18 @@ static __global__ void probe_partial_kernel(const float2* __restrict__ fprobe, f
   for (int b = c * chunk; b < b1; ++b) s = cadd(s, fprobe[((size_t)b * Mp + p) * WW + e]);
   float2* dst = partial + ((size_t)c * Mp + p) * WW + e;
   *dst = accumulate ? cadd(*dst, s) : s;
+}
+
+// partial[0][p][e] = sum over c of partial[c][p][e] in chunk order (0 + partial[0] + partial[1]
+// + ..., the order probe_final_kernel would add them in), one thread per element: the chunk sum
+// spread over the whole GPU instead of the final kernel's one block per mode.
+static __global__ void probe_chunks_kernel(float2* __restrict__ partial, int nchunk, int Mp, int WW) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (e >= WW) return;
+  float2 s = make_float2(0.f, 0.f);
+  for (int c = 0; c < nchunk; ++c) s = cadd(s, partial[((size_t)c * Mp + p) * WW + e]);
+  partial[(size_t)p * WW + e] = s;
 }
 
 // probe_grad = IFFT(mask * sum_c partial[c]) (objective.py:703 and :927-933), written in the
@@ -1029,15 +1113,31 @@ static __global__ void finalize_scalars_kernel(const double* __restrict__ loss_p
     loss_sse[1] = b;
   }
   if (!step_pos) return;
+  // A position that appears more than once in the sequence keeps the gradient of its last
+  // occurrence, as the reference's batch-by-batch assignment pos_grad[tcs] = ... leaves it
+  // (objective.py:655-656): the sequence is walked in rounds of blockDim.x entries separated
+  // by barriers, and inside a round an entry writes only if no later entry of the round has
+  // the same position.
+  __shared__ int sseq[256];
   const double sh = -2.0 / ((double)W * (double)W);
-  for (int i = threadIdx.x; i < nseq; i += blockDim.x) {
+  for (int base = 0; base < nseq; base += blockDim.x) {
+    const int i = base + (int)threadIdx.x;
+    const int s = i < nseq ? seq[i] : -1;
+    __syncthreads();   // the previous round's comparisons are done
+    sseq[threadIdx.x] = s;
+    __syncthreads();
+    if (i >= nseq) continue;
+    const int nr = min((int)blockDim.x, nseq - base);
+    bool later = false;
+    for (int j = (int)threadIdx.x + 1; j < nr; ++j) later |= (sseq[j] == s);
+    if (later) continue;
     double gy = 0.0, gx = 0.0;
     for (int p = 0; p < Mp; ++p) {
       gy += pos_part[((size_t)i * Mp + p) * 2];
       gx += pos_part[((size_t)i * Mp + p) * 2 + 1];
     }
-    pos_grad[2 * seq[i]] = (float)(sh * gy);
-    pos_grad[2 * seq[i] + 1] = (float)(sh * gx);
+    pos_grad[2 * s] = (float)(sh * gy);
+    pos_grad[2 * s + 1] = (float)(sh * gx);
   }
 }
 

@@ -188,15 +188,29 @@ struct WinFFT {
   // real layout -> frequency layout, unnormalised, exp(-2 pi i ...) kernel
   static __device__ __forceinline__ void forward(float2 (&v)[32], float2* xbuf,
                                                  const float2* tw1, const float2* tw2) {
+    forward_round1(v, tw1);
+    forward_rest(v, xbuf, tw1, tw2, [] {});
+  }
+
+  // The forward transform in two parts, so that a caller can overlap work that must finish
+  // before the exchange buffer is overwritten (a cluster barrier, a pending copy) with the
+  // register-only first round. forward_round1 touches no shared memory besides the twiddles;
+  // forward_rest calls after_first_sync() right after its first barrier, when every thread of
+  // the block has finished everything it did before forward_rest.
+  static __device__ __forceinline__ void forward_round1(float2 (&v)[32], const float2* tw1) {
     const int t = threadIdx.x;
-    // ---- round 1
     DFT<32, -1>::template run<32, 1, 0>(v);
-    {
-      const int n2 = t % A;   // varies inside a warp: multiply unconditionally (row n2=0 is 1)
+    const int n2 = t % A;   // varies inside a warp: multiply unconditionally (row n2=0 is 1)
 #pragma unroll
-      for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmul(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
-    }
+    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmul(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
+  }
+
+  template <typename AfterSync>
+  static __device__ __forceinline__ void forward_rest(float2 (&v)[32], float2* xbuf, const float2* tw1,
+                                                     const float2* tw2, AfterSync&& after_first_sync) {
+    const int t = threadIdx.x;
     __syncthreads();
+    after_first_sync();
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) xbuf[x1(t, k1)] = v[k1];
     __syncthreads();

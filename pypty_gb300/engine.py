@@ -93,6 +93,7 @@ class Engine:
         self.device = torch.device(device if device is not None else "cuda")
         self._ws = None
         self._aux = {}
+        self._aux_events = {}
         # two page-locked geometry buffers used in turn, each with the event of the call that
         # last read it: the host fills one while the GPU may still run the previous call
         self._stages = [None, None]
@@ -113,6 +114,22 @@ class Engine:
         if buf is None or buf.numel() < nbytes:
             buf = self._aux[key] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
         return buf
+
+    def _ordered_aux(self, key: str, nbytes: int, stream):
+        """aux(key) for a call on `stream`, ordered after the previous call that used the same
+        buffer (possibly on another stream); returns (buffer, mark) -- call mark() after the
+        launch so that the next user waits for it."""
+        buf = self.aux(key, nbytes)
+        ev = self._aux_events.get(key)
+        if ev is not None:
+            stream.wait_event(ev)
+
+        def mark():
+            e = self._aux_events.get(key)
+            if e is None:
+                e = self._aux_events[key] = torch.cuda.Event()
+            e.record(stream)
+        return buf, mark
 
     def _staging(self, geo: Geometry, stream):
         """Page-locked copies of the geometry (the C ABI uploads them asynchronously). The call
@@ -229,8 +246,8 @@ class Engine:
         4D probe (W, W, Mp, S): every position's probe scenario (the probe gradient is then
         (W, W, Mp, S) too); exit_waves (n_sequence, Mp, Mo, W, W) complex64 CUDA tensor: filled
         with every position's exit wave; tilts
-        (n_tilts, 6) host array (the reference's tilt array plus its correction; one row or
-        one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
+        (n_tilts, 6) host array or CUDA tensor (the reference's tilt array plus its correction;
+        one row or one per position) with tilt_mode 0-4 and step_tilts; masks (n_masks, W, W) float32 in pattern order; beam_current
         (n_positions,) float32; aberrations (n_sets, n_abs) float32 with aberration_marker
         (n_positions,) int32; pos_correction as in ``loss_and_direction``. Returns (loss_sse,
         object_grad, probe_grad, pos_grad, beam_current_grad or None, aberrations_grad or
@@ -291,14 +308,21 @@ class Engine:
         sb_grad = torch.zeros(tuple(sb_d.shape), dtype=torch.float32, device=self.device) \
             if sb_d is not None and step_static_background else None
         tilts_h = None
+        tilts_d = None
         tilts_grad = None
         if tilts is not None:
-            tilts_h = np.ascontiguousarray(np.asarray(tilts.cpu() if torch.is_tensor(tilts) else tilts,
-                                                      dtype=np.float32).reshape(-1, 6))
-            if tilts_h.shape[0] not in (1, problem.n_positions):
+            if torch.is_tensor(tilts) and tilts.is_cuda:
+                # device rows (an optimizer's trial tilts): read in place, no host round trip
+                tilts_d = dev(tilts.reshape(-1, 6), torch.float32)
+                n_rows = int(tilts_d.shape[0])
+            else:
+                tilts_h = np.ascontiguousarray(np.asarray(tilts.cpu() if torch.is_tensor(tilts) else tilts,
+                                                          dtype=np.float32).reshape(-1, 6))
+                n_rows = int(tilts_h.shape[0])
+            if n_rows not in (1, problem.n_positions):
                 raise ValueError("tilts must have one row or one row per position")
             if step_tilts:
-                tilts_grad = torch.zeros(tuple(tilts_h.shape), dtype=torch.float32, device=self.device)
+                tilts_grad = torch.zeros((n_rows, 6), dtype=torch.float32, device=self.device)
         v = _lib.Variant(recon_type=_lib.RECON_TYPES[recon_type], defocus=float(defocus), cs=float(cs),
                          tan_x=float(tan_x), tan_y=float(tan_y),
                          n_masks=0 if masks_d is None else int(masks_d.shape[0]),
@@ -315,8 +339,9 @@ class Engine:
                          data_pad=int(data_pad), use_padded_intensity=int(bool(use_padded_intensity)),
                          shift_y=int(data_shift_vector[0]), shift_x=int(data_shift_vector[1]),
                          data_multiplier=float(data_multiplier),
-                         n_tilts=0 if tilts_h is None else int(tilts_h.shape[0]),
+                         n_tilts=0 if tilts is None else n_rows,
                          tilts_host=None if tilts_h is None else tilts_h.ctypes.data,
+                         tilts_device=None if tilts_d is None else tilts_d.data_ptr(),
                          tilt_mode=int(tilt_mode), step_tilts=int(tilts_grad is not None),
                          tilts_grad=None if tilts_grad is None else tilts_grad.data_ptr(),
                          upsample_pattern=up,
@@ -407,10 +432,12 @@ class Engine:
         out = torch.empty_like(x) if out is None else out
         n = ctypes.c_size_t(0)
         _lib.check(_lib.lib().pty_fft2_workspace_bytes(W, ctypes.byref(n)), "pty_fft2_workspace_bytes")
-        ws = self.workspace(int(n.value))
+        # its own buffer (not the loss-and-gradient workspace), ordered after its last user
+        ws, mark = self._ordered_aux("fft2", int(n.value), stream)
         batch = x.numel() // (W * W)
         st = _lib.lib().pty_fft2(_ptr(x), _ptr(out), batch, W, int(inverse), int(shift), _ptr(ws),
                                  ws.numel(), stream.cuda_stream)
+        mark()
         _lib.check(st, "pty_fft2")
         return out
 
@@ -430,9 +457,11 @@ class Engine:
         n = ctypes.c_size_t(0)
         name = "pty_fft2_bf16x3" if terms == 2 else "pty_fft2_bf16x6"
         _lib.check(getattr(_lib.lib(), name + "_workspace_bytes")(batch, W, ctypes.byref(n)), name + "_workspace_bytes")
-        ws = self.aux("fft2_tensor_core", int(n.value))
-        _lib.check(getattr(_lib.lib(), name)(_ptr(x), _ptr(out), batch, W, int(inverse), _ptr(ws), ws.numel(),
-                                             stream.cuda_stream), name)
+        ws, mark = self._ordered_aux("fft2_tensor_core", int(n.value), stream)
+        st = getattr(_lib.lib(), name)(_ptr(x), _ptr(out), batch, W, int(inverse), _ptr(ws), ws.numel(),
+                                       stream.cuda_stream)
+        mark()
+        _lib.check(st, name)
         return out
 
     @staticmethod

@@ -26,6 +26,8 @@ implementation.
 """
 from __future__ import annotations
 
+import warnings
+
 import numpy as np
 import torch
 
@@ -33,6 +35,31 @@ from . import _lib
 from .engine import Geometry, default_engine, make_problem
 
 N_CONSTRAINTS = 14   # entries of constraint_contributions (pypty/objective.py:768-921)
+
+
+class ComputePrecisionWarning(RuntimeWarning):
+    """Inputs or ``default_complex`` ask for complex128, but the GPU path computes in
+    complex64 (the results come back in the caller's dtype)."""
+
+
+def _precision_check(this_obj, full_probe, default_complex):
+    """The reference's default dtype is "double" (``pypty/iterative.py:58-60``: complex128
+    arrays, ``default_complex`` complex128). The kernels compute in complex64 with FP64 loss
+    and step-size reductions; this warns (once per call site, Python's default filter) when
+    double precision was asked for, instead of narrowing silently."""
+    def is_c128(x):
+        try:
+            return np.dtype(x) == np.complex128
+        except TypeError:
+            return False
+    asked = is_c128(default_complex) or any(
+        is_c128(getattr(a, "dtype", None)) or (isinstance(a, torch.Tensor) and a.dtype == torch.complex128)
+        for a in (this_obj, full_probe))
+    if asked:
+        warnings.warn("pypty_gb300 computes the loss and gradients in complex64 (FP64 loss and "
+                      "step-size reductions); complex128 inputs are rounded to complex64 and the "
+                      "results returned as complex128", ComputePrecisionWarning, stacklevel=3)
+    return asked
 
 
 def _unsupported(cond, what):
@@ -69,18 +96,25 @@ _PINNED = {}
 def measured_tensor(measured_array, device, load_one_by_one):
     """The measured patterns as the kernels read them. With ``load_one_by_one`` (the
     reference keeps the dataset in host memory and copies each batch, ``objective.py:398-409``)
-    a host array is pinned once and read in place by the kernels over the host link, so a
-    dataset larger than HBM needs no device copy; otherwise it is copied to the device."""
+    a host array is copied into a pinned buffer and read in place by the kernels over the host
+    link, so a dataset larger than HBM needs no device copy; otherwise it is copied to the
+    device. The reference reads the caller's array on every call, so the pinned buffer is
+    refreshed from it on every call too (a host copy), unless the array is read-only and
+    cannot have changed since the buffer was filled."""
     if isinstance(measured_array, torch.Tensor) and (measured_array.is_cuda or measured_array.is_pinned()):
         return measured_array.to(torch.float32).contiguous()
     if not load_one_by_one:
         return _device_tensor(measured_array, torch.float32, device)
     key = id(measured_array)
     hit = _PINNED.get(key)
-    if hit is None or hit[0] is not measured_array:
-        host = np.ascontiguousarray(_to_numpy(measured_array), dtype=np.float32)
+    host = _to_numpy(measured_array)
+    if hit is None or hit[0] is not measured_array or tuple(hit[1].shape) != tuple(host.shape):
         _PINNED.clear()                      # one dataset pinned at a time
-        _PINNED[key] = hit = (measured_array, torch.from_numpy(host).pin_memory())
+        pinned = torch.empty(tuple(host.shape), dtype=torch.float32, pin_memory=True)
+        np.copyto(pinned.numpy(), host, casting="unsafe")
+        _PINNED[key] = hit = (measured_array, pinned)
+    elif not (isinstance(host, np.ndarray) and not host.flags.writeable):
+        np.copyto(hit[1].numpy(), host, casting="unsafe")   # the caller may have changed it in place
     return hit[1]
 
 
@@ -106,7 +140,8 @@ def prepare(this_obj, full_probe, this_pos_array, this_pos_correction, this_tilt
     build the C-ABI problem and scan geometry: returns (problem, geometry, variant) where
     variant is None for the fused far-field path, else the keyword arguments of
     ``Engine.loss_and_direction_variants``. ``NotImplementedError`` names the first
-    unsupported flag."""
+    unsupported flag. Warns ``ComputePrecisionWarning`` when complex128 is asked for."""
+    _precision_check(this_obj, full_probe, default_complex)
     _unsupported(recon_type not in _lib.RECON_TYPES, "recon_type=%r" % (recon_type,))
     _unsupported(propmethod != "multislice", "propmethod=%r" % (propmethod,))
     compressed = algorithm_type in _lib.COMPRESSED_ALGORITHMS

@@ -252,7 +252,7 @@ class LBFGS:
             c = self.cfg
             kw = dict(self.variant)
             if self.tilts is not None:   # the reference evaluates tilts + tilts_correction (objective.py:343)
-                kw["tilts"] = (self.tilts + tcorr).cpu().numpy() if tcorr is not None else self.tilts.cpu().numpy()
+                kw["tilts"] = (self.tilts + tcorr) if tcorr is not None else self.tilts   # stays on the device
                 kw["step_tilts"] = c.update_tilts
             if ab is not None:
                 kw["aberrations"], kw["step_aberrations"] = ab, c.update_aberrations

@@ -1,7 +1,7 @@
 """Generate golden vectors by running the reference's own NumPy path.
 
-Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
-/root/reference)::
+Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT`` names the
+reference checkout; it is required)::
 
     python tests/golden/make_golden.py [case names]   # every case and the core case without names
 

@@ -1,7 +1,7 @@
 """Golden vectors of the optimizer step, from the reference's own NumPy path.
 
-Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
-/root/reference)::
+Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT`` names the
+reference checkout; it is required)::
 
     python tests/golden/make_golden_lbfgs.py [clean lbfgs refine static scenarios]   # all without names
 

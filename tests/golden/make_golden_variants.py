@@ -2,8 +2,8 @@
 measured-data preprocessing, detector-upsampling and static-background branches, produced by
 running the reference's own NumPy path.
 
-Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT``, default
-/root/reference)::
+Run where the reference sources are mounted (``PYPTY_REFERENCE_ROOT`` names the
+reference checkout; it is required)::
 
     python tests/golden/make_golden_variants.py [case names]   # every case without names
 

@@ -10,7 +10,8 @@ import os
 import sys
 import types
 
-REFERENCE_ROOT = os.environ.get("PYPTY_REFERENCE_ROOT", "/root/reference")
+# the checkout of the reference sources; required (no default location)
+REFERENCE_ROOT = os.environ.get("PYPTY_REFERENCE_ROOT", "")
 
 
 class _Anything:
@@ -36,8 +37,9 @@ def import_reference():
     """Return the reference ``pypty`` package (NumPy backend)."""
     if "pypty" in sys.modules and hasattr(sys.modules["pypty"], "objective"):
         return sys.modules["pypty"]
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "pypty")):
-        raise ImportError("reference sources not found under %s" % REFERENCE_ROOT)
+    if not REFERENCE_ROOT or not os.path.isdir(os.path.join(REFERENCE_ROOT, "pypty")):
+        raise ImportError("set PYPTY_REFERENCE_ROOT to the reference checkout (the directory holding pypty/); "
+                          "got %r" % REFERENCE_ROOT)
     _stub("h5py", File=_Anything)
     mpl = _stub("matplotlib")
     for sub in ["pyplot", "patches", "patheffects", "colors", "cm", "gridspec"]:

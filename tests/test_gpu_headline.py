@@ -1,0 +1,129 @@
+"""Parity at the benchmarked workload itself: 128 px probe with 3 incoherent modes, 20 slices
+2 A apart, a 512 x 512 x 20 object, a 32 x 32 scan at 0.4 A with U(+-0.2 A) jitter, Poisson
+loss (``ml``), position refinement on -- the inputs ``bench.py`` builds (same seeds, measured
+patterns simulated by the library's forward model plus Poisson noise).
+
+* A 24-position subset spread over the scan (corners and edges included) against the FP64
+  oracle (complex128 restatement of ``pypty/objective.py:47-967``): the fused path in one
+  batch (compute_batch 256, the benchmark's batch) and in ragged batches of 7, loss relative
+  error <= 1e-5, object / probe / position gradients <= 1e-4 relative L2 (the complex64
+  tolerances).
+* The layered path on the same subset with each DFT engine (FP32 register FFT, BF16x3 and
+  BF16x6 tensor-core GEMMs) against the same oracle; the FP32 engine within the complex64
+  tolerances, the tensor-core engines within the bounds written below, every error printed.
+* All 1024 positions in batches of 256, exactly the benchmark's call, against the same
+  positions run as four separate 256-position calls: the loss and the gradients are sums over
+  positions, so the full call must equal the sum of its parts (loss to FP64 rounding, each
+  position's gradient bit for bit, object and probe gradients to float32 rounding). With the
+  subset pinned to the oracle, this carries parity to the benchmark's full call and its loss.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from golden_io import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+LOSS_TOL = 1e-5
+GRAD_TOL = 1e-4
+# loss, gradient bounds per DFT engine at this depth (20 slices, 3 modes); measured on a GB300:
+# FP32 FFT 5.6e-9 / 1.0e-5..4.1e-5, BF16x6 6.8e-9 / 3.2e-5..1.8e-4 (the tensor core's biased
+# accumulation inside each MMA over ~80 chained DFT passes), BF16x3 carries its 2^-17 split error
+ENGINE_TOL = {"fp32_fft": (1e-5, 1e-4), "bf16x6": (1e-5, 5e-4), "bf16x3": (5e-5, 2e-3)}
+
+SUBSET = np.array([0, 31, 45, 130, 211, 300, 377, 402, 470, 511, 555, 600, 640, 703, 768, 777, 800, 851, 900,
+                   930, 961, 992, 1010, 1023])
+
+
+@pytest.fixture(scope="module")
+def headline():
+    import torch
+
+    import bench
+    from pypty_gb300.engine import Engine, Geometry, make_problem
+    dev = torch.device("cuda", 0)
+    eng = Engine(dev)
+    cfg = dict(bench.CONFIGS["multislice"], name="multislice")
+    wl = bench.build_workload(cfg)
+    geo = Geometry.make(wl["ipos"], wl["corr"])
+    common = dict(algorithm=cfg["algorithm"], wavelength=wl["wavelength"], pixel_size_x=wl["px"],
+                  pixel_size_y=wl["px"], slice_distance=wl["dz"], compute_batch=cfg["batch"])
+    prob = make_problem(cfg["W"], wl["obj0"].shape, cfg["Mp"], geo, step_pos=True, **common)
+    meas_d = bench.simulate_measured(eng, prob, wl, geo)
+    torch.cuda.synchronize(dev)
+    return dict(eng=eng, wl=wl, cfg=cfg, common=common, meas_d=meas_d, meas=meas_d.cpu().numpy(),
+                obj_d=torch.from_numpy(wl["obj0"]).to(dev), probe_d=torch.from_numpy(wl["probe"]).to(dev))
+
+
+@pytest.fixture(scope="module")
+def fp64_subset(headline):
+    from oracle import ptycho_oracle as orc
+    wl = headline["wl"]
+    return orc.loss_and_direction(
+        wl["obj0"].astype(np.complex128), wl["probe"].astype(np.complex128), wl["ipos"],
+        wl["corr"].astype(np.float64), wl["dz"], 1.0, headline["meas"].astype(np.float64), "ml",
+        wl["wavelength"], 1, 1, 1, wl["px"], wl["px"], 2 / 3, 0.0, SUBSET, 1, 7,
+        float_dtype=np.float64, complex_dtype=np.complex128)
+
+
+def _call(h, sequence, batch, layered=None):
+    import torch
+    from pypty_gb300.engine import Geometry, make_problem
+    wl, cfg = h["wl"], h["cfg"]
+    geo = Geometry.make(wl["ipos"], wl["corr"], sequence)
+    kw = dict(h["common"], compute_batch=batch)
+    prob = make_problem(cfg["W"], wl["obj0"].shape, cfg["Mp"], geo, step_pos=True, **kw)
+    if layered is None:
+        out = h["eng"].loss_and_direction(prob, h["obj_d"], h["probe_d"], geo, h["meas_d"])
+    else:
+        out = h["eng"].loss_and_direction_layered(prob, h["obj_d"], h["probe_d"], geo, h["meas_d"], engine=layered)
+    torch.cuda.synchronize()
+    ls = out[0].cpu().numpy()
+    return float(ls[0]), float(ls[1]), out[1].cpu().numpy(), out[2].cpu().numpy(), out[3].cpu().numpy()
+
+
+def _errors(got, ref):
+    return dict(loss=abs(got[0] - ref[0]) / abs(ref[0]), sse=abs(got[1] - ref[1]) / abs(ref[1]),
+                object_grad=rel_l2(got[2], ref[2]), probe_grad=rel_l2(got[3], ref[3]),
+                pos_grad=rel_l2(got[4], ref[4]))
+
+
+@pytest.mark.parametrize("batch", [256, 7])
+def test_headline_subset_against_fp64_oracle(headline, fp64_subset, batch):
+    e = _errors(_call(headline, SUBSET, batch), fp64_subset)
+    print("headline subset, fused path, batch %d: %s" % (batch, e))
+    assert e["loss"] <= LOSS_TOL and e["sse"] <= LOSS_TOL
+    assert e["object_grad"] <= GRAD_TOL and e["probe_grad"] <= GRAD_TOL and e["pos_grad"] <= GRAD_TOL
+
+
+@pytest.mark.parametrize("engine_name", ["fp32_fft", "bf16x6", "bf16x3"])
+def test_headline_subset_layered_engines(headline, fp64_subset, engine_name):
+    e = _errors(_call(headline, SUBSET, 7, layered=engine_name), fp64_subset)
+    print("headline subset, layered %s: %s" % (engine_name, e))
+    lt, gt = ENGINE_TOL[engine_name]
+    assert e["loss"] <= lt
+    assert e["object_grad"] <= gt and e["probe_grad"] <= gt and e["pos_grad"] <= gt
+
+
+def test_headline_full_call_is_the_sum_of_its_batches(headline):
+    n = headline["wl"]["ipos"].shape[0]
+    full = _call(headline, np.arange(n), 256)
+    parts = [_call(headline, np.arange(k, min(k + 256, n)), 256) for k in range(0, n, 256)]
+    print("headline full call: loss %.10e sse %.10e" % (full[0], full[1]))
+    loss_sum = float(np.sum([p[0] for p in parts]))
+    assert np.isfinite(full[0])
+    assert abs(full[0] - loss_sum) <= 1e-12 * abs(full[0])
+    assert abs(full[1] - float(np.sum([p[1] for p in parts]))) <= 1e-12 * abs(full[1])
+    og = np.sum([p[2].astype(np.complex128) for p in parts], axis=0)
+    pg = np.sum([p[3].astype(np.complex128) for p in parts], axis=0)
+    posg = np.sum([p[4] for p in parts], axis=0)
+    assert rel_l2(full[2], og) <= 1e-5
+    assert rel_l2(full[3], pg) <= 1e-5
+    assert np.array_equal(full[4], posg)   # each position's gradient depends on that position alone

@@ -284,3 +284,17 @@ def test_windows_at_object_edges(engine, W):
         assert rel_l2(g, ref[k]) <= max(GRAD_TOL, 3 * rel_l2(r32[k], ref[k])), (k, rel_l2(g, ref[k]))
     # the object gradient reaches the last row and column
     assert np.abs(og[-1]).max() > 0 and np.abs(og[:, -1]).max() > 0
+
+
+def test_pinned_patterns_follow_in_place_changes():
+    """With load_one_by_one the patterns are read from a pinned host buffer; the reference
+    reads the caller's array on every call (objective.py:398-409), so a change made in place
+    between two calls must reach the kernels."""
+    import torch
+    from pypty_gb300 import objective
+    meas = np.ones((3, 64, 64), np.float32)
+    a = objective.measured_tensor(meas, torch.device("cuda", 0), True)
+    assert a.is_pinned() and float(a[1, 2, 3]) == 1.0
+    meas[1, 2, 3] = 7.0
+    b = objective.measured_tensor(meas, torch.device("cuda", 0), True)
+    assert float(b[1, 2, 3]) == 7.0

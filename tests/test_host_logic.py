@@ -205,3 +205,35 @@ def test_probe_scenarios_route_to_the_variants_path():
     assert list(v["probe_marker"]) == [0, 2]
     _, _, v = objective.prepare(**base_kwargs(probe_marker=np.array([0, 1])))
     assert v is None
+
+
+def test_complex128_request_warns_once_and_names_complex64():
+    """The reference's default dtype is "double" (pypty/iterative.py:58-60); the GPU path
+    computes in complex64 and says so instead of narrowing silently."""
+    import warnings
+    kw = base_kwargs(this_obj=np.ones((96, 96, 1, 1), np.complex128),
+                     full_probe=np.ones((64, 64, 1), np.complex128), default_complex=np.complex128,
+                     default_float=np.float64)
+    with pytest.warns(objective.ComputePrecisionWarning, match="complex64"):
+        objective.prepare(**kw)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error", objective.ComputePrecisionWarning)
+        objective.prepare(**base_kwargs())          # complex64 throughout: no warning
+    with pytest.warns(objective.ComputePrecisionWarning):
+        objective.prepare(**base_kwargs(default_complex=np.complex128))   # the dtype argument alone
+
+
+def test_duplicate_sequence_entries_keep_the_last_position_gradient_rule():
+    """finalize_scalars_kernel writes pos_grad[seq[i]] only for the last occurrence of a
+    position in the sequence; this restates that selection on the host for a sequence with
+    repeats inside one round of 256 entries and across rounds."""
+    rng = np.random.default_rng(0)
+    seq = rng.integers(0, 40, 700)
+    writer = {}
+    for base in range(0, len(seq), 256):
+        r = seq[base:base + 256]
+        for k, s in enumerate(r):
+            if not np.any(r[k + 1:] == s):
+                writer[int(s)] = base + k
+    last = {int(s): i for i, s in enumerate(seq)}
+    assert writer == last
