@@ -206,13 +206,14 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(cfg, wl, algorithm, budget_s=15.0):
+def cpu_baseline(cfg, wl, algorithm, budget_s=15.0, cores=None):
     """The oracle (NumPy restatement of the reference path) on a bounded sample of positions,
-    on all host cores (scipy.fft workers): a short calibration call sizes the sample so that
-    the timed call takes about `budget_s` seconds."""
+    on `cores` host cores (scipy.fft workers; default all): a short calibration call sizes the
+    sample so that the timed call takes about `budget_s` seconds. cores=1 is the reference as
+    shipped (pypty/fft.py:111-156 passes scipy.fft no workers)."""
     import scipy.fft
     from oracle import ptycho_oracle as orc
-    cores = os.cpu_count() or 1
+    cores = cores or os.cpu_count() or 1
     n_max = wl["ipos"].shape[0]
 
     def run(n):
@@ -724,8 +725,12 @@ def main():
             line["optimizer"] = {"error": str(exc)}
     if not args.no_cpu_baseline:
         cb = cpu_baseline(cfg, wl, cfg["algorithm"])
-        cb.pop("seconds", None)
-        cb.pop("positions", None)
+        one = cpu_baseline(cfg, wl, cfg["algorithm"], budget_s=10.0, cores=1)
+        for d in (cb, one):
+            d.pop("seconds", None)
+            d.pop("positions", None)
+        cb["one_core"] = {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"],
+                          "note": "scipy.fft single-threaded, as the reference ships"}
         line["cpu_baseline"] = cb
     print(json.dumps(line))
     if world > 1:

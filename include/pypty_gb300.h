@@ -504,6 +504,21 @@ int pty_profile_end(double* ms_by_kernel, int32_t* launches_by_kernel, int32_t n
 const char* pty_kernel_name(int32_t id);
 int pty_kernel_count(void);
 
+/*
+ * Launch-graph cache of pty_loss_and_direction (no counterpart in the reference, which
+ * issues its array operations one by one from Python). The second call with the same
+ * problem (every field, and the values of slice_distances), the same pointers, workspace
+ * size and stream captures the call's launch sequence into a CUDA graph; later calls with
+ * that key replay it with one graph launch. The graph's copies of positions_host,
+ * pos_correction_host and sequence_host read those buffers when it runs, so their current
+ * contents are used; the host checks of every call still run first. Not cached: calls while
+ * the launch profiler records, calls on a stream that is itself being captured, 256 px
+ * windows, and calls whose host buffers are pageable (their copies cannot be captured).
+ * Up to 16 keys are kept (least recently used replaced). pty_graph_cache_info reports the
+ * keys seen, the graphs built, the keys found uncapturable and the calls served by replay.
+ */
+int pty_graph_cache_info(int32_t* keys, int32_t* graphs, int32_t* uncapturable, int64_t* replays);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,7 @@ SIGNATURES = {
     "pty_profile_end": ([_F64P, _I32P, _I32], ctypes.c_int),
     "pty_kernel_name": ([_I32], ctypes.c_char_p),
     "pty_kernel_count": ([], ctypes.c_int),
+    "pty_graph_cache_info": ([_I32P, _I32P, _I32P, ctypes.POINTER(_I64)], ctypes.c_int),
     "pty_fourier_clean_workspace_bytes": ([_I32, _I32, ctypes.POINTER(_SZ)], ctypes.c_int),
     "pty_fourier_clean": ([_VP, _VP, _F64, _VP, _I32, _I32, _I64, _F32, _F32, _VP, _VP, _SZ, _VP], ctypes.c_int),
     "pty_fourier_clean_prepare": ([_I32, _I32, _F32, _F32, _VP, _VP, _SZ, _VP], ctypes.c_int),

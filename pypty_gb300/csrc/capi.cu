@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 
 #include "plan.h"
 
@@ -34,6 +36,154 @@ int upload_geometry(const pty_problem_t* p, const Plan& q, void* ws, const int32
   return PTY_OK;
 }
 
+int launch_path(const pty_problem_t* p, const Plan& q, const void* obj, const void* probe, const int32_t* pos,
+                const float* corr, const int32_t* seq, const float* measured, double* loss_sse,
+                void* object_grad, void* probe_grad, float* pos_grad, float* patterns, void* ws,
+                cudaStream_t st);
+
+// ------------------------------------------------------------------ launch-graph cache
+// A call of pty_loss_and_direction is 15-40 launches plus three small copies. Repeated calls
+// with the same problem and the same buffers (an optimizer's line search, a benchmark loop)
+// replay one CUDA graph instead: the second call with a given key captures the launch sequence
+// on the caller's stream, later ones launch the instantiated graph. The geometry copies in the
+// graph read the caller's host buffers when the graph runs, so their current contents are used;
+// the host-side checks (validation, positions in range) still run on every call. Calls are not
+// cached while the launch profiler records, when the caller's stream is itself being captured,
+// for 256-px windows, or when a host buffer is pageable (its copy cannot be captured).
+struct GraphKey {
+  int device;
+  pty_problem_t prob;
+  uint64_t dist_hash;
+  const void* ptr[10];
+  size_t ws_bytes;
+  cudaStream_t st;
+  bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
+};
+
+struct GraphEntry {
+  GraphKey key;
+  bool used = false;
+  bool uncapturable = false;
+  int calls = 0;
+  uint64_t last = 0;
+  cudaGraphExec_t exec = nullptr;
+};
+
+constexpr int kGraphSlots = 16;
+std::mutex g_graph_mu;
+GraphEntry g_graphs[kGraphSlots];
+uint64_t g_graph_clock = 0;
+
+GraphKey make_key(const pty_problem_t* p, const void* const (&ptrs)[10], size_t ws_bytes, cudaStream_t st) {
+  GraphKey k;
+  std::memset(&k, 0, sizeof(k));   // padding bytes take part in the comparison
+  cudaGetDevice(&k.device);
+  k.prob = *p;
+  k.prob.slice_distances = nullptr;
+  uint64_t h = 1469598103934665603ull;   // FNV-1a over the per-step distances (baked into the launches)
+  if (p->slice_distances) {
+    const unsigned char* b = reinterpret_cast<const unsigned char*>(p->slice_distances);
+    for (size_t i = 0; i < (size_t)(p->n_slices > 1 ? p->n_slices - 1 : 0) * sizeof(float); ++i) h = (h ^ b[i]) * 1099511628211ull;
+    h ^= 1;
+  }
+  k.dist_hash = h;
+  for (int i = 0; i < 10; ++i) k.ptr[i] = ptrs[i];
+  k.ws_bytes = ws_bytes;
+  k.st = st;
+  return k;
+}
+
+// host pointers must be page-locked (or device memory) for their copies to be captured
+bool capturable_host(const void* ptr) {
+  if (!ptr) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Stream to capture on: a private non-blocking stream per device (capture is not permitted on
+// the legacy default stream that callers often use; a capture executes nothing, so the stream
+// it is recorded on does not matter for the graph).
+cudaStream_t capture_stream(int device) {
+  static cudaStream_t streams[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  if (!streams[device] && cudaStreamCreateWithFlags(&streams[device], cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    streams[device] = nullptr;
+  }
+  return streams[device];
+}
+
+// Runs the call through the cache; returns false when the caller should launch directly.
+bool run_cached(const pty_problem_t* p, const Plan& q, const void* obj, const void* probe, const int32_t* pos,
+                const float* corr, const int32_t* seq, const float* measured, double* loss_sse, void* object_grad,
+                void* probe_grad, float* pos_grad, void* ws, size_t ws_bytes, cudaStream_t st, int* rc) {
+  if (q.W > 128 || prof_active()) return false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return false;
+  }
+  const void* ptrs[10] = {obj, probe, pos, corr, seq, measured, loss_sse, object_grad, probe_grad, pos_grad};
+  const GraphKey key = make_key(p, ptrs, ws_bytes, st);
+  std::lock_guard<std::mutex> lock(g_graph_mu);
+  GraphEntry* e = nullptr;
+  GraphEntry* victim = &g_graphs[0];
+  for (GraphEntry& g : g_graphs) {
+    if (g.used && g.key == key) {
+      e = &g;
+      break;
+    }
+    if (!g.used || (victim->used && g.last < victim->last)) victim = &g;
+  }
+  if (!e) {   // first call with this key: record it and launch directly
+    if (victim->exec) {
+      cudaStreamSynchronize(victim->key.st);   // its last replay may still run
+      cudaGraphExecDestroy(victim->exec);
+    }
+    *victim = GraphEntry{};
+    victim->key = key;
+    victim->used = true;
+    victim->calls = 1;
+    victim->last = ++g_graph_clock;
+    return false;
+  }
+  e->last = ++g_graph_clock;
+  e->calls += 1;
+  if (e->uncapturable) return false;
+  if (!e->exec) {
+    if (!capturable_host(pos) || !capturable_host(seq) || !capturable_host(corr)) {
+      e->uncapturable = true;
+      return false;
+    }
+    cudaStream_t cap = capture_stream(key.device);
+    if (!cap || cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      e->uncapturable = true;
+      return false;
+    }
+    const int r = launch_path(p, q, obj, probe, pos, corr, seq, measured, loss_sse, object_grad, probe_grad,
+                              pos_grad, nullptr, ws, cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cap, &graph);
+    cudaGraphExec_t exec = nullptr;
+    const bool ok = r == PTY_OK && ec == cudaSuccess && graph &&
+                    cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+      cudaGetLastError();
+      e->uncapturable = true;
+      return false;   // nothing ran: the caller launches directly
+    }
+    e->exec = exec;
+  }
+  *rc = cudaGraphLaunch(e->exec, st) == cudaSuccess ? PTY_OK : PTY_ERR_CUDA;
+  return true;
+}
+
 int run_common(const pty_problem_t* p, const void* obj, const void* probe, const int32_t* pos,
                const float* corr, const int32_t* seq, const float* measured, double* loss_sse,
                void* object_grad, void* probe_grad, float* pos_grad, float* patterns, void* ws,
@@ -46,6 +196,18 @@ int run_common(const pty_problem_t* p, const void* obj, const void* probe, const
   const Plan q = make_plan(p);
   if (ws_bytes < q.total) return PTY_ERR_WORKSPACE;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!patterns && run_cached(p, q, obj, probe, pos, corr, seq, measured, loss_sse, object_grad, probe_grad,
+                              pos_grad, ws, ws_bytes, st, &rc))
+    return rc;
+  return launch_path(p, q, obj, probe, pos, corr, seq, measured, loss_sse, object_grad, probe_grad, pos_grad,
+                     patterns, ws, st);
+}
+
+int launch_path(const pty_problem_t* p, const Plan& q, const void* obj, const void* probe, const int32_t* pos,
+                const float* corr, const int32_t* seq, const float* measured, double* loss_sse,
+                void* object_grad, void* probe_grad, float* pos_grad, float* patterns, void* ws,
+                cudaStream_t st) {
+  int rc;
   if ((rc = upload_geometry(p, q, ws, pos, corr, seq, st))) return rc;
   if (q.W == 64)
     return run_path<64>(p, q, static_cast<const float2*>(obj), static_cast<const float2*>(probe), measured,
@@ -190,6 +352,26 @@ const char* pty_kernel_name(int32_t id) { return (id >= 0 && id < KID_COUNT) ? k
 
 int pty_kernel_count(void) { return KID_COUNT; }
 
+
+int pty_graph_cache_info(int32_t* keys, int32_t* graphs, int32_t* uncapturable, int64_t* replays) {
+  std::lock_guard<std::mutex> lock(g_graph_mu);
+  int32_t k = 0, g = 0, u = 0;
+  int64_t r = 0;
+  for (const GraphEntry& e : g_graphs) {
+    if (!e.used) continue;
+    ++k;
+    if (e.exec) {
+      ++g;
+      r += e.calls - 2;   // the first call launched directly, the second captured and launched
+    }
+    if (e.uncapturable) ++u;
+  }
+  if (keys) *keys = k;
+  if (graphs) *graphs = g;
+  if (uncapturable) *uncapturable = u;
+  if (replays) *replays = r;
+  return PTY_OK;
+}
 
 int pty_version(void) { return 100; }
 

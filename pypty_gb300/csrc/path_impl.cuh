@@ -60,24 +60,47 @@ struct Path {
     return PTY_OK;
   }
 
+  // Independent launches of a call's ends (the twiddles and probe spectrum beside the tables and
+  // the object transpose; the probe-gradient transform beside the object-gradient transpose and
+  // the scalars) run on two streams: fork() makes the side stream wait for st, join() makes st
+  // wait for the side stream. While the launch profiler records, everything stays on st.
+  cudaStream_t fork() {
+    SideStream* sd = nullptr;
+    if (prof_active() || side_stream(&sd) != PTY_OK) return st;
+    if (cudaEventRecord(sd->ev[0], st) != cudaSuccess || cudaStreamWaitEvent(sd->s, sd->ev[0], 0) != cudaSuccess)
+      return st;
+    return sd->s;
+  }
+  int join(cudaStream_t other) {
+    if (other == st) return PTY_OK;
+    SideStream* sd = nullptr;
+    if (side_stream(&sd) != PTY_OK) return PTY_ERR_CUDA;
+    prof_mark(other, -1);
+    if (cudaEventRecord(sd->ev[1], other) != cudaSuccess || cudaStreamWaitEvent(st, sd->ev[1], 0) != cudaSuccess)
+      return PTY_ERR_CUDA;
+    return PTY_OK;
+  }
+
   int prepare(const float2* obj, const float2* probe) {
     int rc = attributes();
     if (rc) return rc;
-    prof_mark(st, KID_TWIDDLES);
-    build_twiddles_kernel<W><<<1, 256, 0, st>>>(tw);
+    cudaStream_t fs = fork();
+    prof_mark(fs, KID_TWIDDLES);
+    build_twiddles_kernel<W><<<1, 256, 0, fs>>>(tw);
+    if (p->probe_shift) {
+      prof_mark(fs, KID_PROBE_FFT);
+      probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, fs>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
+    }
     prof_mark(st, KID_TABLES);
     tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);
     if (q.per_step)
       launch_step_props<W>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
                            ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
-    if (p->probe_shift) {
-      prof_mark(st, KID_PROBE_FFT);
-      probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, st>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
-    }
     const int nyx = q.Ny * q.Nx;
     prof_mark(st, KID_OBJ_TO_SLICES);
     obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(obj, at<float2>(ws, q.o_obj), nyx, q.zm);
     if (cudaMemsetAsync(at<int>(ws, q.o_err), 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
+    if ((rc = join(fs))) return rc;
     return cuda_status();
   }
 
@@ -203,22 +226,24 @@ struct Path {
   int finalize(double* loss_sse, float2* object_grad, float2* probe_grad, float* pos_grad, bool with_grads) {
     const int nyx = q.Ny * q.Nx;
     const bool do_pos = with_grads && p->step_pos;
+    cudaStream_t fs = st;
     if (with_grads) {
+      if (p->step_probe) {
+        fs = fork();
+        prof_mark(fs, KID_PROBE_FINAL);
+        // the chunk sum over the GPU first (into chunk 0), then one block per mode transforms
+        probe_chunks_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp), 256, 0, fs>>>(at<float2>(ws, q.o_partial),
+                                                                                     q.nchunk, q.Mp, (int)WW);
+        probe_final_kernel<W><<<q.Mp, T, Smem<W>::bytes, fs>>>(at<float2>(ws, q.o_partial), 1, q.Mp,
+                                                               ta.mask_sc, tw, probe_grad);
+      } else if (probe_grad) {
+        cudaMemsetAsync(probe_grad, 0, WW * q.Mp * sizeof(float2), st);
+      }
       if (p->step_obj) {
         prof_mark(st, KID_SLICES_TO_OBJ);
         slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(at<float2>(ws, q.o_grad), object_grad, nyx, q.zm);
       } else if (object_grad) {
         cudaMemsetAsync(object_grad, 0, (size_t)nyx * q.zm * sizeof(float2), st);
-      }
-      if (p->step_probe) {
-        prof_mark(st, KID_PROBE_FINAL);
-        // the chunk sum over the GPU first (into chunk 0), then one block per mode transforms
-        probe_chunks_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp), 256, 0, st>>>(at<float2>(ws, q.o_partial),
-                                                                                     q.nchunk, q.Mp, (int)WW);
-        probe_final_kernel<W><<<q.Mp, T, Smem<W>::bytes, st>>>(at<float2>(ws, q.o_partial), 1, q.Mp,
-                                                               ta.mask_sc, tw, probe_grad);
-      } else if (probe_grad) {
-        cudaMemsetAsync(probe_grad, 0, WW * q.Mp * sizeof(float2), st);
       }
       if (pos_grad) cudaMemsetAsync(pos_grad, 0, (size_t)q.N * 2 * sizeof(float), st);
     }
@@ -226,6 +251,8 @@ struct Path {
     finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                 at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
                                                 do_pos ? 1 : 0, at<int>(ws, q.o_err), loss_sse, pos_grad);
+    int rc = join(fs);
+    if (rc) return rc;
     prof_mark(st, -1);
     return cuda_status();
   }
