@@ -38,27 +38,47 @@ namespace dg {
 constexpr int BM = 128, BK = 64, THREADS = 512, STAGES = 2;
 constexpr int NPART = THREADS / 128;   // warps per TMEM lane quadrant: each drains BN / NPART columns
 
-// S = number of BF16 terms per FP32 operand: 2 (BF16x3: products hh, hl, lh) or 3 (BF16x6:
-// products with term indices i + j <= 2, ~FP32 accuracy); BN shrinks to 128 for S = 3 so that
-// two stages fit in shared memory.
+// S = number of BF16 slices per FP32 operand of A:
+//   S = 2 (BF16x3): floating split a = hi + lo (hi = bf16(a), lo = bf16(a - hi)), the same for
+//         B; products hh, hl, lh in one accumulator (~2^-17 relative per product).
+//   S = 3 (BF16x6, exact accumulation): fixed-point integer slices. Every row of A is scaled per
+//         64-wide K block by 2^(7 - E) (2^E just above the block's largest magnitude) and cut
+//         into integers s0, s1, s2 in [-128, 128] with a 2^(7-E) = s0 + s1 2^-8 + s2 2^-16 (+ <=
+//         2^-17); B = 2^-7 (u0 + u1 2^-8 + u2 2^-16) likewise with a fixed scale (|B| <= 1).
+//         Integers of 8 bits are exact in BF16 and their products exact in FP32, so the main
+//         product s0 u0, summed over a 64-wide K block (< 2^20), is exact however the tensor
+//         core accumulates; the five correction products (s0 u1, s1 u0 at 2^-8; s0 u2, s1 u1,
+//         s2 u0 at 2^-16, pre-scaled by 2^-8 in the slices: s2 in A, u2 and a copy of u1 in B)
+//         share a second accumulator whose truncation, scaled 2^-8 below the main one, stays
+//         under FP32 rounding. The only roundings left are the round-to-nearest drains, so the
+//         error does not pile up with a bias over chained transforms.
+// B carries TB slices: 2 for S = 2, 4 (u0, u1, u2 2^-8, u1 2^-8) for S = 3. BN shrinks to 128
+// for S = 3 so that two stages fit in shared memory.
 template <int W, int S>
 struct Cfg {
+  static constexpr bool EXACT = S == 3;
+  static constexpr int TB = EXACT ? 4 : S;
   static constexpr int NTOT = 2 * W;
   static constexpr int BNMAX = S == 2 ? 256 : 128;
   static constexpr int BN = NTOT < BNMAX ? NTOT : BNMAX;
   static constexpr int NT = NTOT / BN;
   static constexpr int KC = (2 * W) / BK;
-  static constexpr int A_BYTES = BM * BK * 2;          // one term
+  static constexpr int A_BYTES = BM * BK * 2;          // one slice
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE = S * A_BYTES + S * B_BYTES;
+  static constexpr int STAGE = S * A_BYTES + TB * B_BYTES;
   static constexpr int SMEM = STAGES * STAGE + 1024;   // + slack for 1024-byte alignment
-  static constexpr size_t IMG_BYTES = (size_t)S * NT * KC * B_BYTES;   // every term's image, one direction
-  // TMEM: two K-block buffers (ping-pong); with S = 3 each holds the main product hi*hi and,
-  // separately, the correction products (2^-8 smaller, so their accumulation error is too)
+  static constexpr size_t IMG_BYTES = (size_t)TB * NT * KC * B_BYTES;   // every slice's image, one direction
+  // TMEM: two K-block buffers (ping-pong); with S = 3 each holds the main product s0 u0 and,
+  // separately, the correction products
   static constexpr int ACCS = S == 3 ? 2 : 1;
   static constexpr int TMEM_COLS = 2 * ACCS * BN;
   static_assert(TMEM_COLS <= 512, "TMEM holds 512 columns");
 };
+
+// ring of per-row scale exponents of the exact variant: block kc's are written in iteration kc
+// and read by the drain in iteration kc + 1; iteration kc + 4 rewrites the slot, after two
+// block barriers that every drain of kc precedes
+constexpr int EXP_RING = 4;
 
 // Pre-split, pre-swizzled images of B^T for one direction: [term][nt][kc][BN x 64 block].
 template <int W, int S>
@@ -79,12 +99,27 @@ __global__ void dft_matrix_kernel(uint8_t* img, int inverse) {
     const int so = n & 1, si = kk & 1;
     const double v = so == 0 ? (si == 0 ? wr : -wi) : (si == 0 ? wi : wr);
     const size_t blk = ((size_t)nt * C::KC + kc) * C::B_BYTES + umma::sw128_offset(r, k);
-    double rest = v;
+    auto put = [&](int term, double x) {   // x exactly representable in BF16 by construction
+      *reinterpret_cast<__nv_bfloat16*>(img + (size_t)term * C::NT * C::KC * C::B_BYTES + blk) =
+          __float2bfloat16_rn((float)x);
+    };
+    if constexpr (C::EXACT) {
+      // 128 v = u0 + u1 2^-8 + u2 2^-16 + (|.| <= 2^-17), u_i integers in [-128, 128] (exact in double)
+      const double x0 = 128.0 * v, u0 = rint(x0);
+      const double x1 = (x0 - u0) * 256.0, u1 = rint(x1);
+      const double u2 = rint((x1 - u1) * 256.0);
+      put(0, u0);
+      put(1, u1);
+      put(2, u2 * 0.00390625);   // 2^-16 products, pre-scaled into the 2^-8 accumulator
+      put(3, u1 * 0.00390625);   // for s1 u1
+    } else {
+      double rest = v;
 #pragma unroll
-    for (int term = 0; term < S; ++term) {
-      const __nv_bfloat16 t = __float2bfloat16_rn((float)rest);
-      rest -= (double)__bfloat162float(t);
-      *reinterpret_cast<__nv_bfloat16*>(img + (size_t)term * C::NT * C::KC * C::B_BYTES + blk) = t;
+      for (int term = 0; term < S; ++term) {
+        const __nv_bfloat16 t = __float2bfloat16_rn((float)rest);
+        rest -= (double)__bfloat162float(t);
+        put(term, (double)__bfloat162float(t));
+      }
     }
   }
 }
@@ -99,6 +134,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], drain_bar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int s_abort;   // a bounded wait ran out somewhere in the CTA: issue nothing more
+  __shared__ int16_t rowexp[C::EXACT ? EXP_RING : 1][BM];   // exact variant: per-row scale exponents
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // the N tiles of one row tile are adjacent in the grid: the second read of A hits L2
   const long long row0 = (long long)blockIdx.y * BM;
@@ -137,19 +173,30 @@ __global__ void __launch_bounds__(THREADS, 1)
     drained = kc;
     mbar_wait(&drain_bar[buf], drain_par[buf], &e);
     umma::fence_after_sync();
+    // exact variant: this thread's row (TMEM lane 32 q + lane) carries scale 2^(E - 7) from A and
+    // 2^-7 from B
+    float rs = 1.0f;
+    if constexpr (C::EXACT) rs = ldexpf(1.0f, (int)rowexp[kc % EXP_RING][32 * q + lane] - 14);
 #pragma unroll
     for (int c0 = 0; c0 < HALF; c0 += 32) {
       const uint32_t col = (uint32_t)(buf * C::ACCS * C::BN + h * HALF + c0);
       float v[32];
       umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
-      if constexpr (C::ACCS == 2) {
+      if constexpr (C::EXACT) {
         float w[32];
         umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col + C::BN, w);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] += w[j];
-      }
+        for (int j = 0; j < 32; ++j) acc[c0 + j] = fmaf(fmaf(w[j], 0.00390625f, v[j]), rs, acc[c0 + j]);
+      } else {
+        if constexpr (C::ACCS == 2) {
+          float w[32];
+          umma::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col + C::BN, w);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) acc[c0 + j] += v[j];
+          for (int j = 0; j < 32; ++j) v[j] += w[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[c0 + j] += v[j];
+      }
     }
     umma::fence_before_sync();
   };
@@ -182,9 +229,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint8_t* sB = sA + S * C::A_BYTES;
     if (kc >= STAGES) mbar_wait(&empty_bar[s], empty_par[s], &e);   // the MMAs of kc - STAGES are done
     if (tid == 0 && !e) {
-      mbar_expect_tx(&full_bar[s], S * C::B_BYTES);
+      mbar_expect_tx(&full_bar[s], C::TB * C::B_BYTES);
 #pragma unroll
-      for (int term = 0; term < S; ++term)
+      for (int term = 0; term < C::TB; ++term)
         bulk_copy_g2s(sB + term * C::B_BYTES, img_nt + term * TERM + (size_t)kc * C::B_BYTES, C::B_BYTES,
                       &full_bar[s]);
       copy_pending[s] = true;
@@ -195,6 +242,34 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int r = qq >> 4, c4 = qq & 15;
       const uint32_t off = umma::sw128_offset(r, 4 * c4);
       float4 rest = pre[i];
+      if constexpr (C::EXACT) {
+        // the row's 64 values of this K block sit in 16 consecutive lanes (c4 = 0..15): their
+        // largest magnitude m = f 2^E (f in [0.5, 1)) sets the scale 2^(7 - E), |a 2^(7-E)| < 128
+        float m = fmaxf(fmaxf(fabsf(rest.x), fabsf(rest.y)), fmaxf(fabsf(rest.z), fabsf(rest.w)));
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        int E = 0;
+        frexpf(m, &E);
+        E = max(E, -100);   // a (near-)zero block: keep the scale finite
+        if (c4 == 0) rowexp[kc % EXP_RING][r] = (int16_t)E;
+        const float up = ldexpf(1.0f, 7 - E);
+        float x[4] = {rest.x * up, rest.y * up, rest.z * up, rest.w * up};
+        uint16_t t[3][4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          // x = s0 + s1 2^-8 + s2 2^-16 (+ <= 2^-17); every subtraction below is exact
+          const float s0 = rintf(x[c]);
+          const float x1 = (x[c] - s0) * 256.0f, s1 = rintf(x1);
+          const float s2 = rintf((x1 - s1) * 256.0f);
+          t[0][c] = umma::bf16_bits(s0);
+          t[1][c] = umma::bf16_bits(s1);
+          t[2][c] = umma::bf16_bits(s2 * 0.00390625f);   // pre-scaled into the 2^-8 accumulator
+        }
+#pragma unroll
+        for (int term = 0; term < 3; ++term)
+          *reinterpret_cast<uint2*>(sA + term * C::A_BYTES + off) =
+              make_uint2(t[term][0] | ((uint32_t)t[term][1] << 16), t[term][2] | ((uint32_t)t[term][3] << 16));
+      } else {
 #pragma unroll
       for (int term = 0; term < S; ++term) {
         // successive BF16 terms; every residual x - bf16(x) is exact in FP32
@@ -208,6 +283,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           rest.z -= umma::bf16_value(t2);
           rest.w -= umma::bf16_value(t3);
         }
+      }
       }
     }
     if (kc + 1 < C::KC) load_a(kc + 1);
@@ -235,6 +311,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int k = 0; k < BK / 16; ++k) {
         const uint32_t o = 32u * k;
+        if constexpr (C::EXACT) {
+          // (A slice, B slice, accumulator): s0 u0 -> main; s0 u1, s1 u0, s0 (u2 2^-8),
+          // s1 (u1 2^-8), (s2 2^-8) u0 -> corrections
+          constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 3, 0};
+#pragma unroll
+          for (int j = 0; j < 6; ++j)
+            umma::mma_bf16(j == 0 ? d : dc, umma::desc_sw128(a0 + pa[j] * C::A_BYTES + o),
+                           umma::desc_sw128(b0 + pb[j] * C::B_BYTES + o), idesc,
+                           k > 0 || j > 1 ? 1u : 0u);
+        } else {
         // every product of terms (i, j) with i + j < S, largest first
 #pragma unroll
         for (int sum = 0; sum < S; ++sum)
@@ -245,6 +331,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             umma::mma_bf16(main ? d : dc, umma::desc_sw128(a0 + i * C::A_BYTES + o),
                            umma::desc_sw128(b0 + (sum - i) * C::B_BYTES + o), idesc, !first);
           }
+        }
       }
       umma::mma_commit(&empty_bar[s]);
       umma::mma_commit(&drain_bar[kc & 1]);

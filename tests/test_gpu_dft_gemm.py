@@ -1,8 +1,9 @@
 """Window DFTs on the tensor cores (tcgen05, BF16x3 split precision) against FP64 NumPy.
 
 The error is stated, not hidden: relative L2 against the complex128 DFT must stay below
-3e-5 for BF16x3 (the products carry ~2^-17 relative error) and 2e-6 for BF16x6 (three BF16
-terms, six products); the FP32 register FFT is ~1e-7.
+3e-5 for BF16x3 (the products carry ~2^-17 relative error; measured 4.7-5.4e-6) and 1e-6 for
+BF16x6 (three fixed-point integer slices per operand, six products, exact accumulation of the
+main product; measured 3.1e-7); the FP32 register FFT is ~1.2-1.4e-7.
 """
 import numpy as np
 import pytest
@@ -12,7 +13,7 @@ from golden_io import rel_l2
 pytestmark = pytest.mark.gpu
 
 BF16X3_TOL = 3e-5
-BF16X6_TOL = 2e-6   # three BF16 terms: FP32-level
+BF16X6_TOL = 1e-6   # three fixed-point slices: FP32-level
 
 
 @pytest.fixture(scope="module")
