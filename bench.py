@@ -238,7 +238,12 @@ def cpu_baseline(cfg, wl, algorithm, budget_s=15.0, cores=None):
 def run_warm_start(args, cfg):
     """Learned vs flat start (the warm-start configuration): train on simulated specimens, then
     reconstruct held-out specimens with the GPU-resident L-BFGS from both starts and report the
-    wall time to 0.02 rad phase RMSE (inference included for the learned start)."""
+    wall time to 0.02 rad phase RMSE (inference included for the learned start).
+
+    The RMSE that decides is the one of the depth-averaged phase (projected phase / Z, per
+    slice scale): the 20 slices are 2 A apart, a tenth of the probe's depth of field (~22 A at
+    300 kV and 30 mrad), so their individual phases are not determined by the data and no start
+    reaches 0.02 rad per slice; the per-slice RMSE is reported beside it."""
     import torch
     from pypty_gb300 import warmstart as ws
     from pypty_gb300.engine import Engine
@@ -247,7 +252,7 @@ def run_warm_start(args, cfg):
     eng = Engine(dev)
     scene = ws.make_scene(eng, W=cfg["W"], Z=cfg["Z"], Mp=cfg["Mp"], obj_n=cfg["N_obj"], n_scan=cfg["n_scan"])
     t0 = time.perf_counter()
-    xs, ys = ws.make_dataset(scene, args.train, eng, seed=100)
+    xs, ys = ws.make_dataset(scene, args.train, eng, seed=100, target_cutoff=0.25)
     torch.cuda.synchronize(dev)
     t_data = time.perf_counter() - t0
     stats = (xs.mean(dim=(0, 2, 3)), xs.std(dim=(0, 2, 3)) + 1e-6)
@@ -276,41 +281,44 @@ def run_warm_start(args, cfg):
         start[:F, :F, :, 0] = torch.exp(1j * pred.permute(1, 2, 0).to(torch.complex64))
         torch.cuda.synchronize(dev)
         t_inf = time.perf_counter() - t_inf0
-        tgt = ws.predictable_target(phase[:, :F, :F], 0.1, eng)
-        row = {"inference_s": round(t_inf, 4), "pred_std": round(float(pred.std()), 5),
-               "target_std": round(float(tgt.std()), 5),
-               "pred_target_corr": round(float(torch.corrcoef(torch.stack([pred.flatten(), tgt.flatten()]))[0, 1]), 4)}
-        for proj in (False, True):
-            key = "projected" if proj else "slices"
-            cf, _ = ws.reconstruct(scene, meas, phase, flat, eng, epochs=args.recon_epochs, region=region,
-                                   projected=proj, target=-1.0)
-            cl, _ = ws.reconstruct(scene, meas, phase, start, eng, epochs=args.recon_epochs, region=region,
-                                   projected=proj, target=-1.0)
-            r0f = ws.phase_rmse(flat, phase, region, proj)
-            r0l = ws.phase_rmse(start, phase, region, proj)
-            levels = {"0.02": 0.02, "0.9_flat0": 0.9 * r0f, "0.75_flat0": 0.75 * r0f, "0.5_flat0": 0.5 * r0f}
+        tgt = ws.predictable_target(phase[:, :F, :F], 0.25, eng)
+        a, b = pred[0, c0:c1, c0:c1].flatten(), tgt[0, c0:c1, c0:c1].flatten()
+        row = {"inference_s": round(t_inf, 4), "pred_target_corr": round(float(torch.corrcoef(torch.stack([a, b]))[0, 1]), 4)}
+        cf, _ = ws.reconstruct(scene, meas, phase, flat, eng, epochs=args.recon_epochs, region=region, target=None)
+        cl, _ = ws.reconstruct(scene, meas, phase, start, eng, epochs=args.recon_epochs, region=region, target=None)
+        for key, idx, dm in (("depth_mean", 2, True), ("slices", 1, False)):
+            r0f = ws.phase_rmse(flat, phase, region, depth_mean=dm)
+            r0l = ws.phase_rmse(start, phase, region, depth_mean=dm)
+            levels = {"0.02": 0.02, "0.75_flat0": 0.75 * r0f, "0.5_flat0": 0.5 * r0f}
             row[key] = {"rmse0": {"flat": round(r0f, 4), "learned": round(r0l, 4)},
-                        "final": {"flat": round(cf[-1][1], 4), "learned": round(cl[-1][1], 4)},
-                        "time_to": {name: {"flat": ws.time_to(cf, lv), "learned": ws.time_to(cl, lv, t_inf)}
-                                    for name, lv in levels.items()},
-                        "flat_curve": [(round(a, 3), round(b, 4)) for a, b in cf[::5]],
-                        "learned_curve": [(round(a, 3), round(b, 4)) for a, b in cl[::5]]}
+                        "final": {"flat": round(cf[-1][idx], 4) if cf else None,
+                                  "learned": round(cl[-1][idx], 4) if cl else None},
+                        "time_to": {name: {"flat": ws.time_to(cf, lv, 0.0, idx, r0f),
+                                           "learned": ws.time_to(cl, lv, t_inf, idx, r0l)}
+                                    for name, lv in levels.items()}}
+        row["flat_curve"] = [(round(c[0], 3), round(c[1], 4), round(c[2], 4)) for c in cf[::5]]
+        row["learned_curve"] = [(round(c[0], 3), round(c[1], 4), round(c[2], 4)) for c in cl[::5]]
         rows.append(row)
 
-    def mean_time(key, level, who):
+    def stat(key, level, who):
         v = [r[key]["time_to"][level][who] for r in rows]
-        return float(np.mean(v)) if all(x is not None for x in v) else None
+        got = [x for x in v if x is not None]
+        return {"mean_s": float(np.mean(got)) if len(got) == len(v) else None, "reached": len(got), "of": len(v)}
 
-    summary = {key: {lv: {"flat_s": mean_time(key, lv, "flat"), "learned_s": mean_time(key, lv, "learned")}
-                     for lv in ("0.02", "0.9_flat0", "0.75_flat0", "0.5_flat0")} for key in ("slices", "projected")}
-    v_l, v_f = summary["slices"]["0.02"]["learned_s"], summary["slices"]["0.02"]["flat_s"]
-    line = {"metric": "time to 0.02 rad phase RMSE, learned vs plain init", "impl": "ours",
+    summary = {key: {lv: {"flat": stat(key, lv, "flat"), "learned": stat(key, lv, "learned")}
+                     for lv in ("0.02", "0.75_flat0", "0.5_flat0")} for key in ("depth_mean", "slices")}
+    for key in ("depth_mean", "slices"):
+        summary[key]["rmse0"] = {who: float(np.mean([r[key]["rmse0"][who] for r in rows])) for who in ("flat", "learned")}
+    v_l, v_f = summary["depth_mean"]["0.02"]["learned"]["mean_s"], summary["depth_mean"]["0.02"]["flat"]["mean_s"]
+    line = {"metric": "time to 0.02 rad phase RMSE (depth-averaged phase), learned vs plain init", "impl": "ours",
             "value": v_l, "unit": "s", "higher_is_better": False, "plain_s": v_f,
-            "ratio_learned_over_plain": (v_l / v_f) if v_l and v_f else None,
+            "ratio_learned_over_plain": (v_l / v_f) if v_l is not None and v_f else None,
             "summary": summary, "n_gpus": 1, "data": "synthetic", "dtype": "bf16 network, c64 reconstruction",
             "config": {"workload": cfg["desc"], "train_specimens": args.train, "test_specimens": args.test,
-                       "epochs": args.epochs, "recon_epochs": args.recon_epochs, "frame_px": F, "region": region},
+                       "epochs": args.epochs, "recon_epochs": args.recon_epochs, "frame_px": F, "region": region,
+                       "loss": "lsq_sqrt (amplitude)", "network_target": "depth-mean phase band-limited to 0.25 Nyquist"},
             "train": {"dataset_s": round(t_data, 2), "train_s": round(t_train, 2), "loss": [round(h, 5) for h in hist]},
+            "mean_pred_target_corr": float(np.mean([r["pred_target_corr"] for r in rows])),
             "specimens": rows}
     print(json.dumps(line))
 
@@ -519,11 +527,11 @@ def main():
                     help="256-px windows: keep every k-th slice's wave, recompute the rest")
     ap.add_argument("--no-optimizer", action="store_true",
                     help="skip the optimizer-step measurement (fourier_clean, L-BFGS epoch)")
-    ap.add_argument("--train", type=int, default=256, help="warm-start: training specimens")
-    ap.add_argument("--test", type=int, default=4, help="warm-start: held-out specimens")
+    ap.add_argument("--train", type=int, default=2000, help="warm-start: training specimens")
+    ap.add_argument("--test", type=int, default=100, help="warm-start: held-out specimens")
     ap.add_argument("--epochs", type=int, default=8, help="warm-start: training epochs")
-    ap.add_argument("--recon-epochs", type=int, default=80, help="warm-start: L-BFGS epochs per reconstruction")
-    ap.add_argument("--lr", type=float, default=3e-4, help="warm-start: Adam learning rate")
+    ap.add_argument("--recon-epochs", type=int, default=20, help="warm-start: L-BFGS epochs per reconstruction")
+    ap.add_argument("--lr", type=float, default=1e-3, help="warm-start: Adam learning rate")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config], name=args.config)
     if args.impl == "reference":

@@ -59,7 +59,10 @@ def make_probe(W, px_A, acc_voltage_kV, alpha_mrad, defocus_A, n_modes=1,
     """Defocused aperture probe with ``n_modes`` orthogonal incoherent modes.
 
     Mode 0 is the aperture-limited defocused probe. Higher modes multiply the aperture
-    function by low-order polynomials of (kx, ky) and are Gram-Schmidt orthogonalised.
+    function by low-order polynomials of (kx, ky) and are Gram-Schmidt orthogonalised. Every
+    mode is centred in the window (pixel (W/2, W/2)), as the reference builds its probe
+    (``fftshift(ifft2(...))``, ``pypty/utils.py:804``), so that a window at scan position p
+    illuminates the object around p + W/2.
     The modes are scaled so that mode j carries ``mode_powers[j]`` of the power and the
     mean far-field pattern of the unshifted probe through vacuum integrates to ``dose``:
     the FFT is unnormalised and modes are averaged, so W^2 * sum_j sum|P_j|^2 / n_modes
@@ -80,7 +83,7 @@ def make_probe(W, px_A, acc_voltage_kV, alpha_mrad, defocus_A, n_modes=1,
         raise ValueError("at most %d probe modes" % len(polys))
     modes = []
     for j in range(n_modes):
-        m = np.fft.ifft2(base * polys[j])
+        m = np.fft.fftshift(np.fft.ifft2(base * polys[j]))
         for q in modes:
             m = m - np.vdot(q, m) * q
         m = m / np.sqrt(np.vdot(m, m).real)
