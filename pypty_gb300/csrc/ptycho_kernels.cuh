@@ -413,9 +413,11 @@ struct FusedSmem {
 //                   field, loss and dL/dPsi after the last slice), IFFT
 //   steps Z+1..2Z   slice z = 2Z-s: object-gradient contribution, g *= conj(O_z), FFT,
 //                   *= conj(P), IFFT (z = 0: probe-gradient spectrum and position gradient)
-// Operands are prefetched by TMA bulk copies: the next step's window (O_z, or conj(psi_z) in
-// the adjoint) lands in the exchange buffer while the inverse transform finishes its last
-// register-only round; the adjoint's O_z arrives in the side buffer one step ahead.
+// Operands are prefetched by TMA bulk copies. O_z arrives in the side buffer (its first NST
+// elements per thread; the rest is loaded from global memory at the step) one step ahead,
+// in the forward and the adjoint alike; the adjoint's first step reuses the forward's last
+// O_z. The adjoint's conj(psi_z) lands in the exchange buffer while the inverse transform
+// finishes its last register-only round.
 // PH = 0: the whole pass (phase 0) with every phase branch compiled out; PH = 1: a.phase at
 // run time (the split halves and the multislice_core phases).
 template <int W, int PH>
@@ -487,7 +489,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   };
 
   float2 v[32];
-  bool side_next = false;         // the side buffer is free and its next copy not yet issued
+  int side_next = -1;       // the slice whose O_z the side buffer takes next (-1: none)
+  bool side_held = false;   // the side buffer holds the next step's O_z, already waited for
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
   const bool adjoint_only = (phase == 2 || phase == 4);
   const int s_begin = adjoint_only ? Z + 1 : 0;
@@ -497,8 +500,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     ld_native<W>(gb, v);
     issue_x(Z + 1);
     if (adj_stack) issue_side(Z - 1);
-  } else if (!a.probe_shift) {
-    issue_x(1);   // step 0 has no inverse transform to hide the copy behind
+  } else {
+    issue_side(0);   // the forward steps read O_z from the side buffer
   }
   for (int s = s_begin; s < s_end; ++s) {
     const bool fwd = (s >= 1 && s <= Z);
@@ -513,6 +516,14 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         for (int i = 0; i < 32; ++i) v[i] = a.probe[(size_t)(G::ry(t) * W + G::rx(t, i)) * a.Mp + p];
       }
     } else if (fwd) {
+      // O_z: elements NST.. straight from global memory (issued first), the rest from the side
+      // buffer, copied in during the previous step; the exchange buffer is not refilled
+      float4 otail[(32 - NST) / 2];
+      {
+        const float4* og = reinterpret_cast<const float4*>(obl_ptr(z));
+#pragma unroll
+        for (int j = NST / 2; j < 16; ++j) otail[j - NST / 2] = og[j * T + t];
+      }
       if (adj_stack) {
         float2 c[32];
 #pragma unroll
@@ -522,17 +533,19 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         // every earlier stack store of this thread as well
         if (z == Z - 1) fence_async_global();
       }
-      if (z == Z - 1 && adj_stack && phase == 0) issue_side(Z - 1);
-      mbar_wait(&bars[0], ph_x, a.err);
+      mbar_wait(&bars[1], ph_side, a.err);
       {
-        const float4* ob = reinterpret_cast<const float4*>(xbuf);
+        const float4* sd = reinterpret_cast<const float4*>(side);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const float4 q = ob[j * T + t];
+          const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
           v[2 * j] = cmul(v[2 * j], make_float2(q.x, q.y));
           v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
         }
       }
+      // the adjoint's first step (the same slice) reads the side buffer as it is
+      if (z + 1 < Z) side_next = z + 1;
+      else side_held = true;
       if (phase == 3 && z == Z - 1) {
         st_native<W>(a.exit_out + (((size_t)b * a.Mp + p) * a.Mo + m) * WW, v);   // the exit wave
         break;
@@ -561,7 +574,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
         }
         // g *= conj(O_z): elements < NST from the side buffer, the rest from the registers
-        mbar_wait(&bars[1], ph_side, a.err);
+        if (side_held) side_held = false;
+        else mbar_wait(&bars[1], ph_side, a.err);
         {
           const float4* sd = reinterpret_cast<const float4*>(side);
 #pragma unroll
@@ -571,7 +585,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
             v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
           }
         }
-        side_next = z > 0;   // the side buffer's next copy goes out after the next block barrier
+        if (z > 0) side_next = z - 1;   // its copy goes out after the next block barrier
       } else {
         const float4* ob = reinterpret_cast<const float4*>(xbuf);
 #pragma unroll
@@ -612,9 +626,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     if (s > 0) {
       F::forward_round1(v, tw1);
       F::forward_rest(v, xbuf, tw1, tw2, [&] {
-        if (side_next) {   // every thread has read the side buffer: refill it for slice z - 1
-          issue_side(z - 1);
-          side_next = false;
+        if (side_next >= 0) {   // every thread has read the side buffer: refill it
+          issue_side(side_next);
+          side_next = -1;
         }
       });
     }
@@ -757,11 +771,13 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // behind its register-only last round)
     F::inverse_head(v, xbuf, tw1, tw2);
     if (s + 1 < s_end) {
-      __syncthreads();   // every thread has finished reading the exchange buffer
-      issue_x(s + 1);
+      if (s + 1 > Z) {     // the adjoint steps read their first operand from the exchange buffer
+        __syncthreads();   // every thread has finished reading it
+        issue_x(s + 1);
+      }
       // every block asks for its operands at about the same time: bring the operand two steps
       // ahead (and, in the adjoint, the object window the side buffer takes next) into L2 now,
-      // so that the copies of the next steps read L2 instead of waiting for HBM
+      // so that the copies and loads of the next steps read L2 instead of waiting for HBM
       if (t == 0) {
         if (s + 2 < s_end) prefetch_l2(xsrc(s + 2), (uint32_t)(WW * sizeof(float2)));
         if (!fwd && adj_stack && z >= 2) prefetch_l2(obl_ptr(z - 2), (uint32_t)(WW * sizeof(float2)));
