@@ -469,28 +469,35 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 
   auto obl_ptr = [&](int z) { return a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW; };
   auto stack_ptr = [&](int z) { return a.stack + ((((size_t)b * Z + z) * a.Mp + p) * a.Mo + m) * WW; };
-  // the window step s reads from the exchange buffer (s >= 1)
-  auto xsrc = [&](int s) -> const float2* {
-    if (s <= Z) return obl_ptr(s - 1);
-    const int z = 2 * Z - s;
-    return adj_stack ? stack_ptr(z) : obl_ptr(z);
-  };
+  // O_z of step s >= 1: the adjoint steps read it from the exchange buffer, the forward steps
+  // through the side buffer
+  auto xsrc = [&](int s) -> const float2* { return obl_ptr(s <= Z ? s - 1 : 2 * Z - s); };
   auto issue_x = [&](int s) {
     if (t == 0) {
       fence_async_shared();
       bulk_load(xbuf, xsrc(s), (uint32_t)(WW * sizeof(float2)), &bars[0]);
     }
   };
-  auto issue_side = [&](int z) {
+  constexpr uint32_t kSideBytes = (uint32_t)(NST * T * sizeof(float2));
+  // the side buffer takes the first NST elements per thread (a prefix of the native layout) of
+  // a window: O_z in the forward, conj(psi_z) from the stack in the adjoint
+  auto issue_side = [&](const float2* src) {
     if (t == 0) {
       fence_async_shared();
-      bulk_load(side, obl_ptr(z), (uint32_t)(NST * T * sizeof(float2)), &bars[1]);
+      bulk_load(side, src, kSideBytes, &bars[1]);
     }
+  };
+  // the window of slice z that the staged side buffer goes to: the stack (forward) or this
+  // mode's gradient contribution (adjoint)
+  auto store_ptr = [&](int z, bool to_stack) {
+    return to_stack ? stack_ptr(z) : a.gsum + ((((size_t)b * Z + z) * a.Mo + m) * a.Mp + p) * WW;
   };
 
   float2 v[32];
-  int side_next = -1;       // the slice whose O_z the side buffer takes next (-1: none)
-  bool side_held = false;   // the side buffer holds the next step's O_z, already waited for
+  int side_next = -1;        // the slice whose window prefix the side buffer takes next
+  bool side_held = false;    // the side buffer holds the next step's operand, waited for
+  int store_z = -1;          // the side buffer is staged for a bulk store to store_ptr(store_z, ...)
+  bool store_stack = false;
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
   const bool adjoint_only = (phase == 2 || phase == 4);
   const int s_begin = adjoint_only ? Z + 1 : 0;
@@ -499,9 +506,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // adjoint half: resume from dL/d(exit wave) kept by the forward half
     ld_native<W>(gb, v);
     issue_x(Z + 1);
-    if (adj_stack) issue_side(Z - 1);
+    if (adj_stack) issue_side(stack_ptr(Z - 1));
   } else {
-    issue_side(0);   // the forward steps read O_z from the side buffer
+    issue_side(obl_ptr(0));
   }
   for (int s = s_begin; s < s_end; ++s) {
     const bool fwd = (s >= 1 && s <= Z);
@@ -524,26 +531,30 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
 #pragma unroll
         for (int j = NST / 2; j < 16; ++j) otail[j - NST / 2] = og[j * T + t];
       }
-      if (adj_stack) {
-        float2 c[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) c[i] = cconj(v[i]);
-        st_native<W>(stack_ptr(z), c);
-        // the adjoint reads the stack back by TMA: one proxy fence after the last store orders
-        // every earlier stack store of this thread as well
-        if (z == Z - 1) fence_async_global();
-      }
+      float4* sd = reinterpret_cast<float4*>(side);
+      float4* st = adj_stack ? reinterpret_cast<float4*>(stack_ptr(z)) : nullptr;
       mbar_wait(&bars[1], ph_side, a.err);
-      {
-        const float4* sd = reinterpret_cast<const float4*>(side);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
-          v[2 * j] = cmul(v[2 * j], make_float2(q.x, q.y));
-          v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
+      for (int j = 0; j < 16; ++j) {
+        const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
+        if (adj_stack) {
+          // conj(psi_z) to the stack: elements < NST in place of O_z in the side buffer, whence
+          // a bulk copy takes them out behind the transform; the rest straight from the registers
+          const float4 c = make_float4(v[2 * j].x, -v[2 * j].y, v[2 * j + 1].x, -v[2 * j + 1].y);
+          if (j < NST / 2) sd[j * T + t] = c;
+          else st[j * T + t] = c;
+        }
+        v[2 * j] = cmul(v[2 * j], make_float2(q.x, q.y));
+        v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(q.z, q.w));
+      }
+      if (adj_stack) {
+        fence_async_shared();
+        // the adjoint's first step (the same slice) reads conj(psi_z) from the side buffer itself
+        if (!(z == Z - 1 && phase == 0)) {
+          store_z = z;
+          store_stack = true;
         }
       }
-      // the adjoint's first step (the same slice) reads the side buffer as it is
       if (z + 1 < Z) side_next = z + 1;
       else side_held = true;
       if (phase == 3 && z == Z - 1) {
@@ -551,42 +562,40 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         break;
       }
     } else {
-      mbar_wait(&bars[0], ph_x, a.err);
       if (adj_stack) {
-        // elements NST.. of O_z come straight from global memory; issue them first
-        float4 otail[(32 - NST) / 2];
+        // conj(psi_z): elements NST.. straight from global memory (this thread stored them in
+        // the forward), the rest in the side buffer
+        float4 stail[(32 - NST) / 2];
         {
-          const float4* og = reinterpret_cast<const float4*>(obl_ptr(z));
+          const float4* sg = reinterpret_cast<const float4*>(stack_ptr(z));
 #pragma unroll
-          for (int j = NST / 2; j < 16; ++j) otail[j - NST / 2] = og[j * T + t];
+          for (int j = NST / 2; j < 16; ++j) stail[j - NST / 2] = sg[j * T + t];
         }
+        if (side_held) side_held = false;
+        else mbar_wait(&bars[1], ph_side, a.err);
         // contribution conj(psi_z) * g of this probe mode, to its own window of the gradient
         // buffer ([position][slice][object mode][probe mode]); grad_windows_kernel adds the
         // probe modes in ascending order before the band limit (multislice_core.py:184-191), so
-        // the adjoint needs no cluster barrier and no remote reads
-        float4* g4 = reinterpret_cast<float4*>(a.gsum + ((((size_t)b * Z + z) * a.Mo + m) * a.Mp + p) * WW);
-        const float4* x4 = reinterpret_cast<const float4*>(xbuf);
+        // the adjoint needs no cluster barrier and no remote reads. Elements < NST replace
+        // conj(psi_z) in the side buffer, whence a bulk copy takes them out behind the transform.
+        float4* g4 = reinterpret_cast<float4*>(store_ptr(z, false));
+        float4* sd = reinterpret_cast<float4*>(side);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const float4 q = x4[j * T + t];
+          const float4 q = (j < NST / 2) ? sd[j * T + t] : stail[j - NST / 2];
           const float2 g0 = cmul(make_float2(q.x, q.y), v[2 * j]);
           const float2 g1 = cmul(make_float2(q.z, q.w), v[2 * j + 1]);
-          g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
+          if (j < NST / 2) sd[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
+          else g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
         }
-        // g *= conj(O_z): elements < NST from the side buffer, the rest from the registers
-        if (side_held) side_held = false;
-        else mbar_wait(&bars[1], ph_side, a.err);
-        {
-          const float4* sd = reinterpret_cast<const float4*>(side);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float4 q = (j < NST / 2) ? sd[j * T + t] : otail[j - NST / 2];
-            v[2 * j] = cmulc(v[2 * j], make_float2(q.x, q.y));
-            v[2 * j + 1] = cmulc(v[2 * j + 1], make_float2(q.z, q.w));
-          }
-        }
-        if (z > 0) side_next = z - 1;   // its copy goes out after the next block barrier
-      } else {
+        fence_async_shared();
+        store_z = z;
+        store_stack = false;
+        if (z > 0) side_next = z - 1;
+      }
+      // g *= conj(O_z), O_z in the exchange buffer
+      mbar_wait(&bars[0], ph_x, a.err);
+      {
         const float4* ob = reinterpret_cast<const float4*>(xbuf);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -625,12 +634,23 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // ------------------------------------------------ forward FFT
     if (s > 0) {
       F::forward_round1(v, tw1);
+      const bool staged = store_z >= 0;
+      auto side_src = [&](int zz) { return fwd ? obl_ptr(zz) : stack_ptr(zz); };
       F::forward_rest(v, xbuf, tw1, tw2, [&] {
-        if (side_next >= 0) {   // every thread has read the side buffer: refill it
-          issue_side(side_next);
+        // every thread has finished with the side buffer: copy its staged part out, or refill it
+        if (staged) {
+          if (t == 0) bulk_store(store_ptr(store_z, store_stack), side, kSideBytes);
+          store_z = -1;
+        } else if (side_next >= 0) {
+          issue_side(side_src(side_next));
           side_next = -1;
         }
       });
+      if (side_next >= 0) {   // refill the side buffer once the bulk store has read it
+        if (t == 0) bulk_wait_read();
+        issue_side(side_src(side_next));
+        side_next = -1;
+      }
     }
 
     // ------------------------------------------------ frequency op
@@ -771,20 +791,28 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // behind its register-only last round)
     F::inverse_head(v, xbuf, tw1, tw2);
     if (s + 1 < s_end) {
-      if (s + 1 > Z) {     // the adjoint steps read their first operand from the exchange buffer
+      if (s + 1 > Z) {     // the adjoint steps read O_z from the exchange buffer
         __syncthreads();   // every thread has finished reading it
+        // the adjoint's side-buffer copies read the stack's bulk-stored parts back
+        if (s == Z && t == 0) bulk_wait_all();
         issue_x(s + 1);
       }
-      // every block asks for its operands at about the same time: bring the operand two steps
-      // ahead (and, in the adjoint, the object window the side buffer takes next) into L2 now,
-      // so that the copies and loads of the next steps read L2 instead of waiting for HBM
+      // every block asks for its operands at about the same time: bring O_z two steps ahead
+      // (and, in the adjoint, the stack window the side buffer takes after the next) into L2
+      // now, so that the copies and loads of the next steps read L2 instead of waiting for HBM
       if (t == 0) {
         if (s + 2 < s_end) prefetch_l2(xsrc(s + 2), (uint32_t)(WW * sizeof(float2)));
-        if (!fwd && adj_stack && z >= 2) prefetch_l2(obl_ptr(z - 2), (uint32_t)(WW * sizeof(float2)));
+        const int zs = 2 * Z - s - 2;
+        if (adj_stack && s >= Z && zs >= 0) prefetch_l2(stack_ptr(zs), (uint32_t)(WW * sizeof(float2)));
       }
     }
     F::inverse_tail(v, tw1);
   }
+  if (store_z >= 0) {   // staged by a step that left the loop before its forward transform
+    __syncthreads();
+    if (t == 0) bulk_store(store_ptr(store_z, store_stack), side, kSideBytes);
+  }
+  if (t == 0) bulk_wait_all();   // the bulk stores are complete before the block exits
   if (phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
 }
 

@@ -418,6 +418,26 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
   }
 }
 
+// Issue (one thread) a copy of `bytes` from shared `src` to global `dst` in chunks of at most
+// 64 KiB as one bulk group. The writer threads of `src` have run fence_async_shared() and a
+// block barrier before this; `src` may be overwritten after bulk_wait_read() in this thread.
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  constexpr uint32_t kChunk = 64u * 1024u;
+  for (uint32_t o = 0; o < bytes; o += kChunk) {
+    const uint32_t n = bytes - o < kChunk ? bytes - o : kChunk;
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(static_cast<char*>(dst) + o),
+                 "r"(smem_u32(src) + o), "r"(n)
+                 : "memory");
+  }
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// every bulk store of this thread has finished reading its shared-memory source
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// every bulk store of this thread has completed its writes to global memory
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Host/device builder of the twiddle tables in global memory (see load_twiddles).
 template <int W>
 __global__ void build_twiddles_kernel(float2* g_tw) {
