@@ -88,9 +88,10 @@ def alg_bytes_per_position(W, Z, Mp, Mo=1):
 def fused_bytes_per_position(W, Z, Mp, Mo=1):
     """Bytes the fused multislice kernel must move per position: band-limited object
     windows read forward and adjoint (16 Z Mo), wave stack write + read (16 Z Mp Mo),
-    probe-mode-summed gradient windows written (8 Z Mo), measured pattern read (4),
-    per-position probe-gradient spectra written (8 Mp)."""
-    return W * W * (16 * Z * Mo + 16 * Z * Mp * Mo + 8 * Z * Mo + 4 + 8 * Mp)
+    one object-gradient contribution window per probe mode written (8 Z Mp Mo; the modes are
+    summed in order by the band-limit kernel), measured pattern read (4), per-position
+    probe-gradient spectra written (8 Mp)."""
+    return W * W * (16 * Z * Mo + 16 * Z * Mp * Mo + 8 * Z * Mp * Mo + 4 + 8 * Mp)
 
 
 # DRAM bytes (read + write) per position of the fused kernel(s), from one ncu capture each

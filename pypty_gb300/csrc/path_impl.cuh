@@ -28,6 +28,14 @@ struct Path {
   cudaStream_t fst;    // stream of fused(): st, or alternately st and a third stream when overlapping
   float2* tw;
   TableArgs ta{};
+  // One slice and one object mode: the reference's (Ny, Nx, Z, Mo) layout is the slice layout,
+  // so the windows read the caller's object and the scatter writes the caller's gradient
+  // directly (no transposes).
+  const float2* obj_src = nullptr;
+  float2* grad_out = nullptr;
+  bool lists_done = false;         // batch 0's tile lists were built while the tables were
+  cudaStream_t pbranch = nullptr;  // one batch: the probe-gradient sum and the scalars run here,
+                                   // beside the object-gradient band limit and scatter
 
   Path(const pty_problem_t* p_, const Plan& q_, void* ws_, cudaStream_t st_)
       : p(p_), q(q_), ws(ws_), st(st_), side(st_), fst(st_) {
@@ -81,7 +89,9 @@ struct Path {
     return PTY_OK;
   }
 
-  int prepare(const float2* obj, const float2* probe) {
+  // early_lists: the call has one batch and object gradients, so batch 0's tile lists (which
+  // depend only on the geometry) are built beside the tables
+  int prepare(const float2* obj, const float2* probe, bool early_lists = false) {
     int rc = attributes();
     if (rc) return rc;
     cudaStream_t fs = fork();
@@ -91,14 +101,25 @@ struct Path {
       prof_mark(fs, KID_PROBE_FFT);
       probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, fs>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
     }
+    if (early_lists && q.nbatch == 1 && p->step_obj) {
+      prof_mark(fs, KID_TILE_LISTS);
+      tile_lists_kernel<<<q.ntiles, 256, 0, fs>>>(at<int>(ws, q.o_pos), seq_of(0), batch_count(0), W, q.ntx,
+                                                  at<int>(ws, q.o_lists), at<int>(ws, q.o_counts));
+      lists_done = true;
+    }
     prof_mark(st, KID_TABLES);
     tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);
     if (q.per_step)
       launch_step_props<W>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
                            ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
     const int nyx = q.Ny * q.Nx;
-    prof_mark(st, KID_OBJ_TO_SLICES);
-    obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(obj, at<float2>(ws, q.o_obj), nyx, q.zm);
+    if (q.zm == 1) {
+      obj_src = obj;
+    } else {
+      prof_mark(st, KID_OBJ_TO_SLICES);
+      obj_to_slices_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(obj, at<float2>(ws, q.o_obj), nyx, q.zm);
+      obj_src = at<float2>(ws, q.o_obj);
+    }
     if (cudaMemsetAsync(at<int>(ws, q.o_err), 0, sizeof(int), st) != cudaSuccess) return PTY_ERR_CUDA;
     if ((rc = join(fs))) return rc;
     return cuda_status();
@@ -113,7 +134,7 @@ struct Path {
 
   int windows(int ib) {
     WindowArgs wa{};
-    wa.obj = at<float2>(ws, q.o_obj);
+    wa.obj = obj_src;
     wa.pos = at<int>(ws, q.o_pos);
     wa.seq = seq_of(ib);
     wa.mask_sc = ta.mask_sc;
@@ -153,6 +174,7 @@ struct Path {
     fa.prop_edge = ta.prop_edge;
     fa.pyx = ta.pyx;
     fa.use_sep = (p->smooth_rolloff == 0.0f && !q.per_step) ? 1 : 0;
+    fa.mask_bin = p->smooth_rolloff == 0.0f ? 1 : 0;   // tables_kernel's mask is then 0/1
     fa.prop_steps = q.per_step ? at<float2>(ws, q.o_steps) : nullptr;
     fa.mask = ta.mask;
     fa.sx = ta.sx;
@@ -195,28 +217,31 @@ struct Path {
     const int* d_pos = at<int>(ws, q.o_pos);
     if (p->step_obj) {
       float2* gs = gsum(ib);
+      float2* gdst = grad_out ? grad_out : at<float2>(ws, q.o_grad);
       prof_mark(side, KID_GRAD_WINDOWS);
       grad_windows_kernel<W><<<(unsigned)(Bn * q.zm), T, Smem<W>::bytes, side>>>(gs, ta.mask_sc, tw, q.Mp);
       int* lists = at<int>(ws, q.o_lists);
       int* counts = at<int>(ws, q.o_counts);
-      prof_mark(side, KID_TILE_LISTS);
-      tile_lists_kernel<<<q.ntiles, 256, 0, side>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
+      if (!lists_done) {
+        prof_mark(side, KID_TILE_LISTS);
+        tile_lists_kernel<<<q.ntiles, 256, 0, side>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
+      }
       prof_mark(side, KID_SCATTER);
       float2* scpart = q.sgroups > 1 ? at<float2>(ws, q.o_scpart) : nullptr;
       scatter_tiles_kernel<<<dim3(q.ntiles, q.zm, q.sgroups), dim3(32, 8), 0, side>>>(
-          gs, d_pos, seq_b, lists, counts, at<float2>(ws, q.o_grad), Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0,
-          q.sgroups, scpart, q.Mp);
+          gs, d_pos, seq_b, lists, counts, gdst, Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0, q.sgroups, scpart,
+          q.Mp);
       if (q.sgroups > 1)
-        scatter_merge_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(scpart, at<float2>(ws, q.o_grad),
-                                                                            q.sgroups, q.Ny, q.Nx, q.ntx, q.zm,
-                                                                            ib > 0 ? 1 : 0);
+        scatter_merge_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(scpart, gdst, q.sgroups, q.Ny, q.Nx,
+                                                                            q.ntx, q.zm, ib > 0 ? 1 : 0);
     }
     if (p->step_probe) {
       const int nch = (Bn + q.chunk - 1) / q.chunk;
+      cudaStream_t ps = pbranch ? pbranch : side;
       // chunks beyond this batch's count keep their previous value: the first batch has the
       // largest count, so every chunk read later was written
-      prof_mark(side, KID_PROBE_PARTIAL);
-      probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, side>>>(
+      prof_mark(ps, KID_PROBE_PARTIAL);
+      probe_partial_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp, nch), 256, 0, ps>>>(
           fprobe(ib), at<float2>(ws, q.o_partial), Bn, q.Mp, (int)WW, q.chunk, ib > 0 ? 1 : 0);
     }
     return cuda_status();
@@ -226,10 +251,10 @@ struct Path {
   int finalize(double* loss_sse, float2* object_grad, float2* probe_grad, float* pos_grad, bool with_grads) {
     const int nyx = q.Ny * q.Nx;
     const bool do_pos = with_grads && p->step_pos;
-    cudaStream_t fs = st;
+    cudaStream_t fs = pbranch ? pbranch : st;
     if (with_grads) {
       if (p->step_probe) {
-        fs = fork();
+        if (!pbranch) fs = fork();
         prof_mark(fs, KID_PROBE_FINAL);
         // the chunk sum over the GPU first (into chunk 0), then one block per mode transforms
         probe_chunks_kernel<<<dim3((unsigned)((WW + 255) / 256), q.Mp), 256, 0, fs>>>(at<float2>(ws, q.o_partial),
@@ -240,15 +265,20 @@ struct Path {
         cudaMemsetAsync(probe_grad, 0, WW * q.Mp * sizeof(float2), st);
       }
       if (p->step_obj) {
-        prof_mark(st, KID_SLICES_TO_OBJ);
-        slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(at<float2>(ws, q.o_grad), object_grad, nyx, q.zm);
+        if (!grad_out) {
+          prof_mark(st, KID_SLICES_TO_OBJ);
+          slices_to_obj_kernel<<<(nyx + 255) / 256, 256, 0, st>>>(at<float2>(ws, q.o_grad), object_grad, nyx,
+                                                                  q.zm);
+        }
       } else if (object_grad) {
         cudaMemsetAsync(object_grad, 0, (size_t)nyx * q.zm * sizeof(float2), st);
       }
-      if (pos_grad) cudaMemsetAsync(pos_grad, 0, (size_t)q.N * 2 * sizeof(float), st);
     }
-    prof_mark(st, KID_FINALIZE);
-    finalize_scalars_kernel<<<1, 256, 0, st>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
+    // the scalars depend on the fused kernels alone: beside the scatter when there is a branch
+    cudaStream_t ss = pbranch ? pbranch : st;
+    if (with_grads && pos_grad) cudaMemsetAsync(pos_grad, 0, (size_t)q.N * 2 * sizeof(float), ss);
+    prof_mark(ss, KID_FINALIZE);
+    finalize_scalars_kernel<<<1, 256, 0, ss>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                 at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
                                                 do_pos ? 1 : 0, at<int>(ws, q.o_err), loss_sse, pos_grad);
     int rc = join(fs);
@@ -328,13 +358,15 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
              const float* measured, double* loss_sse, float2* object_grad, float2* probe_grad,
              float* pos_grad, float* patterns, void* ws, cudaStream_t st) {
   Path<W> P(p, q, ws, st);
-  int rc = P.prepare(obj, probe);
+  int rc = P.prepare(obj, probe, !patterns);
   if (rc) return rc;
+  if (!patterns && q.zm == 1 && p->step_obj && object_grad) P.grad_out = object_grad;
   if (q.nbuf == 2 && !prof_active()) {
     if ((rc = run_batches_overlapped(P, probe, measured, patterns))) return rc;
   } else {
     for (int ib = 0; ib < q.nbatch; ++ib) {
       if ((rc = P.windows(ib)) || (rc = P.fused(ib, 0, probe, measured, patterns))) return rc;
+      if (!patterns && q.nbatch == 1) P.pbranch = P.fork();   // after the fused kernel
       if (!patterns && (rc = P.gradients(ib))) return rc;
     }
   }
@@ -361,6 +393,7 @@ int run_backward(const pty_problem_t* p, const Plan& q, double* loss_sse, float2
   Path<W> P(p, q, ws, st);
   int rc = Path<W>::attributes();
   if (rc) return rc;
+  if (q.zm == 1 && p->step_obj && object_grad) P.grad_out = object_grad;
   if ((rc = P.fused(0, 2, nullptr, nullptr, nullptr)) || (rc = P.gradients(0))) return rc;
   return P.finalize(loss_sse, object_grad, probe_grad, pos_grad, true);
 }

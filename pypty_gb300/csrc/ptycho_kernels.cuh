@@ -297,6 +297,8 @@ struct FusedArgs {
   const float2* prop_edge;
   const float2* pyx;        // separable propagator factors (used when the mask is binary)
   int use_sep;
+  int mask_bin;             // the band-limit mask is 0/1 (no smooth roll-off): the mask bits and
+                            // the separable shift ramp stand in for the float mask
   const float2* prop_steps; // per-step tables [Z-1] (slice distances), step 0 with the edge
                             // power; nullptr: prop / prop_edge for every step
   const float* mask;        // natural, unscaled
@@ -331,6 +333,52 @@ __device__ __forceinline__ float2 shift_ramp(const FusedArgs& a, int ky, int kx,
   float s, c;
   sincosf(th, &s, &c);
   return make_float2(c * mk, s * mk);
+}
+
+// The same ramp for a binary mask, inside the mask: exp(i sx[kx] dx) * exp(i sy[ky] dy). A
+// thread's 32 frequency-layout elements i = q*Bq + r span Q distinct kx (by q) and Bq distinct
+// ky (by r), so Q + Bq sincos evaluations serve all 32 (the caller zeroes the elements outside
+// the mask). f(i, ky, kx, ramp) is called for every element, i a compile-time constant.
+template <int W, typename Fn>
+__device__ __forceinline__ void visit_sep_ramp(const FusedArgs& a, int t, float dy, float dx, Fn&& f) {
+  using G = Geo<W>;
+  constexpr int Q = G::Q, Bq = G::Bq;
+  auto phase = [](float s, float d) {
+    float sn, cs;
+    sincosf(__fmul_rn(s, d), &sn, &cs);
+    return make_float2(cs, sn);
+  };
+  if constexpr (Q <= Bq) {   // the Q x factors kept, one y factor at a time
+    float2 ex[Q];
+    static_for<0, Q>([&](auto QQ) {
+      constexpr int q = decltype(QQ)::value;
+      ex[q] = phase(a.sx[G::fkx(t, q * Bq)], dx);
+    });
+    static_for<0, Bq>([&](auto RR) {
+      constexpr int r = decltype(RR)::value;
+      const int ky = G::fky(t, r);
+      const float2 ey = phase(a.sy[ky], dy);
+      static_for<0, Q>([&](auto QQ) {
+        constexpr int q = decltype(QQ)::value;
+        f(std::integral_constant<int, q * Bq + r>{}, ky, G::fkx(t, q * Bq), cmul(ex[q], ey));
+      });
+    });
+  } else {                   // the Bq y factors kept, one x factor at a time
+    float2 ey[Bq];
+    static_for<0, Bq>([&](auto RR) {
+      constexpr int r = decltype(RR)::value;
+      ey[r] = phase(a.sy[G::fky(t, r)], dy);
+    });
+    static_for<0, Q>([&](auto QQ) {
+      constexpr int q = decltype(QQ)::value;
+      const int kx = G::fkx(t, q * Bq);
+      const float2 ex = phase(a.sx[kx], dx);
+      static_for<0, Bq>([&](auto RR) {
+        constexpr int r = decltype(RR)::value;
+        f(std::integral_constant<int, q * Bq + r>{}, G::fky(t, r), kx, cmul(ex, ey[r]));
+      });
+    });
+  }
 }
 
 // A thread's running sum of float32 terms, compensated: every add is Knuth's TwoSum, so hi + lo
@@ -428,6 +476,10 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   constexpr int T = G::T;
   constexpr int NST = S::NST;
   constexpr size_t WW = (size_t)W * W;
+  // W = 64 (few slices, latency-bound far field and probe steps): mask bits instead of the
+  // float mask, the separable shift ramp, measured values loaded a chunk ahead. At W = 128 the
+  // extra live values spill (measured slower), so these stay compiled out there.
+  constexpr bool kLean = (W == 64);
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
   double* red;
@@ -487,17 +539,15 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       bulk_load(side, src, kSideBytes, &bars[1]);
     }
   };
-  // the window of slice z that the staged side buffer goes to: the stack (forward) or this
-  // mode's gradient contribution (adjoint)
-  auto store_ptr = [&](int z, bool to_stack) {
-    return to_stack ? stack_ptr(z) : a.gsum + ((((size_t)b * Z + z) * a.Mo + m) * a.Mp + p) * WW;
-  };
+  // the window that the staged side buffer goes to: code z < Z is the stack window of slice z
+  // (forward), code Z + z this mode's gradient contribution of slice z (adjoint)
+  auto contrib_ptr = [&](int z) { return a.gsum + ((((size_t)b * Z + z) * a.Mo + m) * a.Mp + p) * WW; };
+  auto store_ptr = [&](int code) { return code < Z ? stack_ptr(code) : contrib_ptr(code - Z); };
 
   float2 v[32];
   int side_next = -1;        // the slice whose window prefix the side buffer takes next
   bool side_held = false;    // the side buffer holds the next step's operand, waited for
-  int store_z = -1;          // the side buffer is staged for a bulk store to store_ptr(store_z, ...)
-  bool store_stack = false;
+  int store_code = -1;       // the side buffer is staged for a bulk store to store_ptr(store_code)
   float2* gb = a.gbuf + (((size_t)b * a.Mp + p) * a.Mo + m) * WW;
   const bool adjoint_only = (phase == 2 || phase == 4);
   const int s_begin = adjoint_only ? Z + 1 : 0;
@@ -550,10 +600,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       if (adj_stack) {
         fence_async_shared();
         // the adjoint's first step (the same slice) reads conj(psi_z) from the side buffer itself
-        if (!(z == Z - 1 && phase == 0)) {
-          store_z = z;
-          store_stack = true;
-        }
+        if (!(z == Z - 1 && phase == 0)) store_code = z;
       }
       if (z + 1 < Z) side_next = z + 1;
       else side_held = true;
@@ -578,7 +625,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         // probe modes in ascending order before the band limit (multislice_core.py:184-191), so
         // the adjoint needs no cluster barrier and no remote reads. Elements < NST replace
         // conj(psi_z) in the side buffer, whence a bulk copy takes them out behind the transform.
-        float4* g4 = reinterpret_cast<float4*>(store_ptr(z, false));
+        float4* g4 = reinterpret_cast<float4*>(contrib_ptr(z));
         float4* sd = reinterpret_cast<float4*>(side);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -589,8 +636,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           else g4[j * T + t] = make_float4(g0.x, g0.y, g1.x, g1.y);
         }
         fence_async_shared();
-        store_z = z;
-        store_stack = false;
+        store_code = Z + z;
         if (z > 0) side_next = z - 1;
       }
       // g *= conj(O_z), O_z in the exchange buffer
@@ -634,13 +680,13 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     // ------------------------------------------------ forward FFT
     if (s > 0) {
       F::forward_round1(v, tw1);
-      const bool staged = store_z >= 0;
+      const bool staged = store_code >= 0;
       auto side_src = [&](int zz) { return fwd ? obl_ptr(zz) : stack_ptr(zz); };
       F::forward_rest(v, xbuf, tw1, tw2, [&] {
         // every thread has finished with the side buffer: copy its staged part out, or refill it
         if (staged) {
-          if (t == 0) bulk_store(store_ptr(store_z, store_stack), side, kSideBytes);
-          store_z = -1;
+          if (t == 0) bulk_store(store_ptr(store_code), side, kSideBytes);
+          store_code = -1;
         } else if (side_next >= 0) {
           issue_side(side_src(side_next));
           side_next = -1;
@@ -658,10 +704,18 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       if (!a.probe_shift) continue;   // the unshifted probe is already in real space
       const float2* pf = a.probe_f + (size_t)p * WW;
       const float inv = 1.0f / (float)WW;
+      if (kLean && a.mask_bin) {
+        const uint32_t mbits = sbits[t];
+        visit_sep_ramp<W>(a, t, dy, dx, [&](auto I, int, int, float2 ramp) {
+          constexpr int i = decltype(I)::value;
+          v[i] = ((mbits >> i) & 1u) ? cscale(cmul(pf[nidx<W>(i, t)], ramp), inv) : make_float2(0.f, 0.f);
+        });
+      } else {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int ky = G::fky(t, i), kx = G::fkx(t, i);
-        v[i] = cscale(cmul(pf[nidx<W>(i, t)], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
+        for (int i = 0; i < 32; ++i) {
+          const int ky = G::fky(t, i), kx = G::fkx(t, i);
+          v[i] = cscale(cmul(pf[nidx<W>(i, t)], shift_ramp<W>(a, ky, kx, a.mask[ky * W + kx], dy, dx)), inv);
+        }
       }
     } else if (fwd && z < Z - 1) {
       if (a.use_sep && !(z == 0 && a.use_edge)) {
@@ -680,10 +734,19 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     } else if (fwd) {
       // far field: Psi = FFT(exit) * mask, I = mean over modes |Psi|^2 (objective.py:501-512)
       __syncthreads();
+      if (kLean && a.mask_bin) {
+        const uint32_t mbits = sbits[t];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        v[i] = cscale(v[i], a.mask[G::fky(t, i) * W + G::fkx(t, i)]);
-        fs0[i * T + t] = cabs2(v[i]);
+        for (int i = 0; i < 32; ++i) {
+          if (!((mbits >> i) & 1u)) v[i] = make_float2(0.f, 0.f);
+          fs0[i * T + t] = cabs2(v[i]);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          v[i] = cscale(v[i], a.mask[G::fky(t, i) * W + G::fkx(t, i)]);
+          fs0[i * T + t] = cabs2(v[i]);
+        }
       }
       cluster.sync();
 #pragma unroll 1
@@ -706,16 +769,25 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       const float inv_modes = 1.0f / (float)nmodes;
       const float* meas = a.measured + (size_t)gi * WW;
       FSum lsum_c, ssum_c;
-      // eight pixels at a time: their measured values are loaded together, then used in order
-#pragma unroll 1
-      for (int i0 = 0; i0 < 32; i0 += 8) {
-        float mv[8];
+      // eight pixels at a time, used in order (W = 64: the next eight measured values are
+      // loaded while the current ones are used)
+      auto load8 = [&](int i0, float (&dst)[8]) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
           const int i = i0 + k;
           const int ky = G::fky(t, i), kx = G::fkx(t, i);
           const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
-          mv[k] = a.simulate ? 0.0f : meas[didx];
+          dst[k] = a.simulate ? 0.0f : meas[didx];
+        }
+      };
+      float mv[8], nx[8];
+      if constexpr (kLean) load8(0, mv);
+#pragma unroll 1
+      for (int i0 = 0; i0 < 32; i0 += 8) {
+        if constexpr (kLean) {
+          if (i0 + 8 < 32) load8(i0 + 8, nx);
+        } else {
+          load8(i0, mv);
         }
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -731,6 +803,10 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           float d = loss_pixel(a.algorithm, I, mv[k], lsum_c, ssum_c);
           if (nmodes > 1) d = d / (float)nmodes;           // objective.py:586-587
           fs1[i * T + t] = d;
+        }
+        if constexpr (kLean) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) mv[k] = nx[k];
         }
       }
       if (a.simulate) return;
@@ -808,9 +884,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     }
     F::inverse_tail(v, tw1);
   }
-  if (store_z >= 0) {   // staged by a step that left the loop before its forward transform
+  if (store_code >= 0) {   // staged by a step that left the loop before its forward transform
     __syncthreads();
-    if (t == 0) bulk_store(store_ptr(store_z, store_stack), side, kSideBytes);
+    if (t == 0) bulk_store(store_ptr(store_code), side, kSideBytes);
   }
   if (t == 0) bulk_wait_all();   // the bulk stores are complete before the block exits
   if (phase == 1) st_native<W>(gb, v);   // forward half: keep dL/d(exit wave)
