@@ -34,8 +34,9 @@ struct Path {
   const float2* obj_src = nullptr;
   float2* grad_out = nullptr;
   bool lists_done = false;         // batch 0's tile lists were built while the tables were
-  cudaStream_t pbranch = nullptr;  // one batch: the probe-gradient sum and the scalars run here,
-                                   // beside the object-gradient band limit and scatter
+  cudaStream_t pbranch = nullptr;  // one batch: the probe-gradient sum runs here, beside the
+                                   // object-gradient band limit and scatter
+  cudaStream_t sbranch = nullptr;  // one batch: the FP64 scalars and position gradient
 
   Path(const pty_problem_t* p_, const Plan& q_, void* ws_, cudaStream_t st_)
       : p(p_), q(q_), ws(ws_), st(st_), side(st_), fst(st_) {
@@ -79,6 +80,14 @@ struct Path {
       return st;
     return sd->s;
   }
+  // a second branch (the stream of the second fused kernel when batches overlap, free otherwise)
+  cudaStream_t fork2() {
+    SideStream* sd = nullptr;
+    if (prof_active() || side_stream(&sd) != PTY_OK) return st;
+    if (cudaEventRecord(sd->ev[2], st) != cudaSuccess || cudaStreamWaitEvent(sd->s2, sd->ev[2], 0) != cudaSuccess)
+      return st;
+    return sd->s2;
+  }
   int join(cudaStream_t other) {
     if (other == st) return PTY_OK;
     SideStream* sd = nullptr;
@@ -101,6 +110,9 @@ struct Path {
       prof_mark(fs, KID_PROBE_FFT);
       probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, fs>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
     }
+    if (q.sgroups > 1 && cudaMemsetAsync(at<int>(ws, q.o_done), 0, (size_t)q.ntiles * q.zm * sizeof(int), fs) !=
+                             cudaSuccess)
+      return PTY_ERR_CUDA;
     if (early_lists && q.nbatch == 1 && p->step_obj) {
       prof_mark(fs, KID_TILE_LISTS);
       tile_lists_kernel<<<q.ntiles, 256, 0, fs>>>(at<int>(ws, q.o_pos), seq_of(0), batch_count(0), W, q.ntx,
@@ -227,13 +239,13 @@ struct Path {
         tile_lists_kernel<<<q.ntiles, 256, 0, side>>>(d_pos, seq_b, Bn, W, q.ntx, lists, counts);
       }
       prof_mark(side, KID_SCATTER);
+      // sgroups > 1: the last run block of each tile adds the runs in order (counters in o_done,
+      // zeroed by prepare() and by each merging block)
       float2* scpart = q.sgroups > 1 ? at<float2>(ws, q.o_scpart) : nullptr;
+      int* done = q.sgroups > 1 ? at<int>(ws, q.o_done) : nullptr;
       scatter_tiles_kernel<<<dim3(q.ntiles, q.zm, q.sgroups), dim3(32, 8), 0, side>>>(
           gs, d_pos, seq_b, lists, counts, gdst, Bn, W, q.Ny, q.Nx, q.ntx, q.zm, ib > 0 ? 1 : 0, q.sgroups, scpart,
-          q.Mp);
-      if (q.sgroups > 1)
-        scatter_merge_kernel<<<dim3(q.ntiles, q.zm), dim3(32, 8), 0, side>>>(scpart, gdst, q.sgroups, q.Ny, q.Nx,
-                                                                            q.ntx, q.zm, ib > 0 ? 1 : 0);
+          q.Mp, done);
     }
     if (p->step_probe) {
       const int nch = (Bn + q.chunk - 1) / q.chunk;
@@ -275,13 +287,14 @@ struct Path {
       }
     }
     // the scalars depend on the fused kernels alone: beside the scatter when there is a branch
-    cudaStream_t ss = pbranch ? pbranch : st;
+    cudaStream_t ss = sbranch ? sbranch : st;
     if (with_grads && pos_grad) cudaMemsetAsync(pos_grad, 0, (size_t)q.N * 2 * sizeof(float), ss);
     prof_mark(ss, KID_FINALIZE);
     finalize_scalars_kernel<<<1, 256, 0, ss>>>(at<double>(ws, q.o_loss_part), at<double>(ws, q.o_pos_part),
                                                 at<int>(ws, q.o_seq), q.nseq, q.Mp, W, (double)p->loss_weight,
                                                 do_pos ? 1 : 0, at<int>(ws, q.o_err), loss_sse, pos_grad);
     int rc = join(fs);
+    if (!rc && sbranch) rc = join(sbranch);
     if (rc) return rc;
     prof_mark(st, -1);
     return cuda_status();
@@ -366,7 +379,10 @@ int run_path(const pty_problem_t* p, const Plan& q, const float2* obj, const flo
   } else {
     for (int ib = 0; ib < q.nbatch; ++ib) {
       if ((rc = P.windows(ib)) || (rc = P.fused(ib, 0, probe, measured, patterns))) return rc;
-      if (!patterns && q.nbatch == 1) P.pbranch = P.fork();   // after the fused kernel
+      if (!patterns && q.nbatch == 1) {   // branches after the fused kernel
+        P.pbranch = P.fork();
+        P.sbranch = P.fork2();
+      }
       if (!patterns && (rc = P.gradients(ib))) return rc;
     }
   }

@@ -37,6 +37,7 @@ struct Plan {
   // blocks to fill the GPU; o_scpart holds their partial tiles
   int sgroups;
   size_t o_scpart;
+  size_t o_done;   // per (slice, tile) count of finished run blocks (sgroups > 1)
 };
 
 // blocks the scatter aims for: two per SM of a 152-SM GB300
@@ -138,6 +139,7 @@ inline Plan make_plan(const pty_problem_t* p, bool split = false) {
     q.sgroups = std::max(1, std::min(g, 32));
   }
   q.o_scpart = take(q.sgroups > 1 ? (size_t)q.sgroups * q.ntiles * q.zm * kTileSize * kTileSize * c8 : 0);
+  q.o_done = take(q.sgroups > 1 ? (size_t)q.ntiles * q.zm * sizeof(int) : 0);
   q.total = o;
   return q;
 }

@@ -1041,14 +1041,17 @@ static __global__ void tile_lists_kernel(const int* __restrict__ pos, const int*
 // blockDim = (32, 8); grid = (ntiles, Z*Mo, groups). With groups = 1 a block adds its tile's
 // whole list onto the gradient plane. With groups > 1 (few tiles: a small object or a single
 // slice) the list is cut into `groups` consecutive runs; block (tile, k, g) sums run g alone
-// into part[g][k][tile] and scatter_merge_kernel adds the runs in order -- still a fixed order,
-// now with groups x more blocks at work.
+// into part[g][k][tile], and the last of the tile's run blocks to finish (an integer counter per
+// (slice, tile) in `done`, zero before the launch and reset by that block) adds the runs onto
+// the plane in run order -- still a fixed order, now with groups x more blocks at work.
 static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const int* __restrict__ pos,
                                      const int* __restrict__ seq, const int* __restrict__ lists,
                                      const int* __restrict__ counts, float2* __restrict__ grad,
                                      int Bb, int W, int Ny, int Nx, int ntx, int zm, int accumulate,
-                                     int groups = 1, float2* __restrict__ part = nullptr, int wmul = 1) {
+                                     int groups = 1, float2* __restrict__ part = nullptr, int wmul = 1,
+                                     int* __restrict__ done = nullptr) {
   __shared__ int s_b[256], s_y[256], s_x[256];
+  __shared__ int s_last;
   const int tile = blockIdx.x, k = blockIdx.y, g = blockIdx.z;
   const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
   const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
@@ -1116,34 +1119,32 @@ static __global__ void scatter_tiles_kernel(const float2* __restrict__ gw, const
     float2* pt = part + (((size_t)g * zm + k) * (gridDim.x) + tile) * (TS * TS);
 #pragma unroll
     for (int r = 0; r < 4; ++r) pt[(ly + 8 * r) * TS + lx] = acc[r];
+    // the last of the tile's run blocks to finish adds the runs in run order; the integer
+    // counter only decides which block that is
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&done[k * gridDim.x + tile], 1) == groups - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    float2 sum[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int y = ty0 + ly + 8 * r;
+      sum[r] = (accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
+    }
+    for (int gg = 0; gg < groups; ++gg) {
+      const float2* pg = part + (((size_t)gg * zm + k) * gridDim.x + tile) * (TS * TS);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) sum[r] = cadd(sum[r], __ldcg(pg + (ly + 8 * r) * TS + lx));
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int y = ty0 + ly + 8 * r;
+      if (y < Ny && x < Nx) plane[(size_t)y * Nx + x] = sum[r];
+    }
+    if (tid == 0) done[k * gridDim.x + tile] = 0;   // ready for the next batch's launch
     return;
-  }
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int y = ty0 + ly + 8 * r;
-    if (y < Ny && x < Nx) plane[(size_t)y * Nx + x] = acc[r];
-  }
-}
-
-// The runs of scatter_tiles_kernel with groups > 1, added onto the plane in run order.
-// blockDim = (32, 8); grid = (ntiles, Z*Mo)
-static __global__ void scatter_merge_kernel(const float2* __restrict__ part, float2* __restrict__ grad, int groups,
-                                            int Ny, int Nx, int ntx, int zm, int accumulate) {
-  const int tile = blockIdx.x, k = blockIdx.y;
-  const int ty0 = (tile / ntx) * TS, tx0 = (tile % ntx) * TS;
-  const int lx = threadIdx.x, ly = threadIdx.y;
-  const int x = tx0 + lx;
-  float2* plane = grad + (size_t)k * Ny * Nx;
-  float2 acc[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int y = ty0 + ly + 8 * r;
-    acc[r] = (accumulate && y < Ny && x < Nx) ? plane[(size_t)y * Nx + x] : make_float2(0.f, 0.f);
-  }
-  for (int g = 0; g < groups; ++g) {
-    const float2* pt = part + (((size_t)g * zm + k) * gridDim.x + tile) * (TS * TS);
-#pragma unroll
-    for (int r = 0; r < 4; ++r) acc[r] = cadd(acc[r], pt[(ly + 8 * r) * TS + lx]);
   }
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
