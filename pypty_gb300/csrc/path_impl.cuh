@@ -33,7 +33,7 @@ struct Path {
   // directly (no transposes).
   const float2* obj_src = nullptr;
   float2* grad_out = nullptr;
-  bool lists_done = false;         // batch 0's tile lists were built while the tables were
+  bool lists_done = false;         // batch 0's tile lists were built by prepare()
   cudaStream_t pbranch = nullptr;  // one batch: the probe-gradient sum runs here, beside the
                                    // object-gradient band limit and scatter
   cudaStream_t sbranch = nullptr;  // one batch: the FP64 scalars and position gradient
@@ -56,6 +56,7 @@ struct Path {
     ta.wavelength = p->wavelength;
     ta.edge_mult = p->edge_mult;
     ta.use_edge = (p->edge_mult > 1.0f && q.Z > 1) ? 1 : 0;
+    ta.tw = tw;   // tables_kernel writes the twiddle tables too
   }
 
   static int attributes() {
@@ -69,10 +70,10 @@ struct Path {
     return PTY_OK;
   }
 
-  // Independent launches of a call's ends (the twiddles and probe spectrum beside the tables and
-  // the object transpose; the probe-gradient transform beside the object-gradient transpose and
-  // the scalars) run on two streams: fork() makes the side stream wait for st, join() makes st
-  // wait for the side stream. While the launch profiler records, everything stays on st.
+  // Independent launches of a call's ends (the probe spectrum beside the tile lists and the
+  // object transpose; the probe-gradient transform beside the object-gradient transpose and the
+  // scalars) run on side streams: fork() makes the side stream wait for st, join() makes st wait
+  // for it. While the launch profiler records, everything stays on st.
   cudaStream_t fork() {
     SideStream* sd = nullptr;
     if (prof_active() || side_stream(&sd) != PTY_OK) return st;
@@ -98,32 +99,31 @@ struct Path {
     return PTY_OK;
   }
 
-  // early_lists: the call has one batch and object gradients, so batch 0's tile lists (which
-  // depend only on the geometry) are built beside the tables
+  // The tables (with the twiddles) first; then the probe spectrum on a branch beside the tile
+  // lists (early_lists: the call has one batch and object gradients, so batch 0's lists, which
+  // depend only on the geometry, are built here) and the object transpose.
   int prepare(const float2* obj, const float2* probe, bool early_lists = false) {
     int rc = attributes();
     if (rc) return rc;
+    prof_mark(st, KID_TABLES);
+    tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);   // with the twiddles
+    if (q.per_step)
+      launch_step_props<W>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
+                           ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
     cudaStream_t fs = fork();
-    prof_mark(fs, KID_TWIDDLES);
-    build_twiddles_kernel<W><<<1, 256, 0, fs>>>(tw);
     if (p->probe_shift) {
       prof_mark(fs, KID_PROBE_FFT);
       probe_fft_kernel<W><<<q.Mp, T, Smem<W>::bytes, fs>>>(probe, q.Mp, tw, at<float2>(ws, q.o_probe_f));
     }
-    if (q.sgroups > 1 && cudaMemsetAsync(at<int>(ws, q.o_done), 0, (size_t)q.ntiles * q.zm * sizeof(int), fs) !=
-                             cudaSuccess)
+    if (q.sgroups > 1 &&
+        cudaMemsetAsync(at<int>(ws, q.o_done), 0, (size_t)q.ntiles * q.zm * sizeof(int), st) != cudaSuccess)
       return PTY_ERR_CUDA;
     if (early_lists && q.nbatch == 1 && p->step_obj) {
-      prof_mark(fs, KID_TILE_LISTS);
-      tile_lists_kernel<<<q.ntiles, 256, 0, fs>>>(at<int>(ws, q.o_pos), seq_of(0), batch_count(0), W, q.ntx,
+      prof_mark(st, KID_TILE_LISTS);
+      tile_lists_kernel<<<q.ntiles, 256, 0, st>>>(at<int>(ws, q.o_pos), seq_of(0), batch_count(0), W, q.ntx,
                                                   at<int>(ws, q.o_lists), at<int>(ws, q.o_counts));
       lists_done = true;
     }
-    prof_mark(st, KID_TABLES);
-    tables_kernel<W><<<(unsigned)((WW + 255) / 256), 256, 0, st>>>(ta);
-    if (q.per_step)
-      launch_step_props<W>(ta.mask, p->slice_distances, q.Z - 1, ta.px, ta.py, ta.wavelength, ta.edge_mult,
-                           ta.use_edge, 0.0f, 0.0f, at<float2>(ws, q.o_steps), st);
     const int nyx = q.Ny * q.Nx;
     if (q.zm == 1) {
       obj_src = obj;

@@ -36,6 +36,7 @@ struct TableArgs {
   float* sy;
   float px, py, cutoff, rolloff, distance, wavelength, edge_mult;
   int use_edge;
+  float2* tw;           // W <= 128, not null: the window FFT's twiddle tables are written too
 };
 
 // scipy.fft.fftfreq(n, d) as the reference evaluates it with a float32 pixel size d:
@@ -108,6 +109,9 @@ inline void launch_step_props(const float* mask, const float* distances_host, in
 template <int W>
 __global__ void tables_kernel(TableArgs a) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (W <= 128) {
+    if (a.tw && idx < Geo<W>::TW1 + Geo<W>::TW2) a.tw[idx] = twiddle_entry<W>(idx);
+  }
   if (idx < W) {
     // fftfreq(W) with d = 1 is exact in float64: k / W
     const int kk = (idx < W / 2) ? idx : idx - W;

@@ -438,23 +438,29 @@ __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.w
 // every bulk store of this thread has completed its writes to global memory
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
-// Host/device builder of the twiddle tables in global memory (see load_twiddles).
+// Entry i of the twiddle tables in global memory (see load_twiddles).
+template <int W>
+__device__ __forceinline__ float2 twiddle_entry(int i) {
+  using G = Geo<W>;
+  int e;
+  if (i < G::TW1) {
+    int n2 = i / 32, k1 = (i % 32) ^ n2;
+    e = (k1 * n2) % W;
+  } else {
+    int j = i - G::TW1, m2 = j / G::C, j1 = j % G::C;
+    e = (j1 * m2) % W;
+  }
+  float s, c;
+  sincospif(2.0f * (float)e / (float)W, &s, &c);   // exact argument: e/W is a dyadic rational
+  return make_float2(c, -s);
+}
+
+// Builder of the twiddle tables in global memory.
 template <int W>
 __global__ void build_twiddles_kernel(float2* g_tw) {
   using G = Geo<W>;
-  for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < G::TW1 + G::TW2; i += blockDim.x * gridDim.x) {
-    int e;
-    if (i < G::TW1) {
-      int n2 = i / 32, k1 = (i % 32) ^ n2;
-      e = (k1 * n2) % W;
-    } else {
-      int j = i - G::TW1, m2 = j / G::C, j1 = j % G::C;
-      e = (j1 * m2) % W;
-    }
-    float s, c;
-    sincospif(2.0f * (float)e / (float)W, &s, &c);   // exact argument: e/W is a dyadic rational
-    g_tw[i] = make_float2(c, -s);
-  }
+  for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < G::TW1 + G::TW2; i += blockDim.x * gridDim.x)
+    g_tw[i] = twiddle_entry<W>(i);
 }
 
 }  // namespace pty
