@@ -448,7 +448,11 @@ struct FusedSmem {
   static constexpr size_t pyx_off = side_off + sizeof(float2) * NST * Geo<W>::T;
   static constexpr size_t bits_off = pyx_off + sizeof(float2) * 2 * W;
   static constexpr size_t bar_off = bits_off + sizeof(uint32_t) * Geo<W>::T;
-  static constexpr size_t bytes = bar_off + 2 * sizeof(uint64_t);
+  // W = 64: the position's measured pattern (W^2 floats, detector order), copied in at the
+  // start, and the probe-shift ramp of the first step (frequency layout), reused by the last
+  static constexpr size_t meas_off = (bar_off + 2 * sizeof(uint64_t) + 15) & ~(size_t)15;
+  static constexpr size_t ramp_off = meas_off + (W == 64 ? sizeof(float) * W * W : 0);
+  static constexpr size_t bytes = ramp_off + (W == 64 ? sizeof(float2) * W * W : 0);
 };
 
 // One thread block per (position, probe mode, object mode); the Mp*Mo blocks of a position
@@ -481,8 +485,9 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   constexpr int NST = S::NST;
   constexpr size_t WW = (size_t)W * W;
   // W = 64 (few slices, latency-bound far field and probe steps): mask bits instead of the
-  // float mask, the separable shift ramp, measured values loaded a chunk ahead. At W = 128 the
-  // extra live values spill (measured slower), so these stay compiled out there.
+  // float mask, the separable shift ramp, the measured pattern copied into shared memory at the
+  // start. At W = 128 the extra live values spill and shared memory is full, so these stay
+  // compiled out there.
   constexpr bool kLean = (W == 64);
   extern __shared__ __align__(16) unsigned char smem[];
   float2 *xbuf, *tw1, *tw2;
@@ -521,6 +526,19 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
     sbits[t] = mbits;   // kept in shared memory: registers are needed for the window
   }
   __syncthreads();
+  float* smeas = reinterpret_cast<float*>(smem + S::meas_off);    // W = 64 only
+  float2* sramp = reinterpret_cast<float2*>(smem + S::ramp_off);  // W = 64 only
+  if constexpr (kLean) {
+    if (!a.simulate && a.measured) {   // the far field waits for these copies
+      const float* src = a.measured + (size_t)gi * WW;
+      if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        for (int e = 4 * t; e < (int)WW; e += 4 * T) cp_async16(smeas + e, src + e);
+      } else {
+        for (int e = t; e < (int)WW; e += T) cp_async4(smeas + e, src + e);
+      }
+      cp_async_commit();
+    }
+  }
   uint32_t ph_x = 0, ph_side = 0;
 
   auto obl_ptr = [&](int z) { return a.obl + (((size_t)b * Z + z) * a.Mo + m) * WW; };
@@ -713,6 +731,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         visit_sep_ramp<W>(a, t, dy, dx, [&](auto I, int, int, float2 ramp) {
           constexpr int i = decltype(I)::value;
           v[i] = ((mbits >> i) & 1u) ? cscale(cmul(pf[nidx<W>(i, t)], ramp), inv) : make_float2(0.f, 0.f);
+          sramp[i * T + t] = ramp;   // the same ramp serves the probe-gradient step (phase 0)
         });
       } else {
 #pragma unroll
@@ -737,6 +756,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       }
     } else if (fwd) {
       // far field: Psi = FFT(exit) * mask, I = mean over modes |Psi|^2 (objective.py:501-512)
+      if constexpr (kLean) cp_async_wait_all();   // the measured pattern; the cluster barrier below
+                                                  // makes every thread's part visible
       __syncthreads();
       if (kLean && a.mask_bin) {
         const uint32_t mbits = sbits[t];
@@ -781,7 +802,7 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
           const int i = i0 + k;
           const int ky = G::fky(t, i), kx = G::fkx(t, i);
           const int didx = ((ky + W / 2) & (W - 1)) * W + ((kx + W / 2) & (W - 1));
-          dst[k] = a.simulate ? 0.0f : meas[didx];
+          dst[k] = a.simulate ? 0.0f : (kLean ? smeas[didx] : meas[didx]);
         }
       };
       float mv[8], nx[8];
@@ -841,7 +862,21 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
       // probe-gradient spectrum with the shift adjoint, position gradient (objective.py:641-656)
       const float2* pf = a.probe_f + (size_t)p * WW;
       FSum gy_c, gx_c;
-      if (a.probe_shift) {
+      if (kLean && a.probe_shift && a.mask_bin && phase == 0) {
+        // the first step's ramp, kept in shared memory by this thread
+        const uint32_t mbits = sbits[t];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int ky = G::fky(t, i), kx = G::fkx(t, i);
+          const float mk = ((mbits >> i) & 1u) ? 1.0f : 0.0f;
+          v[i] = cmulc(v[i], cscale(sramp[i * T + t], mk));
+          if (a.step_pos) {   // as below
+            const float im = cmulc(v[i], pf[nidx<W>(i, t)]).y;
+            gy_c += -(a.sy[ky] * mk) * im;
+            gx_c += -(a.sx[kx] * mk) * im;
+          }
+        }
+      } else if (a.probe_shift) {
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           const int ky = G::fky(t, i), kx = G::fkx(t, i);

@@ -396,6 +396,18 @@ __device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t& parity, int* 
   parity ^= 1u;
 }
 
+// Asynchronous copies global -> shared through the load path (cp.async: any global address,
+// device memory or mapped pinned host memory), 16 or 4 bytes per copy with both addresses
+// aligned to the size; a thread's copies are complete after its cp_async_wait_all().
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Issue (one thread) an L2 prefetch of `bytes` at `src` (16-byte aligned, a multiple of 16
 // bytes) in chunks of at most 64 KiB; nothing waits on it.
 __device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
