@@ -3,10 +3,9 @@
 // Every thread owns 32 complex values. A 2D transform is three register rounds separated
 // by two exchanges through shared memory:
 //
-//   round 1  thread (y, n2), n2 < A=W/32 : 32-point DFT along x over x = A*n1 + n2,
-//            twiddle w_W^(k1*n2)
-//   round 2  thread (k1, m2), m2 < Bq    : A-point DFT over n2 (finishes kx = k1 + 32*k2),
-//            C-point DFT along y over y = Bq*m1 + m2, twiddle w_W^(j1*m2)
+//   round 1  thread (y, n2), n2 < A=W/32 : 32-point DFT along x over x = A*n1 + n2
+//   round 2  thread (k1, m2), m2 < Bq    : twiddle w_W^(k1*n2), A-point DFT over n2 (finishes
+//            kx = k1 + 32*k2), C-point DFT along y over y = Bq*m1 + m2, twiddle w_W^(j1*m2)
 //   round 3  thread (j1, g), g < S3      : Bq-point DFT over m2 (finishes ky = j1 + C*j2),
 //            the thread holds kx = g + S3*q
 //
@@ -168,6 +167,9 @@ struct Geo {
 
 // Twiddle tables (built once per launch into shared memory from a global copy):
 //   tw1[n2*32 + (k1 ^ n2)] = w_W^(k1*n2),  tw2[m2*C + j1] = w_W^(j1*m2),  w_W = exp(-2 pi i/W)
+// The x twiddle w_W^(k1*n2) between the 32-point and the A-point DFT along x is applied in round
+// 2, where a thread holds one k1 and every n2: A - 1 distinct factors per thread (A - 1 table
+// reads, C * (A - 1) multiplies) instead of 31 reads and multiplies per thread in round 1.
 template <int W>
 __device__ __forceinline__ void load_twiddles(float2* s_tw1, float2* s_tw2, const float2* g_tw) {
   using G = Geo<W>;
@@ -198,11 +200,8 @@ struct WinFFT {
   // forward_rest calls after_first_sync() right after its first barrier, when every thread of
   // the block has finished everything it did before forward_rest.
   static __device__ __forceinline__ void forward_round1(float2 (&v)[32], const float2* tw1) {
-    const int t = threadIdx.x;
+    (void)tw1;   // the x twiddle is applied in round 2
     DFT<32, -1>::template run<32, 1, 0>(v);
-    const int n2 = t % A;   // varies inside a warp: multiply unconditionally (row n2=0 is 1)
-#pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmul(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
   }
 
   template <typename AfterSync>
@@ -221,6 +220,15 @@ struct WinFFT {
       for (int m1 = 0; m1 < C; ++m1)
 #pragma unroll
         for (int n2 = 0; n2 < A; ++n2) v[m1 * A + n2] = xbuf[x1((Bq * m1 + m2) * A + n2, k1)];
+      {   // x twiddle w_W^(k1*n2): this thread's k1 is fixed
+        float2 w[A];
+#pragma unroll
+        for (int n2 = 1; n2 < A; ++n2) w[n2] = tw1[n2 * 32 + (k1 ^ n2)];
+#pragma unroll
+        for (int m1 = 0; m1 < C; ++m1)
+#pragma unroll
+          for (int n2 = 1; n2 < A; ++n2) v[m1 * A + n2] = cmul(v[m1 * A + n2], w[n2]);
+      }
       static_for<0, C>([&](auto M1) { DFT<A, -1>::template run<32, 1, decltype(M1)::value * A>(v); });
       static_for<0, A>([&](auto K2) { DFT<C, -1>::template run<32, A, decltype(K2)::value>(v); });
       if (m2 != 0) {
@@ -260,9 +268,7 @@ struct WinFFT {
   // run inverse_head (everything up to the last xbuf read), synchronise, refill xbuf
   // asynchronously, and then run inverse_tail while the copy is in flight.
   static __device__ __forceinline__ void inverse_tail(float2 (&v)[32], const float2* tw1) {
-    const int n2 = threadIdx.x % A;
-#pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmulc(v[k1], tw1[n2 * 32 + (k1 ^ n2)]);
+    (void)tw1;   // the conjugate x twiddle was applied in round 2 of inverse_head
     DFT<32, +1>::template run<32, 1, 0>(v);
   }
 
@@ -296,6 +302,15 @@ struct WinFFT {
       }
       static_for<0, A>([&](auto K2) { DFT<C, +1>::template run<32, A, decltype(K2)::value>(v); });
       static_for<0, C>([&](auto M1) { DFT<A, +1>::template run<32, 1, decltype(M1)::value * A>(v); });
+      {   // conjugate x twiddle w_W^(-k1*n2), this thread's k1 fixed
+        float2 w[A];
+#pragma unroll
+        for (int n2 = 1; n2 < A; ++n2) w[n2] = tw1[n2 * 32 + (k1 ^ n2)];
+#pragma unroll
+        for (int m1 = 0; m1 < C; ++m1)
+#pragma unroll
+          for (int n2 = 1; n2 < A; ++n2) v[m1 * A + n2] = cmulc(v[m1 * A + n2], w[n2]);
+      }
       __syncthreads();
 #pragma unroll
       for (int m1 = 0; m1 < C; ++m1)

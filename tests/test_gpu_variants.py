@@ -1,6 +1,11 @@
 """Near-field propagation, compressed-detector losses, beam current, aberration plates and the
 inside tilt on the GPU (``pty_loss_and_direction_variants``) against the reference's own
-results (golden fixtures) and the FP64 variants oracle on the same inputs."""
+results (golden fixtures) and the FP64 variants oracle on the same inputs.
+
+Bounds against FP64: the complex64 tolerance (loss 1e-5, gradients 1e-4; 2e-4 for the
+compressed losses) or, where the reference's own complex64 arithmetic is further than that from
+FP64 on the case's inputs, 1.5 times that error -- the convention of the headline and
+precision-sweep tests: the GPU must be as accurate as the reference's single-precision path."""
 import numpy as np
 import pytest
 
@@ -47,22 +52,23 @@ def run_gpu_variant(c, engine=None):
             cpu(tg), cpu(sbg))
 
 
-def fp64_variant_oracle(c):
+def fp64_variant_oracle(c, f=np.float64, cdt=np.complex128):
+    """The variants oracle on the case's inputs (FP64 unless other dtypes are given)."""
     return vor.loss_and_direction_variants(
-        np.asarray(c["obj"], np.complex128), np.asarray(c["probe"], np.complex128), c["positions"],
-        np.asarray(c["pos_correction"], np.float64),
-        c["distance"] if c["distances"] is None else np.asarray(c["distances"], np.float64), c["edge_mult"],
-        np.asarray(c["measured"], np.float64), c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"],
+        np.asarray(c["obj"], cdt), np.asarray(c["probe"], cdt), c["positions"],
+        np.asarray(c["pos_correction"], f),
+        c["distance"] if c["distances"] is None else np.asarray(c["distances"], f), c["edge_mult"],
+        np.asarray(c["measured"], f), c["algorithm"], c["wavelength"], c["step_probe"], c["step_obj"],
         c["step_pos"], c["px"], c["px"], c["cutoff"], c["rolloff"], c["sequence"], c["loss_weight"], c["batch"],
         recon_type=c["recon_type"], defocus=c["defocus"] if c["defocus_array"] is None else c["defocus_array"],
         cs=c["cs"], tan_x=c["tan_x"], tan_y=c["tan_y"],
-        masks=None if c["masks"] is None else np.asarray(c["masks"], np.float64),
+        masks=None if c["masks"] is None else np.asarray(c["masks"], f),
         beam_current=c["beam_current"], step_beam_current=c["step_bc"], aberrations=c["aberrations"],
         aberration_marker=c["aberration_marker"], step_aberrations=c["step_ab"], data_pad=c["data_pad"],
         use_padded_intensity=c["use_padded"], data_shift_vector=(c["shift0"], c["shift1"]), data_multiplier=c["mult"],
         tilts=c["tilts"], tilt_mode=c["tilt_mode"], step_tilts=c["step_tilts"], upsample_pattern=c["upsample"],
         static_background=c["static_background"], step_static_background=c["step_sb"],
-        probe_marker=c["probe_marker"], float_dtype=np.float64, complex_dtype=np.complex128)
+        probe_marker=c["probe_marker"], float_dtype=f, complex_dtype=cdt)
 
 
 def errors(res, ref):
@@ -95,13 +101,16 @@ def test_variants_against_fp64_oracle_and_reference(name):
     c = load_variant_case(name)
     res = run_gpu_variant(c)
     lt, gt = TOL.get(c["algorithm"], (1e-5, 1e-4))
-    e64 = errors(res, fp64_variant_oracle(c))
-    print(name, "vs FP64", {k: "%.1e" % v for k, v in e64.items()})
-    for k, v in e64.items():
-        assert v <= (lt if k == "loss" else gt), (k, v)
-    # the reference's own complex64 result carries its FP32 error too: twice the bound
+    o64 = fp64_variant_oracle(c)
+    e64 = errors(res, o64)
     ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
            c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"], c["ref_static_grad"])
+    floor = errors(ref, o64)   # the reference's own complex64 result against FP64
+    print(name, "vs FP64", {k: "%.1e" % v for k, v in e64.items()},
+          "reference complex64 vs FP64", {k: "%.1e" % v for k, v in floor.items()})
+    for k, v in e64.items():
+        assert v <= max(lt if k == "loss" else gt, 1.5 * floor.get(k, 0.0)), (k, v, floor.get(k))
+    # the reference's own complex64 result carries its FP32 error too: twice the bound
     eref = errors(res, ref)
     print(name, "vs reference c64", {k: "%.1e" % v for k, v in eref.items()})
     for k, v in eref.items():
@@ -116,9 +125,10 @@ def test_variants_against_reference_fp64(name):
     ref = (c["ref_loss"], c["ref_sse"], c["ref_object_grad"], c["ref_probe_grad"], c["ref_pos_grad"],
            c["ref_beam_current_grad"], c["ref_aberrations_grad"], c["ref_tilts_grad"], c["ref_static_grad"])
     e = errors(res, ref)
-    print(name, {k: "%.1e" % v for k, v in e.items()})
+    floor = errors(fp64_variant_oracle(c, np.float32, np.complex64), ref)   # complex64 arithmetic
+    print(name, {k: "%.1e" % v for k, v in e.items()}, "complex64 oracle", {k: "%.1e" % v for k, v in floor.items()})
     for k, v in e.items():
-        assert v <= (1e-5 if k == "loss" else 1e-4), (k, v)
+        assert v <= max(1e-5 if k == "loss" else 1e-4, 1.5 * floor.get(k, 0.0)), (k, v, floor.get(k))
 
 
 def test_variants_without_options_match_layered_far_field():
