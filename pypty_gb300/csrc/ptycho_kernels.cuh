@@ -912,13 +912,21 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
         if (s == Z && t == 0) bulk_wait_all();
         issue_x(s + 1);
       }
-      // every block asks for its operands at about the same time: bring O_z two steps ahead
-      // (and, in the adjoint, the stack window the side buffer takes after the next) into L2
-      // now, so that the copies and loads of the next steps read L2 instead of waiting for HBM
+      // every block asks for its operands at about the same time: bring what the next steps
+      // read late into L2 now, so that they read L2 instead of waiting for HBM -- the adjoint's
+      // O_z two steps ahead (copied into the exchange buffer just in time) and the parts of the
+      // side-buffer windows that are read by plain loads (their prefixes arrive by TMA a whole
+      // step ahead)
       if (t == 0) {
-        if (s + 2 < s_end) prefetch_l2(xsrc(s + 2), (uint32_t)(WW * sizeof(float2)));
+        constexpr uint32_t kTailBytes = (uint32_t)((WW - (size_t)NST * T) * sizeof(float2));
+        if (s + 2 < s_end) {
+          if (s + 2 <= Z)   // forward: the side copy (a step ahead) takes the prefix; the tail is loaded
+            prefetch_l2(xsrc(s + 2) + (size_t)NST * T, kTailBytes);
+          else              // adjoint: O_z goes to the exchange buffer just in time
+            prefetch_l2(xsrc(s + 2), (uint32_t)(WW * sizeof(float2)));
+        }
         const int zs = 2 * Z - s - 2;
-        if (adj_stack && s >= Z && zs >= 0) prefetch_l2(stack_ptr(zs), (uint32_t)(WW * sizeof(float2)));
+        if (adj_stack && s >= Z && zs >= 0) prefetch_l2(stack_ptr(zs) + (size_t)NST * T, kTailBytes);
       }
     }
     F::inverse_tail(v, tw1);
