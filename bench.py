@@ -97,9 +97,9 @@ def fused_bytes_per_position(W, Z, Mp, Mo=1):
 # DRAM bytes (read + write) per position of the fused kernel(s), from one ncu capture each
 # (dram__bytes_read.sum + dram__bytes_write.sum of the launch / positions in it); a launch of
 # the same shape moves the same bytes per position, so traffic per launch scales by positions:
-#   (128, 20, 3): fused_multislice_kernel<128>, multislice-small, 64 positions, 1.3708 GB
+#   (128, 20, 3): fused_multislice_kernel<128>, multislice-small, 64 positions, 1.7056 GB
 #   (256, 8, 5):  fused256_kernel<1> + <2>, precision-sweep-small, 64 positions, 10.674 GB
-TRAFFIC_PER_POSITION = {(128, 20, 3): 1.3708e9 / 64, (256, 8, 5): 10.674e9 / 64}
+TRAFFIC_PER_POSITION = {(128, 20, 3): 1.7056e9 / 64, (256, 8, 5): 10.674e9 / 64}
 
 
 def fft_flops_per_position(W, Z, Mp, Mo=1):
