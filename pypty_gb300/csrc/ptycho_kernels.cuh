@@ -469,11 +469,14 @@ struct FusedSmem {
 //                   field, loss and dL/dPsi after the last slice), IFFT
 //   steps Z+1..2Z   slice z = 2Z-s: object-gradient contribution, g *= conj(O_z), FFT,
 //                   *= conj(P), IFFT (z = 0: probe-gradient spectrum and position gradient)
-// Operands are prefetched by TMA bulk copies. O_z arrives in the side buffer (its first NST
-// elements per thread; the rest is loaded from global memory at the step) one step ahead,
-// in the forward and the adjoint alike; the adjoint's first step reuses the forward's last
-// O_z. The adjoint's conj(psi_z) lands in the exchange buffer while the inverse transform
-// finishes its last register-only round.
+// Operands: the side buffer (each thread's first NST elements, a prefix of the native layout)
+// takes every step's streamed window by TMA one step ahead -- O_z in the forward, conj(psi_z)
+// from the stack in the adjoint -- and the rest of that window is loaded at the step. The step
+// writes its outgoing window (conj(psi_z) in the forward, this mode's gradient contribution in
+// the adjoint) into the side buffer in place of what it read, and a TMA bulk store takes it out
+// behind the forward transform. The adjoint's O_z lands in the exchange buffer while the
+// inverse transform finishes its last register-only round; the adjoint's first step finds
+// conj(psi_{Z-1}) still in the side buffer.
 // PH = 0: the whole pass (phase 0) with every phase branch compiled out; PH = 1: a.phase at
 // run time (the split halves and the multislice_core phases).
 template <int W, int PH>
