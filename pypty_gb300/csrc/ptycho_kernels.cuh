@@ -532,7 +532,8 @@ __global__ void __launch_bounds__(Geo<W>::T, Geo<W>::MINB) fused_multislice_kern
   float* smeas = reinterpret_cast<float*>(smem + S::meas_off);    // W = 64 only
   float2* sramp = reinterpret_cast<float2*>(smem + S::ramp_off);  // W = 64 only
   if constexpr (kLean) {
-    if (!a.simulate && a.measured) {   // the far field waits for these copies
+    // only passes that reach the far field (which waits for these copies) issue them
+    if (!a.simulate && a.measured && (phase <= 1)) {
       const float* src = a.measured + (size_t)gi * WW;
       if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
         for (int e = 4 * t; e < (int)WW; e += 4 * T) cp_async16(smeas + e, src + e);
