@@ -15,8 +15,9 @@
 // slice, propagator, masks, loss) happens directly in those layouts, so a multislice step
 // is FFT -> multiply -> IFFT without any extra data movement.
 //
-// Shared-memory exchanges use XOR swizzles chosen so that every half-warp of 8-byte
-// accesses touches 16 distinct bank pairs (no bank conflicts) for both W.
+// Shared-memory exchanges use XOR swizzles chosen so that every half-warp of 8-byte accesses
+// touches 16 distinct bank pairs and every quarter-warp of round 1's 16-byte accesses 8 distinct
+// bank quads (no bank conflicts) for both W.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -184,7 +185,9 @@ struct WinFFT {
   using G = Geo<W>;
   static constexpr int A = G::A, C = G::C, Bq = G::Bq, Q = G::Q, S3 = G::S3;
 
-  static __device__ __forceinline__ int x1(int r, int k1) { return r * 32 + (k1 ^ (r & 15)); }
+  // the XOR masks are even, so a row's elements 2j and 2j+1 stay adjacent: round 1 moves them
+  // as one 16-byte word (round 2 reads single elements), conflict-free both ways
+  static __device__ __forceinline__ int x1(int r, int k1) { return r * 32 + (k1 ^ ((r & 7) << 1)); }
   static __device__ __forceinline__ int x2(int s, int kx) { return s * W + (kx ^ ((s & 1) << 3)); }
 
   // real layout -> frequency layout, unnormalised, exp(-2 pi i ...) kernel
@@ -211,7 +214,9 @@ struct WinFFT {
     __syncthreads();
     after_first_sync();
 #pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) xbuf[x1(t, k1)] = v[k1];
+    for (int j = 0; j < 16; ++j)
+      reinterpret_cast<float4*>(xbuf)[x1(t, 2 * j) >> 1] =
+          make_float4(v[2 * j].x, v[2 * j].y, v[2 * j + 1].x, v[2 * j + 1].y);
     __syncthreads();
     // ---- round 2
     {
@@ -319,7 +324,11 @@ struct WinFFT {
     }
     __syncthreads();
 #pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) v[k1] = xbuf[x1(t, k1)];
+    for (int j = 0; j < 16; ++j) {
+      const float4 q = reinterpret_cast<const float4*>(xbuf)[x1(t, 2 * j) >> 1];
+      v[2 * j] = make_float2(q.x, q.y);
+      v[2 * j + 1] = make_float2(q.z, q.w);
+    }
   }
 };
 
